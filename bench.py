@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""EBE-PCG benchmark of the p121 solve on GB300.
+
+Workload: the 100x100x100 20-node hexahedron cube (nip=27, E=100, v=0.3, every
+dof of the base face fixed, uniform top pressure with total load -1), ~12.2M
+equations, synthetic (generated in memory; no dataset).
+
+  step   = one PCG iteration over the whole mesh (element products, node
+           scatter, fused updates and reductions) of the mixed-precision
+           solver's inner loop (FP32 storkm, FP64 vectors and scalars);
+  value  = equations x steps / device time of the K timed steps (DOF.iter/s);
+  e2e    = one full mixed-precision solve to ||f-Ku||/||f|| <= 1e-8 through
+           pf_solve with host buffers (load vector in, displacements out),
+           DOF.iter/s over its wall time;
+  time_to_1e8 = wall time of that solve and of the plain FP64 solve.
+
+--impl reference times the CPU restatement of p121's PCG (oracle/, OpenMP on
+all host cores) on a bounded slab of the same cube.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "EBE-PCG DOF·iter/s & time-to-1e-8, mixed vs FP64 on 1 GB300; serving p50/p99 ms"
+UNIT = "DOF·iter/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=100, help="elements per cube edge")
+    ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_init(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+        return rank, world, local, dist
+    return 0, 1, 0, None
+
+
+def dist_max(dist, local, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], device=f"cuda:{local}", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(dist, local, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([float(v)], device=f"cuda:{local}", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_tag):
+    """DRAM bytes per launch from the committed ncu summary of that kernel, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
+    try:
+        txt = open(path).read()
+    except OSError:
+        return None
+    m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
+
+
+# ---------------------------------------------------------------------------
+def elem_bytes(nels, nslots, sbytes):
+    """Algorithmic bytes of one element-product launch: storkm, connectivity,
+    the gathered vector (each slot once) and the element results."""
+    return nels * (3600 * sbytes + 20 * 4 + 60 * sbytes) + nslots * 8
+
+
+def cpu_port_leg(n, k_steps, warm):
+    """The oracle (C restatement of p121's PCG, OpenMP) on an n x n x 8 slab."""
+    from oracle import oracle as O
+    nz = 8
+    prob = oracle_cube(n, n, nz)
+    km = O.form_storkm(prob["gc"], 27, 100.0, 0.3)
+    dg = O.diag(prob["g_g"], km, prob["neq"])
+    O.pcg(prob["g_g"], km, dg, prob["r"], 0.0, max(warm, 1), 0)
+    t0 = time.perf_counter()
+    O.pcg(prob["g_g"], km, dg, prob["r"], 0.0, k_steps, 0)
+    dt = time.perf_counter() - t0
+    return {"value": prob["neq"] * k_steps / dt, "unit": UNIT, "cores": O.lib().orc_num_threads(),
+            "kind": "port", "seconds": dt,
+            "sample": f"{n}x{n}x{nz} slab of the same cube (neq {prob['neq']}), nip 27, FP64, "
+                      f"{k_steps} p121 PCG iterations of the C restatement"}
+
+
+def oracle_cube(nxe, nye, nze):
+    """Fixed-base, top-pressure cube built with the oracle's own routines."""
+    from oracle import oracle as O
+    L = O.lib()
+    nels = nxe * nye * nze
+    g_num = np.zeros((nels, 20), np.int32)
+    gc = np.zeros((nels, 3, 20))
+    coord = np.zeros(60)
+    num = np.zeros(20, np.int32)
+    for e in range(nels):
+        L.orc_geometry_20bxz(e + 1, nxe, nze, 1.0, 1.0, 1.0, coord, num)
+        g_num[e] = num
+        gc[e] = coord.reshape(3, 20)
+    nn = int(g_num.max())
+    base = np.unique(g_num[:, [0, 6, 7, 8, 11, 12, 18, 19]][np.arange(nels) % (nxe * nze) >= nxe * (nze - 1)])
+    rest = np.zeros((len(base) + 1, 4), np.int32)
+    rest[0] = [1, 1, 1, 1]                     # keeps find_g3 inside rest
+    rest[1:, 0] = base
+    g_g = O.steering(g_num, rest)
+    neq = int(g_g.max())
+    r = np.zeros(neq + 1)
+    p = 1.0 / (nxe * nye)
+    top = np.nonzero(np.arange(nels) % (nxe * nze) < nxe)[0]
+    for e in top:
+        for a in (3, 5, 15, 17):
+            r[g_g[e, 3 * a - 1]] += p / 12.0
+        for a in (4, 10, 11, 16):
+            r[g_g[e, 3 * a - 1]] -= p / 3.0
+    return dict(g_num=g_num, gc=gc, g_g=g_g, neq=neq, r=r[1:].copy(), nn=nn)
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    n = args.size
+    leg = cpu_port_leg(n, args.steps, args.warmup)
+    line = {
+        "metric": METRIC, "value": leg["value"], "unit": UNIT, "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * leg["seconds"] / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_of(args),
+        "cpu_baseline": {k: leg[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": leg["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "ParaFEM's Fortran/MPI p121 cannot be built here (no Fortran compiler or MPI); "
+                "the timed reference is the C restatement of its PCG in oracle/",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def config_of(args):
+    n = args.size
+    return {"workload": f"p121 cube {n}x{n}x{n} hex20, nip 27, E 100, v 0.3, fixed base, top pressure "
+                        f"(total -1), mixed FP32-storkm PCG + FP64 defect correction",
+            "nels": n ** 3, "global_batch": 1, "parallelism": "replicas",
+            "l2": "inputs larger than L2 (storkm FP32 %.1f GB)" % (n ** 3 * 14400 / 1e9)}
+
+
+def run_gb300(args, rank, world, local, dist):
+    import parafem_gb300 as P
+    n = args.size
+    t0 = time.perf_counter()
+    prob = P.cube_problem(n, n, n)
+    t_host = time.perf_counter() - t0
+    s = P.Solver(local)
+    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+    s.set_material(100.0, 0.3)
+    t1 = time.perf_counter()
+    s.form_storkm(27)
+    t_form = time.perf_counter() - t1
+    neq = prob["neq"]
+    nels = n ** 3
+    r = prob["r"]
+    extra = {"host_setup_s": t_host, "storkm_formation_s": t_form}
+
+    # e2e: one full mixed solve through the C-ABI with host buffers
+    solves = {}
+    e2e_val = None
+    if args.no_solves:
+        s.solve(r, 1e-8, 1, P.MODE_MIXED)          # loads the right-hand side only
+    else:
+        barrier(dist)
+        t2 = time.perf_counter()
+        x, it_m, rel_m = s.solve(r, 1e-8, 20000, P.MODE_MIXED)
+        t_mixed = time.perf_counter() - t2
+        st_m = s.stats()
+        t_mixed = dist_max(dist, local, t_mixed)
+        e2e_val = dist_sum(dist, local, neq * it_m) / t_mixed
+        solves["mixed"] = {"wall_s": t_mixed, "device_s": st_m["solve_ms"] / 1e3, "inner_iters": it_m,
+                           "outer": st_m["outer"], "relres": rel_m}
+        t3 = time.perf_counter()
+        x64, it_64, rel_64 = s.solve(r, 1e-8, 20000, P.MODE_FP64_RES)
+        t_64 = dist_max(dist, local, time.perf_counter() - t3)
+        st_64 = s.stats()
+        solves["fp64"] = {"wall_s": t_64, "device_s": st_64["solve_ms"] / 1e3, "iters": it_64,
+                          "relres": rel_64}
+        solves["mixed_over_fp64_time"] = t_mixed / t_64
+        solves["mixed_vs_fp64_rel_err_2"] = float(np.linalg.norm(x - x64) / np.linalg.norm(x64))
+
+    # timed steps: K iterations of the FP32-storkm PCG, device resident
+    s.bench_iterations(32, max(args.warmup, 3))
+    clk = Clocks(local).start() if rank == 0 else None
+    l0 = s.launches()
+    barrier(dist)
+    ms_tot, ms_elem, ms_scat = s.bench_iterations(32, args.steps)
+    barrier(dist)
+    launches = s.launches() - l0
+    clocks = clk.stop() if clk else None
+    ms_tot = dist_max(dist, local, ms_tot)
+    value = dist_sum(dist, local, neq) * args.steps / (ms_tot / 1e3)
+    # FP64 steps (the plain drop-in path) for reference
+    s.bench_iterations(64, 3)
+    ms64, ms64_elem, _ = s.bench_iterations(64, max(args.steps // 2, 3))
+    k64 = max(args.steps // 2, 3)
+    extra["fp64_dof_iter_s"] = neq * k64 / (ms64 / 1e3)
+    extra["fp64_elem_ms"] = ms64_elem / k64
+
+    peak, peak_kind = measured_peaks()
+    nslots = 3 * prob["nn"]
+    b_launch = elem_bytes(nels, nslots, 4)
+    avg_s = ms_elem / args.steps / 1e3
+    achieved = b_launch / avg_s / 1e9
+    roof = {"kernel": "k_elem<float> (FP32 storkm element products)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": b_launch,
+            "avg_launch_ms": avg_s * 1e3, "traffic": ncu_traffic("k_elem_f32_cube100"),
+            "scatter_avg_ms": ms_scat / args.steps}
+    b64 = elem_bytes(nels, nslots, 8)
+    extra["fp64_elem_hbm_frac"] = b64 / (ms64_elem / k64 / 1e3) / 1e9 / peak
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-storkm/f64-vectors", "data": "synthetic",
+        "config": config_of(args),
+        "e2e": None if e2e_val is None else {
+            "value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": int(neq * 8),
+            "d2h_bytes_per_step": int(neq * 8), "step": "one full mixed solve to relres 1e-8"},
+        "time_to_1e8": solves, "roofline": roof, "gpu_launches": int(launches),
+        "clocks": clocks, "extra": extra,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = {k: v for k, v in cpu_port_leg(n, 20, 2).items() if k != "seconds"}
+        except Exception as exc:  # the baseline is reported, never the target
+            line["cpu_baseline"] = {"error": str(exc)}
+    s.close()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse_args()
+    rank, world, local, dist = dist_init(args.gpus)
+    try:
+        if args.impl == "reference":
+            return run_reference(args, rank)
+        return run_gb300(args, rank, world, local, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

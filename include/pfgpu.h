@@ -1,0 +1,186 @@
+/*
+ * pfgpu.h -- C-ABI of the GB300 element-by-element PCG library (libpfgpu.so).
+ *
+ * The library replaces the solve section of ParaFEM's p121 driver
+ * (src/programs/5th_ed/p121/p121.f90:39-104: storkm formation, Jacobi
+ * diagonal, preconditioned CG with checon_par) and, as a second entry
+ * layer, the element-product offload of the xx3 experiment
+ * (src/programs/dev/xx3/cuda_helpers.cu:183-368).
+ *
+ * Conventions follow xx3's ISO_C_BINDING layer (xx3.f90:56-148):
+ *   - every argument is passed by reference;
+ *   - host arrays are caller-owned and Fortran column-major;
+ *   - device objects are opaque handles held by the caller (void**);
+ *   - every entry point returns int: 0 = EXIT_SUCCESS, 1 = EXIT_FAILURE.
+ * Unlike xx3 nothing is printed on failure: the message is kept per thread
+ * and returned by pf_last_error.  All entry points are synchronous.
+ *
+ * Array layouts (Fortran shapes, 1-based ids as p121 holds them):
+ *   g_num(20,nels)      node numbers in Smith-Griffiths order
+ *   g_g(60,nels)        equation numbers, 0 = restrained (find_g3 output)
+ *   g_coord(20,3,nels)  nodal coordinates per element
+ *   storkm(60,60,nels)  element stiffness matrices
+ *   r, xnew(neq)        load and displacement vectors in equation order
+ */
+#ifndef PFGPU_H
+#define PFGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PF_SUCCESS 0
+#define PF_FAILURE 1
+
+/* pf_solve modes */
+#define PF_MODE_P121     0 /* FP64 storkm, checon_par test (p121.f90:88-104)      */
+#define PF_MODE_FP64_RES 1 /* FP64 storkm, stop at ||r||2/||f||2 <= tol           */
+#define PF_MODE_MIXED    2 /* FP32-storkm inner PCG + FP64 defect correction,
+                              stop at the FP64 true ||f-Ku||2/||f||2 <= tol        */
+
+/* pf_form_storkm flags */
+#define PF_FORM_EXACT_WEIGHTS 1 /* exact 5/9, 8/9 Gauss factors instead of
+                                   p121's single-precision literals
+                                   (new_library.f90:1493)                        */
+#define PF_FORM_NO_FP32       2 /* do not keep the FP32 copy of storkm            */
+
+/* ---------------------------------------------------------------------- */
+/* xx3 layer: same names and argument meaning as
+ * src/programs/dev/xx3/cuda_helpers.cu, so xx3.f90 links unchanged.       */
+
+/* cuda_helpers.cu:183 set_gpu */
+int set_gpu(const int *device_id);
+/* cuda_helpers.cu:198 allocate_memory_on_gpu (sizes multiplied in 64 bits) */
+int allocate_memory_on_gpu(const int *n_elements, const int *element_size,
+                           void **device_pointer);
+/* cuda_helpers.cu:216 free_memory_on_gpu */
+int free_memory_on_gpu(void **device_pointer);
+/* cuda_helpers.cu:232 copy_data_to_gpu */
+int copy_data_to_gpu(const int *n_elements, const int *element_size,
+                     const void *host_data, void **device_pointer);
+/* cuda_helpers.cu:255 copy_data_from_gpu */
+int copy_data_from_gpu(const int *n_elements, const int *element_size,
+                       void *host_data, void **device_pointer);
+/* cuda_helpers.cu:278 matrix_vector_multiplies: for every matrix m,
+ * rhs(:,m) = matrix(:,:,m) . lhs(:,m), FP64, column-major matrices. */
+int matrix_vector_multiplies(int *n_mat, int *n_row, int *n_col,
+                             void **d_lhs_vector, void **d_matrix,
+                             void **d_rhs_vector);
+
+/* ---------------------------------------------------------------------- */
+/* Solve layer (replaces p121.f90:39-104).                                 */
+
+/* Copies the calling thread's last error message (NUL-terminated). */
+int pf_last_error(char *buf, const int *len);
+
+/* Creates a solver context on a device (set_gpu(numpe-1) of xx3.f90:412). */
+int pf_ctx_create(const int *device, void **ctx);
+int pf_ctx_destroy(void **ctx);
+
+/* Mesh and steering: the arrays p121 holds after find_g3 (p121.f90:33-49).
+ * nn: number of nodes (ids in g_num are 1..nn); neq = MAXVAL(g_g). */
+int pf_setup(void **ctx, const int *nels, const int *nn, const int *neq,
+             const int *g_num, const int *g_g, const double *g_coord);
+
+/* Material: n = 1 (one E, v for every element, p121.f90:54) or n = nels
+ * (per element, as rfemsolve.f90:217-221). */
+int pf_set_material(void **ctx, const int *n, const double *e, const double *v);
+
+/* storkm integration and Jacobi diagonal on the GPU (p121.f90:54-69):
+ * SAMPLE / SHAPE_DER / DEEMAT / BEEMAT / INVERT, K = sum B'DB det w. */
+int pf_form_storkm(void **ctx, const int *nip, const int *flags);
+
+/* Host-formed storkm(60,60,nels) instead of pf_form_storkm (FP64; the FP32
+ * copy for PF_MODE_MIXED is derived on the device). */
+int pf_set_storkm(void **ctx, const double *storkm);
+
+/* Copies elements first..first+count-1 (0-based) of the FP64 storkm back. */
+int pf_get_storkm(void **ctx, const int *first, const int *count, double *storkm);
+
+/* Assembled (not inverted) Jacobi diagonal in equation order (neq). */
+int pf_get_diag(void **ctx, double *diag);
+
+/* One element-by-element product u = K p in equation order (GATHER,
+ * element MATMUL, SCATTER of p121.f90:92-97).  prec 64: FP64 storkm,
+ * 32: FP32 storkm. */
+int pf_ebe_matvec(void **ctx, const int *prec, const double *p, double *u);
+
+/* The PCG solve (p121.f90:86-104).  r: loads (neq); xnew: result (neq);
+ * iters: PCG iterations (inner iterations for PF_MODE_MIXED);
+ * relres: final FP64 ||f - K xnew||2 / ||f||2 (computed on the device). */
+int pf_solve(void **ctx, const double *r, const double *tol, const int *limit,
+             const int *mode, double *xnew, int *iters, double *relres);
+
+/* Statistics of the last pf_solve, written to stats[0..n-1]:
+ *  [0] iterations  [1] outer corrections  [2] solve milliseconds (device)
+ *  [3] final stopping metric  [4] FP64 matvecs  [5] FP32 matvecs
+ *  [6] true relative residual */
+int pf_solve_stats(void **ctx, double *stats, const int *n);
+
+/* Times `steps` PCG iterations on the resident state (prec 64 or 32) with
+ * CUDA events on the library stream.  ms_total: all steps; ms_elem: summed
+ * duration of the element-product kernel launches; ms_scatter: summed
+ * duration of the node-scatter kernel launches. */
+int pf_bench_iterations(void **ctx, const int *prec, const int *steps,
+                        double *ms_total, double *ms_elem, double *ms_scatter);
+
+/* Centroid stresses of one element from a displacement vector
+ * (p121.f90:112-123): sigma(6) = D . B(0,0,0) . u_e; iel is 1-based. */
+int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *sigma);
+
+/* Number of kernels this library launched since the context was created. */
+int pf_kernel_launches(void **ctx, long long *count);
+
+/* ---------------------------------------------------------------------- */
+/* Host-side driver layer (C++, no GPU work): deck I/O and generators.     */
+
+/* p12meshgen's p121 case (src/tools/preprocessing/p12meshgen/p12meshgen.f90:118-323):
+ * reads job.mg and writes job.dat, job.d, job.bnd, job.lds. */
+int pf_p12meshgen(const char *job);
+
+/* Runs the whole p121 job (p121.f90:1-141) on the GPU: reads job.dat/.d/
+ * .bnd/.lds, solves, writes job.res and job.ensi.DISPL-000001.
+ * mode: PF_MODE_*; iters and central (xnew(1)) are returned. */
+int pf_p121_run(const char *job, const int *device, const int *mode,
+                int *iters, double *central);
+
+/* Structured 20-node cube mesh in GEOMETRY_20BXZ numbering
+ * (src/modules/shared/geometry.f90:172-290), nxe x nye x nze elements of
+ * size aa x bb x cc.  First call with g_num == NULL returns the sizes
+ * (nels, nn); the second fills g_num(20,nels) and g_coord(20,3,nels). */
+int pf_mesh_cube(const int *nxe, const int *nye, const int *nze, const double *aa,
+                 const double *bb, const double *cc, int *nels, int *nn,
+                 int *g_num, double *g_coord);
+
+/* Restraints and loads of the synthetic cube problems:
+ *   bc 0: cube_bc20 rollers + fixed base (geometry.f90:425-504)
+ *   bc 1: every dof fixed on the base face z = -nze*cc, nothing else
+ * Fills node_fix(3,nn) with 1 = free, 0 = fixed.  */
+int pf_cube_restraints(const int *nxe, const int *nye, const int *nze, const int *bc,
+                       int *node_fix);
+
+/* Equation numbering (REARRANGE + find_g3, new_library.f90:3059-3212):
+ * node_fix(3,nn) -> g_g(60,nels) and neq. */
+int pf_number_equations(const int *nels, const int *nn, const int *g_num,
+                        const int *node_fix, int *g_g, int *neq);
+
+/* Consistent nodal loads of a uniform pressure p (force per area, acting
+ * in -z) on the top face z = 0 of a GEOMETRY_20BXZ cube mesh, added into r
+ * (equation order, neq): per top face, corners +pA/12 and mid-sides -pA/3,
+ * the rule behind load_p121's 1:-4 pattern (loading.f90:437-495). */
+int pf_cube_top_pressure(const int *nxe, const int *nze, const int *nels,
+                         const double *aa, const double *bb, const double *p,
+                         const int *g_g, const int *neq, double *r);
+
+/* Per-element material field from a counter-based generator (Philox4x32-10,
+ * key = seed, counter = element index): E log-uniform in [e_lo, e_hi],
+ * v uniform in [v_lo, v_hi]. */
+int pf_random_material(const int *nels, const long long *seed, const double *e_lo,
+                       const double *e_hi, const double *v_lo, const double *v_hi,
+                       double *e, double *v);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PFGPU_H */

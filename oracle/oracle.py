@@ -1,0 +1,267 @@
+"""CPU oracle for the p121 EBE-PCG path (TEST INFRASTRUCTURE ONLY).
+
+Wraps ``p121_oracle.c`` (a plain-C restatement of ParaFEM's p121 solve) and
+adds a numpy reader for p121 decks.  Only the tests, the smoke check and the
+CPU-baseline leg of ``bench.py`` import this module; the product library never
+does.
+
+Reference routines restated (paths inside the ParaFEM tree):
+  src/programs/5th_ed/p121/p121.f90:27-141           driver
+  src/modules/mpi/input.f90:3336 (READ_P121), :1037-1060 (READ_G_NUM_PP),
+    :893-896 (READ_G_COORD_PP), :2622 (READ_REST), :2399 (READ_LOADS)
+  src/modules/shared/new_library.f90 SAMPLE/SHAPE_DER/DEEMAT/BEEMAT/REARRANGE/
+    find_g3/ABAQUS2SG, src/modules/mpi/maths.f90 DOT_PRODUCT_P/INVERT/
+    DETERMINANT/checon_par, src/modules/mpi/loading.f90 LOAD/load_p121,
+    src/modules/shared/geometry.f90 GEOMETRY_20BXZ/cube_bc20
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "liborc.so")
+_lock = threading.Lock()
+_lib = None
+
+_I = ctypes.c_int
+_D = ctypes.c_double
+_PI = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_PD = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def build(force: bool = False) -> str:
+    """Compile the C restatement into ``oracle/_build/liborc.so`` (gcc, OpenMP)."""
+    src = os.path.join(HERE, "p121_oracle.c")
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+        return LIB_PATH
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp",
+                           "-ffp-contract=off", "-o", tmp, src, "-lm"])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            L = ctypes.CDLL(build())
+            L.orc_geometry_20bxz.argtypes = [_I, _I, _I, _D, _D, _D, _PD, _PI]
+            L.orc_cube_bc20.argtypes = [_I, _I, _I, _PI]
+            L.orc_cube_bc20.restype = _I
+            L.orc_load_p121.argtypes = [_I, _I, _I, _PI, _PD]
+            L.orc_load_p121.restype = _I
+            L.orc_rearrange.argtypes = [_I, _PI]
+            L.orc_find_g3.argtypes = [_PI, _PI, _I, _PI]
+            L.orc_abaqus2sg.argtypes = [_I, _PI]
+            L.orc_sample.argtypes = [_I, _PD, _PD, _I]
+            L.orc_sample.restype = _I
+            L.orc_shape_der20.argtypes = [_PD, _D, _D, _D]
+            L.orc_deemat.argtypes = [_PD, _D, _D]
+            L.orc_form_storkm.argtypes = [_I, _I, _I, _PD, _PD, _PD, _I, _PD]
+            L.orc_diag.argtypes = [_I, _I, _PI, _PD, _PD]
+            L.orc_load.argtypes = [_I, _I, _PI, _PI, _I, _PI, _PD, _PD]
+            L.orc_pcg.argtypes = [_I, _I, _PI, _PD, _PD, _PD, _D, _I, _I, _PD,
+                                  ctypes.POINTER(ctypes.c_double), ctypes.c_void_p]
+            L.orc_pcg.restype = _I
+            L.orc_ebe_matvec.argtypes = [_I, _I, _PI, _PD, _PD, _PD]
+            L.orc_centroid_stress.argtypes = [_PD, _PD, _D, _D, _PD]
+            L.orc_num_threads.restype = _I
+            L.orc_set_num_threads.argtypes = [_I]
+            _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------------------
+# Deck reading (p121 text formats)
+# ---------------------------------------------------------------------------
+@dataclass
+class Deck:
+    element: str
+    meshgen: int
+    partitioner: int
+    nels: int
+    nn: int
+    nr: int
+    nip: int
+    nod: int
+    loaded_nodes: int
+    e: float
+    v: float
+    tol: float
+    limit: int
+    coords: np.ndarray      # (nn, 3) float64, node id i at row i-1
+    g_num: np.ndarray       # (nels, 20) int32, Smith-Griffiths order after abaqus2sg
+    rest: np.ndarray        # (nr, 4) int32 as read (1 = free, 0 = fixed)
+    load_node: np.ndarray   # (loaded_nodes,) int32
+    load_val: np.ndarray    # (loaded_nodes, 3) float64
+
+
+def _fortran_float(tok: str) -> float:
+    return float(tok.replace("D", "E").replace("d", "e"))
+
+
+def read_deck(job: str) -> Deck:
+    """Read job.dat/.d/.bnd/.lds as READ_P121 and friends do."""
+    with open(job + ".dat") as f:
+        toks = f.read().split()
+    element = toks[0].strip("'\"")
+    meshgen, part, nels, nn, nr, nip, nod, ln = (int(t) for t in toks[1:9])
+    e, v, tol = (_fortran_float(t) for t in toks[9:12])
+    limit = int(toks[12])
+    with open(job + ".d") as f:
+        lines = f.read().splitlines()
+    i0 = lines.index("*NODES") + 1
+    i1 = lines.index("*ELEMENTS")
+    coords = np.loadtxt(lines[i0:i1], dtype=np.float64)[:, 1:4]
+    if coords.shape[0] != nn:
+        raise ValueError(f"{job}.d has {coords.shape[0]} nodes, .dat says {nn}")
+    el = np.loadtxt(lines[i1 + 1:i1 + 1 + nels], dtype=np.int64)
+    g_num = np.ascontiguousarray(el[:, 4:4 + nod], dtype=np.int32)
+    if meshgen == 2:
+        lib().orc_abaqus2sg(nels, g_num)
+    rest = np.loadtxt(job + ".bnd", dtype=np.int32, ndmin=2).reshape(-1, 4)[:nr]
+    if ln > 0:
+        lds = np.loadtxt(job + ".lds", dtype=np.float64, ndmin=2).reshape(-1, 4)[:ln]
+        load_node = np.ascontiguousarray(lds[:, 0].astype(np.int32))
+        load_val = np.ascontiguousarray(lds[:, 1:4])
+    else:
+        load_node = np.zeros(0, np.int32)
+        load_val = np.zeros((0, 3))
+    return Deck(element, meshgen, part, nels, nn, nr, nip, nod, ln, e, v, tol, limit,
+                coords, g_num, np.ascontiguousarray(rest), load_node, load_val)
+
+
+# ---------------------------------------------------------------------------
+# Restated steps
+# ---------------------------------------------------------------------------
+def steering(g_num: np.ndarray, rest: np.ndarray) -> np.ndarray:
+    """REARRANGE + find_g3 for every element -> g_g (nels, 60), 1-based, 0 = fixed."""
+    L = lib()
+    rr = np.ascontiguousarray(rest, dtype=np.int32).copy()
+    L.orc_rearrange(rr.shape[0], rr)
+    nels = g_num.shape[0]
+    g_g = np.zeros((nels, 60), np.int32)
+    row = np.zeros(60, np.int32)
+    for e in range(nels):
+        L.orc_find_g3(np.ascontiguousarray(g_num[e]), row, rr.shape[0], rr)
+        g_g[e] = row
+    return g_g
+
+
+def element_coords(coords: np.ndarray, g_num: np.ndarray) -> np.ndarray:
+    """g_coord_pp(nod,ndim,nels) as a C array (nels, 3, 20)."""
+    return np.ascontiguousarray(coords[g_num - 1].transpose(0, 2, 1))
+
+
+def form_storkm(g_coord: np.ndarray, nip: int, e, v, exact_weights: bool = False) -> np.ndarray:
+    nels = g_coord.shape[0]
+    e_arr = np.ascontiguousarray(np.atleast_1d(np.asarray(e, np.float64)))
+    v_arr = np.ascontiguousarray(np.atleast_1d(np.asarray(v, np.float64)))
+    per = int(e_arr.size > 1)
+    km = np.zeros((nels, 60, 60), np.float64)   # km[e, j, i] = K_e(i, j)
+    lib().orc_form_storkm(nels, nip, int(exact_weights), g_coord, e_arr, v_arr, per, km)
+    return km
+
+
+def diag(g_g: np.ndarray, storkm: np.ndarray, neq: int) -> np.ndarray:
+    out = np.zeros(neq)
+    lib().orc_diag(g_g.shape[0], neq, np.ascontiguousarray(g_g), storkm, out)
+    return out
+
+
+def load_vector(g_num, g_g, load_node, load_val, neq) -> np.ndarray:
+    r = np.zeros(neq)
+    lib().orc_load(g_num.shape[0], neq, np.ascontiguousarray(g_num), np.ascontiguousarray(g_g),
+                   int(load_node.size), np.ascontiguousarray(load_node, dtype=np.int32),
+                   np.ascontiguousarray(load_val, dtype=np.float64), r)
+    return r
+
+
+def pcg(g_g, storkm, dg, rhs, tol, limit, stop_mode=0, history=False):
+    """p121 PCG.  stop_mode 0: checon_par; 1: relative residual.
+
+    Returns (iterations, x, final stopping metric[, metric history])."""
+    neq = rhs.size
+    x = np.zeros(neq)
+    m = ctypes.c_double(0.0)
+    hist = np.zeros(max(int(limit), 1)) if history else None
+    it = lib().orc_pcg(g_g.shape[0], neq, np.ascontiguousarray(g_g), storkm, dg,
+                       np.ascontiguousarray(rhs, dtype=np.float64), float(tol), int(limit),
+                       int(stop_mode), x, ctypes.byref(m),
+                       hist.ctypes.data if history else None)
+    if history:
+        return it, x, m.value, hist[:it].copy()
+    return it, x, m.value
+
+
+def ebe_matvec(g_g, storkm, p):
+    u = np.zeros(p.size)
+    lib().orc_ebe_matvec(g_g.shape[0], p.size, np.ascontiguousarray(g_g), storkm,
+                         np.ascontiguousarray(p, dtype=np.float64), u)
+    return u
+
+
+def centroid_stress(coord_e: np.ndarray, eld: np.ndarray, e: float, v: float) -> np.ndarray:
+    s = np.zeros(6)
+    lib().orc_centroid_stress(np.ascontiguousarray(coord_e.reshape(-1)),
+                              np.ascontiguousarray(eld), float(e), float(v), s)
+    return s
+
+
+def nodal_displacements(g_num, g_g, x, nn) -> np.ndarray:
+    """Node-wise displacement field (nn, 3); fixed dofs are zero."""
+    disp = np.zeros((nn, 3))
+    x0 = np.concatenate([[0.0], x])
+    disp[g_num.reshape(-1) - 1] = x0[g_g.reshape(-1, 3)]
+    return disp
+
+
+@dataclass
+class P121Result:
+    nn: int
+    nr: int
+    neq: int
+    total_load: float
+    iters: int
+    x: np.ndarray
+    central: float
+    stress: np.ndarray
+    disp: np.ndarray
+    storkm: np.ndarray
+    g_g: np.ndarray
+
+
+def run_p121(deck: Deck, exact_weights: bool = False, keep_storkm: bool = True) -> P121Result:
+    """The whole p121 job of p121.f90:27-141 on one rank."""
+    g_g = steering(deck.g_num, deck.rest)
+    neq = int(g_g.max())
+    gc = element_coords(deck.coords, deck.g_num)
+    km = form_storkm(gc, deck.nip, deck.e, deck.v, exact_weights)
+    dg = diag(g_g, km, neq)
+    r = load_vector(deck.g_num, g_g, deck.load_node, deck.load_val, neq)
+    q = _seq_sum(r)
+    it, x, _ = pcg(g_g, km, dg, r, deck.tol, deck.limit, 0)
+    x0 = np.concatenate([[0.0], x])
+    eld = x0[g_g[0]]
+    sig = centroid_stress(gc[0], eld, deck.e, deck.v)
+    disp = nodal_displacements(deck.g_num, g_g, x, deck.nn)
+    return P121Result(deck.nn, deck.nr, neq, q, it, x, float(x[0]), sig, disp,
+                      km if keep_storkm else None, g_g)
+
+
+def _seq_sum(a: np.ndarray) -> float:
+    """SUM_P on one rank: a left-to-right sum (src/modules/mpi/maths.f90:271)."""
+    s = 0.0
+    for val in a.tolist():
+        s += val
+    return s

@@ -1,0 +1,645 @@
+// pf_abi.cu -- the C-ABI of libpfgpu.so (declared in include/pfgpu.h).
+//
+// Host side of the solve layer: context lifetime, mesh set-up (the
+// node-centric scatter tables that replace MAKE_GGL's halo tables,
+// src/modules/mpi/gather_scatter.f90:1387-1784), and the solve drivers of
+// p121.f90:86-104.  All device work is issued on the context's stream; every
+// entry point synchronises before it returns, as xx3's layer does
+// (src/programs/dev/xx3/cuda_helpers.cu:355-365).
+#include "pf_internal.h"
+#include "pfgpu.h"
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace pf {
+
+static thread_local std::string g_err;
+
+void set_error(const char *fmt, ...)
+{
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+#define CK(call)                                                                         \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return PF_FAILURE;                                                           \
+        }                                                                                \
+    } while (0)
+
+#define TRY(call)                        \
+    do {                                 \
+        if ((call) != 0) return PF_FAILURE; \
+    } while (0)
+
+template <typename T>
+static int dalloc(T **ptr, size_t count, const char *what)
+{
+    *ptr = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)ptr, count * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cannot allocate %s (%zu bytes): %s", what, count * sizeof(T), cudaGetErrorString(e));
+        *ptr = nullptr;
+        return 1;
+    }
+    return 0;
+}
+
+template <typename T>
+static void dfree(T *&p)
+{
+    if (p) cudaFree((void *)p);
+    p = nullptr;
+}
+
+static Ctx *get_ctx(void **h)
+{
+    if (!h || !*h) {
+        set_error("null solver context");
+        return nullptr;
+    }
+    Ctx *c = (Ctx *)*h;
+    if (cudaSetDevice(c->device) != cudaSuccess) {
+        set_error("cannot select device %d", c->device);
+        return nullptr;
+    }
+    return c;
+}
+
+static void free_mesh(Ctx &c)
+{
+    dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
+    dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
+    dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
+    dfree(c.d); dfree(c.p); dfree(c.u); dfree(c.rres); dfree(c.eqbuf); dfree(c.utemp); dfree(c.part);
+    c.nels = c.nn = c.neq = c.nslots = 0;
+    c.nmat = 0;
+    c.have_km = false;
+}
+
+static int sync(Ctx &c)
+{
+    CK(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// Reads the device PCG state into the pinned mirror.
+static int pull_state(Ctx &c)
+{
+    CK(cudaMemcpyAsync(c.hst, c.st, sizeof(PcgState), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+// Runs PCG iterations until the device state says stop.  The state is read
+// back every `chunk` iterations; iterations launched after the stop return
+// at once (every kernel checks the flag).
+static int run_pcg(Ctx &c, int prec, double *xsol, int limit)
+{
+    int launched = 0;
+    int chunk = 4;
+    for (;;) {
+        for (int i = 0; i < chunk && launched < limit; ++i, ++launched)
+            TRY(launch_pcg_iteration(c, prec, xsol));
+        TRY(pull_state(c));
+        if (c.hst->stop || launched >= limit) break;
+        if (chunk < 32) chunk *= 2;
+    }
+    if (c.hst->err) {
+        set_error("PCG breakdown after %d iterations (non-finite r.d or |x|)", c.hst->iters);
+        return 1;
+    }
+    return 0;
+}
+
+// ||f - K64 x||_2 / ||f||_2 on the device (fills c.rres).
+static int true_relres(Ctx &c, const double *x, double ff, double *out, double *dev2)
+{
+    TRY(launch_residual(c, c.f, x, c.rres));
+    TRY(launch_sum_partials(c, 1, dev2));
+    double rr = 0.0;
+    CK(cudaMemcpyAsync(&rr, dev2, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    *out = ff > 0.0 ? std::sqrt(rr) / std::sqrt(ff) : 0.0;
+    return 0;
+}
+
+}  // namespace pf
+
+using namespace pf;
+
+// ===========================================================================
+// xx3 layer (src/programs/dev/xx3/cuda_helpers.cu:183-368)
+extern "C" int set_gpu(const int *device_id)
+{
+    if (!device_id) { set_error("set_gpu: null argument"); return PF_FAILURE; }
+    CK(cudaSetDevice(*device_id));
+    return PF_SUCCESS;
+}
+
+extern "C" int allocate_memory_on_gpu(const int *n_elements, const int *element_size, void **device_pointer)
+{
+    if (!n_elements || !element_size || !device_pointer || *n_elements < 0 || *element_size < 0) {
+        set_error("allocate_memory_on_gpu: invalid arguments");
+        return PF_FAILURE;
+    }
+    const size_t bytes = (size_t)*n_elements * (size_t)*element_size;
+    CK(cudaMalloc(device_pointer, bytes ? bytes : 1));
+    return PF_SUCCESS;
+}
+
+extern "C" int free_memory_on_gpu(void **device_pointer)
+{
+    if (!device_pointer) { set_error("free_memory_on_gpu: null argument"); return PF_FAILURE; }
+    CK(cudaFree(*device_pointer));
+    *device_pointer = nullptr;
+    return PF_SUCCESS;
+}
+
+extern "C" int copy_data_to_gpu(const int *n_elements, const int *element_size, const void *host_data,
+                                void **device_pointer)
+{
+    if (!n_elements || !element_size || !device_pointer || (!host_data && *n_elements > 0)) {
+        set_error("copy_data_to_gpu: invalid arguments");
+        return PF_FAILURE;
+    }
+    CK(cudaMemcpy(*device_pointer, host_data, (size_t)*n_elements * (size_t)*element_size,
+                  cudaMemcpyHostToDevice));
+    return PF_SUCCESS;
+}
+
+extern "C" int copy_data_from_gpu(const int *n_elements, const int *element_size, void *host_data,
+                                  void **device_pointer)
+{
+    if (!n_elements || !element_size || !device_pointer || (!host_data && *n_elements > 0)) {
+        set_error("copy_data_from_gpu: invalid arguments");
+        return PF_FAILURE;
+    }
+    CK(cudaMemcpy(host_data, *device_pointer, (size_t)*n_elements * (size_t)*element_size,
+                  cudaMemcpyDeviceToHost));
+    return PF_SUCCESS;
+}
+
+static long long g_xx3_launches = 0;
+
+extern "C" int matrix_vector_multiplies(int *n_mat, int *n_row, int *n_col, void **d_lhs_vector,
+                                        void **d_matrix, void **d_rhs_vector)
+{
+    if (!n_mat || !n_row || !n_col || !d_lhs_vector || !d_matrix || !d_rhs_vector || *n_mat < 0 ||
+        *n_row < 1 || *n_col < 1) {
+        set_error("matrix_vector_multiplies: invalid arguments");
+        return PF_FAILURE;
+    }
+    if (*n_mat == 0) return PF_SUCCESS;
+    if (launch_matvec_generic(*n_mat, *n_row, *n_col, (const double *)*d_lhs_vector,
+                              (const double *)*d_matrix, (double *)*d_rhs_vector, &g_xx3_launches))
+        return PF_FAILURE;
+    CK(cudaDeviceSynchronize());
+    return PF_SUCCESS;
+}
+
+// ===========================================================================
+// solve layer
+extern "C" int pf_last_error(char *buf, const int *len)
+{
+    if (!buf || !len || *len <= 0) return PF_FAILURE;
+    const size_t n = (size_t)*len - 1;
+    const size_t m = g_err.size() < n ? g_err.size() : n;
+    memcpy(buf, g_err.data(), m);
+    buf[m] = '\0';
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_ctx_create(const int *device, void **ctx)
+{
+    if (!device || !ctx) { set_error("pf_ctx_create: null argument"); return PF_FAILURE; }
+    *ctx = nullptr;
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (*device < 0 || *device >= ndev) {
+        set_error("pf_ctx_create: device %d out of range (%d devices)", *device, ndev);
+        return PF_FAILURE;
+    }
+    CK(cudaSetDevice(*device));
+    Ctx *c = new (std::nothrow) Ctx();
+    if (!c) { set_error("pf_ctx_create: out of host memory"); return PF_FAILURE; }
+    c->device = *device;
+    cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, c->device);
+    if (c->nsm < 1) c->nsm = 1;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc((void **)&c->st, sizeof(PcgState)) != cudaSuccess ||
+        cudaMallocHost((void **)&c->hst, sizeof(PcgState)) != cudaSuccess) {
+        set_error("pf_ctx_create: cannot create stream/state");
+        if (c->stream) cudaStreamDestroy(c->stream);
+        if (c->st) cudaFree(c->st);
+        delete c;
+        return PF_FAILURE;
+    }
+    memset(c->hst, 0, sizeof(PcgState));
+    *ctx = c;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_ctx_destroy(void **ctx)
+{
+    if (!ctx || !*ctx) return PF_SUCCESS;
+    Ctx *c = (Ctx *)*ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    free_mesh(*c);
+    if (c->st) cudaFree(c->st);
+    if (c->hst) cudaFreeHost(c->hst);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    *ctx = nullptr;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const int *neq_p, const int *g_num,
+                        const int *g_g, const double *g_coord)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!nels_p || !nn_p || !neq_p || !g_num || !g_g || !g_coord) {
+        set_error("pf_setup: null argument");
+        return PF_FAILURE;
+    }
+    const int nels = *nels_p, nn = *nn_p, neq = *neq_p;
+    if (nels < 1 || nn < 1 || neq < 0 || (long long)nn * 3 > 0x7fffffffLL || (long long)nels * 20 > 0x7fffffffLL) {
+        set_error("pf_setup: invalid sizes nels=%d nn=%d neq=%d", nels, nn, neq);
+        return PF_FAILURE;
+    }
+    CK(cudaStreamSynchronize(c.stream));
+    free_mesh(c);
+    const int ns = 3 * nn;
+    std::vector<int> conn((size_t)nels * 20), slot_eq(ns, -1), eq_slot(neq > 0 ? neq : 1, -1);
+    std::vector<int> cnt(nn + 1, 0);
+    for (size_t e = 0; e < (size_t)nels; ++e)
+        for (int a = 0; a < 20; ++a) {
+            const int nd = g_num[e * 20 + a];
+            if (nd < 1 || nd > nn) {
+                set_error("pf_setup: g_num(%d,%zu)=%d outside 1..%d", a + 1, e + 1, nd, nn);
+                return PF_FAILURE;
+            }
+            conn[e * 20 + a] = nd - 1;
+            cnt[nd]++;
+            for (int d = 0; d < 3; ++d) {
+                const int q = g_g[e * 60 + 3 * a + d];
+                if (q < 0 || q > neq) {
+                    set_error("pf_setup: g_g(%d,%zu)=%d outside 0..%d", 3 * a + d + 1, e + 1, q, neq);
+                    return PF_FAILURE;
+                }
+                int &se = slot_eq[3 * (nd - 1) + d];
+                if (se < 0) se = q;
+                else if (se != q) {
+                    set_error("pf_setup: node %d dof %d has equations %d and %d in different elements", nd,
+                              d + 1, se, q);
+                    return PF_FAILURE;
+                }
+            }
+        }
+    std::vector<uint8_t> fm(nn, 0);
+    for (int s = 0; s < ns; ++s) {
+        if (slot_eq[s] < 0) slot_eq[s] = 0;   // node used by no element
+        const int q = slot_eq[s];
+        if (q > 0) {
+            if (eq_slot[q - 1] >= 0) {
+                set_error("pf_setup: equation %d belongs to two dofs", q);
+                return PF_FAILURE;
+            }
+            eq_slot[q - 1] = s;
+            fm[s / 3] |= (uint8_t)(1u << (s % 3));
+        }
+    }
+    for (int q = 0; q < neq; ++q)
+        if (eq_slot[q] < 0) {
+            set_error("pf_setup: equation %d is not used by any element", q + 1);
+            return PF_FAILURE;
+        }
+    // node -> (element, local node) table, ascending element order per node
+    std::vector<int> ptr(nn + 1, 0);
+    for (int n = 0; n < nn; ++n) ptr[n + 1] = ptr[n] + cnt[n + 1];
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1), list((size_t)nels * 20);
+    for (size_t e = 0; e < (size_t)nels; ++e)
+        for (int a = 0; a < 20; ++a) {
+            const int n = conn[e * 20 + a];
+            list[fill[n]++] = (int)(e * 20 + a);
+        }
+
+    c.nels = nels; c.nn = nn; c.neq = neq; c.nslots = ns;
+    long long g = ((long long)ns + 255) / 256;
+    if (g > (long long)c.nsm * 4) g = (long long)c.nsm * 4;
+    c.G = (int)(g < 1 ? 1 : g);
+    const size_t ne = (size_t)nels;
+    if (dalloc(&c.conn, ne * 20, "connectivity") || dalloc(&c.node_ptr, nn + 1, "node table") ||
+        dalloc(&c.node_list, ne * 20, "node table") || dalloc(&c.slot_eq, ns, "slot map") ||
+        dalloc(&c.eq_slot, neq, "equation map") || dalloc(&c.freemask, nn, "restraint mask") ||
+        dalloc(&c.coord, ne * 60, "coordinates") || dalloc(&c.km64, ne * 3600, "FP64 storkm") ||
+        dalloc(&c.km32, ne * 3600, "FP32 storkm") || dalloc(&c.ediag, ne * 60, "element diagonals") ||
+        dalloc(&c.diag, ns, "diag") || dalloc(&c.dinv, ns, "diag") || dalloc(&c.f, ns, "f") ||
+        dalloc(&c.x, ns, "x") || dalloc(&c.c, ns, "c") || dalloc(&c.r, ns, "r") || dalloc(&c.d, ns, "d") ||
+        dalloc(&c.p, ns, "p") || dalloc(&c.u, ns, "u") || dalloc(&c.rres, ns, "rres") ||
+        dalloc(&c.eqbuf, neq + 8, "equation buffer") || dalloc((double **)&c.utemp, ne * 60, "utemp") ||
+        dalloc(&c.part, (size_t)8 * c.G + 16, "partials")) {
+        free_mesh(c);
+        return PF_FAILURE;
+    }
+    CK(cudaMemcpyAsync(c.conn, conn.data(), ne * 20 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.node_ptr, ptr.data(), (nn + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.node_list, list.data(), ne * 20 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.slot_eq, slot_eq.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    if (neq > 0)
+        CK(cudaMemcpyAsync(c.eq_slot, eq_slot.data(), neq * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.freemask, fm.data(), nn, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.coord, g_coord, ne * 60 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemsetAsync(c.x, 0, ns * sizeof(double), c.stream));
+    CK(cudaMemsetAsync(c.f, 0, ns * sizeof(double), c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_material(void **ctx, const int *n, const double *e, const double *v)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!n || !e || !v || c.nels == 0 || (*n != 1 && *n != c.nels)) {
+        set_error("pf_set_material: n must be 1 or nels (after pf_setup)");
+        return PF_FAILURE;
+    }
+    for (int i = 0; i < *n; ++i)
+        if (!(e[i] > 0.0) || !(v[i] > -1.0 && v[i] < 0.5)) {
+            set_error("pf_set_material: invalid E=%g v=%g for element %d", e[i], v[i], i + 1);
+            return PF_FAILURE;
+        }
+    dfree(c.mat_e);
+    dfree(c.mat_v);
+    if (dalloc(&c.mat_e, *n, "material") || dalloc(&c.mat_v, *n, "material")) return PF_FAILURE;
+    c.nmat = *n;
+    CK(cudaMemcpyAsync(c.mat_e, e, *n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.mat_v, v, *n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!nip || !flags || (*nip != 8 && *nip != 27)) {
+        set_error("pf_form_storkm: nip must be 8 or 27");
+        return PF_FAILURE;
+    }
+    if (c.nels == 0 || c.nmat == 0) {
+        set_error("pf_form_storkm: call pf_setup and pf_set_material first");
+        return PF_FAILURE;
+    }
+    const bool exact = (*flags & PF_FORM_EXACT_WEIGHTS) != 0;
+    TRY(launch_form_storkm(c, *nip, exact, true));
+    TRY(launch_assemble_diag(c));
+    TRY(sync(c));
+    c.have_km = true;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_storkm(void **ctx, const double *storkm)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!storkm || c.nels == 0) { set_error("pf_set_storkm: call pf_setup first"); return PF_FAILURE; }
+    CK(cudaMemcpyAsync(c.km64, storkm, (size_t)c.nels * 3600 * sizeof(double), cudaMemcpyHostToDevice,
+                       c.stream));
+    TRY(launch_cast_km32(c));
+    TRY(launch_assemble_diag(c));
+    TRY(sync(c));
+    c.have_km = true;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, double *storkm)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!first || !count || !storkm || !c.have_km || *first < 0 || *count < 0 || *first + *count > c.nels) {
+        set_error("pf_get_storkm: invalid range or no storkm");
+        return PF_FAILURE;
+    }
+    CK(cudaMemcpyAsync(storkm, c.km64 + (size_t)*first * 3600, (size_t)*count * 3600 * sizeof(double),
+                       cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_get_diag(void **ctx, double *diag)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!diag || !c.have_km) { set_error("pf_get_diag: no storkm"); return PF_FAILURE; }
+    TRY(launch_slot_to_eq(c, c.diag, c.eqbuf));
+    CK(cudaMemcpyAsync(diag, c.eqbuf, (size_t)c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, double *u)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32)) {
+        set_error("pf_ebe_matvec: invalid arguments or no storkm");
+        return PF_FAILURE;
+    }
+    CK(cudaMemcpyAsync(c.eqbuf, p, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
+    TRY(launch_matvec(c, *prec, c.rres, c.u));
+    TRY(launch_slot_to_eq(c, c.u, c.eqbuf));
+    CK(cudaMemcpyAsync(u, c.eqbuf, (size_t)c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+// Mixed precision: FP32-storkm inner PCG on the FP64 defect, FP64 update
+// of the solution and FP64 true residual from the FP64 storkm.
+static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2)
+{
+    const double eta_min = 1e-5;   // inner relative tolerance floor
+    const int max_outer = 50;
+    CK(cudaMemsetAsync(c.x, 0, (size_t)c.nslots * sizeof(double), c.stream));
+    CK(cudaMemcpyAsync(c.rres, c.f, (size_t)c.nslots * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    double rel = 1.0;
+    int inner_total = 0, outer = 0, mv64 = 0;
+    while (rel > tol && outer < max_outer && inner_total < limit) {
+        ++outer;
+        double eta = 0.5 * tol / rel;
+        if (eta < eta_min) eta = eta_min;
+        if (eta > 0.5) eta = 0.5;
+        TRY(launch_pcg_init(c, c.rres, c.c, STOP_RELRES, eta, limit - inner_total));
+        TRY(run_pcg(c, 32, c.c, limit - inner_total));
+        inner_total += c.hst->iters;
+        TRY(launch_axpy(c, c.x, c.c));
+        TRY(true_relres(c, c.x, ff, &rel, dev2));
+        ++mv64;
+    }
+    c.stats[0] = inner_total;
+    c.stats[1] = outer;
+    c.stats[3] = rel;
+    c.stats[4] = mv64;
+    c.stats[5] = inner_total;
+    return 0;
+}
+
+extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const int *limit, const int *mode,
+                        double *xnew, int *iters, double *relres)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!r || !tol || !limit || !mode || !xnew || !iters || !c.have_km || *limit < 1 ||
+        (*mode != PF_MODE_P121 && *mode != PF_MODE_FP64_RES && *mode != PF_MODE_MIXED)) {
+        set_error("pf_solve: invalid arguments or no storkm");
+        return PF_FAILURE;
+    }
+    for (int i = 0; i < 8; ++i) c.stats[i] = 0.0;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    double *dev2 = c.part + 8 * (size_t)c.G;   // spare doubles after the partials
+    CK(cudaMemcpyAsync(c.eqbuf, r, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    TRY(launch_eq_to_slot(c, c.eqbuf, c.f));
+    CK(cudaEventRecord(e0, c.stream));
+    int rc = 0;
+    double ff = 0.0;
+    {
+        // f.f via the init kernel's r.r partial
+        TRY(launch_pcg_init(c, c.f, c.x, *mode == PF_MODE_P121 ? STOP_CHECON : STOP_RELRES, *tol, *limit));
+        TRY(pull_state(c));
+        ff = c.hst->ff;
+    }
+    if (*mode == PF_MODE_MIXED) {
+        rc = solve_mixed(c, *tol, *limit, ff, dev2);
+    } else {
+        rc = run_pcg(c, 64, c.x, *limit);
+        c.stats[0] = c.hst->iters;
+        c.stats[1] = 0;
+        c.stats[3] = c.hst->metric;
+        c.stats[4] = c.hst->iters;
+    }
+    if (rc) return PF_FAILURE;
+    CK(cudaEventRecord(e1, c.stream));
+    double rel = 0.0;
+    TRY(true_relres(c, c.x, ff, &rel, dev2));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c.stats[2] = ms;
+    c.stats[6] = rel;
+    TRY(launch_slot_to_eq(c, c.x, c.eqbuf));
+    CK(cudaMemcpyAsync(xnew, c.eqbuf, (size_t)c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    *iters = (int)c.stats[0];
+    if (relres) *relres = rel;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_solve_stats(void **ctx, double *stats, const int *n)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp || !stats || !n) return PF_FAILURE;
+    for (int i = 0; i < *n && i < 8; ++i) stats[i] = cp->stats[i];
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps, double *ms_total,
+                                   double *ms_elem, double *ms_scatter)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!prec || !steps || *steps < 1 || !c.have_km || (*prec != 32 && *prec != 64)) {
+        set_error("pf_bench_iterations: invalid arguments or no storkm");
+        return PF_FAILURE;
+    }
+    const int n = *steps;
+    // never-converging run on the resident load vector (tol 0, no limit hit)
+    TRY(launch_pcg_init(c, c.f, c.c, STOP_RELRES, 0.0, n + 1));
+    TRY(pull_state(c));
+    if (c.hst->stop) {
+        set_error("pf_bench_iterations: the resident load vector is zero (run pf_solve first)");
+        return PF_FAILURE;
+    }
+    std::vector<cudaEvent_t> ev(3 * (size_t)n + 1);
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    CK(cudaEventRecord(ev[0], c.stream));
+    for (int i = 0; i < n; ++i) {
+        TRY(launch_elem(c, *prec, c.p));
+        CK(cudaEventRecord(ev[3 * i + 1], c.stream));
+        TRY(launch_scatter(c, *prec, 0, c.p, c.u));
+        CK(cudaEventRecord(ev[3 * i + 2], c.stream));
+        TRY(launch_update1(c, c.c));
+        TRY(launch_update2(c));
+        CK(cudaEventRecord(ev[3 * i + 3], c.stream));
+    }
+    CK(cudaStreamSynchronize(c.stream));
+    double te = 0, ts = 0;
+    for (int i = 0; i < n; ++i) {
+        float a = 0, b = 0;
+        CK(cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]));
+        CK(cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]));
+        te += a;
+        ts += b;
+    }
+    float tot = 0;
+    CK(cudaEventElapsedTime(&tot, ev[0], ev[3 * (size_t)n]));
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (ms_total) *ms_total = tot;
+    if (ms_elem) *ms_elem = te;
+    if (ms_scatter) *ms_scatter = ts;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *sigma)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!iel || !xnew || !sigma || *iel < 1 || *iel > c.nels || c.nmat == 0) {
+        set_error("pf_centroid_stress: invalid element or no material");
+        return PF_FAILURE;
+    }
+    double *sig = c.part + 8 * (size_t)c.G + 2;
+    CK(cudaMemcpyAsync(c.eqbuf, xnew, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
+    TRY(launch_centroid_stress(c, *iel - 1, c.rres, sig));
+    CK(cudaMemcpyAsync(sigma, sig, 6 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_kernel_launches(void **ctx, long long *count)
+{
+    if (!count) return PF_FAILURE;
+    *count = g_xx3_launches;
+    if (ctx && *ctx) *count += ((Ctx *)*ctx)->launches;
+    return PF_SUCCESS;
+}

@@ -1,0 +1,666 @@
+// pf_host.cpp -- host-side driver layer of libpfgpu.so (no device work).
+//
+// Deck I/O in the text formats of ParaFEM's p121 tools, the structured cube
+// generator and its restraint/load sets, equation numbering, and the p121
+// job driver that calls the solve layer.  The formats and numbering schemes
+// are fixed by the reference decks, so they follow:
+//   p12meshgen.f90:118-323 (src/tools/preprocessing/p12meshgen) .mg -> .dat/.d/.bnd/.lds
+//   geometry.f90:172-290 GEOMETRY_20BXZ node numbering, :425-504 cube_bc20
+//   loading.f90:386-480 load_p121 patch pattern
+//   input.f90:3336 READ_P121, :1037-1060 READ_G_NUM_PP, :893-896 READ_G_COORD_PP,
+//     :2622 READ_REST, :2399 READ_LOADS
+//   new_library.f90:3059-3212 REARRANGE + find_g3, :3569-3597 ABAQUS2SG
+//   p121.f90:70-141 .res lines and the Ensight displacement file
+#include "pfgpu.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace pf {
+void set_error(const char *fmt, ...);
+}
+using pf::set_error;
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Fortran edit descriptors used by the decks and result files
+std::string fmt_E(double v, int w, int d)
+{
+    const bool neg = std::signbit(v);
+    const double a = std::fabs(v);
+    std::string digits;
+    int ex = 0;
+    if (a == 0.0) {
+        digits.assign(d, '0');
+    } else {
+        char buf[64];
+        snprintf(buf, sizeof buf, "%.*e", d - 1, a);   // m.mmmme+XX
+        digits.push_back(buf[0]);
+        if (d > 1) digits.append(buf + 2, d - 1);
+        ex = atoi(strchr(buf, 'e') + 1) + 1;
+    }
+    char eb[16];
+    snprintf(eb, sizeof eb, "E%c%02d", ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+    std::string s = std::string(neg ? "-" : "") + "0." + digits + eb;
+    if ((int)s.size() < w) s.insert(0, w - s.size(), ' ');
+    return s;
+}
+
+std::string fmt_I(long long v, int w)
+{
+    char buf[64];
+    snprintf(buf, sizeof buf, "%*lld", w, v);
+    return buf;
+}
+
+std::string fmt_F(double v, int w, int d)
+{
+    char buf[64];
+    snprintf(buf, sizeof buf, "%*.*f", w, d, v);
+    return buf;
+}
+
+bool read_tokens(const std::string &path, std::vector<std::string> &tok)
+{
+    std::ifstream f(path);
+    if (!f) return false;
+    std::string t;
+    while (f >> t) {
+        // list-directed input: quotes delimit strings, commas separate values
+        std::string u;
+        for (char ch : t)
+            if (ch != '\'' && ch != '"') u.push_back(ch == ',' ? ' ' : ch);
+        std::istringstream ss(u);
+        std::string w;
+        while (ss >> w) tok.push_back(w);
+    }
+    return true;
+}
+
+double to_d(const std::string &s)
+{
+    std::string t = s;
+    for (char &ch : t)
+        if (ch == 'd' || ch == 'D') ch = 'E';
+    return strtod(t.c_str(), nullptr);
+}
+
+// ---------------------------------------------------------------------------
+// Structured 20-node cube in GEOMETRY_20BXZ numbering.  Each y-layer holds a
+// "face" plane of F1 nodes (z-levels of 2*nxe+1 nodes alternating with
+// rows of nxe+1 z-midside nodes, top level first) followed by a "mid" plane
+// of F2 = (nxe+1)(nze+1) y-midside nodes.
+struct CubeNumbering {
+    long long nxe, nze, F1, F2, L, pitch;
+    CubeNumbering(int nx, int nz)
+        : nxe(nx), nze(nz), F1((2LL * nx + 1) * (nz + 1) + (nx + 1LL) * nz), F2((nx + 1LL) * (nz + 1)),
+          L(F1 + F2), pitch(3LL * nx + 2)
+    {
+    }
+    long long face(long long j, long long lev, long long xh) const { return 1 + j * L + lev * pitch + xh; }
+    long long half(long long j, long long lev, long long xc) const
+    {
+        return 1 + j * L + lev * pitch + (2 * nxe + 1) + xc;
+    }
+    long long mid(long long j, long long lev, long long xc) const { return 1 + j * L + F1 + lev * (nxe + 1) + xc; }
+};
+
+// Nodes and coordinates of element iel (1-based), Smith-Griffiths order.
+void cube_element(int iel, int nxe, int nze, double aa, double bb, double cc, int num[20], double co[60])
+{
+    const CubeNumbering N(nxe, nze);
+    const long long e = iel - 1;
+    const long long j = e / ((long long)nxe * nze);           // y layer
+    const long long rem = e % ((long long)nxe * nze);
+    const long long k = rem / nxe, i = rem % nxe;             // z layer (0 = top), x column
+    const long long nodes[20] = {
+        N.face(j, k + 1, 2 * i), N.half(j, k, i), N.face(j, k, 2 * i), N.face(j, k, 2 * i + 1),
+        N.face(j, k, 2 * i + 2), N.half(j, k, i + 1), N.face(j, k + 1, 2 * i + 2), N.face(j, k + 1, 2 * i + 1),
+        N.mid(j, k + 1, i), N.mid(j, k, i), N.mid(j, k, i + 1), N.mid(j, k + 1, i + 1),
+        N.face(j + 1, k + 1, 2 * i), N.half(j + 1, k, i), N.face(j + 1, k, 2 * i), N.face(j + 1, k, 2 * i + 1),
+        N.face(j + 1, k, 2 * i + 2), N.half(j + 1, k, i + 1), N.face(j + 1, k + 1, 2 * i + 2),
+        N.face(j + 1, k + 1, 2 * i + 1)};
+    for (int a = 0; a < 20; ++a) num[a] = (int)nodes[a];
+    // x: 0 = left, 1 = mid, 2 = right; y: 0 front, 1 mid, 2 back; z: 0 bottom, 1 mid, 2 top
+    static const int xs[20] = {0, 0, 0, 1, 2, 2, 2, 1, 0, 0, 2, 2, 0, 0, 0, 1, 2, 2, 2, 1};
+    static const int ys[20] = {0, 0, 0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2, 2, 2, 2, 2, 2, 2};
+    static const int zs[20] = {0, 1, 2, 2, 2, 1, 0, 0, 0, 2, 2, 0, 0, 1, 2, 2, 2, 1, 0, 0};
+    const double x0 = (double)i * aa, x1 = (double)(i + 1) * aa;
+    const double y0 = (double)j * bb, y1 = (double)(j + 1) * bb;
+    const double zt = -(double)k * cc, zb = -(double)(k + 1) * cc;
+    const double xv[3] = {x0, .5 * (x0 + x1), x1};
+    const double yv[3] = {y0, .5 * (y0 + y1), y1};
+    const double zv[3] = {zb, .5 * (zb + zt), zt};
+    for (int a = 0; a < 20; ++a) {
+        co[a] = xv[xs[a]];
+        co[20 + a] = yv[ys[a]];
+        co[40 + a] = zv[zs[a]];
+    }
+}
+
+long long cube_nn(long long nxe, long long nye, long long nze)
+{
+    return ((2 * nxe + 1) * (nze + 1) + (nxe + 1) * nze) * (nye + 1) + (nxe + 1) * (nze + 1) * nye;
+}
+
+// Restraints per node (1 free, 0 fixed), bc 0 = cube_bc20, bc 1 = fixed base.
+void cube_fix(int nxe, int nye, int nze, int bc, std::vector<int> &fix)
+{
+    const CubeNumbering N(nxe, nze);
+    const long long nn = cube_nn(nxe, nye, nze);
+    fix.assign((size_t)nn * 3, 1);
+    auto set = [&](long long node, int fx, int fy, int fz) {
+        int *f = &fix[(size_t)(node - 1) * 3];
+        f[0] &= fx;
+        f[1] &= fy;
+        f[2] &= fz;
+    };
+    for (long long j = 0; j <= nye; ++j) {
+        const bool yface = (j == 0 || j == nye);
+        for (long long lev = 0; lev <= nze; ++lev) {
+            const bool base = lev == nze;
+            for (long long xh = 0; xh <= 2 * nxe; ++xh) {
+                const long long nd = N.face(j, lev, xh);
+                const bool xface = (xh == 0 || xh == 2 * nxe);
+                if (base) set(nd, 0, 0, 0);
+                else if (bc == 0) set(nd, xface ? 0 : 1, yface ? 0 : 1, 1);
+            }
+            if (lev < nze)
+                for (long long xc = 0; xc <= nxe; ++xc) {
+                    const long long nd = N.half(j, lev, xc);
+                    const bool xface = (xc == 0 || xc == nxe);
+                    if (bc == 0) set(nd, xface ? 0 : 1, yface ? 0 : 1, 1);
+                }
+        }
+        if (j < nye)
+            for (long long lev = 0; lev <= nze; ++lev)
+                for (long long xc = 0; xc <= nxe; ++xc) {
+                    const long long nd = N.mid(j, lev, xc);
+                    const bool xface = (xc == 0 || xc == nxe);
+                    if (lev == nze) set(nd, 0, 0, 0);
+                    else if (bc == 0) set(nd, xface ? 0 : 1, 1, 1);
+                }
+    }
+}
+
+// Sequential equation numbering over nodes and dofs, skipping fixed dofs:
+// the numbering REARRANGE + find_g3 produce for a restraint list sorted by
+// node (new_library.f90:3059-3212).
+int number_nodes(int nn, const int *fix, std::vector<int> &node_eq)
+{
+    node_eq.assign((size_t)nn * 3, 0);
+    long long q = 0;
+    for (size_t s = 0; s < (size_t)nn * 3; ++s)
+        if (fix[s]) node_eq[s] = (int)++q;
+    return (int)q;
+}
+
+// load_p121 patch pattern for 20-node meshes (loading.f90:386-480): node and
+// multiplier in the order the reference lists them.
+void load_p121_pattern(int nle, int nxe, int nze, std::vector<int> &node, std::vector<double> &mult)
+{
+    const CubeNumbering N(nxe, nze);
+    node.clear();
+    mult.clear();
+    auto row = [&](long long j, bool outer) {
+        for (int xh = 0; xh <= 2 * nle; ++xh) {
+            node.push_back((int)N.face(j, 0, xh));
+            const bool end = (xh == 0 || xh == 2 * nle);
+            mult.push_back(outer ? (end ? -1.0 : (xh % 2 ? 4.0 : -2.0)) : (end ? -2.0 : (xh % 2 ? 8.0 : -4.0)));
+        }
+    };
+    row(0, true);
+    for (int j = 0; j < nle; ++j) {
+        for (int xc = 0; xc <= nle; ++xc) {
+            node.push_back((int)N.mid(j, 0, xc));
+            mult.push_back((xc == 0 || xc == nle) ? 4.0 : 8.0);
+        }
+        row(j + 1, j == nle - 1);
+    }
+}
+
+struct Deck {
+    std::string element;
+    int meshgen = 0, partitioner = 0, nels = 0, nn = 0, nr = 0, nip = 0, nod = 0, loaded = 0, limit = 0;
+    double e = 0, v = 0, tol = 0;
+    std::vector<double> coords;   // (3, nn)
+    std::vector<int> g_num;       // (20, nels)
+    std::vector<int> rest;        // (4, nr) row-major per node
+    std::vector<int> lnode;
+    std::vector<double> lval;     // (3, loaded)
+};
+
+int read_deck(const std::string &job, Deck &D)
+{
+    std::vector<std::string> t;
+    if (!read_tokens(job + ".dat", t) || t.size() < 13) {
+        set_error("cannot read %s.dat", job.c_str());
+        return 1;
+    }
+    D.element = t[0];
+    D.meshgen = atoi(t[1].c_str());
+    D.partitioner = atoi(t[2].c_str());
+    D.nels = atoi(t[3].c_str());
+    D.nn = atoi(t[4].c_str());
+    D.nr = atoi(t[5].c_str());
+    D.nip = atoi(t[6].c_str());
+    D.nod = atoi(t[7].c_str());
+    D.loaded = atoi(t[8].c_str());
+    D.e = to_d(t[9]);
+    D.v = to_d(t[10]);
+    D.tol = to_d(t[11]);
+    D.limit = atoi(t[12].c_str());
+    if (D.element != "hexahedron" || D.nod != 20) {
+        set_error("%s.dat: only 20-node hexahedra are supported (got %s, nod=%d)", job.c_str(),
+                  D.element.c_str(), D.nod);
+        return 1;
+    }
+    std::ifstream f(job + ".d");
+    if (!f) {
+        set_error("cannot read %s.d", job.c_str());
+        return 1;
+    }
+    std::string line;
+    std::getline(f, line);
+    std::getline(f, line);
+    D.coords.assign((size_t)3 * D.nn, 0.0);
+    for (int i = 0; i < D.nn; ++i) {
+        if (!std::getline(f, line)) { set_error("%s.d: short node list", job.c_str()); return 1; }
+        std::istringstream ss(line);
+        std::string id, a, b, c;
+        ss >> id >> a >> b >> c;
+        D.coords[3 * (size_t)i] = to_d(a);
+        D.coords[3 * (size_t)i + 1] = to_d(b);
+        D.coords[3 * (size_t)i + 2] = to_d(c);
+    }
+    std::getline(f, line);   // *ELEMENTS
+    D.g_num.assign((size_t)20 * D.nels, 0);
+    for (int e = 0; e < D.nels; ++e) {
+        if (!std::getline(f, line)) { set_error("%s.d: short element list", job.c_str()); return 1; }
+        std::istringstream ss(line);
+        long long k;
+        ss >> k >> k >> k >> k;
+        for (int a = 0; a < 20; ++a) ss >> D.g_num[20 * (size_t)e + a];
+        if (!ss) { set_error("%s.d: bad element line %d", job.c_str(), e + 1); return 1; }
+    }
+    if (D.meshgen == 2) {   // ABAQUS2SG (new_library.f90:3569-3597)
+        static const int from[20] = {4, 12, 1, 9, 2, 10, 3, 11, 20, 17, 18, 19, 8, 16, 5, 13, 6, 14, 7, 15};
+        int tmp[20];
+        for (int e = 0; e < D.nels; ++e) {
+            int *g = &D.g_num[20 * (size_t)e];
+            std::copy(g, g + 20, tmp);
+            for (int a = 0; a < 20; ++a) g[a] = tmp[from[a] - 1];
+        }
+    }
+    std::vector<std::string> tb;
+    if (!read_tokens(job + ".bnd", tb) || tb.size() < (size_t)4 * D.nr) {
+        set_error("cannot read %d restraints from %s.bnd", D.nr, job.c_str());
+        return 1;
+    }
+    D.rest.resize((size_t)4 * D.nr);
+    for (size_t i = 0; i < (size_t)4 * D.nr; ++i) D.rest[i] = atoi(tb[i].c_str());
+    if (D.loaded > 0) {
+        std::vector<std::string> tl;
+        if (!read_tokens(job + ".lds", tl) || tl.size() < (size_t)4 * D.loaded) {
+            set_error("cannot read %d loads from %s.lds", D.loaded, job.c_str());
+            return 1;
+        }
+        D.lnode.resize(D.loaded);
+        D.lval.resize((size_t)3 * D.loaded);
+        for (int i = 0; i < D.loaded; ++i) {
+            D.lnode[i] = atoi(tl[4 * (size_t)i].c_str());
+            for (int d = 0; d < 3; ++d) D.lval[3 * (size_t)i + d] = to_d(tl[4 * (size_t)i + 1 + d]);
+        }
+    }
+    return 0;
+}
+
+// rest -> per-node fixity (rest rows: node, then 0 = fixed / nonzero = free)
+int rest_to_fix(int nn, int nr, const int *rest, std::vector<int> &fix)
+{
+    fix.assign((size_t)nn * 3, 1);
+    int last = 0;
+    for (int i = 0; i < nr; ++i) {
+        const int nd = rest[4 * (size_t)i];
+        if (nd < 1 || nd > nn) {
+            set_error("restraint row %d names node %d outside 1..%d", i + 1, nd, nn);
+            return 1;
+        }
+        if (nd <= last) {
+            set_error("restraint rows must be sorted by node (row %d: node %d after %d)", i + 1, nd, last);
+            return 1;
+        }
+        last = nd;
+        for (int d = 0; d < 3; ++d) fix[(size_t)(nd - 1) * 3 + d] = rest[4 * (size_t)i + 1 + d] != 0 ? 1 : 0;
+    }
+    return 0;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" int pf_mesh_cube(const int *nxe, const int *nye, const int *nze, const double *aa, const double *bb,
+                            const double *cc, int *nels, int *nn, int *g_num, double *g_coord)
+{
+    if (!nxe || !nye || !nze || !aa || !bb || !cc || !nels || !nn || *nxe < 1 || *nye < 1 || *nze < 1) {
+        set_error("pf_mesh_cube: invalid arguments");
+        return PF_FAILURE;
+    }
+    const long long ne = (long long)*nxe * *nye * *nze;
+    const long long nnl = cube_nn(*nxe, *nye, *nze);
+    if (ne * 60 > 0x7fffffffLL * 4 || nnl * 3 > 0x7fffffffLL) {
+        set_error("pf_mesh_cube: mesh too large");
+        return PF_FAILURE;
+    }
+    *nels = (int)ne;
+    *nn = (int)nnl;
+    if (!g_num) return PF_SUCCESS;
+    for (long long e = 0; e < ne; ++e) {
+        double co[60];
+        cube_element((int)(e + 1), *nxe, *nze, *aa, *bb, *cc, g_num + 20 * e, co);
+        if (g_coord) std::copy(co, co + 60, g_coord + 60 * e);
+    }
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_cube_restraints(const int *nxe, const int *nye, const int *nze, const int *bc, int *node_fix)
+{
+    if (!nxe || !nye || !nze || !bc || !node_fix || (*bc != 0 && *bc != 1)) {
+        set_error("pf_cube_restraints: invalid arguments");
+        return PF_FAILURE;
+    }
+    std::vector<int> fix;
+    cube_fix(*nxe, *nye, *nze, *bc, fix);
+    std::copy(fix.begin(), fix.end(), node_fix);
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_number_equations(const int *nels, const int *nn, const int *g_num, const int *node_fix, int *g_g,
+                                   int *neq)
+{
+    if (!nels || !nn || !g_num || !node_fix || !g_g || !neq) {
+        set_error("pf_number_equations: null argument");
+        return PF_FAILURE;
+    }
+    std::vector<int> node_eq;
+    *neq = number_nodes(*nn, node_fix, node_eq);
+    for (size_t e = 0; e < (size_t)*nels; ++e)
+        for (int a = 0; a < 20; ++a) {
+            const int nd = g_num[20 * e + a];
+            if (nd < 1 || nd > *nn) {
+                set_error("pf_number_equations: node %d outside 1..%d", nd, *nn);
+                return PF_FAILURE;
+            }
+            for (int d = 0; d < 3; ++d) g_g[60 * e + 3 * a + d] = node_eq[(size_t)(nd - 1) * 3 + d];
+        }
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_cube_top_pressure(const int *nxe, const int *nze, const int *nels, const double *aa,
+                                    const double *bb, const double *p, const int *g_g, const int *neq, double *r)
+{
+    if (!nxe || !nze || !nels || !aa || !bb || !p || !g_g || !neq || !r) {
+        set_error("pf_cube_top_pressure: null argument");
+        return PF_FAILURE;
+    }
+    const double A = *aa * *bb;
+    const double corner = *p * A / 12.0, midside = -*p * A / 3.0;
+    // top-face nodes of an element: corners 3,5,15,17 and mid-sides 4,10,11,16
+    static const int cn[4] = {3, 5, 15, 17}, ms[4] = {4, 10, 11, 16};
+    const long long per_layer = (long long)*nxe * *nze;
+    for (long long e = 0; e < *nels; ++e) {
+        const long long k = (e % per_layer) / *nxe;
+        if (k != 0) continue;
+        for (int t = 0; t < 4; ++t) {
+            const int qc = g_g[60 * e + 3 * (cn[t] - 1) + 2];
+            if (qc > 0 && qc <= *neq) r[qc - 1] += corner;
+            const int qm = g_g[60 * e + 3 * (ms[t] - 1) + 2];
+            if (qm > 0 && qm <= *neq) r[qm - 1] += midside;
+        }
+    }
+    return PF_SUCCESS;
+}
+
+namespace {
+inline uint32_t mulhilo(uint32_t a, uint32_t b, uint32_t *hi)
+{
+    const uint64_t pr = (uint64_t)a * b;
+    *hi = (uint32_t)(pr >> 32);
+    return (uint32_t)pr;
+}
+// Philox4x32-10 (Salmon et al., SC'11)
+void philox4x32(uint32_t ctr[4], uint32_t k0, uint32_t k1)
+{
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0, hi1;
+        const uint32_t lo0 = mulhilo(0xD2511F53u, ctr[0], &hi0);
+        const uint32_t lo1 = mulhilo(0xCD9E8D57u, ctr[2], &hi1);
+        const uint32_t c0 = hi1 ^ ctr[1] ^ k0, c2 = hi0 ^ ctr[3] ^ k1;
+        ctr[0] = c0;
+        ctr[1] = lo1;
+        ctr[2] = c2;
+        ctr[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+}  // namespace
+
+extern "C" int pf_random_material(const int *nels, const long long *seed, const double *e_lo, const double *e_hi,
+                                  const double *v_lo, const double *v_hi, double *e, double *v)
+{
+    if (!nels || !seed || !e_lo || !e_hi || !v_lo || !v_hi || !e || !v || !(*e_lo > 0) || !(*e_hi >= *e_lo)) {
+        set_error("pf_random_material: invalid arguments");
+        return PF_FAILURE;
+    }
+    const uint32_t k0 = (uint32_t)((unsigned long long)*seed & 0xffffffffu);
+    const uint32_t k1 = (uint32_t)((unsigned long long)*seed >> 32);
+    const double l0 = std::log(*e_lo), l1 = std::log(*e_hi);
+    for (long long i = 0; i < *nels; ++i) {
+        uint32_t c[4] = {(uint32_t)i, (uint32_t)((unsigned long long)i >> 32), 0u, 0u};
+        philox4x32(c, k0, k1);
+        // 53-bit uniforms in [0,1)
+        const double u1 = (double)((((uint64_t)c[0]) << 21) ^ (c[1] >> 11)) / 9007199254740992.0;
+        const double u2 = (double)((((uint64_t)c[2]) << 21) ^ (c[3] >> 11)) / 9007199254740992.0;
+        e[i] = std::exp(l0 + u1 * (l1 - l0));
+        v[i] = *v_lo + u2 * (*v_hi - *v_lo);
+    }
+    return PF_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" int pf_p12meshgen(const char *job_c)
+{
+    if (!job_c) { set_error("pf_p12meshgen: null job name"); return PF_FAILURE; }
+    const std::string job(job_c);
+    std::vector<std::string> t;
+    if (!read_tokens(job + ".mg", t) || t.size() < 14) {
+        set_error("cannot read %s.mg", job.c_str());
+        return PF_FAILURE;
+    }
+    if (t[0] != "p121") {
+        set_error("%s.mg: only the p121 case is supported (got %s)", job.c_str(), t[0].c_str());
+        return PF_FAILURE;
+    }
+    const std::string iotype = t[1];
+    const int nels = atoi(t[2].c_str()), nxe = atoi(t[3].c_str()), nze = atoi(t[4].c_str());
+    const int nod = atoi(t[5].c_str()), nip = atoi(t[6].c_str());
+    const double aa = to_d(t[7]), bb = to_d(t[8]), cc = to_d(t[9]), e = to_d(t[10]), v = to_d(t[11]);
+    const double tol = to_d(t[12]);
+    const int limit = atoi(t[13].c_str());
+    if (nod != 20 || iotype != "parafem" || nxe < 1 || nze < 1 || nels % (nxe * nze) != 0) {
+        set_error("%s.mg: supported: 'parafem' decks of 20-node cubes (nels divisible by nxe*nze)", job.c_str());
+        return PF_FAILURE;
+    }
+    const int nye = nels / nxe / nze;
+    const long long nn = cube_nn(nxe, nye, nze);
+    const int nle = nxe / 5;
+    // node coordinates (every node is written by some element)
+    std::vector<double> gc((size_t)3 * nn, 0.0);
+    std::vector<int> gnum((size_t)20 * nels);
+    for (int iel = 1; iel <= nels; ++iel) {
+        double co[60];
+        int *num = &gnum[20 * (size_t)(iel - 1)];
+        cube_element(iel, nxe, nze, aa, bb, cc, num, co);
+        for (int a = 0; a < 20; ++a)
+            for (int d = 0; d < 3; ++d) gc[3 * (size_t)(num[a] - 1) + d] = co[a + 20 * d];
+    }
+    std::vector<int> fix;
+    cube_fix(nxe, nye, nze, 0, fix);
+    std::vector<int> lnode;
+    std::vector<double> mult;
+    load_p121_pattern(nle, nxe, nze, lnode, mult);
+
+    FILE *fd = fopen((job + ".d").c_str(), "w");
+    if (!fd) { set_error("cannot write %s.d", job.c_str()); return PF_FAILURE; }
+    fprintf(fd, "*THREE_DIMENSIONAL\n*NODES\n");
+    for (long long i = 0; i < nn; ++i)
+        fprintf(fd, "%s%s%s%s\n", fmt_I(i + 1, 12).c_str(), fmt_E(gc[3 * i], 14, 6).c_str(),
+                fmt_E(gc[3 * i + 1], 14, 6).c_str(), fmt_E(gc[3 * i + 2], 14, 6).c_str());
+    fprintf(fd, "*ELEMENTS\n");
+    static const int abq[20] = {3, 5, 7, 1, 15, 17, 19, 13, 4, 6, 8, 2, 16, 18, 20, 14, 10, 11, 12, 9};
+    for (int iel = 0; iel < nels; ++iel) {
+        std::string s = fmt_I(iel + 1, 12) + " 3 20 1 ";
+        for (int a = 0; a < 20; ++a) s += fmt_I(gnum[20 * (size_t)iel + abq[a] - 1], 12);
+        fprintf(fd, "%s 1\n", s.c_str());
+    }
+    fclose(fd);
+
+    FILE *fb = fopen((job + ".bnd").c_str(), "w");
+    if (!fb) { set_error("cannot write %s.bnd", job.c_str()); return PF_FAILURE; }
+    long long nr = 0;
+    for (long long i = 0; i < nn; ++i) {
+        const int *f = &fix[3 * (size_t)i];
+        if (f[0] && f[1] && f[2]) continue;
+        fprintf(fb, "%s%s%s%s\n", fmt_I(i + 1, 15).c_str(), fmt_I(f[0], 6).c_str(), fmt_I(f[1], 6).c_str(),
+                fmt_I(f[2], 6).c_str());
+        ++nr;
+    }
+    fclose(fb);
+
+    FILE *fl = fopen((job + ".lds").c_str(), "w");
+    if (!fl) { set_error("cannot write %s.lds", job.c_str()); return PF_FAILURE; }
+    for (size_t i = 0; i < lnode.size(); ++i) {
+        const double val = -mult[i] * aa * bb * (25.0 / 12.0);
+        fprintf(fl, "%s  0.00000000E+00  0.00000000E+00%s\n", fmt_I(lnode[i], 12).c_str(),
+                fmt_E(val, 16, 8).c_str());
+    }
+    fclose(fl);
+
+    FILE *ft = fopen((job + ".dat").c_str(), "w");
+    if (!ft) { set_error("cannot write %s.dat", job.c_str()); return PF_FAILURE; }
+    fprintf(ft, "'hexahedron'\n2\n1\n%s%s%s%s%s%s\n", fmt_I(nels, 12).c_str(), fmt_I(nn, 12).c_str(),
+            fmt_I(nr, 12).c_str(), fmt_I(nip, 5).c_str(), fmt_I(nod, 5).c_str(),
+            fmt_I((long long)lnode.size(), 9).c_str());
+    fprintf(ft, "%s%s%s%s\n", fmt_E(e, 12, 4).c_str(), fmt_E(v, 12, 4).c_str(), fmt_E(tol, 12, 4).c_str(),
+            fmt_I(limit, 8).c_str());
+    fclose(ft);
+    return PF_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// The p121 job (p121.f90:1-141) with the solve on the GPU.
+extern "C" int pf_p121_run(const char *job_c, const int *device, const int *mode, int *iters_out,
+                           double *central_out)
+{
+    if (!job_c || !device || !mode) { set_error("pf_p121_run: null argument"); return PF_FAILURE; }
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto secs = [&](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    const std::string job(job_c);
+    Deck D;
+    if (read_deck(job, D)) return PF_FAILURE;
+    std::vector<int> fix;
+    if (rest_to_fix(D.nn, D.nr, D.rest.data(), fix)) return PF_FAILURE;
+    const double t_read = secs(t0);
+    std::vector<int> g_g((size_t)60 * D.nels);
+    int neq = 0;
+    if (pf_number_equations(&D.nels, &D.nn, D.g_num.data(), fix.data(), g_g.data(), &neq)) return PF_FAILURE;
+    std::vector<double> gcoord((size_t)60 * D.nels);
+    for (size_t e = 0; e < (size_t)D.nels; ++e)
+        for (int a = 0; a < 20; ++a)
+            for (int d = 0; d < 3; ++d)
+                gcoord[60 * e + a + 20 * d] = D.coords[3 * (size_t)(D.g_num[20 * e + a] - 1) + d];
+    void *ctx = nullptr;
+    int rc = PF_FAILURE;
+    std::vector<double> r(neq > 0 ? neq : 1, 0.0), x(neq > 0 ? neq : 1, 0.0);
+    double q = 0.0, sigma[6] = {0}, relres = 0.0;
+    int iters = 0, one = 1, flags = 0;
+    double t_setup = 0, t_solve = 0;
+    do {
+        if (pf_ctx_create(device, &ctx)) break;
+        if (pf_setup(&ctx, &D.nels, &D.nn, &neq, D.g_num.data(), g_g.data(), gcoord.data())) break;
+        if (pf_set_material(&ctx, &one, &D.e, &D.v)) break;
+        if (pf_form_storkm(&ctx, &D.nip, &flags)) break;
+        t_setup = secs(t0);
+        // LOAD + SCATTER_NOADD (loading.f90:36-146): r(eq) = value, last node entry wins
+        std::vector<int> node_slot((size_t)D.nn + 1, -1);
+        for (int i = 0; i < D.loaded; ++i)
+            if (D.lnode[i] >= 1 && D.lnode[i] <= D.nn) node_slot[D.lnode[i]] = i;
+        // equation of (node, dof) from the numbering
+        std::vector<int> node_eq;
+        number_nodes(D.nn, fix.data(), node_eq);
+        for (int nd = 1; nd <= D.nn; ++nd) {
+            const int i = node_slot[nd];
+            if (i < 0) continue;
+            for (int d = 0; d < 3; ++d) {
+                const int eq = node_eq[(size_t)(nd - 1) * 3 + d];
+                if (eq > 0) r[eq - 1] = D.lval[3 * (size_t)i + d];
+            }
+        }
+        for (int i = 0; i < neq; ++i) q += r[i];
+        const auto ts = clk::now();
+        if (pf_solve(&ctx, r.data(), &D.tol, &D.limit, mode, x.data(), &iters, &relres)) break;
+        t_solve = secs(ts);
+        int iel = 1;
+        if (pf_centroid_stress(&ctx, &iel, x.data(), sigma)) break;
+        rc = PF_SUCCESS;
+    } while (0);
+    if (ctx) pf_ctx_destroy(&ctx);
+    if (rc) return PF_FAILURE;
+
+    FILE *fr = fopen((job + ".res").c_str(), "w");
+    if (!fr) { set_error("cannot write %s.res", job.c_str()); return PF_FAILURE; }
+    fprintf(fr, "This job ran on %s processes\n", fmt_I(1, 7).c_str());
+    fprintf(fr, "There are %s nodes%s restrained and %s equations\n", fmt_I(D.nn, 12).c_str(),
+            fmt_I(D.nr, 12).c_str(), fmt_I(neq, 12).c_str());
+    fprintf(fr, "Time to read input is:%s\n", fmt_F(t_read, 10, 4).c_str());
+    fprintf(fr, "Time after setup is:%s\n", fmt_F(t_setup, 10, 4).c_str());
+    if (D.loaded > 0) fprintf(fr, "The total load is:%s\n", fmt_E(q, 12, 4).c_str());
+    fprintf(fr, "The number of iterations to convergence was %s\n", fmt_I(iters, 6).c_str());
+    fprintf(fr, "Time to solve equations was  :%s\n", fmt_F(t_solve, 10, 4).c_str());
+    fprintf(fr, "The central nodal displacement is :%s\n", fmt_E(neq > 0 ? x[0] : 0.0, 12, 4).c_str());
+    fprintf(fr, "The Centroid point stresses for element 1 are\n");
+    fprintf(fr, "Point %s\n", fmt_I(1, 5).c_str());
+    std::string sl;
+    for (int k = 0; k < 6; ++k) sl += fmt_E(sigma[k], 12, 4);
+    fprintf(fr, "%s\n", sl.c_str());
+
+    // Ensight Gold per-node vector file (p121.f90:124-138, output.f90:2983-3117)
+    FILE *fe = fopen((job + ".ensi.DISPL-000001").c_str(), "w");
+    if (!fe) { fclose(fr); set_error("cannot write the displacement file"); return PF_FAILURE; }
+    fprintf(fe, "Alya Ensight Gold --- Vector per-node variable file\npart\n     1\ncoordinates\n");
+    std::vector<int> node_eq;
+    number_nodes(D.nn, fix.data(), node_eq);
+    for (int d = 0; d < 3; ++d)
+        for (int nd = 0; nd < D.nn; ++nd) {
+            const int eq = node_eq[(size_t)nd * 3 + d];
+            fprintf(fe, "%s\n", fmt_E(eq > 0 ? x[eq - 1] : 0.0, 12, 5).c_str());
+        }
+    fclose(fe);
+    fprintf(fr, "This analysis took  :%s\n", fmt_F(secs(t0), 10, 4).c_str());
+    fclose(fr);
+    if (iters_out) *iters_out = iters;
+    if (central_out) *central_out = neq > 0 ? x[0] : 0.0;
+    return PF_SUCCESS;
+}

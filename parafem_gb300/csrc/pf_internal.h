@@ -1,0 +1,98 @@
+// pf_internal.h -- device state of one solver context and the kernel entry
+// points shared by the translation units of libpfgpu.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+namespace pf {
+
+// Records a formatted error message for pf_last_error (thread local).
+void set_error(const char *fmt, ...);
+
+// Scalars of one PCG run, resident on the device (pinned host mirror).
+// Only the single-block finish kernel of an iteration writes them, so no
+// kernel writes a value that another block of the same kernel reads.
+struct PcgState {
+    double up;         // r.d entering the next iteration
+    double ff;         // f.f (relative-residual denominator)
+    double metric;     // last stopping metric
+    double rr;         // last r.r
+    double tol;        // stopping tolerance
+    int iters;         // iterations completed
+    int stop;          // 1 once converged or at the limit: later kernels return
+    int converged;
+    int limit;
+    int stop_mode;     // 0 checon_par, 1 relative residual
+    int err;           // device-detected error code (0 = none)
+};
+
+enum { STOP_CHECON = 0, STOP_RELRES = 1 };
+
+struct Ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    long long launches = 0;
+
+    int nels = 0, nn = 0, neq = 0, nslots = 0;   // nslots = 3*nn (node-major dofs)
+    int *conn = nullptr;        // [nels*20] 0-based node index
+    int *node_ptr = nullptr;    // [nn+1] CSR of node -> (element, local node)
+    int *node_list = nullptr;   // [nels*20] e*20+a, ascending e within a node
+    int *slot_eq = nullptr;     // [nslots] 1-based equation or 0 (restrained)
+    int *eq_slot = nullptr;     // [neq] slot of equation q+1
+    uint8_t *freemask = nullptr;// [nn] bit d set when dof d of the node is free
+    double *coord = nullptr;    // [nels*60] g_coord(20,3,e)
+
+    int nmat = 0;               // 1 or nels
+    double *mat_e = nullptr, *mat_v = nullptr;
+
+    double *km64 = nullptr;     // [nels*3600] storkm(60,60,e)
+    float *km32 = nullptr;      // [nels*3600]
+    bool have_km = false;
+
+    double *ediag = nullptr;    // [nels*60] element diagonals
+    double *diag = nullptr;     // [nslots]
+    double *dinv = nullptr;     // [nslots] 1/diag, 0 for restrained
+
+    // vectors over slots
+    double *f = nullptr, *x = nullptr, *c = nullptr, *r = nullptr, *d = nullptr,
+           *p = nullptr, *u = nullptr, *rres = nullptr;
+    double *eqbuf = nullptr;    // [neq] staging in equation order
+    void *utemp = nullptr;      // [nels*60] doubles (element results)
+
+    int G = 0;                  // blocks of the vector kernels = partial count
+    double *part = nullptr;     // [8*G] block partials
+    PcgState *st = nullptr;     // device
+    PcgState *hst = nullptr;    // pinned host mirror
+
+    // last solve statistics
+    double stats[8] = {0};
+};
+
+// Kernel launchers (pf_kernels.cu).  All run on ctx.stream and count launches.
+int launch_form_storkm(Ctx &c, int nip, bool exact_weights, bool keep32);
+int launch_cast_km32(Ctx &c);
+int launch_assemble_diag(Ctx &c);
+int launch_eq_to_slot(Ctx &c, const double *eq, double *slot);
+int launch_slot_to_eq(Ctx &c, const double *slot, double *eq);
+// Element products utemp(:,e) = K_e p_e (prec 64 or 32); p is a slot vector.
+int launch_elem(Ctx &c, int prec, const double *p);
+// Node-centric scatter of utemp: u = sum of contributions (restrained = 0)
+// with block partials of p.u (mode 0), or rres = f - sum with partials of
+// rres.rres (mode 1).
+int launch_scatter(Ctx &c, int prec, int mode, const double *p_or_f, double *out);
+int launch_matvec(Ctx &c, int prec, const double *p, double *u);
+int launch_residual(Ctx &c, const double *f, const double *x, double *rres);
+int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol,
+                    int limit);
+int launch_update1(Ctx &c, double *xsol);
+int launch_update2(Ctx &c);   // update2 + the one-block finish kernel
+int launch_pcg_iteration(Ctx &c, int prec, double *xsol);
+int launch_axpy(Ctx &c, double *y, const double *xv);          // y += x
+int launch_sum_partials(Ctx &c, int nvals, double *out_dev);   // out[k] = sum part[k*G..]
+int launch_centroid_stress(Ctx &c, int iel, const double *xslot, double *sig_dev);
+int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs,
+                          const double *mat, double *rhs, long long *launches);
+
+}  // namespace pf

@@ -1,0 +1,846 @@
+// pf_kernels.cu -- sm_103a kernels of the element-by-element PCG path.
+//
+// Layout on the device (one context):
+//   vectors are node-major "slots": slot 3*n+d is dof d of node n (0-based);
+//   restrained slots hold 0, which plays the role of p121's equation 0
+//   (GATHER sets pl(0)=0, SCATTER drops contributions to it,
+//   src/modules/mpi/gather_scatter.f90:547-854).
+//   storkm(60,60,e) keeps p121's column-major element blocks.
+// Reductions are deterministic: fixed per-thread assignment, xor-shuffle
+// trees, per-block partials summed in a fixed order by the consumer kernel.
+#include "pf_internal.h"
+
+#include <cmath>
+#include <cstdio>
+
+namespace pf {
+
+#define FULLMASK 0xffffffffu
+
+static int check_launch(Ctx &c, const char *name)
+{
+    c.launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("%s: launch failed: %s", name, cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULLMASK, v, o));
+    return v;
+}
+
+// Reduces NV values over the block (kinds bit k set = max, else sum).  The
+// result is valid in every thread on return.  blockDim.x <= 1024.
+template <int NV>
+__device__ __forceinline__ void block_reduce(double (&v)[NV], unsigned kinds)
+{
+    __shared__ double sh[NV][32];
+    __shared__ double res[NV];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = ((kinds >> k) & 1) ? warp_max(v[k]) : warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh[k][wid] = v[k];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double t = (lane < nw) ? sh[k][lane] : 0.0;
+            t = ((kinds >> k) & 1) ? warp_max(t) : warp_sum(t);
+            if (lane == 0) res[k] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = res[k];
+    __syncthreads();
+}
+
+// Block-uniform read of the stop flag: thread 0 reads it once for the whole
+// block, so a block never splits at a barrier when another block of the same
+// kernel sets the flag meanwhile.
+__device__ __forceinline__ bool block_stopped(const PcgState *st)
+{
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) s_stop = st ? st->stop : 0;
+    __syncthreads();
+    const bool v = s_stop != 0;
+    __syncthreads();
+    return v;
+}
+
+// Sums (or maxes) G block partials in a fixed order; same value in every block.
+__device__ __forceinline__ double reduce_partials(const double *part, int G, bool is_max)
+{
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < G; i += blockDim.x) acc = is_max ? fmax(acc, part[i]) : acc + part[i];
+    double v[1] = {acc};
+    block_reduce<1>(v, is_max ? 1u : 0u);
+    return v[0];
+}
+
+// ---------------------------------------------------------------------------
+// SAMPLE (src/modules/shared/new_library.f90:1397-1514), nip 8 or 27.
+// gp[4*i] = (xi, eta, zeta, w).
+__global__ void k_sample(int nip, int exact, double *gp)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double root3 = 1.0 / sqrt(3.0);
+    const double r15 = 0.2 * sqrt(15.0);
+    if (nip == 8) {
+        const int sg[8][3] = {{1, 1, 1}, {1, 1, -1}, {1, -1, 1}, {1, -1, -1},
+                              {-1, 1, 1}, {-1, -1, 1}, {-1, 1, -1}, {-1, -1, -1}};
+        for (int i = 0; i < 8; ++i) {
+            for (int d = 0; d < 3; ++d) gp[4 * i + d] = sg[i][d] * root3;
+            gp[4 * i + 3] = 1.0;
+        }
+    } else if (nip == 27) {
+        const double w3[3] = {5.0 / 9.0, 8.0 / 9.0, 5.0 / 9.0};
+        double v9[9];
+        for (int i = 0; i < 3; ++i) {
+            v9[i] = 5.0 / 9.0 * w3[i];
+            v9[3 + i] = 8.0 / 9.0 * w3[i];
+            v9[6 + i] = 5.0 / 9.0 * w3[i];
+        }
+        // p121 takes 5./9. and 8./9. as default-REAL literals (:1493)
+        const double f59 = exact ? 5.0 / 9.0 : (double)(5.0f / 9.0f);
+        const double f89 = exact ? 8.0 / 9.0 : (double)(8.0f / 9.0f);
+        for (int blk = 0; blk < 3; ++blk) {
+            const double eta = blk == 0 ? -r15 : (blk == 1 ? 0.0 : r15);
+            const double f = blk == 1 ? f89 : f59;
+            for (int i = 0; i < 9; ++i) {
+                const int col = i % 3, row = i / 3;
+                double *g = &gp[4 * (blk * 9 + i)];
+                g[0] = col == 0 ? -r15 : (col == 1 ? 0.0 : r15);
+                g[1] = eta;
+                g[2] = row == 0 ? r15 : (row == 1 ? 0.0 : -r15);
+                g[3] = f * v9[i];
+            }
+        }
+    }
+}
+
+// SHAPE_DER for one node l of the 20-node brick (new_library.f90:865-896).
+__constant__ int c_xii[20] = {-1, -1, -1, 0, 1, 1, 1, 0, -1, -1, 1, 1, -1, -1, -1, 0, 1, 1, 1, 0};
+__constant__ int c_etai[20] = {-1, -1, -1, -1, -1, -1, -1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 1, 1, 1, 1};
+__constant__ int c_zetai[20] = {-1, 0, 1, 1, 1, 0, -1, -1, -1, 1, 1, -1, -1, 0, 1, 1, 1, 0, -1, -1};
+
+__device__ __forceinline__ void shape_der20(int l, double xi, double eta, double zeta, double *d)
+{
+    const double xii = c_xii[l], etai = c_etai[l], zetai = c_zetai[l];
+    const double xi0 = xi * xii, eta0 = eta * etai, zeta0 = zeta * zetai;
+    const int n = l + 1;
+    if (n == 4 || n == 8 || n == 16 || n == 20) {
+        d[0] = -.5 * xi * (1. + eta0) * (1. + zeta0);
+        d[1] = (.25 * etai) * (1. - xi * xi) * (1. + zeta0);
+        d[2] = (.25 * zetai) * (1. - xi * xi) * (1. + eta0);
+    } else if (n >= 9 && n <= 12) {
+        d[0] = (.25 * xii) * (1. - eta * eta) * (1. + zeta0);
+        d[1] = -.5 * eta * (1. + xi0) * (1. + zeta0);
+        d[2] = (.25 * zetai) * (1. + xi0) * (1. - eta * eta);
+    } else if (n == 2 || n == 6 || n == 14 || n == 18) {
+        d[0] = (.25 * xii) * (1. + eta0) * (1. - zeta * zeta);
+        d[1] = (.25 * etai) * (1. + xi0) * (1. - zeta * zeta);
+        d[2] = -.5 * zeta * (1. + xi0) * (1. + eta0);
+    } else {
+        d[0] = (.125 * xii) * (1. + eta0) * (1. + zeta0) * (2. * xi0 + eta0 + zeta0 - 1.);
+        d[1] = (.125 * etai) * (1. + xi0) * (1. + zeta0) * (xi0 + 2. * eta0 + zeta0 - 1.);
+        d[2] = (.125 * zetai) * (1. + xi0) * (1. + eta0) * (xi0 + eta0 + 2. * zeta0 - 1.);
+    }
+}
+
+// DEEMAT nst=6 (new_library.f90:1671-1689): the three distinct entries.
+__device__ __forceinline__ void deemat3(double e, double v, double &d11, double &d12, double &d44)
+{
+    const double v2 = v / (1.0 - v);
+    const double vv = (1.0 - 2.0 * v) / (1.0 - v) * 0.5;
+    const double den = 2.0 * (1.0 + v) * vv;
+    d11 = 1.0 * e / den;
+    d12 = v2 * e / den;
+    d44 = vv * e / den;
+}
+
+// DETERMINANT + INVERT of a 3x3 held column-major (maths.f90:490-633).
+__device__ __forceinline__ double det_invert3(double *m)
+{
+#define M(a, b) m[((a) - 1) + 3 * ((b) - 1)]
+    double det = M(1, 1) * (M(2, 2) * M(3, 3) - M(3, 2) * M(2, 3));
+    det = det - M(1, 2) * (M(2, 1) * M(3, 3) - M(3, 1) * M(2, 3));
+    det = det + M(1, 3) * (M(2, 1) * M(3, 2) - M(3, 1) * M(2, 2));
+    const double j11 = M(2, 2) * M(3, 3) - M(3, 2) * M(2, 3);
+    const double j21 = -M(2, 1) * M(3, 3) + M(3, 1) * M(2, 3);
+    const double j31 = M(2, 1) * M(3, 2) - M(3, 1) * M(2, 2);
+    const double j12 = -M(1, 2) * M(3, 3) + M(3, 2) * M(1, 3);
+    const double j22 = M(1, 1) * M(3, 3) - M(3, 1) * M(1, 3);
+    const double j32 = -M(1, 1) * M(3, 2) + M(3, 1) * M(1, 2);
+    const double j13 = M(1, 2) * M(2, 3) - M(2, 2) * M(1, 3);
+    const double j23 = -M(1, 1) * M(2, 3) + M(2, 1) * M(1, 3);
+    const double j33 = M(1, 1) * M(2, 2) - M(2, 1) * M(1, 2);
+    M(1, 1) = j11 / det; M(1, 2) = j12 / det; M(1, 3) = j13 / det;
+    M(2, 1) = j21 / det; M(2, 2) = j22 / det; M(2, 3) = j23 / det;
+    M(3, 1) = j31 / det; M(3, 2) = j32 / det; M(3, 3) = j33 / det;
+#undef M
+    return det;
+}
+
+// ---------------------------------------------------------------------------
+// storkm integration (p121.f90:54-64).  One 128-thread CTA per element;
+// thread t owns node pairs (a,b) = t, t+128, t+256, t+384 of the 20x20 block
+// grid and accumulates their 3x3 blocks of B'DB*det*w over the Gauss points.
+// The 3x3 block of B'DB for nodes a,b with gradients ga, gb is
+//   (i,i): D11 ga_i gb_i + D44 sum_{k!=i} ga_k gb_k
+//   (i,j): D12 ga_i gb_j + D44 ga_j gb_i
+// which is the dense MATMUL(MATMUL(TRANSPOSE(bee),dee),bee) of p121.f90:61-62
+// with the zero entries of bee (BEEMAT, new_library.f90:976-993) skipped.
+__global__ void __launch_bounds__(128)
+k_form_storkm(int nels, int nip, const double *__restrict__ gp, const double *__restrict__ coord,
+              const double *__restrict__ me, const double *__restrict__ mv, int nmat,
+              double *__restrict__ km64, float *__restrict__ km32, double *__restrict__ ediag)
+{
+    __shared__ double s_coord[60];  // coord(20,3)
+    __shared__ double s_der[60];    // der(3,20)
+    __shared__ double s_jac[9];
+    __shared__ double s_deriv[60];  // deriv(3,20)
+    __shared__ double s_det;
+    __shared__ double s_D[3];
+    const int t = threadIdx.x;
+    for (int e = blockIdx.x; e < nels; e += gridDim.x) {
+        if (t < 60) s_coord[t] = coord[(size_t)e * 60 + t];
+        if (t == 0) {
+            const int m = nmat == 1 ? 0 : e;
+            deemat3(me[m], mv[m], s_D[0], s_D[1], s_D[2]);
+        }
+        double acc[4][9];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int k = 0; k < 9; ++k) acc[q][k] = 0.0;
+        __syncthreads();
+        for (int ig = 0; ig < nip; ++ig) {
+            const double xi = gp[4 * ig], eta = gp[4 * ig + 1], zeta = gp[4 * ig + 2];
+            const double w = gp[4 * ig + 3];
+            if (t < 20) shape_der20(t, xi, eta, zeta, &s_der[3 * t]);
+            __syncthreads();
+            if (t < 9) {   // jac = MATMUL(der, coord)
+                const int a = t % 3, b = t / 3;
+                double s = 0.0;
+                for (int k = 0; k < 20; ++k) s += s_der[a + 3 * k] * s_coord[k + 20 * b];
+                s_jac[a + 3 * b] = s;
+            }
+            __syncthreads();
+            if (t == 0) s_det = det_invert3(s_jac);
+            __syncthreads();
+            if (t < 60) {  // deriv = MATMUL(jac^-1, der)
+                const int a = t % 3, l = t / 3;
+                s_deriv[a + 3 * l] = s_jac[a] * s_der[3 * l] + s_jac[a + 3] * s_der[1 + 3 * l] +
+                                     s_jac[a + 6] * s_der[2 + 3 * l];
+            }
+            __syncthreads();
+            const double det = s_det, D11 = s_D[0], D12 = s_D[1], D44 = s_D[2];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int pr = t + 128 * q;
+                if (pr < 400) {
+                    const int a = pr % 20, b = pr / 20;
+                    const double ga[3] = {s_deriv[3 * a], s_deriv[3 * a + 1], s_deriv[3 * a + 2]};
+                    const double gb[3] = {s_deriv[3 * b], s_deriv[3 * b + 1], s_deriv[3 * b + 2]};
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+#pragma unroll
+                        for (int i = 0; i < 3; ++i) {
+                            double s;
+                            if (i == j) {
+                                const int k1 = (i + 1) % 3, k2 = (i + 2) % 3;
+                                s = D11 * ga[i] * gb[i] + D44 * (ga[k1] * gb[k1] + ga[k2] * gb[k2]);
+                            } else {
+                                s = D12 * ga[i] * gb[j] + D44 * ga[j] * gb[i];
+                            }
+                            acc[q][i + 3 * j] += s * det * w;
+                        }
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int pr = t + 128 * q;
+            if (pr < 400) {
+                const int a = pr % 20, b = pr / 20;
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        const double val = acc[q][i + 3 * j];
+                        const size_t idx = (size_t)e * 3600 + (size_t)(3 * b + j) * 60 + 3 * a + i;
+                        if (km64) km64[idx] = val;
+                        if (km32) km32[idx] = (float)val;
+                        if (a == b && i == j) ediag[(size_t)e * 60 + 3 * a + i] = val;
+                    }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_cast_km32(size_t n, const double *__restrict__ a, float *__restrict__ b)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+__global__ void k_extract_ediag(int nels, const double *__restrict__ km, double *__restrict__ ed)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < (size_t)nels * 60;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const size_t e = i / 60, k = i % 60;
+        ed[i] = km[e * 3600 + k * 61];
+    }
+}
+
+// Jacobi diagonal (p121.f90:65-69, 86): node-centric sum of element
+// diagonals in ascending element order -- the order of the serial SCATTER.
+__global__ void k_assemble_diag(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
+                                const double *__restrict__ ed, const uint8_t *__restrict__ fm,
+                                double *__restrict__ diag, double *__restrict__ dinv)
+{
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
+            const double *q = ed + (size_t)list[k] * 3;
+            a0 += q[0];
+            a1 += q[1];
+            a2 += q[2];
+        }
+        const int m = fm[n];
+        const double a[3] = {a0, a1, a2};
+        for (int d = 0; d < 3; ++d) {
+            const bool fr = (m >> d) & 1;
+            diag[3 * n + d] = fr ? a[d] : 0.0;
+            dinv[3 * n + d] = fr ? 1.0 / a[d] : 0.0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Element products (p121.f90:92-97): one warp per element.  Lanes 0..19
+// fetch the connectivity, every lane gathers p for dofs lane and lane+32,
+// lanes 0..29 then own rows 2*lane and 2*lane+1 and walk the 60 columns of
+// storkm(:,:,e) with 2-wide loads, p(j) broadcast by shuffle.
+template <typename KT> struct Vec2;
+template <> struct Vec2<double> { typedef double2 T; };
+template <> struct Vec2<float> { typedef float2 T; };
+
+template <typename KT, bool GATHER>
+__global__ void __launch_bounds__(256)
+k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
+       const double *__restrict__ p, KT *__restrict__ ut, const PcgState *__restrict__ st)
+{
+    if (st && st->stop) return;
+    typedef typename Vec2<KT>::T V2;
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int j1 = lane + 32;
+    for (int e = warp; e < nels; e += nwarps) {
+        KT p0, p1;
+        if (GATHER) {
+            const int nd = (lane < 20) ? conn[(size_t)e * 20 + lane] : 0;
+            const int n0 = __shfl_sync(FULLMASK, nd, lane / 3);
+            const int n1 = __shfl_sync(FULLMASK, nd, j1 < 60 ? j1 / 3 : 0);
+            p0 = (KT)p[(size_t)3 * n0 + lane % 3];
+            p1 = (j1 < 60) ? (KT)p[(size_t)3 * n1 + j1 % 3] : (KT)0;
+        } else {
+            p0 = (KT)p[(size_t)e * 60 + lane];
+            p1 = (j1 < 60) ? (KT)p[(size_t)e * 60 + j1] : (KT)0;
+        }
+        const KT *ke = km + (size_t)e * 3600 + 2 * lane;
+        KT a0 = 0, a1 = 0;
+#pragma unroll 12
+        for (int j = 0; j < 60; ++j) {
+            const KT pj = __shfl_sync(FULLMASK, j < 32 ? p0 : p1, j & 31);
+            if (lane < 30) {
+                const V2 k2 = __ldg(reinterpret_cast<const V2 *>(ke + 60 * j));
+                a0 = fma(k2.x, pj, a0);
+                a1 = fma(k2.y, pj, a1);
+            }
+        }
+        if (lane < 30) {
+            V2 o;
+            o.x = a0;
+            o.y = a1;
+            reinterpret_cast<V2 *>(ut + (size_t)e * 60)[lane] = o;
+        }
+    }
+}
+
+// Node-centric scatter (SCATTER, gather_scatter.f90:694-854, one rank):
+// each node sums its (element, local node) contributions in ascending
+// element order, so the sum order equals the serial p121 SCATTER and runs
+// are bitwise reproducible without atomics.
+//   MODE 0: out = u (restrained 0), partial p.u       (pf = p)
+//   MODE 1: out = f - u (restrained 0), partial out.out (pf = f)
+template <typename UT, int MODE>
+__global__ void __launch_bounds__(256)
+k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
+          const UT *__restrict__ ut, const uint8_t *__restrict__ fm, const double *__restrict__ pf,
+          double *__restrict__ out, double *__restrict__ part, const PcgState *__restrict__ st)
+{
+    if (block_stopped(st)) return;
+    double loc = 0.0;
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        const int k1 = ptr[n + 1];
+        for (int k = ptr[n]; k < k1; ++k) {
+            const UT *q = ut + (size_t)list[k] * 3;
+            a0 += (double)q[0];
+            a1 += (double)q[1];
+            a2 += (double)q[2];
+        }
+        const int m = fm[n];
+        const double a[3] = {a0, a1, a2};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const size_t s = (size_t)3 * n + d;
+            const bool fr = (m >> d) & 1;
+            if (MODE == 0) {
+                const double uv = fr ? a[d] : 0.0;
+                out[s] = uv;
+                loc = fma(pf[s], uv, loc);
+            } else {
+                const double rv = fr ? pf[s] - a[d] : 0.0;
+                out[s] = rv;
+                loc = fma(rv, rv, loc);
+            }
+        }
+    }
+    double v[1] = {loc};
+    block_reduce<1>(v, 0u);
+    if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+}
+
+// ---------------------------------------------------------------------------
+// PCG (p121.f90:86-104).
+// init: x = 0, r = rhs, d = dinv*r, p = d; partials r.d and r.r
+__global__ void __launch_bounds__(256)
+k_pcg_init(int ns, const double *__restrict__ rhs, const double *__restrict__ dinv,
+           double *__restrict__ x, double *__restrict__ r, double *__restrict__ d,
+           double *__restrict__ p, double *__restrict__ part, int G)
+{
+    double rd = 0.0, rr = 0.0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const double rv = rhs[s];
+        const double dv = dinv[s] * rv;
+        x[s] = 0.0;
+        r[s] = rv;
+        d[s] = dv;
+        p[s] = dv;
+        rd = fma(rv, dv, rd);
+        rr = fma(rv, rv, rr);
+    }
+    double v[2] = {rd, rr};
+    block_reduce<2>(v, 0u);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = v[0];
+        part[G + blockIdx.x] = v[1];
+    }
+}
+
+__global__ void k_pcg_init2(PcgState *st, const double *__restrict__ part, int G, int stop_mode,
+                            double tol, int limit)
+{
+    const double rd = reduce_partials(part, G, false);
+    const double rr = reduce_partials(part + G, G, false);
+    if (threadIdx.x == 0) {
+        st->up = rd;
+        st->ff = rr;
+        st->rr = rr;
+        st->metric = 0.0;
+        st->tol = tol;
+        st->iters = 0;
+        st->converged = 0;
+        st->limit = limit;
+        st->stop_mode = stop_mode;
+        st->err = 0;
+        // a zero load vector is already solved by x = 0
+        st->stop = (rr == 0.0) ? 1 : 0;
+        if (rr == 0.0) st->converged = 1;
+    }
+}
+
+// update1: alpha = up/(p.u); xnew = x + p*alpha (in place, checon_par's
+// x = xnew, maths.f90:1062); r = r - u*alpha; d = diag*r; partials of r.d,
+// r.r, max|xnew|, max|xnew-x| into part[G..5G).  Reads st->up only.
+__global__ void __launch_bounds__(256)
+k_pcg_update1(int ns, const PcgState *__restrict__ st, double *__restrict__ part, int G,
+              double *__restrict__ x, double *__restrict__ r, double *__restrict__ d,
+              const double *__restrict__ p, const double *__restrict__ u,
+              const double *__restrict__ dinv)
+{
+    if (block_stopped(st)) return;
+    const double pu = reduce_partials(part, G, false);
+    const double alpha = st->up / pu;
+    double rd = 0.0, rr = 0.0, mx = 0.0, md = 0.0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const double xo = x[s];
+        const double xn = fma(p[s], alpha, xo);
+        x[s] = xn;
+        mx = fmax(mx, fabs(xn));
+        md = fmax(md, fabs(xn - xo));
+        const double rn = fma(-u[s], alpha, r[s]);
+        r[s] = rn;
+        const double dn = dinv[s] * rn;
+        d[s] = dn;
+        rd = fma(rn, dn, rd);
+        rr = fma(rn, rn, rr);
+    }
+    double v[4] = {rd, rr, mx, md};
+    block_reduce<4>(v, 0xCu);
+    if (threadIdx.x == 0) {
+        part[1 * G + blockIdx.x] = v[0];
+        part[2 * G + blockIdx.x] = v[1];
+        part[3 * G + blockIdx.x] = v[2];
+        part[4 * G + blockIdx.x] = v[3];
+    }
+}
+
+// update2: beta = (r.d)/up; p = d + p*beta.  Reads st->up only.
+__global__ void __launch_bounds__(256)
+k_pcg_update2(int ns, const PcgState *__restrict__ st, const double *__restrict__ part, int G,
+              const double *__restrict__ d, double *__restrict__ p)
+{
+    if (block_stopped(st)) return;
+    const double rd = reduce_partials(part + 1 * G, G, false);
+    const double beta = rd / st->up;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x)
+        p[s] = fma(p[s], beta, d[s]);
+}
+
+// finish (one block): the iteration's bookkeeping -- up for the next
+// iteration, the iteration count and the stopping test (checon_par,
+// maths.f90:1052-1062, or the relative residual).  It is the only kernel
+// of an iteration that writes the state.
+__global__ void __launch_bounds__(256)
+k_pcg_finish(PcgState *__restrict__ st, const double *__restrict__ part, int G)
+{
+    if (block_stopped(st)) return;
+    const double rd = reduce_partials(part + 1 * G, G, false);
+    const double rr = reduce_partials(part + 2 * G, G, false);
+    const double mx = reduce_partials(part + 3 * G, G, true);
+    const double md = reduce_partials(part + 4 * G, G, true);
+    if (threadIdx.x == 0) {
+        const int k = st->iters + 1;
+        const double metric = st->stop_mode == STOP_CHECON ? md / mx : sqrt(rr) / sqrt(st->ff);
+        const bool conv = metric <= st->tol;
+        st->up = rd;
+        st->iters = k;
+        st->rr = rr;
+        st->metric = metric;
+        st->converged = conv ? 1 : 0;
+        if (!isfinite(rd) || !isfinite(mx)) st->err = 1;
+        if (conv || k >= st->limit || st->err) st->stop = 1;
+    }
+}
+
+__global__ void k_sum_partials(const double *__restrict__ part, int G, int nvals,
+                               double *__restrict__ out)
+{
+    for (int k = 0; k < nvals; ++k) {
+        const double v = reduce_partials(part + (size_t)k * G, G, false);
+        if (threadIdx.x == 0) out[k] = v;
+    }
+}
+
+__global__ void k_eq_to_slot(int ns, const int *__restrict__ slot_eq, const double *__restrict__ eq,
+                             double *__restrict__ slot)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const int q = slot_eq[s];
+        slot[s] = q > 0 ? eq[q - 1] : 0.0;
+    }
+}
+
+__global__ void k_slot_to_eq(int neq, const int *__restrict__ eq_slot, const double *__restrict__ slot,
+                             double *__restrict__ eq)
+{
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < neq; q += gridDim.x * blockDim.x)
+        eq[q] = slot[eq_slot[q]];
+}
+
+__global__ void k_axpy(int ns, double *__restrict__ y, const double *__restrict__ x)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x)
+        y[s] += x[s];
+}
+
+// Centroid stress of one element (p121.f90:112-123): nip=1 at the origin.
+__global__ void k_centroid_stress(int e, const int *__restrict__ conn, const double *__restrict__ coord,
+                                  const double *__restrict__ me, const double *__restrict__ mv,
+                                  int nmat, const double *__restrict__ x, double *__restrict__ sig)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double der[60], jac[9], deriv[60], eld[60], eps[6];
+    const double *co = coord + (size_t)e * 60;
+    for (int l = 0; l < 20; ++l) shape_der20(l, 0.0, 0.0, 0.0, &der[3 * l]);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) {
+            double s = 0.0;
+            for (int k = 0; k < 20; ++k) s += der[a + 3 * k] * co[k + 20 * b];
+            jac[a + 3 * b] = s;
+        }
+    det_invert3(jac);
+    for (int l = 0; l < 20; ++l)
+        for (int a = 0; a < 3; ++a)
+            deriv[a + 3 * l] = jac[a] * der[3 * l] + jac[a + 3] * der[1 + 3 * l] + jac[a + 6] * der[2 + 3 * l];
+    for (int l = 0; l < 20; ++l) {
+        const int nd = conn[(size_t)e * 20 + l];
+        for (int d = 0; d < 3; ++d) eld[3 * l + d] = x[(size_t)3 * nd + d];
+    }
+    // eps = bee . eld (BEEMAT rows ex, ey, ez, gxy, gyz, gzx)
+    for (int k = 0; k < 6; ++k) eps[k] = 0.0;
+    for (int m = 0; m < 20; ++m) {
+        const double gx = deriv[3 * m], gy = deriv[3 * m + 1], gz = deriv[3 * m + 2];
+        const double ux = eld[3 * m], uy = eld[3 * m + 1], uz = eld[3 * m + 2];
+        eps[0] += gx * ux;
+        eps[1] += gy * uy;
+        eps[2] += gz * uz;
+        eps[3] += gy * ux + gx * uy;
+        eps[4] += gz * uy + gy * uz;
+        eps[5] += gz * ux + gx * uz;
+    }
+    double d11, d12, d44;
+    const int mi = nmat == 1 ? 0 : e;
+    deemat3(me[mi], mv[mi], d11, d12, d44);
+    sig[0] = d11 * eps[0] + d12 * eps[1] + d12 * eps[2];
+    sig[1] = d12 * eps[0] + d11 * eps[1] + d12 * eps[2];
+    sig[2] = d12 * eps[0] + d12 * eps[1] + d11 * eps[2];
+    sig[3] = d44 * eps[3];
+    sig[4] = d44 * eps[4];
+    sig[5] = d44 * eps[5];
+}
+
+// Generic batched product of the xx3 layer (cuda_helpers.cu:144-177 semantics):
+// one thread per row, FP64.
+__global__ void k_matvec_rows(int n_mat, int n_row, int n_col, const double *__restrict__ lhs,
+                              const double *__restrict__ mat, double *__restrict__ rhs)
+{
+    const size_t total = (size_t)n_mat * n_row;
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < total;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const size_t m = g / n_row, i = g % n_row;
+        const double *a = mat + m * n_row * (size_t)n_col + i;
+        const double *x = lhs + m * n_col;
+        double s = 0.0;
+        for (int j = 0; j < n_col; ++j) s = fma(x[j], a[(size_t)j * n_row], s);
+        rhs[g] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+static int grid_for(const Ctx &c, long long work, int per_block, int max_per_sm)
+{
+    long long g = (work + per_block - 1) / per_block;
+    const long long cap = (long long)c.nsm * max_per_sm;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+int launch_form_storkm(Ctx &c, int nip, bool exact_weights, bool keep32)
+{
+    double *gp = nullptr;
+    if (cudaMallocAsync(&gp, sizeof(double) * 4 * 27, c.stream) != cudaSuccess) {
+        set_error("form_storkm: cannot allocate the Gauss table");
+        return 1;
+    }
+    k_sample<<<1, 1, 0, c.stream>>>(nip, exact_weights ? 1 : 0, gp);
+    if (check_launch(c, "k_sample")) return 1;
+    const int grid = c.nels < c.nsm * 64 ? c.nels : c.nsm * 64;
+    k_form_storkm<<<grid, 128, 0, c.stream>>>(c.nels, nip, gp, c.coord, c.mat_e, c.mat_v, c.nmat,
+                                              c.km64, keep32 ? c.km32 : nullptr, c.ediag);
+    if (check_launch(c, "k_form_storkm")) return 1;
+    cudaFreeAsync(gp, c.stream);
+    return 0;
+}
+
+int launch_cast_km32(Ctx &c)
+{
+    const size_t n = (size_t)c.nels * 3600;
+    k_cast_km32<<<c.nsm * 8, 256, 0, c.stream>>>(n, c.km64, c.km32);
+    if (check_launch(c, "k_cast_km32")) return 1;
+    k_extract_ediag<<<c.nsm * 8, 256, 0, c.stream>>>(c.nels, c.km64, c.ediag);
+    return check_launch(c, "k_extract_ediag");
+}
+
+int launch_assemble_diag(Ctx &c)
+{
+    k_assemble_diag<<<grid_for(c, c.nn, 256, 8), 256, 0, c.stream>>>(
+        c.nn, c.node_ptr, c.node_list, c.ediag, c.freemask, c.diag, c.dinv);
+    return check_launch(c, "k_assemble_diag");
+}
+
+int launch_eq_to_slot(Ctx &c, const double *eq, double *slot)
+{
+    k_eq_to_slot<<<grid_for(c, c.nslots, 256, 8), 256, 0, c.stream>>>(c.nslots, c.slot_eq, eq, slot);
+    return check_launch(c, "k_eq_to_slot");
+}
+
+int launch_slot_to_eq(Ctx &c, const double *slot, double *eq)
+{
+    k_slot_to_eq<<<grid_for(c, c.neq, 256, 8), 256, 0, c.stream>>>(c.neq, c.eq_slot, slot, eq);
+    return check_launch(c, "k_slot_to_eq");
+}
+
+int launch_elem(Ctx &c, int prec, const double *p)
+{
+    const int grid = grid_for(c, c.nels, 8, 8);
+    if (prec == 32) {
+        k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, c.st);
+    } else {
+        k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, p, (double *)c.utemp, c.st);
+    }
+    return check_launch(c, "k_elem");
+}
+
+int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
+{
+    const PcgState *st = mode == 0 ? c.st : nullptr;
+    if (prec == 32) {
+        if (mode == 0)
+            k_scatter<float, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
+                                                           c.freemask, pf, out, c.part, st);
+        else
+            k_scatter<float, 1><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
+                                                           c.freemask, pf, out, c.part, st);
+    } else {
+        if (mode == 0)
+            k_scatter<double, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                            c.freemask, pf, out, c.part, st);
+        else
+            k_scatter<double, 1><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                            c.freemask, pf, out, c.part, st);
+    }
+    return check_launch(c, "k_scatter");
+}
+
+// u = K p outside a PCG run (state-independent).
+int launch_matvec(Ctx &c, int prec, const double *p, double *u)
+{
+    const int grid = grid_for(c, c.nels, 8, 8);
+    if (prec == 32)
+        k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, nullptr);
+    else
+        k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, p, (double *)c.utemp, nullptr);
+    if (check_launch(c, "k_elem")) return 1;
+    if (prec == 32)
+        k_scatter<float, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
+                                                       c.freemask, p, u, c.part, nullptr);
+    else
+        k_scatter<double, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                        c.freemask, p, u, c.part, nullptr);
+    return check_launch(c, "k_scatter");
+}
+
+int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
+{
+    const int grid = grid_for(c, c.nels, 8, 8);
+    k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, x, (double *)c.utemp, nullptr);
+    if (check_launch(c, "k_elem")) return 1;
+    k_scatter<double, 1><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                    c.freemask, f, rres, c.part, nullptr);
+    return check_launch(c, "k_scatter");
+}
+
+int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit)
+{
+    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part, c.G);
+    if (check_launch(c, "k_pcg_init")) return 1;
+    k_pcg_init2<<<1, 256, 0, c.stream>>>(c.st, c.part, c.G, stop_mode, tol, limit);
+    return check_launch(c, "k_pcg_init2");
+}
+
+int launch_update1(Ctx &c, double *xsol)
+{
+    k_pcg_update1<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part, c.G, xsol, c.r, c.d, c.p, c.u, c.dinv);
+    return check_launch(c, "k_pcg_update1");
+}
+
+int launch_update2(Ctx &c)
+{
+    k_pcg_update2<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part, c.G, c.d, c.p);
+    if (check_launch(c, "k_pcg_update2")) return 1;
+    k_pcg_finish<<<1, 256, 0, c.stream>>>(c.st, c.part, c.G);
+    return check_launch(c, "k_pcg_finish");
+}
+
+int launch_pcg_iteration(Ctx &c, int prec, double *xsol)
+{
+    if (launch_elem(c, prec, c.p)) return 1;
+    if (launch_scatter(c, prec, 0, c.p, c.u)) return 1;
+    if (launch_update1(c, xsol)) return 1;
+    return launch_update2(c);
+}
+
+int launch_axpy(Ctx &c, double *y, const double *xv)
+{
+    k_axpy<<<grid_for(c, c.nslots, 256, 8), 256, 0, c.stream>>>(c.nslots, y, xv);
+    return check_launch(c, "k_axpy");
+}
+
+int launch_sum_partials(Ctx &c, int nvals, double *out_dev)
+{
+    k_sum_partials<<<1, 256, 0, c.stream>>>(c.part, c.G, nvals, out_dev);
+    return check_launch(c, "k_sum_partials");
+}
+
+int launch_centroid_stress(Ctx &c, int iel, const double *xslot, double *sig_dev)
+{
+    k_centroid_stress<<<1, 1, 0, c.stream>>>(iel, c.conn, c.coord, c.mat_e, c.mat_v, c.nmat, xslot, sig_dev);
+    return check_launch(c, "k_centroid_stress");
+}
+
+int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs, const double *mat,
+                          double *rhs, long long *launches)
+{
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm < 1) nsm = 1;
+    if (n_row == 60 && n_col == 60) {
+        long long g = ((long long)n_mat + 7) / 8;
+        if (g > nsm * 8LL) g = nsm * 8LL;
+        if (g < 1) g = 1;
+        k_elem<double, false><<<(int)g, 256>>>(n_mat, mat, nullptr, lhs, rhs, nullptr);
+    } else {
+        long long g = ((long long)n_mat * n_row + 127) / 128;
+        if (g > nsm * 16LL) g = nsm * 16LL;
+        if (g < 1) g = 1;
+        k_matvec_rows<<<(int)g, 128>>>(n_mat, n_row, n_col, lhs, mat, rhs);
+    }
+    if (launches) ++*launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("matrix_vector_multiplies: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+}  // namespace pf

@@ -1,0 +1,292 @@
+"""ctypes binding of libpfgpu.so, the GB300 element-by-element PCG library.
+
+The host arrays follow p121's Fortran layouts, expressed as C-contiguous
+numpy arrays with the Fortran leading index last:
+    g_num   (nels, 20)      int32   == g_num_pp(20, nels)
+    g_g     (nels, 60)      int32   == g_g_pp(60, nels)
+    g_coord (nels, 3, 20)   float64 == g_coord_pp(20, 3, nels)
+    storkm  (nels, 60, 60)  float64 == storkm_pp(60, 60, nels): km[e, j, i] = K_e(i, j)
+
+There is no CPU fallback: every call below runs in the compiled library and
+raises PfError when the library reports a failure.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+
+MODE_P121 = 0
+MODE_FP64_RES = 1
+MODE_MIXED = 2
+FORM_EXACT_WEIGHTS = 1
+
+_I = ctypes.c_int
+_IP = ctypes.POINTER(ctypes.c_int)
+_DP = ctypes.POINTER(ctypes.c_double)
+_VPP = ctypes.POINTER(ctypes.c_void_p)
+_LLP = ctypes.POINTER(ctypes.c_longlong)
+
+_lib = None
+
+# (name, argtypes) for every entry point of include/pfgpu.h
+_SIGS = {
+    "set_gpu": [_IP],
+    "allocate_memory_on_gpu": [_IP, _IP, _VPP],
+    "free_memory_on_gpu": [_VPP],
+    "copy_data_to_gpu": [_IP, _IP, ctypes.c_void_p, _VPP],
+    "copy_data_from_gpu": [_IP, _IP, ctypes.c_void_p, _VPP],
+    "matrix_vector_multiplies": [_IP, _IP, _IP, _VPP, _VPP, _VPP],
+    "pf_last_error": [ctypes.c_char_p, _IP],
+    "pf_ctx_create": [_IP, _VPP],
+    "pf_ctx_destroy": [_VPP],
+    "pf_setup": [_VPP, _IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_set_material": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_form_storkm": [_VPP, _IP, _IP],
+    "pf_set_storkm": [_VPP, ctypes.c_void_p],
+    "pf_get_storkm": [_VPP, _IP, _IP, ctypes.c_void_p],
+    "pf_get_diag": [_VPP, ctypes.c_void_p],
+    "pf_ebe_matvec": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_solve": [_VPP, ctypes.c_void_p, _DP, _IP, _IP, ctypes.c_void_p, _IP, _DP],
+    "pf_solve_stats": [_VPP, ctypes.c_void_p, _IP],
+    "pf_bench_iterations": [_VPP, _IP, _IP, _DP, _DP, _DP],
+    "pf_centroid_stress": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_kernel_launches": [_VPP, _LLP],
+    "pf_p12meshgen": [ctypes.c_char_p],
+    "pf_p121_run": [ctypes.c_char_p, _IP, _IP, _IP, _DP],
+    "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_cube_restraints": [_IP, _IP, _IP, _IP, ctypes.c_void_p],
+    "pf_number_equations": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
+    "pf_cube_top_pressure": [_IP, _IP, _IP, _DP, _DP, _DP, ctypes.c_void_p, _IP, ctypes.c_void_p],
+    "pf_random_material": [_IP, _LLP, _DP, _DP, _DP, _DP, ctypes.c_void_p, ctypes.c_void_p],
+}
+
+
+class PfError(RuntimeError):
+    pass
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib():
+    """Load libpfgpu.so, building it first when a source is newer."""
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(path)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def _i(v):
+    return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def _d(v):
+    return ctypes.byref(ctypes.c_double(float(v)))
+
+
+def last_error() -> str:
+    buf = ctypes.create_string_buffer(1024)
+    lib().pf_last_error(buf, _i(1024))
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise PfError(f"{what}: {last_error()}")
+
+
+def _arr(a, dtype):
+    a = np.ascontiguousarray(a, dtype=dtype)
+    return a, a.ctypes.data
+
+
+# ---------------------------------------------------------------------------
+# host-side helpers (no GPU)
+def mesh_cube(nxe, nye, nze, aa=1.0, bb=1.0, cc=1.0):
+    """GEOMETRY_20BXZ cube: returns (g_num (nels,20), g_coord (nels,3,20), nn)."""
+    L = lib()
+    nels, nn = ctypes.c_int(0), ctypes.c_int(0)
+    args = [_i(nxe), _i(nye), _i(nze), _d(aa), _d(bb), _d(cc)]
+    _check(L.pf_mesh_cube(*args, ctypes.byref(nels), ctypes.byref(nn), None, None), "pf_mesh_cube")
+    g_num = np.zeros((nels.value, 20), np.int32)
+    g_coord = np.zeros((nels.value, 3, 20), np.float64)
+    _check(L.pf_mesh_cube(*args, ctypes.byref(nels), ctypes.byref(nn), g_num.ctypes.data,
+                          g_coord.ctypes.data), "pf_mesh_cube")
+    return g_num, g_coord, nn.value
+
+
+def cube_restraints(nxe, nye, nze, bc, nn):
+    fix = np.zeros((nn, 3), np.int32)
+    _check(lib().pf_cube_restraints(_i(nxe), _i(nye), _i(nze), _i(bc), fix.ctypes.data),
+           "pf_cube_restraints")
+    return fix
+
+
+def number_equations(g_num, node_fix):
+    g_num, pn = _arr(g_num, np.int32)
+    node_fix, pf = _arr(node_fix, np.int32)
+    g_g = np.zeros((g_num.shape[0], 60), np.int32)
+    neq = ctypes.c_int(0)
+    _check(lib().pf_number_equations(_i(g_num.shape[0]), _i(node_fix.shape[0]), pn, pf, g_g.ctypes.data,
+                                     ctypes.byref(neq)), "pf_number_equations")
+    return g_g, neq.value
+
+
+def cube_top_pressure(nxe, nze, g_g, neq, p, aa=1.0, bb=1.0, r=None):
+    g_g, pg = _arr(g_g, np.int32)
+    if r is None:
+        r = np.zeros(neq)
+    _check(lib().pf_cube_top_pressure(_i(nxe), _i(nze), _i(g_g.shape[0]), _d(aa), _d(bb), _d(p), pg,
+                                      _i(neq), r.ctypes.data), "pf_cube_top_pressure")
+    return r
+
+
+def random_material(nels, seed, e_lo, e_hi, v_lo, v_hi):
+    e = np.zeros(nels)
+    v = np.zeros(nels)
+    _check(lib().pf_random_material(_i(nels), ctypes.byref(ctypes.c_longlong(int(seed))), _d(e_lo), _d(e_hi),
+                                    _d(v_lo), _d(v_hi), e.ctypes.data, v.ctypes.data), "pf_random_material")
+    return e, v
+
+
+def p12meshgen(job: str):
+    _check(lib().pf_p12meshgen(os.fsencode(job)), "pf_p12meshgen")
+
+
+def p121_run(job: str, mode: int = MODE_P121, device: int = 0):
+    it, cen = ctypes.c_int(0), ctypes.c_double(0.0)
+    _check(lib().pf_p121_run(os.fsencode(job), _i(device), _i(mode), ctypes.byref(it), ctypes.byref(cen)),
+           "pf_p121_run")
+    return it.value, cen.value
+
+
+# ---------------------------------------------------------------------------
+class Solver:
+    """One solver context on one GPU (pf_ctx_create .. pf_ctx_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p(None)
+        _check(lib().pf_ctx_create(_i(device), ctypes.byref(self._h)), "pf_ctx_create")
+        self.nels = self.nn = self.neq = 0
+
+    @property
+    def _ref(self):
+        if not self._h.value:
+            raise PfError("solver context is closed")
+        return ctypes.byref(self._h)
+
+    def close(self):
+        if self._h.value:
+            lib().pf_ctx_destroy(ctypes.byref(self._h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setup(self, g_num, g_g, g_coord, nn, neq):
+        g_num, pn = _arr(g_num, np.int32)
+        g_g, pg = _arr(g_g, np.int32)
+        g_coord, pc = _arr(g_coord, np.float64)
+        nels = g_num.shape[0]
+        if g_g.shape != (nels, 60) or g_coord.shape != (nels, 3, 20):
+            raise ValueError("g_num (nels,20), g_g (nels,60), g_coord (nels,3,20) expected")
+        _check(lib().pf_setup(self._ref, _i(nels), _i(nn), _i(neq), pn, pg, pc), "pf_setup")
+        self.nels, self.nn, self.neq = nels, int(nn), int(neq)
+
+    def set_material(self, e, v):
+        e, pe = _arr(np.atleast_1d(e), np.float64)
+        v, pv = _arr(np.atleast_1d(v), np.float64)
+        _check(lib().pf_set_material(self._ref, _i(e.size), pe, pv), "pf_set_material")
+
+    def form_storkm(self, nip: int, exact_weights: bool = False):
+        _check(lib().pf_form_storkm(self._ref, _i(nip), _i(FORM_EXACT_WEIGHTS if exact_weights else 0)),
+               "pf_form_storkm")
+
+    def set_storkm(self, km):
+        km, pk = _arr(km, np.float64)
+        _check(lib().pf_set_storkm(self._ref, pk), "pf_set_storkm")
+
+    def get_storkm(self, first=0, count=None):
+        count = self.nels - first if count is None else count
+        out = np.zeros((count, 60, 60))
+        _check(lib().pf_get_storkm(self._ref, _i(first), _i(count), out.ctypes.data), "pf_get_storkm")
+        return out
+
+    def get_diag(self):
+        out = np.zeros(self.neq)
+        _check(lib().pf_get_diag(self._ref, out.ctypes.data), "pf_get_diag")
+        return out
+
+    def ebe_matvec(self, p, prec: int = 64):
+        p, pp = _arr(p, np.float64)
+        u = np.zeros(self.neq)
+        _check(lib().pf_ebe_matvec(self._ref, _i(prec), pp, u.ctypes.data), "pf_ebe_matvec")
+        return u
+
+    def solve(self, r, tol, limit, mode=MODE_P121):
+        r, pr = _arr(r, np.float64)
+        x = np.zeros(self.neq)
+        it = ctypes.c_int(0)
+        rel = ctypes.c_double(0.0)
+        _check(lib().pf_solve(self._ref, pr, _d(tol), _i(limit), _i(mode), x.ctypes.data, ctypes.byref(it),
+                              ctypes.byref(rel)), "pf_solve")
+        return x, it.value, rel.value
+
+    def stats(self):
+        s = np.zeros(8)
+        _check(lib().pf_solve_stats(self._ref, s.ctypes.data, _i(8)), "pf_solve_stats")
+        keys = ["iters", "outer", "solve_ms", "metric", "matvec64", "matvec32", "relres"]
+        return dict(zip(keys, s.tolist()))
+
+    def bench_iterations(self, prec: int, steps: int):
+        a, b, c = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
+        _check(lib().pf_bench_iterations(self._ref, _i(prec), _i(steps), ctypes.byref(a), ctypes.byref(b),
+                                         ctypes.byref(c)), "pf_bench_iterations")
+        return a.value, b.value, c.value
+
+    def centroid_stress(self, x, iel: int = 1):
+        x, px = _arr(x, np.float64)
+        s = np.zeros(6)
+        _check(lib().pf_centroid_stress(self._ref, _i(iel), px, s.ctypes.data), "pf_centroid_stress")
+        return s
+
+    def launches(self) -> int:
+        n = ctypes.c_longlong(0)
+        _check(lib().pf_kernel_launches(self._ref, ctypes.byref(n)), "pf_kernel_launches")
+        return n.value
+
+
+def cube_problem(nxe, nye, nze, bc=1, pressure=None, aa=1.0, bb=1.0, cc=1.0):
+    """Synthetic cube problem: mesh, restraints (bc 1 = fixed base), numbering and
+    the top-pressure load vector (total load -1 by default).  Host only."""
+    g_num, g_coord, nn = mesh_cube(nxe, nye, nze, aa, bb, cc)
+    fix = cube_restraints(nxe, nye, nze, bc, nn)
+    g_g, neq = number_equations(g_num, fix)
+    if pressure is None:
+        pressure = 1.0 / (nxe * aa * nye * bb)
+    r = cube_top_pressure(nxe, nze, g_g, neq, pressure, aa, bb)
+    return dict(g_num=g_num, g_coord=g_coord, nn=nn, g_g=g_g, neq=neq, r=r, fix=fix,
+                nxe=nxe, nye=nye, nze=nze)

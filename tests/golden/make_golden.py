@@ -1,0 +1,80 @@
+"""Extract the golden fixtures of the p121 path from a ParaFEM source tree.
+
+Usage: python tests/golden/make_golden.py /path/to/parafem
+
+Reads the reference's own recorded runs (examples/5th_ed/p121) and writes
+  p121_golden.json      .res figures of the demo and book runs, the .mg
+                        inputs, and sha256 of the demo deck files
+  p121_demo_displ.npz   the demo displacement field (p121_demo.ensi.DISPL-000001)
+The fixtures let the tests run where the reference tree is absent.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def parse_res(path):
+    txt = open(path).read()
+    out = {}
+    m = re.search(r"There are\s+(\d+) nodes\s+(\d+) restrained and\s+(\d+) equations", txt)
+    out["nn"], out["nr"], out["neq"] = (int(g) for g in m.groups())
+    m = re.search(r"This job ran on\s+(\d+) processes", txt)
+    out["processes"] = int(m.group(1))
+    m = re.search(r"The total load is:\s*(\S+)", txt)
+    if m:
+        out["total_load_text"] = m.group(1)
+    m = re.search(r"The number of iterations to convergence was\s+(\d+)", txt)
+    out["iterations"] = int(m.group(1))
+    m = re.search(r"The central nodal displacement is :\s*(\S+)", txt)
+    out["central_text"] = m.group(1)
+    lines = txt.splitlines()
+    i = next(k for k, ln in enumerate(lines) if ln.startswith("Point"))
+    out["stress_text"] = lines[i + 1].split()
+    out["lines"] = {
+        "iterations": next(ln for ln in lines if ln.startswith("The number of iterations")),
+        "central": next(ln for ln in lines if ln.startswith("The central nodal")),
+        "stress": lines[i + 1],
+    }
+    tl = [ln for ln in lines if ln.startswith("The total load")]
+    if tl:
+        out["lines"]["total_load"] = tl[0]
+    return out
+
+
+def main(root):
+    ex = os.path.join(root, "examples", "5th_ed", "p121")
+    demo = os.path.join(ex, "demo", "p121_demo")
+    gold = {
+        "source": "examples/5th_ed/p121 of the ParaFEM tree",
+        "demo": parse_res(demo + ".res"),
+        "book": parse_res(os.path.join(ex, "book", "p121.res")),
+        "demo_mg": open(demo + ".mg").read(),
+        "book_mg": open(os.path.join(ex, "book", "p121.mg")).read(),
+        "demo_deck_sha256": {},
+    }
+    for ext in ("dat", "d", "bnd", "lds"):
+        with open(demo + "." + ext, "rb") as f:
+            gold["demo_deck_sha256"][ext] = hashlib.sha256(f.read()).hexdigest()
+    with open(os.path.join(HERE, "p121_golden.json"), "w") as f:
+        json.dump(gold, f, indent=1, sort_keys=True)
+    # displacement field: 4 header lines, then x block, y block, z block (e12.4 text)
+    vals = []
+    with open(demo + ".ensi.DISPL-000001") as f:
+        lines = f.read().splitlines()[4:]
+    vals = np.array([float(t) for t in lines if t.strip()], dtype=np.float64)
+    nn = gold["demo"]["nn"]
+    disp = vals.reshape(3, nn).T.astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "p121_demo_displ.npz"), disp=disp)
+    print("wrote", os.path.join(HERE, "p121_golden.json"), disp.shape)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")

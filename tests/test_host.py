@@ -1,0 +1,109 @@
+"""Host-side logic of libpfgpu.so (no GPU): exports, generators, numbering."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import parafem_gb300 as P
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "pfgpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return re.findall(r"^\s*int\s+(\w+)\s*\(", txt, flags=re.M)
+
+
+def test_library_exports_every_declared_symbol():
+    names = header_functions()
+    assert len(names) >= 25
+    lib = ctypes.CDLL(P.library_path() if os.path.exists(P.library_path()) else P.lib()._name)
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(P.pfgpu.exported_symbols())
+
+
+@pytest.mark.parametrize("nxe,nye,nze", [(1, 1, 1), (2, 3, 4), (5, 2, 3)])
+def test_mesh_cube_matches_geometry_20bxz(nxe, nye, nze):
+    aa, bb, cc = 0.5, 0.25, 0.75
+    g_num, g_coord, nn = P.mesh_cube(nxe, nye, nze, aa, bb, cc)
+    L = O.lib()
+    coord = np.zeros(60)
+    num = np.zeros(20, np.int32)
+    for e in range(nxe * nye * nze):
+        L.orc_geometry_20bxz(e + 1, nxe, nze, aa, bb, cc, coord, num)
+        assert np.array_equal(num, g_num[e])
+        assert np.array_equal(coord.reshape(3, 20), g_coord[e])
+    assert nn == g_num.max()
+    assert len(np.unique(g_num)) == nn
+
+
+@pytest.mark.parametrize("nxe,nye,nze", [(1, 1, 1), (3, 2, 4), (5, 5, 5)])
+def test_cube_bc20_matches(nxe, nye, nze):
+    g_num, _, nn = P.mesh_cube(nxe, nye, nze)
+    fix = P.cube_restraints(nxe, nye, nze, 0, nn)
+    rest = np.zeros((nn, 4), np.int32)
+    nr = O.lib().orc_cube_bc20(nxe, nye, nze, rest)
+    rest = rest[:nr]
+    ref = np.ones((nn, 3), np.int32)
+    ref[rest[:, 0] - 1] = rest[:, 1:]
+    assert np.array_equal(fix, ref)
+    listed = np.nonzero((fix == 0).any(axis=1))[0] + 1
+    assert np.array_equal(listed, rest[:, 0])
+
+
+@pytest.mark.parametrize("bc", [0, 1])
+def test_numbering_matches_rearrange_find_g3(bc):
+    nxe, nye, nze = 4, 3, 5
+    g_num, _, nn = P.mesh_cube(nxe, nye, nze)
+    fix = P.cube_restraints(nxe, nye, nze, bc, nn)
+    g_g, neq = P.number_equations(g_num, fix)
+    rows = np.nonzero((fix == 0).any(axis=1))[0]
+    rest = np.concatenate([(rows + 1)[:, None], fix[rows]], axis=1).astype(np.int32)
+    if bc == 1:
+        # node 1 precedes the first restrained node: list it free so that the
+        # reference's find_g3 stays inside rest (new_library.f90:3130-3212)
+        rest = np.concatenate([[[1, 1, 1, 1]], rest]).astype(np.int32)
+    ref = O.steering(g_num, rest)
+    assert np.array_equal(g_g, ref)
+    assert neq == ref.max()
+
+
+def test_demo_numbering(demo_problem):
+    d = demo_problem["deck"]
+    fix = np.ones((d.nn, 3), np.int32)
+    fix[d.rest[:, 0] - 1] = (d.rest[:, 1:] != 0)
+    g_g, neq = P.number_equations(d.g_num, fix)
+    assert np.array_equal(g_g, demo_problem["g_g"])
+
+
+def test_config1_sizes_and_total_load():
+    prob = P.cube_problem(10, 10, 10)
+    assert prob["nn"] == 4961 and prob["neq"] == 13860
+    assert abs(prob["r"].sum() + 1.0) < 1e-14
+    assert (prob["g_g"] >= 0).all()
+
+
+def test_load_p121_pattern_is_patch_pressure(demo_deck):
+    # load_p121 values are the consistent loads of a uniform pressure of 25 on
+    # the nle x nle corner patch: total -25 * (nle*aa)^2 = -100 for the demo
+    assert abs(demo_deck.load_val[:, 2].sum() + 100.0) < 1e-6
+
+
+def test_random_material_deterministic_and_in_range():
+    e1, v1 = P.random_material(10000, 1234, 1.0, 1000.0, 0.2, 0.35)
+    e2, v2 = P.random_material(10000, 1234, 1.0, 1000.0, 0.2, 0.35)
+    e3, _ = P.random_material(10000, 1235, 1.0, 1000.0, 0.2, 0.35)
+    assert np.array_equal(e1, e2) and np.array_equal(v1, v2) and not np.array_equal(e1, e3)
+    assert e1.min() >= 1.0 and e1.max() <= 1000.0 and v1.min() >= 0.2 and v1.max() <= 0.35
+    # log-uniform: mean of ln(E) ~ ln(1000)/2
+    assert abs(np.log(e1).mean() - np.log(1000.0) / 2) < 0.1
+
+
+def test_errors_are_reported_not_printed(tmp_path):
+    with pytest.raises(P.PfError, match="cannot read"):
+        P.p12meshgen(str(tmp_path / "missing"))
