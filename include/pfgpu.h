@@ -131,6 +131,19 @@ int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *s
 /* Number of kernels this library launched since the context was created. */
 int pf_kernel_launches(void **ctx, long long *count);
 
+/* No counterpart in the reference.  u(neq) = K p for callers that cannot
+ * allocate device memory while they run (memory reserved up front by a pool
+ * or a host framework, cudaMalloc forbidden in the solve phase, or a fixed
+ * device budget).  storkm(60,60,nels), g_g(60,nels), p(neq) and u(neq) are
+ * the caller's DEVICE buffers on the current device.  The library's own
+ * scratch is a fixed array inside libpfgpu.so (about 14.3 MiB, held on every
+ * device that loads the library until exit) that limits nels <= 16384 and
+ * neq <= 262144; larger sizes are rejected.  The first call on a device looks
+ * the array up and should come before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must not be made. */
+int pf_ebe_matvec_noalloc(const int *nels, const int *neq, const double *storkm,
+                          const int *g_g, const double *p, double *u);
+
 /* ---------------------------------------------------------------------- */
 /* Host-side driver layer (C++, no GPU work): deck I/O and generators.     */
 

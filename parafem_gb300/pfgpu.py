@@ -55,6 +55,8 @@ _SIGS = {
     "pf_bench_iterations": [_VPP, _IP, _IP, _DP, _DP, _DP],
     "pf_centroid_stress": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_kernel_launches": [_VPP, _LLP],
+    "pf_ebe_matvec_noalloc": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                              ctypes.c_void_p],
     "pf_p12meshgen": [ctypes.c_char_p],
     "pf_p121_run": [ctypes.c_char_p, _IP, _IP, _IP, _DP],
     "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
