@@ -35,8 +35,11 @@ extern "C" {
 /* pf_solve modes */
 #define PF_MODE_P121     0 /* FP64 storkm, checon_par test (p121.f90:88-104)      */
 #define PF_MODE_FP64_RES 1 /* FP64 storkm, stop at ||r||2/||f||2 <= tol           */
-#define PF_MODE_MIXED    2 /* FP32-storkm inner PCG + FP64 defect correction,
+#define PF_MODE_MIXED    2 /* FP32-storkm PCG with FP64 defect correction by
+                              residual replacement (search direction kept),
                               stop at the FP64 true ||f-Ku||2/||f||2 <= tol        */
+#define PF_MODE_MIXED_RESTART 3 /* FP32-storkm inner PCG restarted on each FP64
+                              defect f-Ku (classic iterative refinement)           */
 
 /* pf_form_storkm flags */
 #define PF_FORM_EXACT_WEIGHTS 1 /* exact 5/9, 8/9 Gauss factors instead of
@@ -101,8 +104,9 @@ int pf_get_storkm(void **ctx, const int *first, const int *count, double *storkm
 int pf_get_diag(void **ctx, double *diag);
 
 /* One element-by-element product u = K p in equation order (GATHER,
- * element MATMUL, SCATTER of p121.f90:92-97).  prec 64: FP64 storkm,
- * 32: FP32 storkm. */
+ * element MATMUL, SCATTER of p121.f90:92-97).  prec 64: FP64 storkm;
+ * 32: packed-symmetric FP32 storkm (the upper triangle, used by
+ * PF_MODE_MIXED); 31: full FP32 storkm. */
 int pf_ebe_matvec(void **ctx, const int *prec, const double *p, double *u);
 
 /* The PCG solve (p121.f90:86-104).  r: loads (neq); xnew: result (neq);
@@ -117,7 +121,7 @@ int pf_solve(void **ctx, const double *r, const double *tol, const int *limit,
  *  [6] true relative residual */
 int pf_solve_stats(void **ctx, double *stats, const int *n);
 
-/* Times `steps` PCG iterations on the resident state (prec 64 or 32) with
+/* Times `steps` PCG iterations on the resident state (prec 64, 32 or 31) with
  * CUDA events on the library stream.  ms_total: all steps; ms_elem: summed
  * duration of the element-product kernel launches; ms_scatter: summed
  * duration of the node-scatter kernel launches. */

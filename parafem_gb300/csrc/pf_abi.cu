@@ -84,6 +84,7 @@ static void free_mesh(Ctx &c)
 {
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
+    dfree(c.km32p);
     dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
     dfree(c.d); dfree(c.p); dfree(c.u); dfree(c.rres); dfree(c.eqbuf); dfree(c.utemp); dfree(c.part);
     c.nels = c.nn = c.neq = c.nslots = 0;
@@ -105,6 +106,21 @@ static int pull_state(Ctx &c)
     return 0;
 }
 
+// Reads and clears the bulk-copy kernels' device error word.
+static int check_kernel_error(Ctx &c)
+{
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, c.kerr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (err) {
+        cudaMemsetAsync(c.kerr, 0, sizeof(int), c.stream);
+        cudaStreamSynchronize(c.stream);
+        set_error("element kernel: a shared-memory bulk-copy wait timed out (code %d)", err);
+        return 1;
+    }
+    return 0;
+}
+
 // Runs PCG iterations until the device state says stop.  The state is read
 // back every `chunk` iterations; iterations launched after the stop return
 // at once (every kernel checks the flag).
@@ -119,6 +135,7 @@ static int run_pcg(Ctx &c, int prec, double *xsol, int limit)
         if (c.hst->stop || launched >= limit) break;
         if (chunk < 32) chunk *= 2;
     }
+    if (check_kernel_error(c)) return 1;
     if (c.hst->err) {
         set_error("PCG breakdown after %d iterations (non-finite r.d or |x|)", c.hst->iters);
         return 1;
@@ -242,6 +259,8 @@ extern "C" int pf_ctx_create(const int *device, void **ctx)
     if (c->nsm < 1) c->nsm = 1;
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc((void **)&c->st, sizeof(PcgState)) != cudaSuccess ||
+        cudaMalloc((void **)&c->kerr, sizeof(int)) != cudaSuccess ||
+        cudaMemset(c->kerr, 0, sizeof(int)) != cudaSuccess ||
         cudaMallocHost((void **)&c->hst, sizeof(PcgState)) != cudaSuccess) {
         set_error("pf_ctx_create: cannot create stream/state");
         if (c->stream) cudaStreamDestroy(c->stream);
@@ -262,6 +281,7 @@ extern "C" int pf_ctx_destroy(void **ctx)
     cudaStreamSynchronize(c->stream);
     free_mesh(*c);
     if (c->st) cudaFree(c->st);
+    if (c->kerr) cudaFree(c->kerr);
     if (c->hst) cudaFreeHost(c->hst);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -338,27 +358,35 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
     for (size_t e = 0; e < (size_t)nels; ++e)
         for (int a = 0; a < 20; ++a) {
             const int n = conn[e * 20 + a];
-            list[fill[n]++] = (int)(e * 20 + a);
+            list[fill[n]++] = (int)(e * 60 + 3 * a);   // offset of the contribution in utemp
         }
 
     c.nels = nels; c.nn = nn; c.neq = neq; c.nslots = ns;
     long long g = ((long long)ns + 255) / 256;
-    if (g > (long long)c.nsm * 4) g = (long long)c.nsm * 4;
+    if (g > (long long)c.nsm * 8) g = (long long)c.nsm * 8;
     c.G = (int)(g < 1 ? 1 : g);
+    long long gs = ((long long)nn + 255) / 256;
+    if (gs > (long long)c.nsm * 16) gs = (long long)c.nsm * 16;
+    c.Gs = (int)(gs < 1 ? 1 : gs);
     const size_t ne = (size_t)nels;
     if (dalloc(&c.conn, ne * 20, "connectivity") || dalloc(&c.node_ptr, nn + 1, "node table") ||
         dalloc(&c.node_list, ne * 20, "node table") || dalloc(&c.slot_eq, ns, "slot map") ||
         dalloc(&c.eq_slot, neq, "equation map") || dalloc(&c.freemask, nn, "restraint mask") ||
         dalloc(&c.coord, ne * 60, "coordinates") || dalloc(&c.km64, ne * 3600, "FP64 storkm") ||
-        dalloc(&c.km32, ne * 3600, "FP32 storkm") || dalloc(&c.ediag, ne * 60, "element diagonals") ||
+        dalloc(&c.km32, ne * 3600, "FP32 storkm") || dalloc(&c.km32p, ne * 1832, "packed FP32 storkm") ||
+        dalloc(&c.ediag, ne * 60, "element diagonals") ||
         dalloc(&c.diag, ns, "diag") || dalloc(&c.dinv, ns, "diag") || dalloc(&c.f, ns, "f") ||
         dalloc(&c.x, ns, "x") || dalloc(&c.c, ns, "c") || dalloc(&c.r, ns, "r") || dalloc(&c.d, ns, "d") ||
         dalloc(&c.p, ns, "p") || dalloc(&c.u, ns, "u") || dalloc(&c.rres, ns, "rres") ||
         dalloc(&c.eqbuf, neq + 8, "equation buffer") || dalloc((double **)&c.utemp, ne * 60, "utemp") ||
-        dalloc(&c.part, (size_t)8 * c.G + 16, "partials")) {
+        dalloc(&c.part, (size_t)c.Gs + 6 * (size_t)c.G + 16, "partials")) {
         free_mesh(c);
         return PF_FAILURE;
     }
+    c.part_s = c.part;
+    c.part_u = c.part_s + c.Gs;
+    c.part_r = c.part_u + 4 * (size_t)c.G;
+    c.scr = c.part_r + 2 * (size_t)c.G;
     CK(cudaMemcpyAsync(c.conn, conn.data(), ne * 20 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.node_ptr, ptr.data(), (nn + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.node_list, list.data(), ne * 20 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
@@ -412,6 +440,7 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
     }
     const bool exact = (*flags & PF_FORM_EXACT_WEIGHTS) != 0;
     TRY(launch_form_storkm(c, *nip, exact, true));
+    TRY(launch_pack_sym32(c));
     TRY(launch_assemble_diag(c));
     TRY(sync(c));
     c.have_km = true;
@@ -427,6 +456,7 @@ extern "C" int pf_set_storkm(void **ctx, const double *storkm)
     CK(cudaMemcpyAsync(c.km64, storkm, (size_t)c.nels * 3600 * sizeof(double), cudaMemcpyHostToDevice,
                        c.stream));
     TRY(launch_cast_km32(c));
+    TRY(launch_pack_sym32(c));
     TRY(launch_assemble_diag(c));
     TRY(sync(c));
     c.have_km = true;
@@ -465,22 +495,25 @@ extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, doubl
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32)) {
+    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32 && *prec != 31)) {
         set_error("pf_ebe_matvec: invalid arguments or no storkm");
         return PF_FAILURE;
     }
     CK(cudaMemcpyAsync(c.eqbuf, p, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
     TRY(launch_matvec(c, *prec, c.rres, c.u));
+    TRY(check_kernel_error(c));
     TRY(launch_slot_to_eq(c, c.u, c.eqbuf));
     CK(cudaMemcpyAsync(u, c.eqbuf, (size_t)c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
 }
 
-// Mixed precision: FP32-storkm inner PCG on the FP64 defect, FP64 update
-// of the solution and FP64 true residual from the FP64 storkm.
-static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2)
+// Mixed precision, restarted defect correction: each outer step solves
+// K32 c = f - K64 x from c = 0 with FP32-storkm PCG, then x += c in FP64 and
+// the FP64 true residual is recomputed.  Every restart discards the Krylov
+// space, so the inner iterations add up to about twice the FP64 count.
+static int solve_mixed_restart(Ctx &c, double tol, int limit, double ff, double *dev2)
 {
     const double eta_min = 1e-5;   // inner relative tolerance floor
     const int max_outer = 50;
@@ -508,6 +541,42 @@ static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2)
     return 0;
 }
 
+// Mixed precision with residual replacement (the default mixed mode): one
+// PCG run whose products use the FP32 storkm while x, r, p, d and every
+// reduction stay FP64.  Whenever the recursive residual has dropped by
+// `drop` since the last anchor, the FP64 true residual f - K64 x replaces it
+// (defect correction) and the search direction is kept, so the Krylov space
+// built so far is not thrown away.  The solve ends when the TRUE relative
+// residual reaches tol.
+static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2)
+{
+    const double drop = 0.1;
+    const int max_corrections = 200;
+    double anchor = 1.0;                       // true relative residual at the last replacement
+    double thr = anchor * drop > tol ? anchor * drop : tol;
+    TRY(launch_pcg_init(c, c.f, c.x, STOP_RELRES, thr, limit));
+    double rel = 1.0;
+    int corrections = 0, mv64 = 0;
+    for (;;) {
+        TRY(pull_state(c));
+        const int done = c.hst->iters;
+        if (!c.hst->stop) TRY(run_pcg(c, 32, c.x, limit - done));
+        TRY(true_relres(c, c.x, ff, &rel, dev2));
+        ++mv64;
+        if (rel <= tol || c.hst->iters >= limit || corrections >= max_corrections) break;
+        anchor = rel;
+        thr = anchor * drop > tol ? anchor * drop : 0.5 * tol;
+        TRY(launch_replace(c, thr));
+        ++corrections;
+    }
+    c.stats[0] = c.hst->iters;
+    c.stats[1] = corrections;
+    c.stats[3] = rel;
+    c.stats[4] = mv64;
+    c.stats[5] = c.hst->iters;
+    return 0;
+}
+
 extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const int *limit, const int *mode,
                         double *xnew, int *iters, double *relres)
 {
@@ -515,7 +584,8 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
     if (!r || !tol || !limit || !mode || !xnew || !iters || !c.have_km || *limit < 1 ||
-        (*mode != PF_MODE_P121 && *mode != PF_MODE_FP64_RES && *mode != PF_MODE_MIXED)) {
+        (*mode != PF_MODE_P121 && *mode != PF_MODE_FP64_RES && *mode != PF_MODE_MIXED &&
+         *mode != PF_MODE_MIXED_RESTART)) {
         set_error("pf_solve: invalid arguments or no storkm");
         return PF_FAILURE;
     }
@@ -523,7 +593,7 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    double *dev2 = c.part + 8 * (size_t)c.G;   // spare doubles after the partials
+    double *dev2 = c.scr;
     CK(cudaMemcpyAsync(c.eqbuf, r, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     TRY(launch_eq_to_slot(c, c.eqbuf, c.f));
     CK(cudaEventRecord(e0, c.stream));
@@ -537,6 +607,8 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
     }
     if (*mode == PF_MODE_MIXED) {
         rc = solve_mixed(c, *tol, *limit, ff, dev2);
+    } else if (*mode == PF_MODE_MIXED_RESTART) {
+        rc = solve_mixed_restart(c, *tol, *limit, ff, dev2);
     } else {
         rc = run_pcg(c, 64, c.x, *limit);
         c.stats[0] = c.hst->iters;
@@ -546,9 +618,11 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
     }
     if (rc) return PF_FAILURE;
     CK(cudaEventRecord(e1, c.stream));
-    double rel = 0.0;
-    TRY(true_relres(c, c.x, ff, &rel, dev2));
+    double rel = c.stats[3];
+    if (*mode == PF_MODE_P121 || *mode == PF_MODE_FP64_RES)   // mixed modes end on a true residual
+        TRY(true_relres(c, c.x, ff, &rel, dev2));
     float ms = 0.f;
+    CK(cudaEventSynchronize(e1));
     CK(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -576,7 +650,7 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (!prec || !steps || *steps < 1 || !c.have_km || (*prec != 32 && *prec != 64)) {
+    if (!prec || !steps || *steps < 1 || !c.have_km || (*prec != 32 && *prec != 31 && *prec != 64)) {
         set_error("pf_bench_iterations: invalid arguments or no storkm");
         return PF_FAILURE;
     }
@@ -601,6 +675,7 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
         CK(cudaEventRecord(ev[3 * i + 3], c.stream));
     }
     CK(cudaStreamSynchronize(c.stream));
+    TRY(check_kernel_error(c));
     double te = 0, ts = 0;
     for (int i = 0; i < n; ++i) {
         float a = 0, b = 0;
@@ -627,7 +702,7 @@ extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew
         set_error("pf_centroid_stress: invalid element or no material");
         return PF_FAILURE;
     }
-    double *sig = c.part + 8 * (size_t)c.G + 2;
+    double *sig = c.scr + 2;
     CK(cudaMemcpyAsync(c.eqbuf, xnew, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
     TRY(launch_centroid_stress(c, *iel - 1, c.rres, sig));

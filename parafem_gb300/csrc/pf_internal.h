@@ -38,7 +38,7 @@ struct Ctx {
     int nels = 0, nn = 0, neq = 0, nslots = 0;   // nslots = 3*nn (node-major dofs)
     int *conn = nullptr;        // [nels*20] 0-based node index
     int *node_ptr = nullptr;    // [nn+1] CSR of node -> (element, local node)
-    int *node_list = nullptr;   // [nels*20] e*20+a, ascending e within a node
+    int *node_list = nullptr;   // [nels*20] utemp offsets e*60+3a, ascending e within a node
     int *slot_eq = nullptr;     // [nslots] 1-based equation or 0 (restrained)
     int *eq_slot = nullptr;     // [neq] slot of equation q+1
     uint8_t *freemask = nullptr;// [nn] bit d set when dof d of the node is free
@@ -48,7 +48,9 @@ struct Ctx {
     double *mat_e = nullptr, *mat_v = nullptr;
 
     double *km64 = nullptr;     // [nels*3600] storkm(60,60,e)
-    float *km32 = nullptr;      // [nels*3600]
+    float *km32 = nullptr;      // [nels*3600] full FP32 copy
+    float *km32p = nullptr;     // [nels*1832] packed upper triangle, FP32
+    int *kerr = nullptr;        // device error word of the bulk-copy kernels (2 = wait timed out)
     bool have_km = false;
 
     double *ediag = nullptr;    // [nels*60] element diagonals
@@ -61,8 +63,13 @@ struct Ctx {
     double *eqbuf = nullptr;    // [neq] staging in equation order
     void *utemp = nullptr;      // [nels*60] doubles (element results)
 
-    int G = 0;                  // blocks of the vector kernels = partial count
-    double *part = nullptr;     // [8*G] block partials
+    int G = 0;                  // blocks of the vector kernels
+    int Gs = 0;                 // blocks of the node scatter
+    double *part = nullptr;     // [Gs + 6*G + 16] block partials, split as:
+    double *part_s = nullptr;   //   [Gs]  scatter partials (p.u or rres.rres)
+    double *part_u = nullptr;   //   [4G]  update partials (r.d, r.r, max|x|, max|dx|)
+    double *part_r = nullptr;   //   [2G]  residual-replacement partials
+    double *scr = nullptr;      //   [16]  scalars read back by the host
     PcgState *st = nullptr;     // device
     PcgState *hst = nullptr;    // pinned host mirror
 
@@ -90,8 +97,14 @@ int launch_update1(Ctx &c, double *xsol);
 int launch_update2(Ctx &c);   // update2 + the one-block finish kernel
 int launch_pcg_iteration(Ctx &c, int prec, double *xsol);
 int launch_axpy(Ctx &c, double *y, const double *xv);          // y += x
-int launch_sum_partials(Ctx &c, int nvals, double *out_dev);   // out[k] = sum part[k*G..]
+int launch_replace(Ctx &c, double tol);   // r = rres, d = diag*r, up = r.d; p kept
+int launch_sum_partials(Ctx &c, int nvals, double *out_dev);   // out[0] = sum of part_s
 int launch_centroid_stress(Ctx &c, int iel, const double *xslot, double *sig_dev);
+// prec codes of the element products: 64 FP64 storkm, 32 packed-symmetric
+// FP32 storkm (bulk-copy staged), 31 full FP32 storkm
+enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31 };
+int launch_pack_sym32(Ctx &c);
+int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);
 int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs,
                           const double *mat, double *rhs, long long *launches);
 

@@ -323,7 +323,7 @@ __global__ void k_assemble_diag(int nn, const int *__restrict__ ptr, const int *
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
-            const double *q = ed + (size_t)list[k] * 3;
+            const double *q = ed + (size_t)list[k];
             a0 += q[0];
             a1 += q[1];
             a2 += q[2];
@@ -393,7 +393,9 @@ k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
 // Node-centric scatter (SCATTER, gather_scatter.f90:694-854, one rank):
 // each node sums its (element, local node) contributions in ascending
 // element order, so the sum order equals the serial p121 SCATTER and runs
-// are bitwise reproducible without atomics.
+// are bitwise reproducible without atomics.  list[] holds the offsets
+// e*60+3a of the contributions in utemp; they are fetched eight at a time so
+// that the loads of one node are in flight together.
 //   MODE 0: out = u (restrained 0), partial p.u       (pf = p)
 //   MODE 1: out = f - u (restrained 0), partial out.out (pf = f)
 template <typename UT, int MODE>
@@ -407,11 +409,28 @@ k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         const int k1 = ptr[n + 1];
-        for (int k = ptr[n]; k < k1; ++k) {
-            const UT *q = ut + (size_t)list[k] * 3;
-            a0 += (double)q[0];
-            a1 += (double)q[1];
-            a2 += (double)q[2];
+        for (int k = ptr[n]; k < k1; k += 8) {
+            int off[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) off[i] = (k + i < k1) ? __ldg(list + k + i) : -1;
+            UT v[8][3];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (off[i] >= 0) {
+                    const UT *q = ut + off[i];
+                    v[i][0] = q[0];
+                    v[i][1] = q[1];
+                    v[i][2] = q[2];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                if (off[i] >= 0) {
+                    a0 += (double)v[i][0];
+                    a1 += (double)v[i][1];
+                    a2 += (double)v[i][2];
+                }
+            }
         }
         const int m = fm[n];
         const double a[3] = {a0, a1, a2};
@@ -485,16 +504,17 @@ __global__ void k_pcg_init2(PcgState *st, const double *__restrict__ part, int G
 }
 
 // update1: alpha = up/(p.u); xnew = x + p*alpha (in place, checon_par's
-// x = xnew, maths.f90:1062); r = r - u*alpha; d = diag*r; partials of r.d,
-// r.r, max|xnew|, max|xnew-x| into part[G..5G).  Reads st->up only.
+// x = xnew, maths.f90:1062); r = r - u*alpha; d = diag*r; block partials of
+// r.d, r.r, max|xnew|, max|xnew-x| into pu[0..4G).  p.u comes from the
+// scatter's Gs partials ps.  Reads st->up only.
 __global__ void __launch_bounds__(256)
-k_pcg_update1(int ns, const PcgState *__restrict__ st, double *__restrict__ part, int G,
-              double *__restrict__ x, double *__restrict__ r, double *__restrict__ d,
-              const double *__restrict__ p, const double *__restrict__ u,
+k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict__ ps, int Gs,
+              double *__restrict__ pu_out, int G, double *__restrict__ x, double *__restrict__ r,
+              double *__restrict__ d, const double *__restrict__ p, const double *__restrict__ u,
               const double *__restrict__ dinv)
 {
     if (block_stopped(st)) return;
-    const double pu = reduce_partials(part, G, false);
+    const double pu = reduce_partials(ps, Gs, false);
     const double alpha = st->up / pu;
     double rd = 0.0, rr = 0.0, mx = 0.0, md = 0.0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
@@ -513,10 +533,10 @@ k_pcg_update1(int ns, const PcgState *__restrict__ st, double *__restrict__ part
     double v[4] = {rd, rr, mx, md};
     block_reduce<4>(v, 0xCu);
     if (threadIdx.x == 0) {
-        part[1 * G + blockIdx.x] = v[0];
-        part[2 * G + blockIdx.x] = v[1];
-        part[3 * G + blockIdx.x] = v[2];
-        part[4 * G + blockIdx.x] = v[3];
+        pu_out[0 * G + blockIdx.x] = v[0];
+        pu_out[1 * G + blockIdx.x] = v[1];
+        pu_out[2 * G + blockIdx.x] = v[2];
+        pu_out[3 * G + blockIdx.x] = v[3];
     }
 }
 
@@ -526,7 +546,7 @@ k_pcg_update2(int ns, const PcgState *__restrict__ st, const double *__restrict_
               const double *__restrict__ d, double *__restrict__ p)
 {
     if (block_stopped(st)) return;
-    const double rd = reduce_partials(part + 1 * G, G, false);
+    const double rd = reduce_partials(part, G, false);
     const double beta = rd / st->up;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x)
         p[s] = fma(p[s], beta, d[s]);
@@ -540,10 +560,10 @@ __global__ void __launch_bounds__(256)
 k_pcg_finish(PcgState *__restrict__ st, const double *__restrict__ part, int G)
 {
     if (block_stopped(st)) return;
-    const double rd = reduce_partials(part + 1 * G, G, false);
-    const double rr = reduce_partials(part + 2 * G, G, false);
-    const double mx = reduce_partials(part + 3 * G, G, true);
-    const double md = reduce_partials(part + 4 * G, G, true);
+    const double rd = reduce_partials(part, G, false);
+    const double rr = reduce_partials(part + 1 * G, G, false);
+    const double mx = reduce_partials(part + 2 * G, G, true);
+    const double md = reduce_partials(part + 3 * G, G, true);
     if (threadIdx.x == 0) {
         const int k = st->iters + 1;
         const double metric = st->stop_mode == STOP_CHECON ? md / mx : sqrt(rr) / sqrt(st->ff);
@@ -555,6 +575,44 @@ k_pcg_finish(PcgState *__restrict__ st, const double *__restrict__ part, int G)
         st->converged = conv ? 1 : 0;
         if (!isfinite(rd) || !isfinite(mx)) st->err = 1;
         if (conv || k >= st->limit || st->err) st->stop = 1;
+    }
+}
+
+// Residual replacement (defect correction keeping the Krylov space): the
+// recursive residual is replaced by the FP64 true residual rres = f - K x;
+// d = diag*r and r.d are recomputed, the search direction p is kept.
+__global__ void __launch_bounds__(256)
+k_pcg_replace(int ns, const double *__restrict__ rres, const double *__restrict__ dinv,
+              double *__restrict__ r, double *__restrict__ d, double *__restrict__ part, int G)
+{
+    double rd = 0.0, rr = 0.0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const double rv = rres[s];
+        const double dv = dinv[s] * rv;
+        r[s] = rv;
+        d[s] = dv;
+        rd = fma(rv, dv, rd);
+        rr = fma(rv, rv, rr);
+    }
+    double v[2] = {rd, rr};
+    block_reduce<2>(v, 0u);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = v[0];
+        part[G + blockIdx.x] = v[1];
+    }
+}
+
+__global__ void k_pcg_replace2(PcgState *st, const double *__restrict__ part, int G, double tol)
+{
+    const double rd = reduce_partials(part, G, false);
+    const double rr = reduce_partials(part + G, G, false);
+    if (threadIdx.x == 0) {
+        st->up = rd;
+        st->rr = rr;
+        st->metric = sqrt(rr) / sqrt(st->ff);
+        st->tol = tol;
+        st->converged = 0;
+        st->stop = (rr == 0.0) ? 1 : 0;
     }
 }
 
@@ -710,8 +768,9 @@ int launch_slot_to_eq(Ctx &c, const double *slot, double *eq)
 
 int launch_elem(Ctx &c, int prec, const double *p)
 {
+    if (prec == PREC_FP32_SYM) return launch_elem_sym32(c, p, c.st);
     const int grid = grid_for(c, c.nels, 8, 8);
-    if (prec == 32) {
+    if (prec == PREC_FP32_FULL) {
         k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, c.st);
     } else {
         k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, p, (double *)c.utemp, c.st);
@@ -722,20 +781,20 @@ int launch_elem(Ctx &c, int prec, const double *p)
 int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
 {
     const PcgState *st = mode == 0 ? c.st : nullptr;
-    if (prec == 32) {
+    if (prec != PREC_FP64) {
         if (mode == 0)
-            k_scatter<float, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
-                                                           c.freemask, pf, out, c.part, st);
+            k_scatter<float, 0><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
+                                                            c.freemask, pf, out, c.part_s, st);
         else
-            k_scatter<float, 1><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
-                                                           c.freemask, pf, out, c.part, st);
+            k_scatter<float, 1><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
+                                                            c.freemask, pf, out, c.part_s, st);
     } else {
         if (mode == 0)
-            k_scatter<double, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
-                                                            c.freemask, pf, out, c.part, st);
+            k_scatter<double, 0><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                             c.freemask, pf, out, c.part_s, st);
         else
-            k_scatter<double, 1><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
-                                                            c.freemask, pf, out, c.part, st);
+            k_scatter<double, 1><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                             c.freemask, pf, out, c.part_s, st);
     }
     return check_launch(c, "k_scatter");
 }
@@ -744,17 +803,21 @@ int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
 int launch_matvec(Ctx &c, int prec, const double *p, double *u)
 {
     const int grid = grid_for(c, c.nels, 8, 8);
-    if (prec == 32)
-        k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, nullptr);
+    if (prec == PREC_FP32_SYM) {
+        if (launch_elem_sym32(c, p, nullptr)) return 1;
+    } else {
+        if (prec == PREC_FP32_FULL)
+            k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, nullptr);
+        else
+            k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, p, (double *)c.utemp, nullptr);
+        if (check_launch(c, "k_elem")) return 1;
+    }
+    if (prec != PREC_FP64)
+        k_scatter<float, 0><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
+                                                        c.freemask, p, u, c.part_s, nullptr);
     else
-        k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, p, (double *)c.utemp, nullptr);
-    if (check_launch(c, "k_elem")) return 1;
-    if (prec == 32)
-        k_scatter<float, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const float *)c.utemp,
-                                                       c.freemask, p, u, c.part, nullptr);
-    else
-        k_scatter<double, 0><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
-                                                        c.freemask, p, u, c.part, nullptr);
+        k_scatter<double, 0><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                         c.freemask, p, u, c.part_s, nullptr);
     return check_launch(c, "k_scatter");
 }
 
@@ -763,30 +826,31 @@ int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
     const int grid = grid_for(c, c.nels, 8, 8);
     k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, x, (double *)c.utemp, nullptr);
     if (check_launch(c, "k_elem")) return 1;
-    k_scatter<double, 1><<<c.G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
-                                                    c.freemask, f, rres, c.part, nullptr);
+    k_scatter<double, 1><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                     c.freemask, f, rres, c.part_s, nullptr);
     return check_launch(c, "k_scatter");
 }
 
 int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit)
 {
-    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part, c.G);
+    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G);
     if (check_launch(c, "k_pcg_init")) return 1;
-    k_pcg_init2<<<1, 256, 0, c.stream>>>(c.st, c.part, c.G, stop_mode, tol, limit);
+    k_pcg_init2<<<1, 256, 0, c.stream>>>(c.st, c.part_u, c.G, stop_mode, tol, limit);
     return check_launch(c, "k_pcg_init2");
 }
 
 int launch_update1(Ctx &c, double *xsol)
 {
-    k_pcg_update1<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part, c.G, xsol, c.r, c.d, c.p, c.u, c.dinv);
+    k_pcg_update1<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_s, c.Gs, c.part_u, c.G, xsol, c.r, c.d, c.p,
+                                             c.u, c.dinv);
     return check_launch(c, "k_pcg_update1");
 }
 
 int launch_update2(Ctx &c)
 {
-    k_pcg_update2<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part, c.G, c.d, c.p);
+    k_pcg_update2<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_u, c.G, c.d, c.p);
     if (check_launch(c, "k_pcg_update2")) return 1;
-    k_pcg_finish<<<1, 256, 0, c.stream>>>(c.st, c.part, c.G);
+    k_pcg_finish<<<1, 256, 0, c.stream>>>(c.st, c.part_u, c.G);
     return check_launch(c, "k_pcg_finish");
 }
 
@@ -804,9 +868,17 @@ int launch_axpy(Ctx &c, double *y, const double *xv)
     return check_launch(c, "k_axpy");
 }
 
+int launch_replace(Ctx &c, double tol)
+{
+    k_pcg_replace<<<c.G, 256, 0, c.stream>>>(c.nslots, c.rres, c.dinv, c.r, c.d, c.part_r, c.G);
+    if (check_launch(c, "k_pcg_replace")) return 1;
+    k_pcg_replace2<<<1, 256, 0, c.stream>>>(c.st, c.part_r, c.G, tol);
+    return check_launch(c, "k_pcg_replace2");
+}
+
 int launch_sum_partials(Ctx &c, int nvals, double *out_dev)
 {
-    k_sum_partials<<<1, 256, 0, c.stream>>>(c.part, c.G, nvals, out_dev);
+    k_sum_partials<<<1, 256, 0, c.stream>>>(c.part_s, c.Gs, nvals, out_dev);
     return check_launch(c, "k_sum_partials");
 }
 

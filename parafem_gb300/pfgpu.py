@@ -22,6 +22,7 @@ from . import _build
 MODE_P121 = 0
 MODE_FP64_RES = 1
 MODE_MIXED = 2
+MODE_MIXED_RESTART = 3
 FORM_EXACT_WEIGHTS = 1
 
 _I = ctypes.c_int

@@ -73,8 +73,9 @@ def test_diag_bitwise_equals_serial_scatter(demo_problem):
     assert np.array_equal(dg, p["diag"])
 
 
-@pytest.mark.parametrize("prec,tol", [(64, 1e-13), (32, 3e-6)])
+@pytest.mark.parametrize("prec,tol", [(64, 1e-13), (32, 3e-6), (31, 3e-6)])
 def test_ebe_matvec_matches_oracle(demo_problem, prec, tol):
+    """64: FP64 storkm; 32: packed-symmetric FP32 (bulk-copy staged); 31: full FP32."""
     p = demo_problem
     d = p["deck"]
     rng = np.random.default_rng(3)
@@ -177,6 +178,33 @@ def test_mixed_precision_reaches_1e8_and_matches_fp64(hetero):
     # at the same residual the mixed solution is as accurate as the FP64 one
     assert errm <= max(1e-7, 3.0 * err64), (errm, err64)
     assert np.linalg.norm(xt - xr) <= 1e-7 * nrm
+
+
+def test_packed_symmetric_product_is_symmetric_and_deterministic(demo_problem):
+    p = demo_problem
+    d = p["deck"]
+    rng = np.random.default_rng(8)
+    a, b = rng.standard_normal(p["neq"]), rng.standard_normal(p["neq"])
+    with P.Solver() as s:
+        s.setup(d.g_num, p["g_g"], p["gc"], d.nn, p["neq"])
+        s.set_storkm(p["km"])
+        ka, kb = s.ebe_matvec(a, 32), s.ebe_matvec(b, 32)
+        ka2 = s.ebe_matvec(a, 32)
+    assert np.array_equal(ka, ka2)
+    # the packed operator is exactly symmetric up to FP32 rounding of the products
+    assert abs(b @ ka - a @ kb) <= 1e-6 * abs(b @ ka)
+
+
+def test_mixed_restart_mode_also_converges():
+    prob = P.cube_problem(6, 6, 6)
+    with P.Solver() as s:
+        s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+        s.set_material(100.0, 0.3)
+        s.form_storkm(27)
+        xr, _, _ = s.solve(prob["r"], 1e-12, 20000, P.MODE_FP64_RES)
+        x3, it3, rel3 = s.solve(prob["r"], 1e-8, 20000, P.MODE_MIXED_RESTART)
+    assert rel3 <= 1e-8
+    assert np.linalg.norm(x3 - xr) <= 1e-6 * np.linalg.norm(xr)
 
 
 def test_xx3_matrix_vector_multiplies():
