@@ -135,6 +135,34 @@ int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *s
 /* Number of kernels this library launched since the context was created. */
 int pf_kernel_launches(void **ctx, long long *count);
 
+/* ---------------------------------------------------------------------- */
+/* Serving layer: continuous batching of many independent solves.  No
+ * counterpart in the reference (p121 solves one mesh per run); every solve
+ * is p121's Jacobi-PCG on FP64 storkm to ||r||2/||f||2 <= tol.            */
+
+#define PF_BUSY 2   /* pf_batch_admit: no room yet; retry after a sync */
+
+/* A batch on one device with a fixed device-memory budget (bytes) for its
+ * arenas and at most max_meshes solves resident at once. */
+int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes, void **batch);
+int pf_batch_destroy(void **batch);
+/* Arena capacity in elements and nodes. */
+int pf_batch_capacity(void **batch, long long *elements, long long *nodes);
+/* Admits one solve (arrays as pf_setup / pf_set_material, r in equation
+ * order).  Returns PF_SUCCESS and its id, PF_BUSY when it does not fit yet,
+ * or PF_FAILURE.  Its storkm is formed on the GPU behind the running work. */
+int pf_batch_admit(void **batch, const int *nels, const int *nn, const int *neq, const int *g_num,
+                   const int *g_g, const double *g_coord, const int *nmat, const double *e, const double *v,
+                   const int *nip, const double *r, const double *tol, const int *limit, int *id);
+/* Enqueues `iters` PCG iterations of every resident solve and returns. */
+int pf_batch_launch(void **batch, const int *iters);
+/* Waits for the enqueued work and retires converged solves. */
+int pf_batch_sync(void **batch, int *n_active, int *n_done);
+/* Pops one retired solve: id, iterations, FP64 true relative residual and
+ * x (neq values; x_cap = capacity of x). */
+int pf_batch_collect(void **batch, int *id, int *iters, double *relres, double *x, const int *x_cap, int *neq);
+int pf_batch_launches(void **batch, long long *count);
+
 /* No counterpart in the reference.  u(neq) = K p for callers that cannot
  * allocate device memory while they run (memory reserved up front by a pool
  * or a host framework, cudaMalloc forbidden in the solve phase, or a fixed

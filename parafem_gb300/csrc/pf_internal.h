@@ -79,6 +79,10 @@ struct Ctx {
 
 // Kernel launchers (pf_kernels.cu).  All run on ctx.stream and count launches.
 int launch_form_storkm(Ctx &c, int nip, bool exact_weights, bool keep32);
+int launch_sample(cudaStream_t stream, int nip, bool exact_weights, double *gp);
+int launch_form_storkm_raw(cudaStream_t stream, int nsm, int nels, int nip, const double *gp,
+                           const double *coord, const double *me, const double *mv, int nmat, double *km64,
+                           float *km32, double *ediag);
 int launch_cast_km32(Ctx &c);
 int launch_assemble_diag(Ctx &c);
 int launch_eq_to_slot(Ctx &c, const double *eq, double *slot);

@@ -58,6 +58,15 @@ _SIGS = {
     "pf_kernel_launches": [_VPP, _LLP],
     "pf_ebe_matvec_noalloc": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p],
+    "pf_batch_create": [_IP, _LLP, _IP, _VPP],
+    "pf_batch_destroy": [_VPP],
+    "pf_batch_capacity": [_VPP, _LLP, _LLP],
+    "pf_batch_admit": [_VPP, _IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP,
+                       ctypes.c_void_p, ctypes.c_void_p, _IP, ctypes.c_void_p, _DP, _IP, _IP],
+    "pf_batch_launch": [_VPP, _IP],
+    "pf_batch_sync": [_VPP, _IP, _IP],
+    "pf_batch_collect": [_VPP, _IP, _IP, _DP, ctypes.c_void_p, _IP, _IP],
+    "pf_batch_launches": [_VPP, _LLP],
     "pf_p12meshgen": [ctypes.c_char_p],
     "pf_p121_run": [ctypes.c_char_p, _IP, _IP, _IP, _DP],
     "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
@@ -280,6 +289,95 @@ class Solver:
         n = ctypes.c_longlong(0)
         _check(lib().pf_kernel_launches(self._ref, ctypes.byref(n)), "pf_kernel_launches")
         return n.value
+
+
+PF_BUSY = 2
+
+
+class Batch:
+    """Continuous-batching engine (pf_batch_*): many solves resident at once,
+    admitted by a device-memory budget, retired when converged."""
+
+    def __init__(self, budget_bytes: int, max_meshes: int = 256, device: int = 0):
+        self._h = ctypes.c_void_p(None)
+        _check(lib().pf_batch_create(_i(device), ctypes.byref(ctypes.c_longlong(int(budget_bytes))),
+                                     _i(max_meshes), ctypes.byref(self._h)), "pf_batch_create")
+
+    @property
+    def _ref(self):
+        if not self._h.value:
+            raise PfError("batch is closed")
+        return ctypes.byref(self._h)
+
+    def close(self):
+        if self._h.value:
+            lib().pf_batch_destroy(ctypes.byref(self._h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def capacity(self):
+        a, b = ctypes.c_longlong(0), ctypes.c_longlong(0)
+        _check(lib().pf_batch_capacity(self._ref, ctypes.byref(a), ctypes.byref(b)), "pf_batch_capacity")
+        return a.value, b.value
+
+    def admit(self, g_num, g_g, g_coord, nn, neq, e, v, r, tol=1e-8, limit=20000, nip=27):
+        """Returns the solve id, or None when the budget is full right now."""
+        g_num, pn = _arr(g_num, np.int32)
+        g_g, pg = _arr(g_g, np.int32)
+        g_coord, pc = _arr(g_coord, np.float64)
+        e, pe = _arr(np.atleast_1d(e), np.float64)
+        v, pv = _arr(np.atleast_1d(v), np.float64)
+        r, pr = _arr(r, np.float64)
+        sid = ctypes.c_int(-1)
+        rc = lib().pf_batch_admit(self._ref, _i(g_num.shape[0]), _i(nn), _i(neq), pn, pg, pc, _i(e.size), pe, pv,
+                                  _i(nip), pr, _d(tol), _i(limit), ctypes.byref(sid))
+        if rc == PF_BUSY:
+            return None
+        _check(rc, "pf_batch_admit")
+        return sid.value
+
+    def launch(self, iters: int):
+        _check(lib().pf_batch_launch(self._ref, _i(iters)), "pf_batch_launch")
+
+    def sync(self):
+        a, d = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().pf_batch_sync(self._ref, ctypes.byref(a), ctypes.byref(d)), "pf_batch_sync")
+        return a.value, d.value
+
+    def collect(self, x_cap: int):
+        sid, it, neq = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+        rel = ctypes.c_double(0.0)
+        x = np.zeros(max(int(x_cap), 1))
+        _check(lib().pf_batch_collect(self._ref, ctypes.byref(sid), ctypes.byref(it), ctypes.byref(rel),
+                                      x.ctypes.data, _i(x.size), ctypes.byref(neq)), "pf_batch_collect")
+        return sid.value, it.value, rel.value, x[:neq.value].copy()
+
+    def launches(self) -> int:
+        n = ctypes.c_longlong(0)
+        _check(lib().pf_batch_launches(self._ref, ctypes.byref(n)), "pf_batch_launches")
+        return n.value
+
+    def run_all(self, x_cap: int, chunk: int = 8):
+        """Iterates until every resident solve has retired; returns the results."""
+        out = {}
+        while True:
+            self.launch(chunk)
+            active, done = self.sync()
+            for _ in range(done):
+                sid, it, rel, x = self.collect(x_cap)
+                out[sid] = (it, rel, x)
+            if active == 0:
+                return out
 
 
 def cube_problem(nxe, nye, nze, bc=1, pressure=None, aa=1.0, bb=1.0, cc=1.0):

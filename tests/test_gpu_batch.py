@@ -1,0 +1,83 @@
+"""Continuous batching (pf_batch_*): each result is the same alone and in the
+mix, agrees with the single-mesh solver, and admission respects the budget."""
+import numpy as np
+import pytest
+
+import parafem_gb300 as P
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [  # (nxe, nye, nze, E seed, pressure)
+    (3, 4, 2, 1, 1.0),
+    (5, 3, 3, 2, 0.7),
+    (4, 4, 4, 3, 1.6),
+    (2, 6, 3, 4, 1.2),
+]
+
+
+def request(spec):
+    nxe, nye, nze, seed, pres = spec
+    prob = P.cube_problem(nxe, nye, nze, pressure=pres)
+    nels = nxe * nye * nze
+    e, v = P.random_material(nels, seed, 10.0, 1000.0, 0.2, 0.35)
+    return prob, e, v
+
+
+def admit(b, prob, e, v, tol=1e-9):
+    return b.admit(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"], e, v, prob["r"], tol=tol)
+
+
+def test_same_alone_and_in_the_mix():
+    reqs = [request(sp) for sp in SPECS]
+    cap = max(p["neq"] for p, _, _ in reqs)
+    alone = []
+    for prob, e, v in reqs:
+        with P.Batch(2 << 30, 8) as b:
+            sid = admit(b, prob, e, v)
+            res = b.run_all(cap)
+            alone.append(res[sid])
+    with P.Batch(2 << 30, 8) as b:
+        ids = [admit(b, *r) for r in reqs[:2]]
+        b.launch(5)                       # two solves iterate ...
+        b.sync()
+        ids += [admit(b, *r) for r in reqs[2:]]   # ... while two more arrive
+        res = b.run_all(cap, chunk=3)
+    for k, sid in enumerate(ids):
+        it_a, rel_a, x_a = alone[k]
+        it_m, rel_m, x_m = res[sid]
+        assert it_a == it_m
+        assert np.array_equal(x_a, x_m)          # bitwise: per-mesh reduction order
+        assert rel_m <= 1e-9
+
+
+def test_batch_matches_single_solver():
+    prob, e, v = request(SPECS[2])
+    with P.Solver() as s:
+        s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+        s.set_material(e, v)
+        s.form_storkm(27)
+        x_ref, it_ref, rel_ref = s.solve(prob["r"], 1e-9, 20000, P.MODE_FP64_RES)
+    with P.Batch(1 << 30, 4) as b:
+        sid = admit(b, prob, e, v)
+        it, rel, x = b.run_all(prob["neq"])[sid]
+    assert abs(it - it_ref) <= 3
+    assert np.linalg.norm(x - x_ref) <= 1e-7 * np.linalg.norm(x_ref)
+    assert rel <= 1e-9
+
+
+def test_admission_is_bounded_by_the_budget():
+    prob, e, v = request(SPECS[2])        # 64 elements
+    with P.Batch(64 * 32_000 * 2 + (1 << 20), 16) as b:   # room for about two such meshes
+        cap_el, _ = b.capacity()
+        admitted = []
+        for _ in range(6):
+            sid = admit(b, prob, e, v)
+            if sid is None:
+                break
+            admitted.append(sid)
+        assert 1 <= len(admitted) < 6
+        assert len(admitted) * 64 <= cap_el
+        res = b.run_all(prob["neq"])
+        assert sorted(res) == admitted
+        # retired solves freed their ranges: the next request fits again
+        assert admit(b, prob, e, v) is not None
