@@ -59,35 +59,43 @@ def parse_args():
 
 
 # ---------------------------------------------------------------------------
+_BACKEND = "nccl"
+
+
 def dist_init(n_gpus):
+    """torch.distributed for N > 1 replicas (one process per GPU).  The
+    backend is NCCL; PF_DIST_BACKEND=gloo runs the same aggregation on CPU."""
+    global _BACKEND
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        _BACKEND = os.environ.get("PF_DIST_BACKEND", "nccl")
+        if _BACKEND == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(_BACKEND)
         return rank, world, local, dist
     return 0, 1, 0, None
 
 
-def dist_max(dist, local, v):
-    if dist is None:
-        return v
+def _reduce(dist, local, v, op):
     import torch
-    t = torch.tensor([float(v)], device=f"cuda:{local}", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = f"cuda:{local}" if _BACKEND == "nccl" else "cpu"
+    t = torch.tensor([float(v)], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def dist_max(dist, local, v):
+    """Max over ranks (the slowest replica's time)."""
+    return v if dist is None else _reduce(dist, local, v, dist.ReduceOp.MAX)
 
 
 def dist_sum(dist, local, v):
-    if dist is None:
-        return v
-    import torch
-    t = torch.tensor([float(v)], device=f"cuda:{local}", dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    """Sum over ranks (the units all replicas processed)."""
+    return v if dist is None else _reduce(dist, local, v, dist.ReduceOp.SUM)
 
 
 def barrier(dist):
