@@ -46,7 +46,7 @@ def parse_args():
     ap.add_argument("--size", type=int, default=100, help="elements per cube edge")
     ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--workload", default="cube100", choices=["cube100", "hetero80", "serving"],
+    ap.add_argument("--workload", default="cube100", choices=["cube100", "hetero80", "serving", "multirhs60"],
                     help="cube100: the headline; hetero80: per-element E and v, accuracy study; "
                          "serving: continuous batching of a Poisson request stream")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
@@ -490,6 +490,53 @@ def run_serving(args, rank, world, local, dist):
     return 0
 
 
+def run_multirhs(args, rank, world, local, dist):
+    """60^3 cube, E=100, v=0.3, 16 load cases of i.i.d. N(0,1) vertical forces
+    on the top-face nodes (seeded): the block solve with tensor-core products
+    against 16 sequential FP64 solves, all to relres 1e-8."""
+    import parafem_gb300 as P
+    n = args.size if args.size != 100 else 60
+    prob = P.cube_problem(n, n, n)
+    s = P.Solver(local)
+    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+    s.set_material(100.0, 0.3)
+    s.form_storkm(27)
+    neq = prob["neq"]
+    R = P.random_top_loads(prob["g_g"], n, n, neq, 16, args.seed)
+    out = {}
+    for prec, name in ((16, "block_tensor_cores"), (32, "block_fp32_cuda_cores")):
+        t0 = time.perf_counter()
+        X, it, rel = s.solve_multi(R, 1e-8, 50000, prec)
+        out[name] = {"wall_s": time.perf_counter() - t0, "device_s": s.stats()["solve_ms"] / 1e3,
+                     "max_iters": int(it.max()), "mean_iters": float(it.mean()), "max_relres": float(rel.max()),
+                     "corrections": s.stats()["outer"]}
+        if prec == 16:
+            Xtc = X
+    t0 = time.perf_counter()
+    errs, its = [], []
+    for j in range(16):
+        x64, it64, rel64 = s.solve(R[:, j], 1e-8, 50000, P.MODE_FP64_RES)
+        errs.append(float(np.linalg.norm(Xtc[:, j] - x64) / np.linalg.norm(x64)))
+        its.append(it64)
+    out["sequential_fp64"] = {"wall_s": time.perf_counter() - t0, "mean_iters": float(np.mean(its)),
+                              "max_iters": int(max(its))}
+    out["block_vs_fp64_rel_err_2_max"] = max(errs)
+    out["speedup_block_tc_vs_sequential_fp64"] = out["sequential_fp64"]["wall_s"] / out["block_tensor_cores"]["wall_s"]
+    s.close()
+    value = neq * 16 * out["block_tensor_cores"]["mean_iters"] / out["block_tensor_cores"]["device_s"]
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": out["block_tensor_cores"]["device_s"] * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3 tensor-core products, f32 accumulation / f64 vectors and reductions",
+            "data": "synthetic",
+            "config": {"workload": f"multi-RHS {n}^3 hex20 cube, E 100, v 0.3, 16 load cases N(0,1) on top-face "
+                                   f"nodes (seed {args.seed}), nip 27, tol 1e-8", "neq": neq, "cases": 16},
+            "multirhs": out}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse_args()
     rank, world, local, dist = dist_init(args.gpus)
@@ -500,6 +547,8 @@ def main():
             return run_hetero(args, rank, world, local, dist)
         if args.workload == "serving":
             return run_serving(args, rank, world, local, dist)
+        if args.workload == "multirhs60":
+            return run_multirhs(args, rank, world, local, dist)
         return run_gb300(args, rank, world, local, dist)
     finally:
         if dist is not None:

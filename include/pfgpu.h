@@ -136,6 +136,25 @@ int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *s
 int pf_kernel_launches(void **ctx, long long *count);
 
 /* ---------------------------------------------------------------------- */
+/* Several load cases of one mesh (block PCG).  No counterpart in p121
+ * (one load case per run); the shared-matrix products follow the idea of
+ * xx9's batched MATMUL (src/programs/dev/xx9/mathsgpu.f90:479).          */
+
+/* k = 16 independent solves K x_j = r_j that share every element-matrix
+ * read: r and xnew are (neq, k) column-major; iters and relres hold k
+ * values (relres: FP64 true residual).  prec 16: block products on the
+ * tensor cores (tcgen05, three-term BF16 splits, FP32 accumulation);
+ * 32: the same products on CUDA cores in FP32.  FP64 vectors, dots and
+ * alpha/beta; FP64 residual replacement as PF_MODE_MIXED. */
+int pf_solve_multi(void **ctx, const int *k, const double *r, const double *tol, const int *limit,
+                   const int *prec, double *xnew, int *iters, double *relres);
+/* Block product U = K P for k = 16 cases (equation order, (neq,k)
+ * column-major); prec 16 (tensor cores), 32 (FP32 CUDA cores), 64 (FP64). */
+int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, const double *p, double *u);
+/* Releases the block solver's device buffers. */
+int pf_multi_free(void);
+
+/* ---------------------------------------------------------------------- */
 /* Serving layer: continuous batching of many independent solves.  No
  * counterpart in the reference (p121 solves one mesh per run); every solve
  * is p121's Jacobi-PCG on FP64 storkm to ||r||2/||f||2 <= tol.            */

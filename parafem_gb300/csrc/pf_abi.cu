@@ -358,7 +358,7 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
     for (size_t e = 0; e < (size_t)nels; ++e)
         for (int a = 0; a < 20; ++a) {
             const int n = conn[e * 20 + a];
-            list[fill[n]++] = (int)(e * 60 + 3 * a);   // offset of the contribution in utemp
+            list[fill[n]++] = (int)(e * 20 + a);   // contribution index: element e, local node a
         }
 
     c.nels = nels; c.nn = nn; c.neq = neq; c.nslots = ns;

@@ -8,7 +8,7 @@
 // HBM stream of an iteration (the idea of xx16's packed DSPMV storage,
 // src/programs/dev/xx16/xx16.f90:393-459).
 //
-// Kernel structure (one persistent CTA of 8 warps per SM):
+// Kernel structure (one persistent CTA of 14 warps per SM):
 //   * every warp owns a ring of NSTAGE shared-memory stages with one
 //     mbarrier each; lane 0 issues cp.async.bulk of the next elements'
 //     packed blocks into the ring (complete_tx on the stage's mbarrier);
@@ -29,8 +29,8 @@ namespace pf {
 
 namespace {
 
-constexpr int kWarps = 8;
-constexpr int kStages = 3;
+constexpr int kWarps = 14;   // 14 warps x 2 stages x 7,328 B = 205 KB of stages per CTA
+constexpr int kStages = 2;
 constexpr int kPacked = 1832;                 // floats per element (1830 + 2 pad)
 constexpr int kPackedBytes = kPacked * 4;     // 7328
 constexpr unsigned kFull = 0xffffffffu;
@@ -117,6 +117,7 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
     float *pslot = reinterpret_cast<float *>(smem + (size_t)kWarps * kStages * kPackedBytes) + w * 64;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kWarps * kStages * kPackedBytes +
                                                  kWarps * 64 * 4) + w * kStages;
+    static_assert((kWarps * kStages * kPackedBytes + kWarps * 64 * 4) % 8 == 0, "mbarrier alignment");
 
     // stop flag: uniform per warp (no block barrier after this point)
     int stopped = 0;
@@ -198,9 +199,9 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
                 ia += (j < ra) ? 1 : j + 1;   // T(ra)+j -> T(ra)+j+1, then T(j)+ra -> T(j+1)+ra
                 ib += (j < rb) ? 1 : j + 1;
             }
-            float *o = ut + (size_t)elem(k) * 60;
-            o[ra] = acc_a;
-            o[rb] = acc_b;
+            float *o = ut + (size_t)elem(k) * 80;   // node-padded: row i at (i/3)*4 + i%3
+            o[(ra / 3) * 4 + ra % 3] = acc_a;
+            o[(rb / 3) * 4 + rb % 3] = acc_b;
         }
         __syncwarp();   // every lane is done with stage s and the p slot
         if (lane == 0 && k + kStages < nmine) {

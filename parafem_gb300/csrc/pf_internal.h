@@ -38,7 +38,7 @@ struct Ctx {
     int nels = 0, nn = 0, neq = 0, nslots = 0;   // nslots = 3*nn (node-major dofs)
     int *conn = nullptr;        // [nels*20] 0-based node index
     int *node_ptr = nullptr;    // [nn+1] CSR of node -> (element, local node)
-    int *node_list = nullptr;   // [nels*20] utemp offsets e*60+3a, ascending e within a node
+    int *node_list = nullptr;   // [nels*20] contribution indices e*20+a, ascending e within a node
     int *slot_eq = nullptr;     // [nslots] 1-based equation or 0 (restrained)
     int *eq_slot = nullptr;     // [neq] slot of equation q+1
     uint8_t *freemask = nullptr;// [nn] bit d set when dof d of the node is free
@@ -61,7 +61,9 @@ struct Ctx {
     double *f = nullptr, *x = nullptr, *c = nullptr, *r = nullptr, *d = nullptr,
            *p = nullptr, *u = nullptr, *rres = nullptr;
     double *eqbuf = nullptr;    // [neq] staging in equation order
-    void *utemp = nullptr;      // [nels*60] doubles (element results)
+    void *utemp = nullptr;      // element results: FP64 [nels][60], or FP32 [nels][20][4]
+                                //   (x, y, z of each local node padded to 16 bytes)
+    int stop_mode = 0;          // stopping test of the PCG run in flight
 
     int G = 0;                  // blocks of the vector kernels
     int Gs = 0;                 // blocks of the node scatter

@@ -191,7 +191,7 @@ __global__ void k_assemble_diag(int nn, const int *__restrict__ ptr, const int *
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
         for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
-            const double *q = ed + (size_t)list[k];
+            const double *q = ed + (size_t)list[k] * 3;
             a0 += q[0];
             a1 += q[1];
             a2 += q[2];
@@ -250,10 +250,16 @@ k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
             }
         }
         if (lane < 30) {
-            V2 o;
-            o.x = a0;
-            o.y = a1;
-            reinterpret_cast<V2 *>(ut + (size_t)e * 60)[lane] = o;
+            if constexpr (sizeof(KT) == 4) {   // FP32 results, node-padded: row i at (i/3)*4 + i%3
+                const int i0 = 2 * lane, i1 = 2 * lane + 1;
+                ut[(size_t)e * 80 + (i0 / 3) * 4 + i0 % 3] = a0;
+                ut[(size_t)e * 80 + (i1 / 3) * 4 + i1 % 3] = a1;
+            } else {
+                V2 o;
+                o.x = a0;
+                o.y = a1;
+                reinterpret_cast<V2 *>(ut + (size_t)e * 60)[lane] = o;
+            }
         }
     }
 }
@@ -261,9 +267,12 @@ k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
 // Node-centric scatter (SCATTER, gather_scatter.f90:694-854, one rank):
 // each node sums its (element, local node) contributions in ascending
 // element order, so the sum order equals the serial p121 SCATTER and runs
-// are bitwise reproducible without atomics.  list[] holds the offsets
-// e*60+3a of the contributions in utemp; they are fetched eight at a time so
-// that the loads of one node are in flight together.
+// are bitwise reproducible without atomics.  list[] holds contribution
+// indices e*20+a.  FP64 results are read as three doubles at (e*20+a)*3;
+// FP32 results are node-padded, so one 16-byte load fetches a contribution,
+// and they are summed in FP32 (the precision of the products themselves).
+// Contributions are fetched eight at a time so that a node's loads are in
+// flight together.
 //   MODE 0: out = u (restrained 0), partial p.u       (pf = p)
 //   MODE 1: out = f - u (restrained 0), partial out.out (pf = f)
 template <typename UT, int MODE>
@@ -275,33 +284,45 @@ k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
     if (block_stopped(st)) return;
     double loc = 0.0;
     for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        UT a0 = 0, a1 = 0, a2 = 0;
         const int k1 = ptr[n + 1];
         for (int k = ptr[n]; k < k1; k += 8) {
-            int off[8];
+            int ci[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) off[i] = (k + i < k1) ? __ldg(list + k + i) : -1;
-            UT v[8][3];
+            for (int i = 0; i < 8; ++i) ci[i] = (k + i < k1) ? __ldg(list + k + i) : -1;
+            if constexpr (sizeof(UT) == 4) {
+                float4 v[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                if (off[i] >= 0) {
-                    const UT *q = ut + off[i];
-                    v[i][0] = q[0];
-                    v[i][1] = q[1];
-                    v[i][2] = q[2];
-                }
-            }
+                for (int i = 0; i < 8; ++i)
+                    if (ci[i] >= 0) v[i] = __ldg(reinterpret_cast<const float4 *>(ut) + ci[i]);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                if (off[i] >= 0) {
-                    a0 += (double)v[i][0];
-                    a1 += (double)v[i][1];
-                    a2 += (double)v[i][2];
-                }
+                for (int i = 0; i < 8; ++i)
+                    if (ci[i] >= 0) {
+                        a0 += v[i].x;
+                        a1 += v[i].y;
+                        a2 += v[i].z;
+                    }
+            } else {
+                double v[8][3];
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (ci[i] >= 0) {
+                        const double *q = ut + (size_t)ci[i] * 3;
+                        v[i][0] = q[0];
+                        v[i][1] = q[1];
+                        v[i][2] = q[2];
+                    }
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (ci[i] >= 0) {
+                        a0 += v[i][0];
+                        a1 += v[i][1];
+                        a2 += v[i][2];
+                    }
             }
         }
         const int m = fm[n];
-        const double a[3] = {a0, a1, a2};
+        const double a[3] = {(double)a0, (double)a1, (double)a2};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const size_t s = (size_t)3 * n + d;
@@ -373,8 +394,11 @@ __global__ void k_pcg_init2(PcgState *st, const double *__restrict__ part, int G
 
 // update1: alpha = up/(p.u); xnew = x + p*alpha (in place, checon_par's
 // x = xnew, maths.f90:1062); r = r - u*alpha; d = diag*r; block partials of
-// r.d, r.r, max|xnew|, max|xnew-x| into pu[0..4G).  p.u comes from the
-// scatter's Gs partials ps.  Reads st->up only.
+// r.d, r.r and, for checon_par only (CHECON), max|xnew| and max|xnew-x|,
+// into pu[0..4G).  p.u comes from the scatter's Gs partials ps.  Reads
+// st->up only.  The max terms cost four FP64 operations per dof, a slow pipe
+// on GB300, so the residual-stopped runs skip them.
+template <bool CHECON>
 __global__ void __launch_bounds__(256)
 k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict__ ps, int Gs,
               double *__restrict__ pu_out, int G, double *__restrict__ x, double *__restrict__ r,
@@ -389,8 +413,10 @@ k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict_
         const double xo = x[s];
         const double xn = fma(p[s], alpha, xo);
         x[s] = xn;
-        mx = fmax(mx, fabs(xn));
-        md = fmax(md, fabs(xn - xo));
+        if (CHECON) {
+            mx = fmax(mx, fabs(xn));
+            md = fmax(md, fabs(xn - xo));
+        }
         const double rn = fma(-u[s], alpha, r[s]);
         r[s] = rn;
         const double dn = dinv[s] * rn;
@@ -430,11 +456,12 @@ k_pcg_finish(PcgState *__restrict__ st, const double *__restrict__ part, int G)
     if (block_stopped(st)) return;
     const double rd = reduce_partials(part, G, false);
     const double rr = reduce_partials(part + 1 * G, G, false);
-    const double mx = reduce_partials(part + 2 * G, G, true);
-    const double md = reduce_partials(part + 3 * G, G, true);
+    const bool checon = st->stop_mode == STOP_CHECON;   // uniform: written only by init kernels
+    const double mx = checon ? reduce_partials(part + 2 * G, G, true) : 1.0;
+    const double md = checon ? reduce_partials(part + 3 * G, G, true) : 0.0;
     if (threadIdx.x == 0) {
         const int k = st->iters + 1;
-        const double metric = st->stop_mode == STOP_CHECON ? md / mx : sqrt(rr) / sqrt(st->ff);
+        const double metric = checon ? md / mx : sqrt(rr) / sqrt(st->ff);
         const bool conv = metric <= st->tol;
         st->up = rd;
         st->iters = k;
@@ -726,6 +753,7 @@ int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
 
 int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit)
 {
+    c.stop_mode = stop_mode;
     k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G);
     if (check_launch(c, "k_pcg_init")) return 1;
     k_pcg_init2<<<1, 256, 0, c.stream>>>(c.st, c.part_u, c.G, stop_mode, tol, limit);
@@ -734,8 +762,12 @@ int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, doub
 
 int launch_update1(Ctx &c, double *xsol)
 {
-    k_pcg_update1<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_s, c.Gs, c.part_u, c.G, xsol, c.r, c.d, c.p,
-                                             c.u, c.dinv);
+    if (c.stop_mode == STOP_CHECON)
+        k_pcg_update1<true><<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_s, c.Gs, c.part_u, c.G, xsol, c.r, c.d,
+                                                       c.p, c.u, c.dinv);
+    else
+        k_pcg_update1<false><<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_s, c.Gs, c.part_u, c.G, xsol, c.r, c.d,
+                                                        c.p, c.u, c.dinv);
     return check_launch(c, "k_pcg_update1");
 }
 

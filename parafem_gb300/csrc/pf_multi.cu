@@ -1,0 +1,807 @@
+// pf_multi.cu -- k load cases of one mesh solved together (block PCG).
+//
+// k independent Jacobi-PCG solves (p121.f90:86-104) share every element
+// matrix read: one iteration computes U = K P for a 60 x k block per element.
+// Vectors are interleaved per slot, v[slot*k + j], so the gather of an
+// element's block and the node scatter touch k consecutive values.
+//
+// Element products:
+//   k_mr_elem_tc   tensor cores (tcgen05.mma, kind::f16, BF16 operands, FP32
+//                  accumulation in TMEM).  K_e and P_e are each split into
+//                  three BF16 terms (x = h1 + h2 + h3, about 24 significant
+//                  bits) and the six products of order <= 2^-16 are summed:
+//                  the block product reaches FP32 accuracy.  A two-term split
+//                  (about 16 bits) leaves too large a perturbation of K for
+//                  the inner PCG to converge on these meshes.
+//   k_mr_elem_cc   the same product on CUDA cores in FP32 (check and fallback
+//                  kernel for the tensor-core one, selectable by prec).
+//   k_mr_elem_64   FP64 (DFMA) block product for the true residual f - K x.
+// The inner PCG runs on the FP32-class product with FP64 vectors, dots and
+// alpha/beta; the recursive residuals are replaced by the FP64 true residual
+// whenever an active load case has dropped 10x (as PF_MODE_MIXED does).
+#include "pf_device.cuh"
+#include "pfgpu.h"
+
+#include <cstring>
+#include <vector>
+
+namespace pf {
+
+namespace {
+
+constexpr int KR = 16;               // load cases per block (the kernels are written for 16)
+constexpr unsigned kFullMask = 0xffffffffu;
+
+// ---------------------------------------------------------------------------
+// tcgen05 helpers (inline PTX)
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Shared-memory matrix descriptor, K-major, no swizzle: core matrices of
+// 8 rows x 16 bytes stored contiguously; LBO = byte distance between core
+// matrices adjacent in K, SBO = between core matrices adjacent in M/N.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version 1 (sm_100 family); base offset 0; no swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
+// N = 16, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_addr(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_init1(uint64_t *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ bool mbar_poll(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+{
+    for (long long i = 0; i < (1LL << 22); ++i)
+        if (mbar_poll(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint16_t bf16_rn(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    u += 0x7FFFu + ((u >> 16) & 1u);   // round to nearest even (finite inputs)
+    return (uint16_t)(u >> 16);
+}
+__device__ __forceinline__ float bf16_to_f(uint16_t h) { return __uint_as_float(((uint32_t)h) << 16); }
+
+// x = h1 + h2 + h3 in BF16 (each remainder is exact in FP32)
+__device__ __forceinline__ void split3(float x, uint16_t &h1, uint16_t &h2, uint16_t &h3)
+{
+    h1 = bf16_rn(x);
+    const float r1 = x - bf16_to_f(h1);
+    h2 = bf16_rn(r1);
+    const float r2 = r1 - bf16_to_f(h2);
+    h3 = bf16_rn(r2);
+}
+
+// byte offset of element (row, k) in a K-major no-swizzle tile with 64 columns of K
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k)
+{
+    return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+constexpr int kTileA = 128 * 64 * 2;   // 16384 B: 128 rows (60 used) x 64 K (60 used)
+constexpr int kTileB = 16 * 64 * 2;    // 2048 B: 16 load cases x 64 K
+constexpr int kTcSmem = 3 * kTileA + 3 * kTileB + 64;
+
+}  // namespace
+
+// Block element products on the tensor cores: ut[e][i][j] = sum_c K_e(i,c) P(slot(c), j).
+// One CTA of 128 threads per element at a time; 32 TMEM columns per CTA.
+__global__ void __launch_bounds__(128)
+k_mr_elem_tc(int nels, const float *__restrict__ km32, const int *__restrict__ conn,
+             const double *__restrict__ P, float *__restrict__ ut, int *__restrict__ err,
+             const int *__restrict__ skip)
+{
+    if (skip && *skip) return;   // a residual replacement is pending: nothing to compute
+    extern __shared__ __align__(1024) unsigned char sm[];
+    unsigned char *A = sm;                     // 3 tiles
+    unsigned char *B = sm + 3 * kTileA;        // 3 tiles
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + 3 * kTileA + 3 * kTileB);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 3 * kTileA + 3 * kTileB + 16);
+    int &s_fail = *reinterpret_cast<int *>(sm + 3 * kTileA + 3 * kTileB + 32);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    // zero every tile once: rows 60..127 and K 60..63 stay zero
+    for (int i = tid; i < (3 * kTileA + 3 * kTileB) / 16; i += blockDim.x)
+        reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_addr(tslot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) mbar_init1(bar);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tslot;
+    uint32_t phase = 0;
+    if (tid == 0) s_fail = 0;
+    __syncthreads();
+
+    for (int e = blockIdx.x; e < nels; e += gridDim.x) {
+        // K_e -> three BF16 tiles (A: row i = output dof, K = input dof c)
+        const float *ke = km32 + (size_t)e * 3600;
+        for (int idx = tid; idx < 3600; idx += blockDim.x) {
+            const int c = idx / 60, i = idx - 60 * c;
+            uint16_t h1, h2, h3;
+            split3(ke[idx], h1, h2, h3);
+            const uint32_t o = kmajor_off(i, c);
+            *reinterpret_cast<uint16_t *>(A + o) = h1;
+            *reinterpret_cast<uint16_t *>(A + kTileA + o) = h2;
+            *reinterpret_cast<uint16_t *>(A + 2 * kTileA + o) = h3;
+        }
+        // P_e -> three BF16 tiles (B: row j = load case, K = dof c)
+        for (int idx = tid; idx < 60 * KR; idx += blockDim.x) {
+            const int c = idx / KR, j = idx - KR * c;
+            const int nd = conn[(size_t)e * 20 + c / 3];
+            const float x = (float)P[((size_t)3 * nd + c % 3) * KR + j];
+            uint16_t h1, h2, h3;
+            split3(x, h1, h2, h3);
+            const uint32_t o = kmajor_off(j, c);
+            *reinterpret_cast<uint16_t *>(B + o) = h1;
+            *reinterpret_cast<uint16_t *>(B + kTileB + o) = h2;
+            *reinterpret_cast<uint16_t *>(B + 2 * kTileB + o) = h3;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
+            const int ta[6] = {0, 0, 1, 0, 1, 2};
+            const int tb[6] = {0, 1, 0, 2, 1, 0};
+            uint32_t acc = 0;
+            for (int t = 0; t < 6; ++t) {
+                const uint32_t a0 = smem_addr(A + ta[t] * kTileA), b0 = smem_addr(B + tb[t] * kTileB);
+                for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
+                    mma_bf16(tmem, umma_desc(a0 + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024), acc);
+                    acc = 1;
+                }
+            }
+            mma_commit(bar);
+        }
+        const bool ok = mbar_wait_bounded(bar, phase);
+        if (!ok) atomicOr(&s_fail, 1);
+        phase ^= 1;
+        __syncthreads();
+        if (s_fail) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (warp < 2) {   // rows 0..63 live in TMEM lanes 0..63 (warps 0 and 1)
+            float v[16];
+            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * warp) << 16), v);
+            const int row = 32 * warp + lane;
+            if (row < 60) {
+                float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)e * 60 + row) * KR);
+                o[0] = make_float4(v[0], v[1], v[2], v[3]);
+                o[1] = make_float4(v[4], v[5], v[6], v[7]);
+                o[2] = make_float4(v[8], v[9], v[10], v[11]);
+                o[3] = make_float4(v[12], v[13], v[14], v[15]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    if (s_fail) {
+        if (tid == 0) atomicExch(err, 3);
+        // give the outstanding MMAs a bounded chance to finish before TMEM goes back
+        mbar_wait_bounded(bar, phase);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
+}
+
+// Block element products on CUDA cores (FP32 or FP64): one warp per element,
+// lanes own rows 2l, 2l+1; P_e staged in shared memory per warp.
+template <typename KT, typename OT>
+__global__ void __launch_bounds__(256)
+k_mr_elem_cc(int nels, const KT *__restrict__ km, const int *__restrict__ conn, const double *__restrict__ P,
+             OT *__restrict__ ut, const int *__restrict__ skip)
+{
+    constexpr int WPB = 32 / (int)sizeof(KT);   // warps per block: 8 (FP32) or 4 (FP64), 30 KB of P blocks
+    __shared__ KT ps[WPB][60 * KR];
+    if (skip && *skip) return;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int e = warp; e < nels; e += nwarps) {
+        for (int idx = lane; idx < 60 * KR; idx += 32) {
+            const int c = idx / KR, j = idx - KR * c;
+            const int nd = conn[(size_t)e * 20 + c / 3];
+            ps[w][idx] = (KT)P[((size_t)3 * nd + c % 3) * KR + j];
+        }
+        __syncwarp();
+        if (lane < 30) {
+            KT a0[KR], a1[KR];
+#pragma unroll
+            for (int j = 0; j < KR; ++j) a0[j] = a1[j] = (KT)0;
+            const KT *ke = km + (size_t)e * 3600 + 2 * lane;
+            for (int c = 0; c < 60; ++c) {
+                const KT k0 = ke[60 * c], k1 = ke[60 * c + 1];
+#pragma unroll
+                for (int j = 0; j < KR; ++j) {
+                    const KT pj = ps[w][c * KR + j];
+                    a0[j] = fma(k0, pj, a0[j]);
+                    a1[j] = fma(k1, pj, a1[j]);
+                }
+            }
+            OT *o0 = ut + ((size_t)e * 60 + 2 * lane) * KR;
+#pragma unroll
+            for (int j = 0; j < KR; ++j) {
+                o0[j] = (OT)a0[j];
+                o0[KR + j] = (OT)a1[j];
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Node scatter for k load cases: thread (node, j), ascending element order.
+// MODE 0: U = sum, partial p.u per case; MODE 1: RRES = F - sum, partial rr.
+template <typename UT, int MODE>
+__global__ void __launch_bounds__(256)
+k_mr_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list, const UT *__restrict__ ut,
+             const uint8_t *__restrict__ fm, const double *__restrict__ pf, double *__restrict__ out,
+             double *__restrict__ part, const int *__restrict__ skip)
+{
+    if (skip && *skip) return;   // uniform: the flag does not change during the kernel
+    const int j = threadIdx.x & (KR - 1);
+    double loc = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nn * KR; t += gridDim.x * blockDim.x) {
+        const int n = t / KR;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
+            const size_t base = (size_t)list[k] * 3 * KR + j;   // list holds e*20+a
+            a0 += (double)ut[base];
+            a1 += (double)ut[base + KR];
+            a2 += (double)ut[base + 2 * KR];
+        }
+        const int m = fm[n];
+        const double a[3] = {a0, a1, a2};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const size_t s = ((size_t)3 * n + d) * KR + j;
+            const bool fr = (m >> d) & 1;
+            if (MODE == 0) {
+                const double uv = fr ? a[d] : 0.0;
+                out[s] = uv;
+                loc = fma(pf[s], uv, loc);
+            } else {
+                const double rv = fr ? pf[s] - a[d] : 0.0;
+                out[s] = rv;
+                loc = fma(rv, rv, loc);
+            }
+        }
+    }
+    // per-case block reduction: lanes l and l+16 share a case
+    loc += __shfl_xor_sync(kFullMask, loc, 16);
+    __shared__ double sh[8][KR];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane < KR) sh[w][lane] = loc;
+    __syncthreads();
+    if (threadIdx.x < KR) {
+        double s = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i][threadIdx.x];
+        part[(size_t)blockIdx.x * KR + threadIdx.x] = s;
+    }
+}
+
+// per-case state
+struct MState {
+    double up[KR], ff[KR], rr[KR], thr[KR];
+    int active[KR];      // 1 until the case's true residual reaches tol
+    int flag[KR];        // recursive residual reached thr (replacement wanted)
+    int iters[KR];
+    int any_flag;        // stop iterating: some active case wants a replacement
+    int err;
+};
+
+// per-case sums of block partials (fixed order, same value in every block)
+__device__ __forceinline__ double case_sum(const double *part, int G, int j)
+{
+    double s = 0.0;
+    for (int b = 0; b < G; ++b) s += part[(size_t)b * KR + j];
+    return s;
+}
+
+template <int NV>
+__device__ __forceinline__ void case_block_reduce(double (&v)[NV], unsigned kinds, double *out, size_t stride)
+{
+    // lanes l and l+16 hold the same case
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const double o = __shfl_xor_sync(kFullMask, v[k], 16);
+        v[k] = ((kinds >> k) & 1) ? fmax(v[k], o) : v[k] + o;
+    }
+    __shared__ double sh[NV][8][KR];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane < KR)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) sh[k][w][lane] = v[k];
+    __syncthreads();
+    if (threadIdx.x < KR)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = 0.0;
+            for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
+                s = ((kinds >> k) & 1) ? fmax(s, sh[k][i][threadIdx.x]) : s + sh[k][i][threadIdx.x];
+            out[k * stride + (size_t)blockIdx.x * KR + threadIdx.x] = s;
+        }
+}
+
+__global__ void __launch_bounds__(256)
+k_mr_init(int ns, const double *__restrict__ F, const double *__restrict__ dinv, double *__restrict__ X,
+          double *__restrict__ R, double *__restrict__ D, double *__restrict__ P, double *__restrict__ part, int G)
+{
+    double rd = 0.0, rr = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const double rv = F[t], dv = dinv[t / KR] * rv;
+        X[t] = 0.0;
+        R[t] = rv;
+        D[t] = dv;
+        P[t] = dv;
+        rd = fma(rv, dv, rd);
+        rr = fma(rv, rv, rr);
+    }
+    double v[2] = {rd, rr};
+    case_block_reduce<2>(v, 0u, part, (size_t)G * KR);
+}
+
+__global__ void k_mr_init2(MState *st, const double *__restrict__ part, int G, double tol)
+{
+    const int j = threadIdx.x;
+    if (j >= KR) return;
+    const double rd = case_sum(part, G, j), rr = case_sum(part + (size_t)G * KR, G, j);
+    st->up[j] = rd;
+    st->ff[j] = rr;
+    st->rr[j] = rr;
+    st->thr[j] = 0.1 > tol ? 0.1 : tol;
+    st->active[j] = rr > 0.0 ? 1 : 0;
+    st->flag[j] = 0;
+    st->iters[j] = 0;
+    if (j == 0) {
+        st->any_flag = 0;
+        st->err = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_mr_update1(int ns, const MState *__restrict__ st, const double *__restrict__ ps, int Gs,
+             double *__restrict__ pu_out, int G, double *__restrict__ X, double *__restrict__ R,
+             double *__restrict__ D, const double *__restrict__ P, const double *__restrict__ U,
+             const double *__restrict__ dinv)
+{
+    if (st->any_flag) return;
+    const int j = threadIdx.x & (KR - 1);
+    const double pu = case_sum(ps, Gs, j);
+    const double alpha = st->active[j] ? st->up[j] / pu : 0.0;
+    double rd = 0.0, rr = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+         t += (size_t)gridDim.x * blockDim.x) {
+        X[t] = fma(P[t], alpha, X[t]);
+        const double rn = fma(-U[t], alpha, R[t]);
+        R[t] = rn;
+        const double dn = dinv[t / KR] * rn;
+        D[t] = dn;
+        rd = fma(rn, dn, rd);
+        rr = fma(rn, rn, rr);
+    }
+    double v[2] = {rd, rr};
+    case_block_reduce<2>(v, 0u, pu_out, (size_t)G * KR);
+}
+
+__global__ void __launch_bounds__(256)
+k_mr_update2(int ns, const MState *__restrict__ st, const double *__restrict__ part, int G,
+             const double *__restrict__ D, double *__restrict__ P)
+{
+    if (st->any_flag) return;
+    const int j = threadIdx.x & (KR - 1);
+    const double rd = case_sum(part, G, j);
+    const double beta = st->active[j] ? rd / st->up[j] : 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+         t += (size_t)gridDim.x * blockDim.x)
+        if (st->active[j]) P[t] = fma(P[t], beta, D[t]);
+}
+
+__global__ void k_mr_finish(MState *st, const double *__restrict__ part, int G, int limit)
+{
+    __shared__ int s_any;
+    if (threadIdx.x == 0) s_any = 0;
+    __syncthreads();
+    if (st->any_flag) return;
+    const int j = threadIdx.x;
+    if (j < KR && st->active[j]) {
+        const double rd = case_sum(part, G, j), rr = case_sum(part + (size_t)G * KR, G, j);
+        st->up[j] = rd;
+        st->rr[j] = rr;
+        st->iters[j] += 1;
+        const bool f = sqrt(rr) / sqrt(st->ff[j]) <= st->thr[j] || st->iters[j] >= limit || !isfinite(rd);
+        st->flag[j] = f ? 1 : 0;
+        if (!isfinite(rd)) st->err = 1;
+        if (f) atomicOr(&s_any, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_any) st->any_flag = 1;
+}
+
+// residual replacement: R = RRES for active cases, D = dinv*R, partials r.d, r.r
+__global__ void __launch_bounds__(256)
+k_mr_replace(int ns, const MState *__restrict__ st, const double *__restrict__ RRES,
+             const double *__restrict__ dinv, double *__restrict__ R, double *__restrict__ D,
+             double *__restrict__ part, int G)
+{
+    const int j = threadIdx.x & (KR - 1);
+    double rd = 0.0, rr = 0.0;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+         t += (size_t)gridDim.x * blockDim.x) {
+        if (!st->active[j]) continue;
+        const double rv = RRES[t], dv = dinv[t / KR] * rv;
+        R[t] = rv;
+        D[t] = dv;
+        rd = fma(rv, dv, rd);
+        rr = fma(rv, rv, rr);
+    }
+    double v[2] = {rd, rr};
+    case_block_reduce<2>(v, 0u, part, (size_t)G * KR);
+}
+
+__global__ void k_mr_replace2(MState *st, const double *__restrict__ part, int G)
+{
+    const int j = threadIdx.x;
+    if (j < KR && st->active[j]) {
+        st->up[j] = case_sum(part, G, j);
+        st->rr[j] = case_sum(part + (size_t)G * KR, G, j);
+        st->flag[j] = 0;
+    }
+    if (j == 0) st->any_flag = 0;
+}
+
+__global__ void k_mr_sums(const double *__restrict__ part, int G, double *__restrict__ out)
+{
+    if (threadIdx.x < KR) out[threadIdx.x] = case_sum(part, G, threadIdx.x);
+}
+
+__global__ void k_mr_eq_to_slot(int ns, const int *__restrict__ slot_eq, int neq, const double *__restrict__ Req,
+                                double *__restrict__ F)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t s = t / KR, j = t % KR;
+        const int q = slot_eq[s];
+        F[t] = q > 0 ? Req[j * (size_t)neq + q - 1] : 0.0;
+    }
+}
+
+__global__ void k_mr_slot_to_eq(int neq, const int *__restrict__ eq_slot, const double *__restrict__ X,
+                                double *__restrict__ Xeq)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)neq * KR;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const size_t j = t / neq, q = t % neq;
+        Xeq[t] = X[(size_t)eq_slot[q] * KR + j];
+    }
+}
+
+// ---------------------------------------------------------------------------
+namespace {
+struct MultiBufs {
+    int ns = 0;
+    double *F = nullptr, *X = nullptr, *R = nullptr, *D = nullptr, *P = nullptr, *U = nullptr, *RR = nullptr,
+           *eq = nullptr;
+    float *ut32 = nullptr;
+    double *ut64 = nullptr, *part = nullptr, *sums = nullptr;
+    MState *st = nullptr;
+    MState *hst = nullptr;
+};
+MultiBufs g_mb;   // one block solve at a time per process
+
+void mb_free()
+{
+    void *p[] = {g_mb.F, g_mb.X, g_mb.R, g_mb.D, g_mb.P, g_mb.U, g_mb.RR, g_mb.eq, g_mb.ut32, g_mb.ut64, g_mb.part,
+                 g_mb.sums, g_mb.st};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    if (g_mb.hst) cudaFreeHost(g_mb.hst);
+    g_mb = MultiBufs();
+}
+}  // namespace
+
+}  // namespace pf
+
+using namespace pf;
+
+#define MCK(call)                                                                        \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+            return PF_FAILURE;                                                           \
+        }                                                                                \
+    } while (0)
+
+static int mr_launched(Ctx &c, const char *name)
+{
+    c.launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("%s: launch failed: %s", name, cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+// U = K P for the block (prec 16: tensor cores, 32: CUDA-core FP32, 64: FP64
+// into ut64).  skip: device flag that turns the launch into a no-op.
+static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
+{
+    MultiBufs &m = g_mb;
+    if (prec == 16) {
+        const int smem = kTcSmem;
+        MCK(cudaFuncSetAttribute(k_mr_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        const int grid = c.nels < c.nsm * 4 ? c.nels : c.nsm * 4;
+        k_mr_elem_tc<<<grid, 128, smem, c.stream>>>(c.nels, c.km32, c.conn, P, m.ut32, c.kerr, skip);
+        return mr_launched(c, "k_mr_elem_tc");
+    }
+    if (prec == 32) {
+        const int grid = (c.nels + 7) / 8 < c.nsm * 8 ? (c.nels + 7) / 8 : c.nsm * 8;
+        k_mr_elem_cc<float, float><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, P, m.ut32, skip);
+        return mr_launched(c, "k_mr_elem_cc<float>");
+    }
+    const int grid = (c.nels + 3) / 4 < c.nsm * 16 ? (c.nels + 3) / 4 : c.nsm * 16;
+    k_mr_elem_cc<double, double><<<grid, 128, 0, c.stream>>>(c.nels, c.km64, c.conn, P, m.ut64, skip);
+    return mr_launched(c, "k_mr_elem_cc<double>");
+}
+
+static int mr_scatter(Ctx &c, int prec, int mode, const double *pf, double *out, const int *skip)
+{
+    MultiBufs &m = g_mb;
+    const int G = c.Gs;
+    if (prec == 64) {
+        if (mode == 0) k_mr_scatter<double, 0><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut64, c.freemask, pf, out, m.part, skip);
+        else k_mr_scatter<double, 1><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut64, c.freemask, pf, out, m.part, skip);
+    } else {
+        if (mode == 0) k_mr_scatter<float, 0><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut32, c.freemask, pf, out, m.part, skip);
+        else k_mr_scatter<float, 1><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut32, c.freemask, pf, out, m.part, skip);
+    }
+    return mr_launched(c, "k_mr_scatter");
+}
+
+static int mr_alloc(Ctx &c)
+{
+    if (g_mb.ns == c.nslots && g_mb.F) return 0;
+    mb_free();
+    const size_t n = (size_t)c.nslots * KR;
+    const size_t parts = (size_t)(c.Gs > c.G ? c.Gs : c.G) * KR * 4 + 64;
+    double **v[] = {&g_mb.F, &g_mb.X, &g_mb.R, &g_mb.D, &g_mb.P, &g_mb.U, &g_mb.RR};
+    for (double **q : v)
+        if (cudaMalloc((void **)q, n * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.eq, (size_t)(c.neq > 0 ? c.neq : 1) * KR * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.ut32, (size_t)c.nels * 60 * KR * 4) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.ut64, (size_t)c.nels * 60 * KR * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.part, parts * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.sums, 64 * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.st, sizeof(MState)) != cudaSuccess) goto fail;
+    if (cudaMallocHost((void **)&g_mb.hst, sizeof(MState)) != cudaSuccess) goto fail;
+    g_mb.ns = c.nslots;
+    return 0;
+fail:
+    mb_free();
+    set_error("pf_solve_multi: cannot allocate the block vectors (%zu slots x %d cases)", (size_t)c.nslots, KR);
+    return 1;
+}
+
+// FP64 true residuals of all cases; returns per-case ||f - K x||^2 in rr_out
+static int mr_true_residual(Ctx &c, double *rr_out)
+{
+    MultiBufs &m = g_mb;
+    if (mr_elem(c, 64, m.X, nullptr)) return 1;
+    if (mr_scatter(c, 64, 1, m.F, m.RR, nullptr)) return 1;
+    k_mr_sums<<<1, 32, 0, c.stream>>>(m.part, c.Gs, m.sums);
+    if (mr_launched(c, "k_mr_sums")) return 1;
+    MCK(cudaMemcpyAsync(rr_out, m.sums, KR * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MCK(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const double *tol, const int *limit,
+                              const int *prec, double *xnew, int *iters, double *relres)
+{
+    if (!ctx || !*ctx || !k || !r || !tol || !limit || !prec || !xnew || !iters || !relres) {
+        set_error("pf_solve_multi: null argument");
+        return PF_FAILURE;
+    }
+    Ctx &c = *(Ctx *)*ctx;
+    MCK(cudaSetDevice(c.device));
+    if (*k != KR) {
+        set_error("pf_solve_multi: k must be %d", KR);
+        return PF_FAILURE;
+    }
+    if (!c.have_km || *limit < 1 || (*prec != 16 && *prec != 32)) {
+        set_error("pf_solve_multi: needs storkm, limit >= 1 and prec 16 (tensor cores) or 32 (CUDA cores)");
+        return PF_FAILURE;
+    }
+    if (mr_alloc(c)) return PF_FAILURE;
+    MultiBufs &m = g_mb;
+    const int G = c.G, Gs = c.Gs;
+    // load cases: r(neq, k) column-major
+    MCK(cudaMemcpyAsync(m.eq, r, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
+    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, c.slot_eq, c.neq, m.eq, m.F);
+    if (mr_launched(c, "k_mr_eq_to_slot")) return PF_FAILURE;
+    cudaEvent_t e0, e1;
+    MCK(cudaEventCreate(&e0));
+    MCK(cudaEventCreate(&e1));
+    MCK(cudaEventRecord(e0, c.stream));
+    k_mr_init<<<G, 256, 0, c.stream>>>(c.nslots, m.F, c.dinv, m.X, m.R, m.D, m.P, m.part, G);
+    if (mr_launched(c, "k_mr_init")) return PF_FAILURE;
+    k_mr_init2<<<1, 32, 0, c.stream>>>(m.st, m.part, G, *tol);
+    if (mr_launched(c, "k_mr_init2")) return PF_FAILURE;
+    double *pu = m.part + (size_t)Gs * KR;   // update partials after the scatter partials
+    int total = 0, chunk = 4, corrections = 0;
+    double rel[KR] = {0};
+    for (;;) {
+        for (int i = 0; i < chunk; ++i) {
+            const int *skip = &m.st->any_flag;
+            if (mr_elem(c, *prec, m.P, skip)) return PF_FAILURE;
+            if (mr_scatter(c, *prec, 0, m.P, m.U, skip)) return PF_FAILURE;
+            k_mr_update1<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.part, Gs, pu, G, m.X, m.R, m.D, m.P, m.U,
+                                                  c.dinv);
+            if (mr_launched(c, "k_mr_update1")) return PF_FAILURE;
+            k_mr_update2<<<G, 256, 0, c.stream>>>(c.nslots, m.st, pu, G, m.D, m.P);
+            if (mr_launched(c, "k_mr_update2")) return PF_FAILURE;
+            k_mr_finish<<<1, 32, 0, c.stream>>>(m.st, pu, G, *limit);
+            if (mr_launched(c, "k_mr_finish")) return PF_FAILURE;
+        }
+        total += chunk;
+        if (chunk < 32) chunk *= 2;
+        MCK(cudaMemcpyAsync(m.hst, m.st, sizeof(MState), cudaMemcpyDeviceToHost, c.stream));
+        MCK(cudaStreamSynchronize(c.stream));
+        int kerr = 0;
+        MCK(cudaMemcpy(&kerr, c.kerr, sizeof(int), cudaMemcpyDeviceToHost));
+        if (kerr) {
+            cudaMemset(c.kerr, 0, sizeof(int));
+            set_error("pf_solve_multi: tensor-core product wait timed out");
+            return PF_FAILURE;
+        }
+        if (m.hst->err) {
+            set_error("pf_solve_multi: PCG breakdown (non-finite r.d)");
+            return PF_FAILURE;
+        }
+        if (!m.hst->any_flag) continue;
+        // some active case reached its threshold (or the limit): FP64 true residuals
+        double rr[KR];
+        if (mr_true_residual(c, rr)) return PF_FAILURE;
+        int n_active = 0;
+        for (int j = 0; j < KR; ++j) {
+            rel[j] = m.hst->ff[j] > 0 ? std::sqrt(rr[j]) / std::sqrt(m.hst->ff[j]) : 0.0;
+            if (m.hst->active[j]) {
+                if (rel[j] <= *tol || m.hst->iters[j] >= *limit) m.hst->active[j] = 0;
+                else {
+                    m.hst->thr[j] = 0.1 * rel[j] > *tol ? 0.1 * rel[j] : 0.5 * *tol;
+                    ++n_active;
+                }
+            }
+        }
+        if (n_active == 0) break;
+        // push the new thresholds and active flags, then replace the residuals
+        MCK(cudaMemcpyAsync(m.st, m.hst, sizeof(MState), cudaMemcpyHostToDevice, c.stream));
+        k_mr_replace<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.RR, c.dinv, m.R, m.D, m.part, G);
+        if (mr_launched(c, "k_mr_replace")) return PF_FAILURE;
+        k_mr_replace2<<<1, 32, 0, c.stream>>>(m.st, m.part, G);
+        if (mr_launched(c, "k_mr_replace2")) return PF_FAILURE;
+        ++corrections;
+        chunk = 4;
+    }
+    MCK(cudaEventRecord(e1, c.stream));
+    k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, c.eq_slot, m.X, m.eq);
+    if (mr_launched(c, "k_mr_slot_to_eq")) return PF_FAILURE;
+    MCK(cudaMemcpyAsync(xnew, m.eq, (size_t)c.neq * KR * 8, cudaMemcpyDeviceToHost, c.stream));
+    MCK(cudaStreamSynchronize(c.stream));
+    float ms = 0.f;
+    MCK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (int j = 0; j < KR; ++j) {
+        iters[j] = m.hst->iters[j];
+        relres[j] = rel[j];
+    }
+    c.stats[0] = 0;
+    for (int j = 0; j < KR; ++j) c.stats[0] = iters[j] > c.stats[0] ? iters[j] : c.stats[0];
+    c.stats[1] = corrections;
+    c.stats[2] = ms;
+    return PF_SUCCESS;
+}
+
+// Block product U = K P for k = 16 cases in equation order (tests): prec 16,
+// 32 or 64.
+extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, const double *p, double *u)
+{
+    if (!ctx || !*ctx || !k || !prec || !p || !u) {
+        set_error("pf_ebe_matvec_multi: null argument");
+        return PF_FAILURE;
+    }
+    Ctx &c = *(Ctx *)*ctx;
+    MCK(cudaSetDevice(c.device));
+    if (*k != KR || !c.have_km || (*prec != 16 && *prec != 32 && *prec != 64)) {
+        set_error("pf_ebe_matvec_multi: k must be %d, prec 16/32/64, storkm formed", KR);
+        return PF_FAILURE;
+    }
+    if (mr_alloc(c)) return PF_FAILURE;
+    MultiBufs &m = g_mb;
+    MCK(cudaMemcpyAsync(m.eq, p, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
+    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, c.slot_eq, c.neq, m.eq, m.P);
+    if (mr_launched(c, "k_mr_eq_to_slot")) return PF_FAILURE;
+    if (mr_elem(c, *prec, m.P, nullptr)) return PF_FAILURE;
+    if (mr_scatter(c, *prec, 0, m.P, m.U, nullptr)) return PF_FAILURE;
+    k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, c.eq_slot, m.U, m.eq);
+    if (mr_launched(c, "k_mr_slot_to_eq")) return PF_FAILURE;
+    MCK(cudaMemcpyAsync(u, m.eq, (size_t)c.neq * KR * 8, cudaMemcpyDeviceToHost, c.stream));
+    MCK(cudaStreamSynchronize(c.stream));
+    int kerr = 0;
+    MCK(cudaMemcpy(&kerr, c.kerr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (kerr) {
+        cudaMemset(c.kerr, 0, sizeof(int));
+        set_error("pf_ebe_matvec_multi: tensor-core product wait timed out");
+        return PF_FAILURE;
+    }
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_multi_free(void)
+{
+    mb_free();
+    return PF_SUCCESS;
+}

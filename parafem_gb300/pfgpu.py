@@ -58,6 +58,10 @@ _SIGS = {
     "pf_kernel_launches": [_VPP, _LLP],
     "pf_ebe_matvec_noalloc": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p],
+    "pf_solve_multi": [_VPP, _IP, ctypes.c_void_p, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p,
+                       ctypes.c_void_p],
+    "pf_ebe_matvec_multi": [_VPP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_multi_free": [],
     "pf_batch_create": [_IP, _LLP, _IP, _VPP],
     "pf_batch_destroy": [_VPP],
     "pf_batch_capacity": [_VPP, _LLP, _LLP],
@@ -279,6 +283,25 @@ class Solver:
                                          ctypes.byref(c)), "pf_bench_iterations")
         return a.value, b.value, c.value
 
+    def solve_multi(self, R, tol, limit, prec=16):
+        """k = 16 load cases together: R (neq, 16) -> X (neq, 16), iters (16,), relres (16,)."""
+        Rf = np.asfortranarray(R, dtype=np.float64)
+        if Rf.shape != (self.neq, 16):
+            raise ValueError("R must be (neq, 16)")
+        X = np.zeros((self.neq, 16), order="F")
+        it = np.zeros(16, np.int32)
+        rel = np.zeros(16)
+        _check(lib().pf_solve_multi(self._ref, _i(16), Rf.ctypes.data, _d(tol), _i(limit), _i(prec),
+                                    X.ctypes.data, it.ctypes.data, rel.ctypes.data), "pf_solve_multi")
+        return X, it, rel
+
+    def ebe_matvec_multi(self, Pm, prec=16):
+        Pf = np.asfortranarray(Pm, dtype=np.float64)
+        U = np.zeros((self.neq, 16), order="F")
+        _check(lib().pf_ebe_matvec_multi(self._ref, _i(16), _i(prec), Pf.ctypes.data, U.ctypes.data),
+               "pf_ebe_matvec_multi")
+        return U
+
     def centroid_stress(self, x, iel: int = 1):
         x, px = _arr(x, np.float64)
         s = np.zeros(6)
@@ -378,6 +401,24 @@ class Batch:
                 out[sid] = (it, rel, x)
             if active == 0:
                 return out
+
+
+def top_face_z_equations(g_g, nxe, nze):
+    """Equations (1-based) of the z dofs of the top-face nodes of a GEOMETRY_20BXZ cube."""
+    g_g = np.asarray(g_g)
+    top = np.nonzero(np.arange(g_g.shape[0]) % (nxe * nze) < nxe)[0]
+    local = np.array([3, 4, 5, 10, 11, 15, 16, 17]) - 1
+    eqs = g_g[top][:, 3 * local + 2].ravel()
+    return np.unique(eqs[eqs > 0])
+
+
+def random_top_loads(g_g, nxe, nze, neq, k, seed):
+    """k load cases of i.i.d. N(0,1) vertical forces on the top-face nodes (seeded)."""
+    eqs = top_face_z_equations(g_g, nxe, nze)
+    rng = np.random.default_rng(seed)
+    R = np.zeros((neq, k), order="F")
+    R[eqs - 1, :] = rng.standard_normal((eqs.size, k))
+    return R
 
 
 def cube_problem(nxe, nye, nze, bc=1, pressure=None, aa=1.0, bb=1.0, cc=1.0):
