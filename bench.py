@@ -46,7 +46,7 @@ def parse_args():
     ap.add_argument("--size", type=int, default=100, help="elements per cube edge")
     ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--workload", default="cube100", choices=["cube100", "hetero80", "serving", "multirhs60"],
+    ap.add_argument("--workload", default="cube100", choices=["cube100", "hetero80", "serving", "multirhs60", "cube10"],
                     help="cube100: the headline; hetero80: per-element E and v, accuracy study; "
                          "serving: continuous batching of a Poisson request stream")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
@@ -54,7 +54,10 @@ def parse_args():
                                                     "0 = all requests at t=0")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serving: device-memory budget of the batch")
     ap.add_argument("--chunk", type=int, default=10, help="serving: PCG iterations per launch/sync cycle")
+    ap.add_argument("--serving-prec", type=int, default=32, choices=[32, 64],
+                    help="serving: 32 = FP32 products with FP64 residual replacement, 64 = FP64")
     ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--limit", type=int, default=50000, help="multirhs60: PCG iteration limit of the block solves")
     return ap.parse_args()
 
 
@@ -271,7 +274,7 @@ def run_gb300(args, rank, world, local, dist):
     neq = prob["neq"]
     nels = n ** 3
     r = prob["r"]
-    extra = {"host_setup_s": t_host, "storkm_formation_s": t_form}
+    extra = {"host_setup_s": t_host, "storkm_formation_s": t_form, "autotune": s.tuning()}
 
     # e2e: one full mixed solve through the C-ABI with host buffers
     solves = {}
@@ -417,7 +420,7 @@ def run_serving(args, rank, world, local, dist):
         rng = np.random.default_rng(args.seed + 1)
         gaps = rng.exponential(1.0 / rate, n_req) if rate > 0 else np.zeros(n_req)
         arrivals = np.cumsum(gaps) - (gaps[0] if rate > 0 else 0.0)
-        b = P.Batch(int(args.budget_gb * (1 << 30)), 512, local)
+        b = P.Batch(int(args.budget_gb * (1 << 30)), 512, local, prec=args.serving_prec)
         cache = {}
 
         def build(i):
@@ -479,7 +482,8 @@ def run_serving(args, rank, world, local, dist):
     line = {"metric": METRIC, "value": best["dof_iter_per_s"], "unit": UNIT, "n_gpus": world,
             "steps": n_req, "warmup": 0, "ms_per_step": best["makespan_s"] * 1e3 / n_req,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 storkm / f64 vectors", "data": "synthetic",
+            "dtype": ("f32 storkm products + f64 residual replacement / f64 vectors" if args.serving_prec == 32
+                      else "f64 storkm / f64 vectors"), "data": "synthetic",
             "config": {"workload": f"serving stream: {n_req} Poisson-arrival requests, hex20 cubes with edges "
                                    f"uniform in 4..40, E log-uniform [10,1000], v uniform [0.2,0.35], fixed "
                                    f"base, top pressure uniform [0.5,2.0], tol 1e-8, budget {args.budget_gb} GB, "
@@ -506,22 +510,28 @@ def run_multirhs(args, rank, world, local, dist):
     out = {}
     for prec, name in ((16, "block_tensor_cores"), (32, "block_fp32_cuda_cores")):
         t0 = time.perf_counter()
-        X, it, rel = s.solve_multi(R, 1e-8, 50000, prec)
-        out[name] = {"wall_s": time.perf_counter() - t0, "device_s": s.stats()["solve_ms"] / 1e3,
+        X, it, rel = s.solve_multi(R, 1e-8, args.limit, prec)
+        st = s.stats_raw()
+        n_it = max(st[6], 1)
+        out[name] = {"wall_s": time.perf_counter() - t0, "device_s": st[2] / 1e3,
                      "max_iters": int(it.max()), "mean_iters": float(it.mean()), "max_relres": float(rel.max()),
-                     "corrections": s.stats()["outer"]}
+                     "corrections": int(st[1]), "launched_iters": int(st[6]),
+                     "elem_ms_per_iter": st[3] / n_it, "scatter_ms_per_iter": st[4] / n_it,
+                     "iter_ms": st[5] / n_it}
         if prec == 16:
             Xtc = X
-    t0 = time.perf_counter()
-    errs, its = [], []
-    for j in range(16):
-        x64, it64, rel64 = s.solve(R[:, j], 1e-8, 50000, P.MODE_FP64_RES)
-        errs.append(float(np.linalg.norm(Xtc[:, j] - x64) / np.linalg.norm(x64)))
-        its.append(it64)
-    out["sequential_fp64"] = {"wall_s": time.perf_counter() - t0, "mean_iters": float(np.mean(its)),
-                              "max_iters": int(max(its))}
-    out["block_vs_fp64_rel_err_2_max"] = max(errs)
-    out["speedup_block_tc_vs_sequential_fp64"] = out["sequential_fp64"]["wall_s"] / out["block_tensor_cores"]["wall_s"]
+    if not args.no_solves:
+        t0 = time.perf_counter()
+        errs, its = [], []
+        for j in range(16):
+            x64, it64, rel64 = s.solve(R[:, j], 1e-8, 50000, P.MODE_FP64_RES)
+            errs.append(float(np.linalg.norm(Xtc[:, j] - x64) / np.linalg.norm(x64)))
+            its.append(it64)
+        out["sequential_fp64"] = {"wall_s": time.perf_counter() - t0, "mean_iters": float(np.mean(its)),
+                                  "max_iters": int(max(its))}
+        out["block_vs_fp64_rel_err_2_max"] = max(errs)
+        out["speedup_block_tc_vs_sequential_fp64"] = (out["sequential_fp64"]["wall_s"] /
+                                                      out["block_tensor_cores"]["wall_s"])
     s.close()
     value = neq * 16 * out["block_tensor_cores"]["mean_iters"] / out["block_tensor_cores"]["device_s"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
@@ -532,6 +542,47 @@ def run_multirhs(args, rank, world, local, dist):
             "config": {"workload": f"multi-RHS {n}^3 hex20 cube, E 100, v 0.3, 16 load cases N(0,1) on top-face "
                                    f"nodes (seed {args.seed}), nip 27, tol 1e-8", "neq": neq, "cases": 16},
             "multirhs": out}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+def run_cube10(args, rank, world, local, dist):
+    """The reference's CPU-runnable case: 10^3 cube, nip 27, E 100, v 0.3,
+    fixed base, top pressure (total -1), checon_par tol 1e-6, limit 5000.
+    GPU drop-in (PF_MODE_P121) vs the C restatement of p121 on all host
+    cores, same inputs; parity of iterations and displacements."""
+    import parafem_gb300 as P
+    from oracle import oracle as O
+    prob = P.cube_problem(10, 10, 10)
+    s = P.Solver(local)
+    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+    s.set_material(100.0, 0.3)
+    t0 = time.perf_counter()
+    s.form_storkm(27)
+    t_form = time.perf_counter() - t0
+    s.solve(prob["r"], 1e-6, 5000, P.MODE_P121)          # warm-up
+    t1 = time.perf_counter()
+    x, it, rel = s.solve(prob["r"], 1e-6, 5000, P.MODE_P121)
+    t_gpu = time.perf_counter() - t1
+    s.close()
+    t2 = time.perf_counter()
+    km = O.form_storkm(prob["g_coord"], 27, 100.0, 0.3)
+    dg = O.diag(prob["g_g"], km, prob["neq"])
+    t3 = time.perf_counter()
+    it_ref, x_ref, _ = O.pcg(prob["g_g"], km, dg, prob["r"], 1e-6, 5000, 0)
+    t_cpu = time.perf_counter() - t3
+    neq = prob["neq"]
+    line = {"metric": METRIC, "value": neq * it / t_gpu, "unit": UNIT, "n_gpus": world, "steps": it,
+            "warmup": 1, "ms_per_step": 1e3 * t_gpu / it, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "p121 10^3 hex20 cube (the CPU-runnable case), nip 27, E 100, v 0.3, fixed "
+                                   "base, top pressure (total -1), checon_par tol 1e-6, limit 5000", "neq": neq},
+            "gpu": {"iters": it, "solve_wall_s": t_gpu, "storkm_formation_s": t_form},
+            "cpu_restatement": {"iters": it_ref, "solve_wall_s": t_cpu, "storkm_and_diag_s": t3 - t2,
+                                "cores": O.lib().orc_num_threads(), "dof_iter_per_s": neq * it_ref / t_cpu},
+            "parity": {"iters_equal": it == it_ref,
+                       "rel_err_2": float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))}}
     if rank == 0:
         print(json.dumps(line))
     return 0
@@ -549,6 +600,8 @@ def main():
             return run_serving(args, rank, world, local, dist)
         if args.workload == "multirhs60":
             return run_multirhs(args, rank, world, local, dist)
+        if args.workload == "cube10":
+            return run_cube10(args, rank, world, local, dist)
         return run_gb300(args, rank, world, local, dist)
     finally:
         if dist is not None:

@@ -132,6 +132,22 @@ int pf_bench_iterations(void **ctx, const int *prec, const int *steps,
  * (p121.f90:112-123): sigma(6) = D . B(0,0,0) . u_e; iel is 1-based. */
 int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *sigma);
 
+/* The autotuner's choice for the packed-symmetric FP32 element kernel, made
+ * at pf_form_storkm / pf_set_storkm by timing every configuration on this
+ * mesh: warps per CTA, shared-memory stages per warp, and the measured
+ * milliseconds per launch of the configurations (14,2), (12,2), (8,3). */
+int pf_tuning(void **ctx, int *warps, int *stages, float *ms);
+
+/* Force configuration *config (0: 14x2, 1: 12x2, 2: 8x3) of that kernel, or
+ * re-run the autotuner (*config = -1).  Every configuration gives bitwise
+ * the same products; only the speed differs. */
+int pf_set_tuning(void **ctx, const int *config);
+
+/* PCG iterations are replayed from a CUDA graph of 8 iterations (captured
+ * on first use per solve mode) when *on != 0, the default; *on == 0 launches
+ * every kernel directly.  Both give bitwise the same iterates. */
+int pf_set_graphs(void **ctx, const int *on);
+
 /* Number of kernels this library launched since the context was created. */
 int pf_kernel_launches(void **ctx, long long *count);
 
@@ -157,13 +173,16 @@ int pf_multi_free(void);
 /* ---------------------------------------------------------------------- */
 /* Serving layer: continuous batching of many independent solves.  No
  * counterpart in the reference (p121 solves one mesh per run); every solve
- * is p121's Jacobi-PCG on FP64 storkm to ||r||2/||f||2 <= tol.            */
+ * is p121's Jacobi-PCG to ||r||2/||f||2 <= tol.                           */
 
 #define PF_BUSY 2   /* pf_batch_admit: no room yet; retry after a sync */
 
 /* A batch on one device with a fixed device-memory budget (bytes) for its
- * arenas and at most max_meshes solves resident at once. */
-int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes, void **batch);
+ * arenas and at most max_meshes solves resident at once.  prec 64: FP64
+ * element products; prec 32: FP32 products with FP64 residual replacement
+ * per mesh (the PF_MODE_MIXED scheme). */
+int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes, const int *prec,
+                    void **batch);
 int pf_batch_destroy(void **batch);
 /* Arena capacity in elements and nodes. */
 int pf_batch_capacity(void **batch, long long *elements, long long *nodes);
@@ -173,8 +192,13 @@ int pf_batch_capacity(void **batch, long long *elements, long long *nodes);
 int pf_batch_admit(void **batch, const int *nels, const int *nn, const int *neq, const int *g_num,
                    const int *g_g, const double *g_coord, const int *nmat, const double *e, const double *v,
                    const int *nip, const double *r, const double *tol, const int *limit, int *id);
-/* Enqueues `iters` PCG iterations of every resident solve and returns. */
+/* Enqueues `iters` PCG iterations of every resident solve and returns.  By
+ * default the chunk is replayed from a CUDA graph, captured again (or
+ * updated in place) only when the set of resident solves changes. */
 int pf_batch_launch(void **batch, const int *iters);
+/* *on == 0: launch every kernel directly instead of replaying the graph.
+ * Both give bitwise the same results. */
+int pf_batch_set_graphs(void **batch, const int *on);
 /* Waits for the enqueued work and retires converged solves. */
 int pf_batch_sync(void **batch, int *n_active, int *n_done);
 /* Pops one retired solve: id, iterations, FP64 true relative residual and

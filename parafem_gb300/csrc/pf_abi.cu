@@ -80,8 +80,18 @@ static Ctx *get_ctx(void **h)
     return c;
 }
 
+static void drop_graph(Ctx &c)
+{
+    if (c.it_graph) cudaGraphExecDestroy(c.it_graph);
+    c.it_graph = nullptr;
+    c.it_prec = c.it_stop_mode = c.it_sym_cfg = -1;
+    c.it_xsol = nullptr;
+    c.it_launches = 0;
+}
+
 static void free_mesh(Ctx &c)
 {
+    drop_graph(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
     dfree(c.km32p);
@@ -121,16 +131,68 @@ static int check_kernel_error(Ctx &c)
     return 0;
 }
 
+constexpr int kGraphIters = 8;   // PCG iterations per graph replay
+
+// The graph of kGraphIters iterations for (prec, xsol) under the current
+// stopping test and element-kernel configuration, captured on first use.
+static int iteration_graph(Ctx &c, int prec, double *xsol, cudaGraphExec_t *out)
+{
+    if (c.it_graph && c.it_prec == prec && c.it_xsol == xsol && c.it_stop_mode == c.stop_mode &&
+        c.it_sym_cfg == c.sym_cfg) {
+        *out = c.it_graph;
+        return 0;
+    }
+    drop_graph(c);
+    const long long l0 = c.launches;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    int bad = 0;
+    for (int i = 0; i < kGraphIters && !bad; ++i) bad = launch_pcg_iteration(c, prec, xsol);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(c.stream, &g);
+    if (bad || ec != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        if (!bad) set_error("PCG iteration graph: capture failed: %s", cudaGetErrorString(ec));
+        c.launches = l0;
+        return 1;
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&c.it_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        c.it_graph = nullptr;
+        set_error("PCG iteration graph: instantiate failed: %s", cudaGetErrorString(ei));
+        c.launches = l0;
+        return 1;
+    }
+    c.it_launches = c.launches - l0;
+    c.launches = l0;
+    c.it_prec = prec;
+    c.it_xsol = xsol;
+    c.it_stop_mode = c.stop_mode;
+    c.it_sym_cfg = c.sym_cfg;
+    *out = c.it_graph;
+    return 0;
+}
+
 // Runs PCG iterations until the device state says stop.  The state is read
 // back every `chunk` iterations; iterations launched after the stop return
-// at once (every kernel checks the flag).
+// at once (every kernel checks the flag).  Whole groups of kGraphIters
+// iterations are replayed from a CUDA graph (one launch instead of five
+// per iteration); the remainder below the limit is launched directly.
 static int run_pcg(Ctx &c, int prec, double *xsol, int limit)
 {
     int launched = 0;
     int chunk = 4;
     for (;;) {
-        for (int i = 0; i < chunk && launched < limit; ++i, ++launched)
-            TRY(launch_pcg_iteration(c, prec, xsol));
+        int todo = chunk < limit - launched ? chunk : limit - launched;
+        if (c.use_graphs && todo >= kGraphIters) {
+            cudaGraphExec_t ge = nullptr;
+            TRY(iteration_graph(c, prec, xsol, &ge));
+            for (; todo >= kGraphIters; todo -= kGraphIters, launched += kGraphIters) {
+                CK(cudaGraphLaunch(ge, c.stream));
+                c.launches += c.it_launches;
+            }
+        }
+        for (; todo > 0; --todo, ++launched) TRY(launch_pcg_iteration(c, prec, xsol));
         TRY(pull_state(c));
         if (c.hst->stop || launched >= limit) break;
         if (chunk < 32) chunk *= 2;
@@ -279,7 +341,7 @@ extern "C" int pf_ctx_destroy(void **ctx)
     Ctx *c = (Ctx *)*ctx;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    free_mesh(*c);
+    free_mesh(*c);   // also drops the iteration graph
     if (c->st) cudaFree(c->st);
     if (c->kerr) cudaFree(c->kerr);
     if (c->hst) cudaFreeHost(c->hst);
@@ -442,6 +504,7 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
     TRY(launch_form_storkm(c, *nip, exact, true));
     TRY(launch_pack_sym32(c));
     TRY(launch_assemble_diag(c));
+    TRY(autotune_sym32(c, c.x));
     TRY(sync(c));
     c.have_km = true;
     return PF_SUCCESS;
@@ -458,6 +521,7 @@ extern "C" int pf_set_storkm(void **ctx, const double *storkm)
     TRY(launch_cast_km32(c));
     TRY(launch_pack_sym32(c));
     TRY(launch_assemble_diag(c));
+    TRY(autotune_sym32(c, c.x));
     TRY(sync(c));
     c.have_km = true;
     return PF_SUCCESS;
@@ -708,6 +772,46 @@ extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew
     TRY(launch_centroid_stress(c, *iel - 1, c.rres, sig));
     CK(cudaMemcpyAsync(sigma, sig, 6 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_tuning(void **ctx, int *warps, int *stages, float *ms)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp || !warps || !stages || !ms) return PF_FAILURE;
+    *warps = cp->sym_warps;
+    *stages = cp->sym_stages;
+    for (int i = 0; i < 3; ++i) ms[i] = cp->tune_ms[i];
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_tuning(void **ctx, const int *config)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp || !config) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (*config < -1 || *config > 2) {
+        set_error("pf_set_tuning: configuration %d is not in -1..2", *config);
+        return PF_FAILURE;
+    }
+    if (!c.km32p) {
+        set_error("pf_set_tuning: form or set storkm first");
+        return PF_FAILURE;
+    }
+    if (*config == -1) {
+        TRY(autotune_sym32(c, c.x));
+        return PF_SUCCESS;
+    }
+    set_sym_config(c, *config);
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_graphs(void **ctx, const int *on)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp || !on) return PF_FAILURE;
+    cp->use_graphs = *on != 0;
+    if (!cp->use_graphs) drop_graph(*cp);
     return PF_SUCCESS;
 }
 

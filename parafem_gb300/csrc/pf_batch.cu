@@ -18,9 +18,13 @@
 // by a device-memory budget fixed at creation (first-fit over the element
 // and node arenas); a request that does not fit yet gets PF_BUSY.
 //
-// The solve is p121's Jacobi-PCG (p121.f90:86-104) on FP64 storkm, stopped
-// at ||r||_2/||f||_2 <= tol; each retired solve reports the FP64 true
-// residual ||f - K x||_2/||f||_2 from one more element product.
+// The solve is p121's Jacobi-PCG (p121.f90:86-104) stopped at
+// ||r||_2/||f||_2 <= tol, with one of two element products chosen at
+// creation: FP64 storkm, or FP32 storkm with FP64 residual replacement per
+// mesh (the PF_MODE_MIXED scheme: a mesh whose recursive residual has
+// dropped 10x pauses, the host computes its FP64 true residual at the next
+// sync and either retires it or replaces its residual and resumes it).
+// Each retired solve reports the FP64 true residual ||f - K x||_2/||f||_2.
 #include "pf_device.cuh"
 #include "pfgpu.h"
 
@@ -99,6 +103,88 @@ k_bt_elem(int nseg, const BSeg *__restrict__ segs, long long total, const double
     }
 }
 
+// FP32 element products of every active mesh (mixed precision): full FP32
+// storkm, node-padded float results
+__global__ void __launch_bounds__(256)
+k_bt_elem32(int nseg, const BSeg *__restrict__ segs, long long total, const float *__restrict__ km,
+            const int *__restrict__ conn, const double *__restrict__ p, float *__restrict__ ut,
+            const PcgState *__restrict__ st)
+{
+    const int lane = threadIdx.x & 31;
+    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int j1 = lane + 32;
+    for (long long g = warp; g < total; g += nwarps) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (segs[mid].el_cum <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        if (st[segs[lo].sid].stop) continue;
+        const size_t e = (size_t)segs[lo].el0 + (size_t)(g - segs[lo].el_cum);
+        const int nd = (lane < 20) ? conn[e * 20 + lane] : 0;
+        const int n0 = __shfl_sync(FULLMASK, nd, lane / 3);
+        const int n1 = __shfl_sync(FULLMASK, nd, j1 < 60 ? j1 / 3 : 0);
+        const float p0 = (float)p[(size_t)3 * n0 + lane % 3];
+        const float p1 = (j1 < 60) ? (float)p[(size_t)3 * n1 + j1 % 3] : 0.f;
+        const float *ke = km + e * 3600 + 2 * lane;
+        float a0 = 0.f, a1 = 0.f;
+#pragma unroll 12
+        for (int j = 0; j < 60; ++j) {
+            const float pj = __shfl_sync(FULLMASK, j < 32 ? p0 : p1, j & 31);
+            if (lane < 30) {
+                const float2 k2 = __ldg(reinterpret_cast<const float2 *>(ke + 60 * j));
+                a0 = fmaf(k2.x, pj, a0);
+                a1 = fmaf(k2.y, pj, a1);
+            }
+        }
+        if (lane < 30) {
+            const int i0 = 2 * lane, i1 = 2 * lane + 1;
+            ut[e * 80 + (i0 / 3) * 4 + i0 % 3] = a0;
+            ut[e * 80 + (i1 / 3) * 4 + i1 % 3] = a1;
+        }
+    }
+}
+
+// residual replacement of one mesh: r = rres, d = dinv*r; partials r.d, r.r
+__global__ void __launch_bounds__(256)
+k_bt_replace1(BSeg S, const double *__restrict__ rres, const double *__restrict__ dinv, double *__restrict__ r,
+              double *__restrict__ d, double *__restrict__ part, int cap)
+{
+    const size_t s0 = (size_t)3 * S.node0 + (size_t)blockIdx.x * kVectorSlots;
+    const size_t s1 = min(s0 + kVectorSlots, (size_t)3 * (S.node0 + S.nn));
+    double rd = 0.0, rr = 0.0;
+    for (size_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
+        const double rv = rres[s], dv = dinv[s] * rv;
+        r[s] = rv;
+        d[s] = dv;
+        rd = fma(rv, dv, rd);
+        rr = fma(rv, rv, rr);
+    }
+    double v[2] = {rd, rr};
+    block_reduce<2>(v, 0u);
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = v[0];
+        part[cap + blockIdx.x] = v[1];
+    }
+}
+
+__global__ void k_bt_replace2(BSeg S, const double *__restrict__ part, int cap, double thr,
+                              PcgState *__restrict__ st)
+{
+    const double rd = reduce_partials(part, S.nbv, false);
+    const double rr = reduce_partials(part + cap, S.nbv, false);
+    if (threadIdx.x == 0) {
+        PcgState &T = st[S.sid];
+        T.up = rd;
+        T.rr = rr;
+        T.tol = thr;
+        T.converged = 0;
+        T.stop = rr == 0.0 ? 1 : 0;
+    }
+}
+
 // element products of one mesh (residual at retirement)
 __global__ void __launch_bounds__(256)
 k_bt_elem1(BSeg S, const double *__restrict__ km, const int *__restrict__ conn, const double *__restrict__ p,
@@ -110,36 +196,53 @@ k_bt_elem1(BSeg S, const double *__restrict__ km, const int *__restrict__ conn, 
     for (int g = warp; g < S.nels; g += nwarps) elem_product((size_t)S.el0 + g, lane, km, conn, p, ut);
 }
 
-// node-centric scatter of one block of one mesh (ascending element order)
-template <int MODE>
+// node-centric scatter of one node (ascending element order).  list[]
+// holds contribution indices e*20+a: FP64 results sit at ci*3, FP32 results
+// are node-padded float4s at ci and are summed in FP32.
+template <typename UT, int MODE>
 __device__ __forceinline__ double scatter_node(int n, const int2 *__restrict__ nptr, const int *__restrict__ list,
-                                               const double *__restrict__ ut, const uint8_t *__restrict__ fm,
+                                               const UT *__restrict__ ut, const uint8_t *__restrict__ fm,
                                                const double *__restrict__ pf, double *__restrict__ out)
 {
     const int2 pr = nptr[n];
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    UT a0 = 0, a1 = 0, a2 = 0;
     for (int k = pr.x; k < pr.y; k += 8) {
-        int off[8];
+        int ci[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) off[i] = (k + i < pr.y) ? __ldg(list + k + i) : -1;
-        double v[8][3];
+        for (int i = 0; i < 8; ++i) ci[i] = (k + i < pr.y) ? __ldg(list + k + i) : -1;
+        if constexpr (sizeof(UT) == 4) {
+            float4 v[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-            if (off[i] >= 0) {
-                v[i][0] = ut[off[i]];
-                v[i][1] = ut[off[i] + 1];
-                v[i][2] = ut[off[i] + 2];
-            }
+            for (int i = 0; i < 8; ++i)
+                if (ci[i] >= 0) v[i] = __ldg(reinterpret_cast<const float4 *>(ut) + ci[i]);
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
-            if (off[i] >= 0) {
-                a0 += v[i][0];
-                a1 += v[i][1];
-                a2 += v[i][2];
-            }
+            for (int i = 0; i < 8; ++i)
+                if (ci[i] >= 0) {
+                    a0 += v[i].x;
+                    a1 += v[i].y;
+                    a2 += v[i].z;
+                }
+        } else {
+            double v[8][3];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (ci[i] >= 0) {
+                    const double *q = ut + (size_t)ci[i] * 3;
+                    v[i][0] = q[0];
+                    v[i][1] = q[1];
+                    v[i][2] = q[2];
+                }
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (ci[i] >= 0) {
+                    a0 += v[i][0];
+                    a1 += v[i][1];
+                    a2 += v[i][2];
+                }
+        }
     }
     const int m = fm[n];
-    const double a[3] = {a0, a1, a2};
+    const double a[3] = {(double)a0, (double)a1, (double)a2};
     double loc = 0.0;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -158,9 +261,10 @@ __device__ __forceinline__ double scatter_node(int n, const int2 *__restrict__ n
     return loc;
 }
 
+template <typename UT>
 __global__ void __launch_bounds__(256)
 k_bt_scatter(const int *__restrict__ blk, const BSeg *__restrict__ segs, const int2 *__restrict__ nptr,
-             const int *__restrict__ list, const double *__restrict__ ut, const uint8_t *__restrict__ fm,
+             const int *__restrict__ list, const UT *__restrict__ ut, const uint8_t *__restrict__ fm,
              const double *__restrict__ p, double *__restrict__ u, double *__restrict__ part,
              const PcgState *__restrict__ st)
 {
@@ -168,7 +272,7 @@ k_bt_scatter(const int *__restrict__ blk, const BSeg *__restrict__ segs, const i
     const BSeg &S = segs[blk[b]];
     if (st[S.sid].stop) return;   // no kernel writes the flag meanwhile: uniform per block
     const int n = S.node0 + (b - S.pbs) * kScatterNodes + threadIdx.x;
-    double v[1] = {n < S.node0 + S.nn ? scatter_node<0>(n, nptr, list, ut, fm, p, u) : 0.0};
+    double v[1] = {n < S.node0 + S.nn ? scatter_node<UT, 0>(n, nptr, list, ut, fm, p, u) : 0.0};
     block_reduce<1>(v, 0u);
     if (threadIdx.x == 0) part[b] = v[0];
 }
@@ -180,7 +284,7 @@ k_bt_residual1(BSeg S, const int2 *__restrict__ nptr, const int *__restrict__ li
                double *__restrict__ rres, double *__restrict__ part)
 {
     const int n = S.node0 + blockIdx.x * kScatterNodes + threadIdx.x;
-    double v[1] = {n < S.node0 + S.nn ? scatter_node<1>(n, nptr, list, ut, fm, f, rres) : 0.0};
+    double v[1] = {n < S.node0 + S.nn ? scatter_node<double, 1>(n, nptr, list, ut, fm, f, rres) : 0.0};
     block_reduce<1>(v, 0u);
     if (threadIdx.x == 0) part[blockIdx.x] = v[0];
 }
@@ -195,7 +299,7 @@ __global__ void k_bt_diag(BSeg S, const int2 *__restrict__ nptr, const int *__re
     const int2 pr = nptr[n];
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
     for (int k = pr.x; k < pr.y; ++k) {
-        const double *q = ed + list[k];
+        const double *q = ed + (size_t)list[k] * 3;
         a0 += q[0];
         a1 += q[1];
         a2 += q[2];
@@ -364,7 +468,9 @@ struct FreeList {
 };
 
 struct Req {
-    int id = 0, nels = 0, nn = 0, neq = 0;
+    int id = 0, nels = 0, nn = 0, neq = 0, limit = 0;
+    double tol = 0.0;
+    int corrections = 0;
     int el0 = 0, node0 = 0, sid = 0;
     int nbs = 0, nbv = 0;
     std::vector<int> eq_slot;   // local slot of equation q+1
@@ -378,11 +484,13 @@ struct Done {
 
 struct Batch {
     int device = 0, nsm = 1;
+    int prec = 64;                   // 64: FP64 products; 32: FP32 products + FP64 residual replacement
     cudaStream_t stream = nullptr;
     long long cap_el = 0, cap_nodes = 0;
     int max_meshes = 0, capb_s = 0, capb_v = 0;
     // arenas
     double *km64 = nullptr, *coord = nullptr, *ediag = nullptr, *ut = nullptr, *mat_e = nullptr, *mat_v = nullptr;
+    float *km32 = nullptr;
     int *conn = nullptr, *list = nullptr;
     int2 *nptr = nullptr;
     uint8_t *fm = nullptr;
@@ -409,6 +517,13 @@ struct Batch {
     std::deque<Done> done;
     int next_id = 0;
     long long launches = 0;
+    // CUDA graph of one pf_batch_launch chunk, re-captured when the tables
+    // change (and updated in place when the topology allows)
+    bool use_graphs = true;
+    long long version = 0;           // bumped by every table rebuild
+    cudaGraphExec_t g_exec = nullptr;
+    int g_iters = 0;
+    long long g_version = -1, g_launches = 0;
 };
 
 #define BCK(call)                                                                        \
@@ -447,7 +562,7 @@ Batch *get_batch(void **h)
 
 void free_batch(Batch &B)
 {
-    void *ptrs[] = {B.km64, B.coord, B.ediag, B.ut, B.mat_e, B.mat_v, B.conn, B.list, B.nptr, B.fm, B.f, B.x, B.r,
+    void *ptrs[] = {B.km32, B.km64, B.coord, B.ediag, B.ut, B.mat_e, B.mat_v, B.conn, B.list, B.nptr, B.fm, B.f, B.x, B.r,
                     B.d, B.p, B.u, B.dinv, B.rres, B.part_s, B.part_u, B.part_i, B.scr, B.gp, B.st, B.d_segs,
                     B.d_blk_s, B.d_blk_v};
     for (void *q : ptrs)
@@ -455,6 +570,7 @@ void free_batch(Batch &B)
     if (B.hst) cudaFreeHost(B.hst);
     if (B.stage) cudaFreeHost(B.stage);
     if (B.stage_ev) cudaEventDestroy(B.stage_ev);
+    if (B.g_exec) cudaGraphExecDestroy(B.g_exec);
     if (B.stream) cudaStreamDestroy(B.stream);
 }
 
@@ -500,6 +616,7 @@ int rebuild_tables(Batch &B)
         BCK(cudaMemcpy(B.d_blk_v, bv.data(), bv.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
     B.dirty = false;
+    ++B.version;
     return 0;
 }
 
@@ -519,8 +636,10 @@ BSeg seg_of(const Req &q)
     return S;
 }
 
-// Retires one converged request: FP64 true residual, results to the host.
-int retire(Batch &B, int id)
+// A paused mesh: FP64 true residual; retire it (results to the host) or, in
+// the mixed mode while the true residual is above tol, replace its residual
+// and let it run on.
+int check_or_retire(Batch &B, int id)
 {
     Req &q = B.active[id];
     const BSeg S = seg_of(q);
@@ -531,20 +650,30 @@ int retire(Batch &B, int id)
     if (launched(B, "k_bt_residual1")) return 1;
     k_bt_sum<<<1, 256, 0, B.stream>>>(B.part_i, q.nbs, B.scr);
     if (launched(B, "k_bt_sum")) return 1;
-    const size_t ns = (size_t)3 * q.nn;
-    std::vector<double> xs(ns);
     double rr = 0.0;
-    BCK(cudaMemcpyAsync(xs.data(), B.x + (size_t)3 * q.node0, ns * sizeof(double), cudaMemcpyDeviceToHost,
-                        B.stream));
     BCK(cudaMemcpyAsync(&rr, B.scr, sizeof(double), cudaMemcpyDeviceToHost, B.stream));
     BCK(cudaStreamSynchronize(B.stream));
     const PcgState &T = B.hst[q.sid];
+    const double relt = T.ff > 0 ? std::sqrt(rr) / std::sqrt(T.ff) : 0.0;
+    if (B.prec == 32 && relt > q.tol && T.iters < q.limit && !T.err) {
+        const double thr = 0.1 * relt > q.tol ? 0.1 * relt : 0.5 * q.tol;
+        k_bt_replace1<<<q.nbv, 256, 0, B.stream>>>(S, B.rres, B.dinv, B.r, B.d, B.part_i, B.capb_v);
+        if (launched(B, "k_bt_replace1")) return 1;
+        k_bt_replace2<<<1, 256, 0, B.stream>>>(S, B.part_i, B.capb_v, thr, B.st);
+        if (launched(B, "k_bt_replace2")) return 1;
+        ++q.corrections;
+        return 0;
+    }
+    const size_t ns = (size_t)3 * q.nn;
+    std::vector<double> xs(ns);
+    BCK(cudaMemcpyAsync(xs.data(), B.x + (size_t)3 * q.node0, ns * sizeof(double), cudaMemcpyDeviceToHost,
+                        B.stream));
+    BCK(cudaStreamSynchronize(B.stream));
     Done dn;
     dn.id = id;
     dn.iters = T.iters;
     dn.neq = q.neq;
-    dn.relres = T.ff > 0 ? std::sqrt(rr) / std::sqrt(T.ff) : 0.0;
-    if (T.err) dn.relres = NAN;
+    dn.relres = T.err ? NAN : relt;
     dn.x.resize(q.neq);
     for (int e = 0; e < q.neq; ++e) dn.x[e] = xs[q.eq_slot[e]];
     B.done.push_back(std::move(dn));
@@ -557,16 +686,94 @@ int retire(Batch &B, int id)
     return 0;
 }
 
+// n batched PCG iterations over every active mesh, launched on B.stream.
+int batch_iterations(Batch &B, int n)
+{
+    long long ge = (B.total_el + 7) / 8;
+    if (ge > (long long)B.nsm * 8) ge = (long long)B.nsm * 8;
+    if (ge < 1) ge = 1;
+    for (int i = 0; i < n; ++i) {
+        if (B.prec == 32) {
+            k_bt_elem32<<<(int)ge, 256, 0, B.stream>>>(B.nseg, B.d_segs, B.total_el, B.km32, B.conn, B.p,
+                                                       (float *)B.ut, B.st);
+            if (launched(B, "k_bt_elem32")) return 1;
+            k_bt_scatter<float><<<B.nblk_s, 256, 0, B.stream>>>(B.d_blk_s, B.d_segs, B.nptr, B.list,
+                                                                (const float *)B.ut, B.fm, B.p, B.u, B.part_s,
+                                                                B.st);
+        } else {
+            k_bt_elem<<<(int)ge, 256, 0, B.stream>>>(B.nseg, B.d_segs, B.total_el, B.km64, B.conn, B.p, B.ut,
+                                                     B.st);
+            if (launched(B, "k_bt_elem")) return 1;
+            k_bt_scatter<double><<<B.nblk_s, 256, 0, B.stream>>>(B.d_blk_s, B.d_segs, B.nptr, B.list, B.ut, B.fm,
+                                                                 B.p, B.u, B.part_s, B.st);
+        }
+        if (launched(B, "k_bt_scatter")) return 1;
+        k_bt_update1<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_s, B.part_u, B.capb_v, B.x,
+                                                      B.r, B.d, B.p, B.u, B.dinv);
+        if (launched(B, "k_bt_update1")) return 1;
+        k_bt_update2<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_u, B.d, B.p);
+        if (launched(B, "k_bt_update2")) return 1;
+        k_bt_finish<<<B.nseg, 256, 0, B.stream>>>(B.d_segs, B.st, B.part_u, B.capb_v);
+        if (launched(B, "k_bt_finish")) return 1;
+    }
+    return 0;
+}
+
+// The graph of n iterations for the current tables: captured, then either
+// patched into the existing executable graph or instantiated.
+int batch_graph(Batch &B, int n)
+{
+    if (B.g_exec && B.g_iters == n && B.g_version == B.version) return 0;
+    const long long l0 = B.launches;
+    if (cudaStreamBeginCapture(B.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        set_error("batch graph: cannot begin capture");
+        return 1;
+    }
+    const int bad = batch_iterations(B, n);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(B.stream, &g);
+    B.g_launches = B.launches - l0;
+    B.launches = l0;
+    if (bad || ec != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        if (!bad) set_error("batch graph: capture failed: %s", cudaGetErrorString(ec));
+        return 1;
+    }
+    if (B.g_exec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(B.g_exec, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(B.g_exec);
+            B.g_exec = nullptr;
+        }
+    }
+    if (!B.g_exec) {
+        const cudaError_t ei = cudaGraphInstantiate(&B.g_exec, g, 0);
+        if (ei != cudaSuccess) {
+            B.g_exec = nullptr;
+            cudaGraphDestroy(g);
+            set_error("batch graph: instantiate failed: %s", cudaGetErrorString(ei));
+            return 1;
+        }
+    }
+    cudaGraphDestroy(g);
+    B.g_iters = n;
+    B.g_version = B.version;
+    return 0;
+}
+
 }  // namespace
 }  // namespace pf
 
 using namespace pf;
 
 // ===========================================================================
-extern "C" int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes, void **batch)
+extern "C" int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes,
+                               const int *prec, void **batch)
 {
-    if (!device || !budget_bytes || !max_meshes || !batch || *max_meshes < 1 || *budget_bytes < (1LL << 20)) {
-        set_error("pf_batch_create: invalid arguments");
+    if (!device || !budget_bytes || !max_meshes || !prec || !batch || *max_meshes < 1 ||
+        *budget_bytes < (1LL << 20) || (*prec != 64 && *prec != 32)) {
+        set_error("pf_batch_create: invalid arguments (prec must be 64 or 32)");
         return PF_FAILURE;
     }
     *batch = nullptr;
@@ -577,13 +784,15 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
         return PF_FAILURE;
     }
     B->device = *device;
+    B->prec = *prec;
     cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, B->device);
     if (B->nsm < 1) B->nsm = 1;
     B->max_meshes = *max_meshes;
     // bytes per element slot: storkm 28800, coord 480, conn 80, element diag 480,
     // results 480, node list 80, material 16; nodes: 7 per element slot at
     // 8 (ptr) + 1 (mask) + 8 vectors x 24 bytes
-    const long long per_el = 28800 + 480 + 80 + 480 + 480 + 80 + 16 + 7 * (8 + 1 + 8 * 24);
+    const long long per_el = 28800 + (B->prec == 32 ? 14400 : 0) + 480 + 80 + 480 + 480 + 80 + 16 +
+                             7 * (8 + 1 + 8 * 24);
     B->cap_el = *budget_bytes / per_el;
     if (B->cap_el > 0x7fffffffLL / 60) B->cap_el = 0x7fffffffLL / 60;
     B->cap_nodes = 7 * B->cap_el;
@@ -595,6 +804,7 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
         if (ok && cudaMalloc(ptr, bytes ? bytes : 1) != cudaSuccess) ok = false;
     };
     al((void **)&B->km64, E * 3600 * 8);
+    if (B->prec == 32) al((void **)&B->km32, E * 3600 * 4);
     al((void **)&B->coord, E * 60 * 8);
     al((void **)&B->ediag, E * 60 * 8);
     al((void **)&B->ut, E * 60 * 8);
@@ -757,7 +967,7 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
     for (size_t el = 0; el < (size_t)nels; ++el)
         for (int a = 0; a < 20; ++a) {
             const int n = g_num[el * 20 + a] - 1;
-            h_list[fill[n]++] = (int)((el0 + el) * 60 + 3 * a);   // local position, global offset
+            h_list[fill[n]++] = (int)((el0 + el) * 20 + a);   // local position, global contribution index
         }
     for (int n = 0; n < nn; ++n) {
         h_nptr[n].x = lbase + beg[n];
@@ -784,7 +994,7 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
     // state: tolerance, limit, stopping test
     PcgState T;
     memset(&T, 0, sizeof T);
-    T.tol = *tol;
+    T.tol = B.prec == 32 ? (0.1 > *tol ? 0.1 : *tol) : *tol;   // mixed: first replacement threshold
     T.limit = *limit;
     T.stop_mode = STOP_RELRES;
     T.stop = 1;   // inactive until the init kernel runs
@@ -803,6 +1013,8 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
     q.nbs = (nn + kScatterNodes - 1) / kScatterNodes;
     q.nbv = (int)((3LL * nn + kVectorSlots - 1) / kVectorSlots);
     q.eq_slot = std::move(eq_slot);
+    q.tol = *tol;
+    q.limit = *limit;
     const BSeg S = seg_of(q);
     // storkm, diagonal, PCG start of this mesh
     if (B.gp_nip != nip) {
@@ -810,7 +1022,8 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
         B.gp_nip = nip;
     }
     if (launch_form_storkm_raw(B.stream, B.nsm, nels, nip, B.gp, B.coord + (size_t)el0 * 60, B.mat_e + el0,
-                               B.mat_v + el0, nmat, B.km64 + (size_t)el0 * 3600, nullptr,
+                               B.mat_v + el0, nmat, B.km64 + (size_t)el0 * 3600,
+                               B.km32 ? B.km32 + (size_t)el0 * 3600 : nullptr,
                                B.ediag + (size_t)el0 * 60))
         return PF_FAILURE;
     B.launches++;
@@ -837,23 +1050,10 @@ extern "C" int pf_batch_launch(void **batch, const int *iters)
     Batch &B = *Bp;
     if (B.dirty && rebuild_tables(B)) return PF_FAILURE;
     if (B.nseg == 0) return PF_SUCCESS;
-    long long ge = (B.total_el + 7) / 8;
-    if (ge > (long long)B.nsm * 8) ge = (long long)B.nsm * 8;
-    if (ge < 1) ge = 1;
-    for (int i = 0; i < *iters; ++i) {
-        k_bt_elem<<<(int)ge, 256, 0, B.stream>>>(B.nseg, B.d_segs, B.total_el, B.km64, B.conn, B.p, B.ut, B.st);
-        if (launched(B, "k_bt_elem")) return PF_FAILURE;
-        k_bt_scatter<<<B.nblk_s, 256, 0, B.stream>>>(B.d_blk_s, B.d_segs, B.nptr, B.list, B.ut, B.fm, B.p, B.u,
-                                                      B.part_s, B.st);
-        if (launched(B, "k_bt_scatter")) return PF_FAILURE;
-        k_bt_update1<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_s, B.part_u, B.capb_v, B.x,
-                                                      B.r, B.d, B.p, B.u, B.dinv);
-        if (launched(B, "k_bt_update1")) return PF_FAILURE;
-        k_bt_update2<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_u, B.d, B.p);
-        if (launched(B, "k_bt_update2")) return PF_FAILURE;
-        k_bt_finish<<<B.nseg, 256, 0, B.stream>>>(B.d_segs, B.st, B.part_u, B.capb_v);
-        if (launched(B, "k_bt_finish")) return PF_FAILURE;
-    }
+    if (!B.use_graphs) return batch_iterations(B, *iters) ? PF_FAILURE : PF_SUCCESS;
+    if (batch_graph(B, *iters)) return PF_FAILURE;
+    BCK(cudaGraphLaunch(B.g_exec, B.stream));
+    B.launches += B.g_launches;
     return PF_SUCCESS;
 }
 
@@ -868,7 +1068,7 @@ extern "C" int pf_batch_sync(void **batch, int *n_active, int *n_done)
     for (int id : B.order)
         if (B.hst[B.active[id].sid].stop) fin.push_back(id);
     for (int id : fin)
-        if (retire(B, id)) return PF_FAILURE;
+        if (check_or_retire(B, id)) return PF_FAILURE;
     if (n_active) *n_active = (int)(B.order.size() + B.pending.size());
     if (n_done) *n_done = (int)B.done.size();
     return PF_SUCCESS;
@@ -897,6 +1097,14 @@ extern "C" int pf_batch_collect(void **batch, int *id, int *iters, double *relre
     *iters = dn.iters;
     *relres = dn.relres;
     B.done.pop_front();
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_batch_set_graphs(void **batch, const int *on)
+{
+    Batch *B = get_batch(batch);
+    if (!B || !on) return PF_FAILURE;
+    B->use_graphs = *on != 0;
     return PF_SUCCESS;
 }
 

@@ -29,8 +29,6 @@ namespace pf {
 
 namespace {
 
-constexpr int kWarps = 14;   // 14 warps x 2 stages x 7,328 B = 205 KB of stages per CTA
-constexpr int kStages = 2;
 constexpr int kPacked = 1832;                 // floats per element (1830 + 2 pad)
 constexpr int kPackedBytes = kPacked * 4;     // 7328
 constexpr unsigned kFull = 0xffffffffu;
@@ -105,6 +103,9 @@ __global__ void k_pack_sym32(int nels, const double *__restrict__ km, float *__r
 }
 
 // u_e = K_e p_e for every element, K_e from the packed FP32 triangle.
+// kWarps warps per CTA, kStages shared-memory stages per warp (tuned at
+// run time among the instantiations below).
+template <int kWarps, int kStages>
 __global__ void __launch_bounds__(kWarps * 32, 1)
 k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ conn,
              const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
@@ -221,9 +222,51 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
     }
 }
 
-size_t elem_sym32_smem_bytes()
+template <int W, int S>
+constexpr size_t sym_smem_bytes()
 {
-    return (size_t)kWarps * kStages * kPackedBytes + kWarps * 64 * 4 + kWarps * kStages * 8;
+    return (size_t)W * S * kPackedBytes + W * 64 * 4 + W * S * 8;
+}
+
+template <int W, int S>
+static int launch_sym_cfg(Ctx &c, const double *p, const PcgState *st)
+{
+    constexpr size_t smem = sym_smem_bytes<W, S>();
+    static_assert(smem <= 227 * 1024, "shared memory per CTA");
+    cudaError_t e;
+    // the attribute is set once per context and configuration, before any
+    // stream capture (the autotuner launches every configuration first)
+    const unsigned long long bit = 1ull << (W * 4 + S);   // W <= 15, S <= 3
+    if (!(c.sym_attr & bit)) {
+        e = cudaFuncSetAttribute(k_elem_sym32<W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) {
+            set_error("k_elem_sym32: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
+            return 1;
+        }
+        c.sym_attr |= bit;
+    }
+    const int grid = c.nels < c.nsm * W ? (c.nels + W - 1) / W : c.nsm;
+    k_elem_sym32<W, S><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km32p, c.conn, p, (float *)c.utemp, st, c.kerr);
+    c.launches++;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("k_elem_sym32: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+// the tuned configurations: (warps per CTA, stages per warp)
+static const int kSymCfg[][2] = {{14, 2}, {12, 2}, {8, 3}};
+constexpr int kNumSymCfg = 3;
+
+static int launch_sym_index(Ctx &c, int idx, const double *p, const PcgState *st)
+{
+    switch (idx) {
+    case 1: return launch_sym_cfg<12, 2>(c, p, st);
+    case 2: return launch_sym_cfg<8, 3>(c, p, st);
+    default: return launch_sym_cfg<14, 2>(c, p, st);
+    }
 }
 
 int launch_pack_sym32(Ctx &c)
@@ -240,22 +283,47 @@ int launch_pack_sym32(Ctx &c)
 
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st)
 {
-    const size_t smem = elem_sym32_smem_bytes();
-    cudaError_t e = cudaFuncSetAttribute(k_elem_sym32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) {
-        set_error("k_elem_sym32: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
+    return launch_sym_index(c, c.sym_cfg, p, st);
+}
+
+// Autotuner: times every configuration on this mesh (one warm-up and three
+// timed launches each, CUDA events on the context stream) and keeps the
+// fastest in c.sym_cfg.
+int autotune_sym32(Ctx &c, const double *p)
+{
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        set_error("autotune: cannot create events");
         return 1;
     }
-    const int grid = c.nels < c.nsm * kWarps ? (c.nels + kWarps - 1) / kWarps : c.nsm;
-    k_elem_sym32<<<grid, kWarps * 32, smem, c.stream>>>(c.nels, c.km32p, c.conn, p, (float *)c.utemp, st,
-                                                         c.kerr);
-    c.launches++;
-    e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        set_error("k_elem_sym32: launch failed: %s", cudaGetErrorString(e));
-        return 1;
+    float best = 1e30f;
+    int best_i = 0;
+    for (int i = 0; i < kNumSymCfg; ++i) {
+        if (launch_sym_index(c, i, p, nullptr)) return 1;
+        cudaEventRecord(a, c.stream);
+        for (int r = 0; r < 3; ++r)
+            if (launch_sym_index(c, i, p, nullptr)) return 1;
+        cudaEventRecord(b, c.stream);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        c.tune_ms[i] = ms / 3.0f;
+        if (ms < best) {
+            best = ms;
+            best_i = i;
+        }
     }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    set_sym_config(c, best_i);
     return 0;
+}
+
+void set_sym_config(Ctx &c, int idx)
+{
+    c.sym_cfg = idx;
+    c.sym_warps = kSymCfg[idx][0];
+    c.sym_stages = kSymCfg[idx][1];
 }
 
 }  // namespace pf

@@ -64,6 +64,16 @@ struct Ctx {
     void *utemp = nullptr;      // element results: FP64 [nels][60], or FP32 [nels][20][4]
                                 //   (x, y, z of each local node padded to 16 bytes)
     int stop_mode = 0;          // stopping test of the PCG run in flight
+    // CUDA graph of kGraphIters PCG iterations, keyed by what its launches bake in
+    cudaGraphExec_t it_graph = nullptr;
+    int it_prec = -1, it_stop_mode = -1, it_sym_cfg = -1;
+    double *it_xsol = nullptr;
+    long long it_launches = 0;  // kernels in one replay
+    bool use_graphs = true;
+    int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel
+    int sym_warps = 14, sym_stages = 2;
+    unsigned long long sym_attr = 0;   // configurations whose shared-memory attribute is set
+    float tune_ms[4] = {0, 0, 0, 0};
 
     int G = 0;                  // blocks of the vector kernels
     int Gs = 0;                 // blocks of the node scatter
@@ -111,6 +121,8 @@ int launch_centroid_stress(Ctx &c, int iel, const double *xslot, double *sig_dev
 enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31 };
 int launch_pack_sym32(Ctx &c);
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);
+int autotune_sym32(Ctx &c, const double *p);   // picks c.sym_cfg by timing on this mesh
+void set_sym_config(Ctx &c, int idx);           // 0: 14 warps x 2 stages, 1: 12 x 2, 2: 8 x 3
 int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs,
                           const double *mat, double *rhs, long long *launches);
 

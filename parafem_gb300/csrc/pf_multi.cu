@@ -135,12 +135,16 @@ __device__ __forceinline__ uint32_t kmajor_off(int row, int k)
 
 constexpr int kTileA = 128 * 64 * 2;   // 16384 B: 128 rows (60 used) x 64 K (60 used)
 constexpr int kTileB = 16 * 64 * 2;    // 2048 B: 16 load cases x 64 K
-constexpr int kTcSmem = 3 * kTileA + 3 * kTileB + 64;
+constexpr int kTcSmem = 2 * 3 * kTileA + 2 * 3 * kTileB + 64;   // two operand sets
 
 }  // namespace
 
 // Block element products on the tensor cores: ut[e][i][j] = sum_c K_e(i,c) P(slot(c), j).
-// One CTA of 128 threads per element at a time; 32 TMEM columns per CTA.
+// A persistent CTA of 128 threads works on a sequence of elements with two
+// sets of operand tiles and two TMEM accumulators: while the MMAs of element
+// t run on the tensor cores, the threads split and store the operands of
+// element t+1, then read back element t-1's accumulator.  Operands are
+// written 8 K-values (16 bytes) at a time.  64 TMEM columns per CTA.
 __global__ void __launch_bounds__(128)
 k_mr_elem_tc(int nels, const float *__restrict__ km32, const int *__restrict__ conn,
              const double *__restrict__ P, float *__restrict__ ut, int *__restrict__ err,
@@ -148,80 +152,40 @@ k_mr_elem_tc(int nels, const float *__restrict__ km32, const int *__restrict__ c
 {
     if (skip && *skip) return;   // a residual replacement is pending: nothing to compute
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char *A = sm;                     // 3 tiles
-    unsigned char *B = sm + 3 * kTileA;        // 3 tiles
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + 3 * kTileA + 3 * kTileB);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + 3 * kTileA + 3 * kTileB + 16);
-    int &s_fail = *reinterpret_cast<int *>(sm + 3 * kTileA + 3 * kTileB + 32);
+    unsigned char *A = sm;                             // [2 buffers][3 terms] tiles
+    unsigned char *B = sm + 2 * 3 * kTileA;            // [2][3]
+    unsigned char *aux = sm + 2 * 3 * kTileA + 2 * 3 * kTileB;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(aux);          // 2 mbarriers
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(aux + 16);
+    int &s_fail = *reinterpret_cast<int *>(aux + 32);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // zero every tile once: rows 60..127 and K 60..63 stay zero
-    for (int i = tid; i < (3 * kTileA + 3 * kTileB) / 16; i += blockDim.x)
+    for (int i = tid; i < (2 * 3 * kTileA + 2 * 3 * kTileB) / 16; i += blockDim.x)
         reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_addr(tslot))
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_addr(tslot))
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) mbar_init1(bar);
+    if (tid == 0) {
+        mbar_init1(&bar[0]);
+        mbar_init1(&bar[1]);
+        s_fail = 0;
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tslot;
-    uint32_t phase = 0;
-    if (tid == 0) s_fail = 0;
-    __syncthreads();
+    uint32_t phase[2] = {0, 0};
 
-    for (int e = blockIdx.x; e < nels; e += gridDim.x) {
-        // K_e -> three BF16 tiles (A: row i = output dof, K = input dof c)
-        const float *ke = km32 + (size_t)e * 3600;
-        for (int idx = tid; idx < 3600; idx += blockDim.x) {
-            const int c = idx / 60, i = idx - 60 * c;
-            uint16_t h1, h2, h3;
-            split3(ke[idx], h1, h2, h3);
-            const uint32_t o = kmajor_off(i, c);
-            *reinterpret_cast<uint16_t *>(A + o) = h1;
-            *reinterpret_cast<uint16_t *>(A + kTileA + o) = h2;
-            *reinterpret_cast<uint16_t *>(A + 2 * kTileA + o) = h3;
-        }
-        // P_e -> three BF16 tiles (B: row j = load case, K = dof c)
-        for (int idx = tid; idx < 60 * KR; idx += blockDim.x) {
-            const int c = idx / KR, j = idx - KR * c;
-            const int nd = conn[(size_t)e * 20 + c / 3];
-            const float x = (float)P[((size_t)3 * nd + c % 3) * KR + j];
-            uint16_t h1, h2, h3;
-            split3(x, h1, h2, h3);
-            const uint32_t o = kmajor_off(j, c);
-            *reinterpret_cast<uint16_t *>(B + o) = h1;
-            *reinterpret_cast<uint16_t *>(B + kTileB + o) = h2;
-            *reinterpret_cast<uint16_t *>(B + 2 * kTileB + o) = h3;
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
-            const int ta[6] = {0, 0, 1, 0, 1, 2};
-            const int tb[6] = {0, 1, 0, 2, 1, 0};
-            uint32_t acc = 0;
-            for (int t = 0; t < 6; ++t) {
-                const uint32_t a0 = smem_addr(A + ta[t] * kTileA), b0 = smem_addr(B + tb[t] * kTileB);
-                for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
-                    mma_bf16(tmem, umma_desc(a0 + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024), acc);
-                    acc = 1;
-                }
-            }
-            mma_commit(bar);
-        }
-        const bool ok = mbar_wait_bounded(bar, phase);
-        if (!ok) atomicOr(&s_fail, 1);
-        phase ^= 1;
-        __syncthreads();
-        if (s_fail) break;
+    // epilogue of the element whose MMAs went into accumulator `buf`
+    auto epilogue = [&](int e, int buf) {
+        if (!mbar_wait_bounded(&bar[buf], phase[buf])) atomicOr(&s_fail, 1);
+        phase[buf] ^= 1;
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (warp < 2) {   // rows 0..63 live in TMEM lanes 0..63 (warps 0 and 1)
             float v[16];
-            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * warp) << 16), v);
+            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * buf), v);
             const int row = 32 * warp + lane;
             if (row < 60) {
                 float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)e * 60 + row) * KR);
@@ -231,17 +195,99 @@ k_mr_elem_tc(int nels, const float *__restrict__ km32, const int *__restrict__ c
                 o[3] = make_float4(v[12], v[13], v[14], v[15]);
             }
         }
+    };
+
+    int t = 0, prev_e = -1;
+    for (int e = blockIdx.x; e < nels; e += gridDim.x, ++t) {
+        const int buf = t & 1;
+        unsigned char *Ab = A + buf * 3 * kTileA, *Bb = B + buf * 3 * kTileB;
+        // operands of element e: K rows i, 8 K-values (input dofs) per task
+        const float *ke = km32 + (size_t)e * 3600;
+        for (int task = tid; task < 60 * 8; task += blockDim.x) {
+            const int q = task / 60, i = task - 60 * q;
+            uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+            for (int r = 0; r < 8; r += 2) {
+                const int c0 = 8 * q + r, c1 = c0 + 1;
+                const float x0 = c0 < 60 ? ke[60 * c0 + i] : 0.f, x1 = c1 < 60 ? ke[60 * c1 + i] : 0.f;
+                uint16_t a1, a2, a3, b1, b2, b3;
+                split3(x0, a1, a2, a3);
+                split3(x1, b1, b2, b3);
+                w1[r / 2] = (uint32_t)a1 | ((uint32_t)b1 << 16);
+                w2[r / 2] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+                w3[r / 2] = (uint32_t)a3 | ((uint32_t)b3 << 16);
+            }
+            const uint32_t o = kmajor_off(i, 8 * q);
+            *reinterpret_cast<uint4 *>(Ab + o) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+            *reinterpret_cast<uint4 *>(Ab + kTileA + o) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+            *reinterpret_cast<uint4 *>(Ab + 2 * kTileA + o) = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+        }
+        {   // P_e: one task per thread, case j, 8 dofs
+            const int j = tid & (KR - 1), q = tid >> 4;   // 16 cases x 8 chunks = 128 tasks
+            uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+            for (int r = 0; r < 8; r += 2) {
+                float xv[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int c = 8 * q + r + h;
+                    xv[h] = 0.f;
+                    if (c < 60) {
+                        const int nd = conn[(size_t)e * 20 + c / 3];
+                        xv[h] = (float)P[((size_t)3 * nd + c % 3) * KR + j];
+                    }
+                }
+                uint16_t a1, a2, a3, b1, b2, b3;
+                split3(xv[0], a1, a2, a3);
+                split3(xv[1], b1, b2, b3);
+                w1[r / 2] = (uint32_t)a1 | ((uint32_t)b1 << 16);
+                w2[r / 2] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+                w3[r / 2] = (uint32_t)a3 | ((uint32_t)b3 << 16);
+            }
+            const uint32_t o = kmajor_off(j, 8 * q);
+            *reinterpret_cast<uint4 *>(Bb + o) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+            *reinterpret_cast<uint4 *>(Bb + kTileB + o) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+            *reinterpret_cast<uint4 *>(Bb + 2 * kTileB + o) = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
+            const int ta[6] = {0, 0, 1, 0, 1, 2};
+            const int tb[6] = {0, 1, 0, 2, 1, 0};
+            uint32_t acc = 0;
+            for (int tt = 0; tt < 6; ++tt) {
+                const uint32_t a0 = smem_addr(Ab + ta[tt] * kTileA), b0 = smem_addr(Bb + tb[tt] * kTileB);
+                for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
+                    mma_bf16(tmem + (uint32_t)(16 * buf), umma_desc(a0 + ks * 256, 128, 1024),
+                             umma_desc(b0 + ks * 256, 128, 1024), acc);
+                    acc = 1;
+                }
+            }
+            mma_commit(&bar[buf]);
+        }
+        // meanwhile: the previous element's accumulator
+        if (prev_e >= 0) epilogue(prev_e, buf ^ 1);
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (s_fail) break;
+        prev_e = e;
+    }
+    if (prev_e >= 0 && !s_fail) {
+        epilogue(prev_e, (t - 1) & 1);
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
     }
     if (s_fail) {
         if (tid == 0) atomicExch(err, 3);
-        // give the outstanding MMAs a bounded chance to finish before TMEM goes back
-        mbar_wait_bounded(bar, phase);
+        // give outstanding MMAs a bounded chance to finish before TMEM goes back
+        mbar_wait_bounded(&bar[0], phase[0]);
+        mbar_wait_bounded(&bar[1], phase[1]);
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(tmem) : "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
 }
 
 // Block element products on CUDA cores (FP32 or FP64): one warp per element,
@@ -302,15 +348,15 @@ k_mr_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list, 
     double loc = 0.0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nn * KR; t += gridDim.x * blockDim.x) {
         const int n = t / KR;
-        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        UT a0 = 0, a1 = 0, a2 = 0;   // FP32 products are summed in FP32, FP64 ones in FP64
         for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
             const size_t base = (size_t)list[k] * 3 * KR + j;   // list holds e*20+a
-            a0 += (double)ut[base];
-            a1 += (double)ut[base + KR];
-            a2 += (double)ut[base + 2 * KR];
+            a0 += ut[base];
+            a1 += ut[base + KR];
+            a2 += ut[base + 2 * KR];
         }
         const int m = fm[n];
-        const double a[3] = {a0, a1, a2};
+        const double a[3] = {(double)a0, (double)a1, (double)a2};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const size_t s = ((size_t)3 * n + d) * KR + j;
@@ -592,7 +638,7 @@ static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
     if (prec == 16) {
         const int smem = kTcSmem;
         MCK(cudaFuncSetAttribute(k_mr_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        const int grid = c.nels < c.nsm * 4 ? c.nels : c.nsm * 4;
+        const int grid = c.nels < c.nsm * 2 ? c.nels : c.nsm * 2;
         k_mr_elem_tc<<<grid, 128, smem, c.stream>>>(c.nels, c.km32, c.conn, P, m.ut32, c.kerr, skip);
         return mr_launched(c, "k_mr_elem_tc");
     }
@@ -692,11 +738,20 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
     double *pu = m.part + (size_t)Gs * KR;   // update partials after the scatter partials
     int total = 0, chunk = 4, corrections = 0;
     double rel[KR] = {0};
+    // per-kernel timing of the iterations: events around the element product
+    // and the scatter of every launched iteration (pool reused per chunk)
+    constexpr int kMaxChunk = 32;
+    cudaEvent_t tev[3 * kMaxChunk];
+    for (auto &ev : tev) MCK(cudaEventCreate(&ev));
+    double ms_elem = 0.0, ms_scat = 0.0, ms_iter = 0.0;
     for (;;) {
         for (int i = 0; i < chunk; ++i) {
             const int *skip = &m.st->any_flag;
+            MCK(cudaEventRecord(tev[3 * i], c.stream));
             if (mr_elem(c, *prec, m.P, skip)) return PF_FAILURE;
+            MCK(cudaEventRecord(tev[3 * i + 1], c.stream));
             if (mr_scatter(c, *prec, 0, m.P, m.U, skip)) return PF_FAILURE;
+            MCK(cudaEventRecord(tev[3 * i + 2], c.stream));
             k_mr_update1<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.part, Gs, pu, G, m.X, m.R, m.D, m.P, m.U,
                                                   c.dinv);
             if (mr_launched(c, "k_mr_update1")) return PF_FAILURE;
@@ -706,9 +761,18 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
             if (mr_launched(c, "k_mr_finish")) return PF_FAILURE;
         }
         total += chunk;
-        if (chunk < 32) chunk *= 2;
         MCK(cudaMemcpyAsync(m.hst, m.st, sizeof(MState), cudaMemcpyDeviceToHost, c.stream));
         MCK(cudaStreamSynchronize(c.stream));
+        for (int i = 0; i < chunk; ++i) {
+            float a = 0.f, b = 0.f, d = 0.f;
+            cudaEventElapsedTime(&a, tev[3 * i], tev[3 * i + 1]);
+            cudaEventElapsedTime(&b, tev[3 * i + 1], tev[3 * i + 2]);
+            if (i + 1 < chunk) cudaEventElapsedTime(&d, tev[3 * i], tev[3 * i + 3]);
+            ms_elem += a;
+            ms_scat += b;
+            ms_iter += d;
+        }
+        if (chunk < kMaxChunk) chunk *= 2;
         int kerr = 0;
         MCK(cudaMemcpy(&kerr, c.kerr, sizeof(int), cudaMemcpyDeviceToHost));
         if (kerr) {
@@ -745,6 +809,7 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
         ++corrections;
         chunk = 4;
     }
+    for (auto &ev : tev) cudaEventDestroy(ev);
     MCK(cudaEventRecord(e1, c.stream));
     k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, c.eq_slot, m.X, m.eq);
     if (mr_launched(c, "k_mr_slot_to_eq")) return PF_FAILURE;
@@ -762,6 +827,10 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
     for (int j = 0; j < KR; ++j) c.stats[0] = iters[j] > c.stats[0] ? iters[j] : c.stats[0];
     c.stats[1] = corrections;
     c.stats[2] = ms;
+    c.stats[3] = ms_elem;   // summed element-product time of the launched iterations
+    c.stats[4] = ms_scat;   // summed scatter time
+    c.stats[5] = ms_iter;   // summed time of the iterations measured start to start
+    c.stats[6] = total;     // iterations launched (including no-op ones after a flag)
     return PF_SUCCESS;
 }
 

@@ -56,13 +56,16 @@ _SIGS = {
     "pf_bench_iterations": [_VPP, _IP, _IP, _DP, _DP, _DP],
     "pf_centroid_stress": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_kernel_launches": [_VPP, _LLP],
+    "pf_tuning": [_VPP, _IP, _IP, ctypes.c_void_p],
+    "pf_set_tuning": [_VPP, _IP],
+    "pf_set_graphs": [_VPP, _IP],
     "pf_ebe_matvec_noalloc": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p],
     "pf_solve_multi": [_VPP, _IP, ctypes.c_void_p, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p,
                        ctypes.c_void_p],
     "pf_ebe_matvec_multi": [_VPP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_multi_free": [],
-    "pf_batch_create": [_IP, _LLP, _IP, _VPP],
+    "pf_batch_create": [_IP, _LLP, _IP, _IP, _VPP],
     "pf_batch_destroy": [_VPP],
     "pf_batch_capacity": [_VPP, _LLP, _LLP],
     "pf_batch_admit": [_VPP, _IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP,
@@ -71,6 +74,7 @@ _SIGS = {
     "pf_batch_sync": [_VPP, _IP, _IP],
     "pf_batch_collect": [_VPP, _IP, _IP, _DP, ctypes.c_void_p, _IP, _IP],
     "pf_batch_launches": [_VPP, _LLP],
+    "pf_batch_set_graphs": [_VPP, _IP],
     "pf_p12meshgen": [ctypes.c_char_p],
     "pf_p121_run": [ctypes.c_char_p, _IP, _IP, _IP, _DP],
     "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
@@ -272,10 +276,17 @@ class Solver:
         return x, it.value, rel.value
 
     def stats(self):
+        """Statistics of the last pf_solve (see pf_solve_stats)."""
+        keys = ["iters", "outer", "solve_ms", "metric", "matvec64", "matvec32", "relres"]
+        return dict(zip(keys, self.stats_raw().tolist()))
+
+    def stats_raw(self):
+        """The 8 raw statistics words; after pf_solve_multi: [0] max iterations,
+        [1] corrections, [2] solve ms, [3] element-product ms, [4] scatter ms,
+        [5] iteration ms, [6] iterations launched."""
         s = np.zeros(8)
         _check(lib().pf_solve_stats(self._ref, s.ctypes.data, _i(8)), "pf_solve_stats")
-        keys = ["iters", "outer", "solve_ms", "metric", "matvec64", "matvec32", "relres"]
-        return dict(zip(keys, s.tolist()))
+        return s
 
     def bench_iterations(self, prec: int, steps: int):
         a, b, c = ctypes.c_double(0), ctypes.c_double(0), ctypes.c_double(0)
@@ -313,6 +324,22 @@ class Solver:
         _check(lib().pf_kernel_launches(self._ref, ctypes.byref(n)), "pf_kernel_launches")
         return n.value
 
+    def tuning(self):
+        """The autotuned (warps, stages) of the packed-symmetric kernel and the timed configurations."""
+        w, st = ctypes.c_int(0), ctypes.c_int(0)
+        ms = np.zeros(3, np.float32)
+        _check(lib().pf_tuning(self._ref, ctypes.byref(w), ctypes.byref(st), ms.ctypes.data), "pf_tuning")
+        return {"warps": w.value, "stages": st.value,
+                "ms": {"14x2": float(ms[0]), "12x2": float(ms[1]), "8x3": float(ms[2])}}
+
+    def set_graphs(self, on: bool) -> None:
+        """Replay PCG iterations from a CUDA graph (default) or launch each kernel directly."""
+        _check(lib().pf_set_graphs(self._ref, ctypes.byref(ctypes.c_int(1 if on else 0))), "pf_set_graphs")
+
+    def set_tuning(self, config: int) -> None:
+        """Force configuration 0 (14x2), 1 (12x2) or 2 (8x3); -1 re-runs the autotuner."""
+        _check(lib().pf_set_tuning(self._ref, ctypes.byref(ctypes.c_int(config))), "pf_set_tuning")
+
 
 PF_BUSY = 2
 
@@ -321,10 +348,11 @@ class Batch:
     """Continuous-batching engine (pf_batch_*): many solves resident at once,
     admitted by a device-memory budget, retired when converged."""
 
-    def __init__(self, budget_bytes: int, max_meshes: int = 256, device: int = 0):
+    def __init__(self, budget_bytes: int, max_meshes: int = 256, device: int = 0, prec: int = 64):
+        """prec 64: FP64 element products; 32: FP32 products with FP64 residual replacement."""
         self._h = ctypes.c_void_p(None)
         _check(lib().pf_batch_create(_i(device), ctypes.byref(ctypes.c_longlong(int(budget_bytes))),
-                                     _i(max_meshes), ctypes.byref(self._h)), "pf_batch_create")
+                                     _i(max_meshes), _i(prec), ctypes.byref(self._h)), "pf_batch_create")
 
     @property
     def _ref(self):
@@ -389,6 +417,11 @@ class Batch:
         n = ctypes.c_longlong(0)
         _check(lib().pf_batch_launches(self._ref, ctypes.byref(n)), "pf_batch_launches")
         return n.value
+
+    def set_graphs(self, on: bool) -> None:
+        """Replay iteration chunks from a CUDA graph (default) or launch each kernel directly."""
+        _check(lib().pf_batch_set_graphs(self._ref, ctypes.byref(ctypes.c_int(1 if on else 0))),
+               "pf_batch_set_graphs")
 
     def run_all(self, x_cap: int, chunk: int = 8):
         """Iterates until every resident solve has retired; returns the results."""

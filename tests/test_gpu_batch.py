@@ -89,3 +89,47 @@ def test_admission_is_bounded_by_the_budget():
         assert sorted(res) == admitted
         # retired solves freed their ranges: the next request fits again
         assert admit(b, prob, e, v) is not None
+
+
+def test_mixed_batch_same_alone_and_in_the_mix_and_accurate():
+    reqs = [request(sp) for sp in SPECS[:3]]
+    cap = max(p["neq"] for p, _, _ in reqs)
+    alone = []
+    for prob, e, v in reqs:
+        with P.Batch(2 << 30, 8, prec=32) as b:
+            sid = admit(b, prob, e, v)
+            alone.append(b.run_all(cap)[sid])
+    with P.Batch(2 << 30, 8, prec=32) as b:
+        ids = [admit(b, *r) for r in reqs]
+        res = b.run_all(cap, chunk=5)
+    for k, sid in enumerate(ids):
+        assert alone[k][0] == res[sid][0]
+        assert np.array_equal(alone[k][2], res[sid][2])
+        prob, e, v = reqs[k]
+        with P.Solver() as s:
+            s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+            s.set_material(e, v)
+            s.form_storkm(27)
+            x_ref, _, _ = s.solve(prob["r"], 1e-12, 20000, P.MODE_FP64_RES)
+        it, rel, x = res[sid]
+        assert 0.0 < rel <= 1e-9
+        assert np.linalg.norm(x - x_ref) <= 1e-7 * np.linalg.norm(x_ref)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_graph_replay_matches_direct_launches(prec):
+    reqs = [request(sp) for sp in SPECS]
+    cap = max(p["neq"] for p, _, _ in reqs)
+    runs = []
+    for graphs in (True, False):
+        with P.Batch(2 << 30, 8, prec=prec) as b:
+            b.set_graphs(graphs)
+            ids = [admit(b, *r) for r in reqs[:3]]
+            b.launch(6)
+            b.sync()
+            ids += [admit(b, *reqs[3])]      # the tables change: a new graph
+            res = b.run_all(cap, chunk=4)
+            runs.append([res[i] for i in ids])
+    for (it_g, rel_g, x_g), (it_d, rel_d, x_d) in zip(*runs):
+        assert it_g == it_d and rel_g == rel_d
+        assert np.array_equal(x_g, x_d)

@@ -195,6 +195,46 @@ def test_packed_symmetric_product_is_symmetric_and_deterministic(demo_problem):
     assert abs(b @ ka - a @ kb) <= 1e-6 * abs(b @ ka)
 
 
+def test_autotuned_configurations_give_bitwise_equal_products(demo_problem):
+    p = demo_problem
+    d = p["deck"]
+    a = np.random.default_rng(9).standard_normal(p["neq"])
+    with P.Solver() as s:
+        s.setup(d.g_num, p["g_g"], p["gc"], d.nn, p["neq"])
+        s.set_storkm(p["km"])
+        t = s.tuning()
+        assert (t["warps"], t["stages"]) in ((14, 2), (12, 2), (8, 3))
+        assert all(v > 0 for v in t["ms"].values())
+        outs = []
+        for cfg in (0, 1, 2):
+            s.set_tuning(cfg)
+            outs.append(s.ebe_matvec(a, 32))
+        s.set_tuning(-1)
+        with pytest.raises(P.PfError):
+            s.set_tuning(3)
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("mode", [P.MODE_P121, P.MODE_MIXED])
+def test_graph_replay_gives_bitwise_equal_iterates(mode):
+    prob = P.cube_problem(7, 7, 7)
+    res = []
+    for graphs in (True, False):
+        with P.Solver() as s:
+            s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+            s.set_material(100.0, 0.3)
+            s.form_storkm(27)
+            s.set_graphs(graphs)
+            s.set_tuning(0)
+            x, it, rel = s.solve(prob["r"], 1e-8, 5000, mode)
+            res.append((x, it, rel, s.launches()))
+    (xa, ia, ra, la), (xb, ib, rb, lb) = res
+    assert ia == ib and ra == rb
+    assert np.array_equal(xa, xb)
+    # a replay launches every kernel of its iterations, counted the same way
+    assert abs(la - lb) <= 5 * 8 * 4
+
+
 def test_mixed_restart_mode_also_converges():
     prob = P.cube_problem(6, 6, 6)
     with P.Solver() as s:
