@@ -46,9 +46,11 @@ def parse_args():
     ap.add_argument("--size", type=int, default=100, help="elements per cube edge")
     ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--workload", default="cube100", choices=["cube100", "hetero80", "serving", "multirhs60", "cube10"],
+    ap.add_argument("--workload", default="cube100",
+                    choices=["cube100", "hetero80", "serving", "multirhs60", "cube10", "shared100"],
                     help="cube100: the headline; hetero80: per-element E and v, accuracy study; "
-                         "serving: continuous batching of a Poisson request stream")
+                         "serving: continuous batching of a Poisson request stream; shared100: one element "
+                         "matrix for every element (PCG_KM)")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
     ap.add_argument("--rates", default="20", help="serving: comma-separated arrival rates (requests/s); "
                                                     "0 = all requests at t=0")
@@ -547,6 +549,68 @@ def run_multirhs(args, rank, world, local, dist):
     return 0
 
 
+def run_shared(args, rank, world, local, dist):
+    """The 100^3 cube of the headline with one element matrix shared by every
+    element (PCG_KM): km of element 1 formed on the GPU, no per-element
+    storkm.  Mixed (tensor-core products) and FP64 time to relres 1e-8,
+    device-resident steps of both, and the tensor-core kernel's roofline."""
+    import parafem_gb300 as P
+    n = args.size
+    prob = P.cube_problem(n, n, n)
+    s = P.Solver(local)
+    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+    s.set_material(100.0, 0.3)
+    km = s.form_km(1, 27)
+    s.set_shared_km(km)
+    neq, nels, r = prob["neq"], n ** 3, prob["r"]
+    out = {}
+    if not args.no_solves:
+        for name, mode in (("mixed", P.MODE_MIXED), ("fp64", P.MODE_FP64_RES)):
+            t0 = time.perf_counter()
+            x, it, rel = s.solve(r, 1e-8, 50000, mode)
+            wall = time.perf_counter() - t0
+            st = s.stats()
+            out[name] = {"iters": it, "relres": rel, "wall_s": wall, "device_s": st["solve_ms"] / 1e3,
+                         "corrections": st["outer"]}
+            if name == "mixed":
+                xm = x
+        out["mixed_over_fp64_time"] = out["mixed"]["wall_s"] / out["fp64"]["wall_s"]
+        out["mixed_vs_fp64_rel_err_2"] = float(np.linalg.norm(xm - x) / np.linalg.norm(x))
+    else:
+        s.solve(r, 1e-8, 1, P.MODE_MIXED)       # loads the right-hand side only
+    s.bench_iterations(32, max(args.warmup, 3))
+    clk = Clocks(local).start() if rank == 0 else None
+    l0 = s.launches()
+    ms_tot, ms_elem, ms_scat = s.bench_iterations(32, args.steps)
+    launches = s.launches() - l0
+    clocks = clk.stop() if clk else None
+    k2 = max(args.steps // 4, 3)
+    ms64, ms64_elem, _ = s.bench_iterations(64, k2)
+    s.close()
+    value = neq * args.steps / (ms_tot / 1e3)
+    peak, peak_kind = measured_peaks()
+    nslots = 3 * prob["nn"]
+    b_launch = elem_bytes(nels, nslots, 0, 16 / 3)   # connectivity, gathered p, node-padded FP32 results
+    avg_s = ms_elem / args.steps / 1e3
+    achieved = b_launch / avg_s / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16x3 tensor-core products, f32 accumulation / f64 vectors and reductions",
+            "data": "synthetic",
+            "config": {"workload": f"{n}^3 hex20 cube, one shared element matrix (PCG_KM), E 100, v 0.3, nip 27, "
+                                   f"fixed base, top pressure", "nels": nels, "neq": neq},
+            "roofline": {"kernel": "k_elem_shared_tc (shared km, tcgen05 BF16x3)", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": b_launch,
+                         "avg_launch_ms": avg_s * 1e3, "traffic": None, "scatter_avg_ms": ms_scat / args.steps},
+            "fp64_step_ms": ms64 / k2, "fp64_elem_ms": ms64_elem / k2,
+            "gpu_launches": int(launches), "clocks": clocks, "solves": out}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def run_cube10(args, rank, world, local, dist):
     """The reference's CPU-runnable case: 10^3 cube, nip 27, E 100, v 0.3,
     fixed base, top pressure (total -1), checon_par tol 1e-6, limit 5000.
@@ -602,6 +666,8 @@ def main():
             return run_multirhs(args, rank, world, local, dist)
         if args.workload == "cube10":
             return run_cube10(args, rank, world, local, dist)
+        if args.workload == "shared100":
+            return run_shared(args, rank, world, local, dist)
         return run_gb300(args, rank, world, local, dist)
     finally:
         if dist is not None:

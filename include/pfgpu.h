@@ -97,6 +97,22 @@ int pf_form_storkm(void **ctx, const int *nip, const int *flags);
  * copy for PF_MODE_MIXED is derived on the device). */
 int pf_set_storkm(void **ctx, const double *storkm);
 
+/* Forms the stiffness matrix of element iel (1-based) of the mesh, with
+ * its material, on the GPU into km(60,60) on the host: the km a PCG_KM
+ * caller integrates once for a uniform mesh. */
+int pf_form_km(void **ctx, const int *iel, const int *nip, const int *flags, double *km);
+
+/* One element matrix km(60,60) for every element, replacing PCG_KM
+ * (src/modules/mpi/maths.f90:1152-1323; the uniform-mesh case of xx9,
+ * src/programs/dev/xx9/mathsgpu.f90).  The Jacobi diagonal is assembled
+ * from diag(km) over the mesh, and every later pf_solve / pf_ebe_matvec /
+ * pf_bench_iterations uses km: FP64 products on CUDA cores for
+ * PF_MODE_P121 and PF_MODE_FP64_RES, tensor-core products (BF16 x3 split,
+ * FP32 accumulation) for the inner iterations of PF_MODE_MIXED.  No
+ * per-element storkm is held; pf_form_storkm / pf_set_storkm switch back.
+ * pf_solve_multi and pf_get_storkm need per-element storkm. */
+int pf_set_shared_km(void **ctx, const double *km);
+
 /* Copies elements first..first+count-1 (0-based) of the FP64 storkm back. */
 int pf_get_storkm(void **ctx, const int *first, const int *count, double *storkm);
 

@@ -18,9 +18,10 @@ LIB = os.path.join(OUT, "libpfgpu.so")
 EXE = os.path.join(OUT, "p121")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["pf_kernels.cu", "pf_elem_sym.cu", "pf_batch.cu", "pf_multi.cu", "pf_abi.cu", "pf_noalloc.cu"]
+CUDA_SOURCES = ["pf_kernels.cu", "pf_elem_sym.cu", "pf_shared.cu", "pf_batch.cu", "pf_multi.cu", "pf_abi.cu",
+                "pf_noalloc.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
-HEADERS = ["pf_internal.h", "pf_device.cuh"]
+HEADERS = ["pf_internal.h", "pf_device.cuh", "pf_tc.cuh"]
 
 _lock = threading.Lock()
 

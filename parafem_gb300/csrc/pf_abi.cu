@@ -94,7 +94,8 @@ static void free_mesh(Ctx &c)
     drop_graph(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
-    dfree(c.km32p);
+    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32);
+    c.shared = false;
     dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
     dfree(c.d); dfree(c.p); dfree(c.u); dfree(c.rres); dfree(c.eqbuf); dfree(c.utemp); dfree(c.part);
     c.nels = c.nn = c.neq = c.nslots = 0;
@@ -434,9 +435,7 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
     if (dalloc(&c.conn, ne * 20, "connectivity") || dalloc(&c.node_ptr, nn + 1, "node table") ||
         dalloc(&c.node_list, ne * 20, "node table") || dalloc(&c.slot_eq, ns, "slot map") ||
         dalloc(&c.eq_slot, neq, "equation map") || dalloc(&c.freemask, nn, "restraint mask") ||
-        dalloc(&c.coord, ne * 60, "coordinates") || dalloc(&c.km64, ne * 3600, "FP64 storkm") ||
-        dalloc(&c.km32, ne * 3600, "FP32 storkm") || dalloc(&c.km32p, ne * 1832, "packed FP32 storkm") ||
-        dalloc(&c.ediag, ne * 60, "element diagonals") ||
+        dalloc(&c.coord, ne * 60, "coordinates") || dalloc(&c.ediag, ne * 60, "element diagonals") ||
         dalloc(&c.diag, ns, "diag") || dalloc(&c.dinv, ns, "diag") || dalloc(&c.f, ns, "f") ||
         dalloc(&c.x, ns, "x") || dalloc(&c.c, ns, "c") || dalloc(&c.r, ns, "r") || dalloc(&c.d, ns, "d") ||
         dalloc(&c.p, ns, "p") || dalloc(&c.u, ns, "u") || dalloc(&c.rres, ns, "rres") ||
@@ -487,6 +486,20 @@ extern "C" int pf_set_material(void **ctx, const int *n, const double *e, const 
     return PF_SUCCESS;
 }
 
+// The per-element storkm arrays (FP64, FP32, packed FP32), allocated on the
+// first pf_form_storkm / pf_set_storkm: a context that only ever uses a
+// shared element matrix never holds them.
+static int ensure_storkm(Ctx &c)
+{
+    const size_t ne = (size_t)c.nels;
+    if (!c.km64 && dalloc(&c.km64, ne * 3600, "FP64 storkm")) return 1;
+    if (!c.km32 && dalloc(&c.km32, ne * 3600, "FP32 storkm")) return 1;
+    if (!c.km32p && dalloc(&c.km32p, ne * 1832, "packed FP32 storkm")) return 1;
+    c.shared = false;
+    drop_graph(c);
+    return 0;
+}
+
 extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
 {
     Ctx *cp = get_ctx(ctx);
@@ -501,6 +514,7 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
         return PF_FAILURE;
     }
     const bool exact = (*flags & PF_FORM_EXACT_WEIGHTS) != 0;
+    TRY(ensure_storkm(c));
     TRY(launch_form_storkm(c, *nip, exact, true));
     TRY(launch_pack_sym32(c));
     TRY(launch_assemble_diag(c));
@@ -516,6 +530,7 @@ extern "C" int pf_set_storkm(void **ctx, const double *storkm)
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
     if (!storkm || c.nels == 0) { set_error("pf_set_storkm: call pf_setup first"); return PF_FAILURE; }
+    TRY(ensure_storkm(c));
     CK(cudaMemcpyAsync(c.km64, storkm, (size_t)c.nels * 3600 * sizeof(double), cudaMemcpyHostToDevice,
                        c.stream));
     TRY(launch_cast_km32(c));
@@ -527,11 +542,78 @@ extern "C" int pf_set_storkm(void **ctx, const double *storkm)
     return PF_SUCCESS;
 }
 
+extern "C" int pf_form_km(void **ctx, const int *iel, const int *nip, const int *flags, double *km)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!iel || !nip || !flags || !km || (*nip != 8 && *nip != 27)) {
+        set_error("pf_form_km: nip must be 8 or 27");
+        return PF_FAILURE;
+    }
+    if (c.nels == 0 || c.nmat == 0 || *iel < 1 || *iel > c.nels) {
+        set_error("pf_form_km: element %d is not in the mesh, or no material", iel ? *iel : 0);
+        return PF_FAILURE;
+    }
+    const size_t e = (size_t)*iel - 1;
+    double *buf = nullptr;   // Gauss table (108) + km (3600) + element diagonal (60)
+    if (dalloc(&buf, 108 + 3600 + 60, "element matrix")) return PF_FAILURE;
+    const int m = c.nmat == 1 ? 0 : (int)e;
+    int bad = launch_sample(c.stream, *nip, (*flags & PF_FORM_EXACT_WEIGHTS) != 0, buf);
+    if (!bad)
+        bad = launch_form_storkm_raw(c.stream, c.nsm, 1, *nip, buf, c.coord + e * 60, c.mat_e + m, c.mat_v + m, 1,
+                                     buf + 108, nullptr, buf + 108 + 3600);
+    if (!bad) c.launches += 2;
+    cudaError_t ec = bad ? cudaSuccess : cudaMemcpyAsync(km, buf + 108, 3600 * sizeof(double), cudaMemcpyDeviceToHost,
+                                                         c.stream);
+    if (ec == cudaSuccess) ec = cudaStreamSynchronize(c.stream);
+    cudaFree(buf);
+    if (bad) return PF_FAILURE;
+    if (ec != cudaSuccess) {
+        set_error("pf_form_km: %s", cudaGetErrorString(ec));
+        return PF_FAILURE;
+    }
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_shared_km(void **ctx, const double *km)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (!km || c.nels == 0) {
+        set_error("pf_set_shared_km: call pf_setup first");
+        return PF_FAILURE;
+    }
+    for (int i = 0; i < 60; ++i)
+        if (!(km[61 * i] > 0.0) || !std::isfinite(km[61 * i])) {
+            set_error("pf_set_shared_km: km(%d,%d) = %g is not a positive stiffness", i + 1, i + 1, km[61 * i]);
+            return PF_FAILURE;
+        }
+    if (!c.skm64 && dalloc(&c.skm64, 3600, "shared km")) return PF_FAILURE;
+    if (!c.skm32 && dalloc(&c.skm32, 3600, "shared km")) return PF_FAILURE;
+    std::vector<float> k32(3600);
+    for (int i = 0; i < 3600; ++i) k32[i] = (float)km[i];
+    CK(cudaMemcpyAsync(c.skm64, km, 3600 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.skm32, k32.data(), 3600 * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    c.shared = true;
+    drop_graph(c);
+    TRY(launch_shared_ediag(c));
+    TRY(launch_assemble_diag(c));
+    TRY(sync(c));
+    c.have_km = true;
+    return PF_SUCCESS;
+}
+
 extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, double *storkm)
 {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.shared) {
+        set_error("pf_get_storkm: the context uses one shared element matrix (pf_set_shared_km)");
+        return PF_FAILURE;
+    }
     if (!first || !count || !storkm || !c.have_km || *first < 0 || *count < 0 || *first + *count > c.nels) {
         set_error("pf_get_storkm: invalid range or no storkm");
         return PF_FAILURE;

@@ -70,6 +70,11 @@ struct Ctx {
     double *it_xsol = nullptr;
     long long it_launches = 0;  // kernels in one replay
     bool use_graphs = true;
+    // one element matrix shared by every element (PCG_KM); per-element storkm unused
+    bool shared = false;
+    double *skm64 = nullptr;    // [3600] column-major
+    float *skm32 = nullptr;     // [3600]
+    bool shared_attr = false;   // shared-memory attribute of the tensor-core kernel set
     int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel
     int sym_warps = 14, sym_stages = 2;
     unsigned long long sym_attr = 0;   // configurations whose shared-memory attribute is set
@@ -122,6 +127,8 @@ enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31 };
 int launch_pack_sym32(Ctx &c);
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);
 int autotune_sym32(Ctx &c, const double *p);   // picks c.sym_cfg by timing on this mesh
+int launch_elem_shared(Ctx &c, int prec, const double *p, const PcgState *st);   // shared km
+int launch_shared_ediag(Ctx &c);
 void set_sym_config(Ctx &c, int idx);           // 0: 14 warps x 2 stages, 1: 12 x 2, 2: 8 x 3
 int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs,
                           const double *mat, double *rhs, long long *launches);

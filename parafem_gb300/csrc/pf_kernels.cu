@@ -688,6 +688,7 @@ int launch_slot_to_eq(Ctx &c, const double *slot, double *eq)
 
 int launch_elem(Ctx &c, int prec, const double *p)
 {
+    if (c.shared) return launch_elem_shared(c, prec, p, c.st);
     if (prec == PREC_FP32_SYM) return launch_elem_sym32(c, p, c.st);
     const int grid = grid_for(c, c.nels, 8, 8);
     if (prec == PREC_FP32_FULL) {
@@ -723,7 +724,9 @@ int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
 int launch_matvec(Ctx &c, int prec, const double *p, double *u)
 {
     const int grid = grid_for(c, c.nels, 8, 8);
-    if (prec == PREC_FP32_SYM) {
+    if (c.shared) {
+        if (launch_elem_shared(c, prec, p, nullptr)) return 1;
+    } else if (prec == PREC_FP32_SYM) {
         if (launch_elem_sym32(c, p, nullptr)) return 1;
     } else {
         if (prec == PREC_FP32_FULL)
@@ -744,8 +747,12 @@ int launch_matvec(Ctx &c, int prec, const double *p, double *u)
 int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
 {
     const int grid = grid_for(c, c.nels, 8, 8);
-    k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, x, (double *)c.utemp, nullptr);
-    if (check_launch(c, "k_elem")) return 1;
+    if (c.shared) {
+        if (launch_elem_shared(c, PREC_FP64, x, nullptr)) return 1;
+    } else {
+        k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, x, (double *)c.utemp, nullptr);
+        if (check_launch(c, "k_elem")) return 1;
+    }
     k_scatter<double, 1><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
                                                      c.freemask, f, rres, c.part_s, nullptr);
     return check_launch(c, "k_scatter");

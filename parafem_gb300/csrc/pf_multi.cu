@@ -7,7 +7,8 @@
 //
 // Element products:
 //   k_mr_elem_tc   tensor cores (tcgen05.mma, kind::f16, BF16 operands, FP32
-//                  accumulation in TMEM).  K_e and P_e are each split into
+//                  accumulation in TMEM), operands from the packed-symmetric
+//                  FP32 storkm by bulk copy.  K_e and P_e are each split into
 //                  three BF16 terms (x = h1 + h2 + h3, about 24 significant
 //                  bits) and the six products of order <= 2^-16 are summed:
 //                  the block product reaches FP32 accuracy.  A two-term split
@@ -20,6 +21,7 @@
 // alpha/beta; the recursive residuals are replaced by the FP64 true residual
 // whenever an active load case has dropped 10x (as PF_MODE_MIXED does).
 #include "pf_device.cuh"
+#include "pf_tc.cuh"
 #include "pfgpu.h"
 
 #include <cstring>
@@ -27,163 +29,108 @@
 
 namespace pf {
 
+using namespace tc;
+
 namespace {
 
 constexpr int KR = 16;               // load cases per block (the kernels are written for 16)
 constexpr unsigned kFullMask = 0xffffffffu;
 
-// ---------------------------------------------------------------------------
-// tcgen05 helpers (inline PTX)
-__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// Shared-memory matrix descriptor, K-major, no swizzle: core matrices of
-// 8 rows x 16 bytes stored contiguously; LBO = byte distance between core
-// matrices adjacent in K, SBO = between core matrices adjacent in M/N.
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
-{
-    uint64_t d = 0;
-    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
-    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-    d |= (uint64_t)1 << 46;   // descriptor version 1 (sm_100 family); base offset 0; no swizzle
-    return d;
-}
-
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major,
-// N = 16, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
-{
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t *bar)
-{
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                     smem_addr(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_init1(uint64_t *bar)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ bool mbar_poll(uint64_t *bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
-{
-    for (long long i = 0; i < (1LL << 22); ++i)
-        if (mbar_poll(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, float (&v)[16])
-{
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ uint16_t bf16_rn(float x)
-{
-    uint32_t u = __float_as_uint(x);
-    u += 0x7FFFu + ((u >> 16) & 1u);   // round to nearest even (finite inputs)
-    return (uint16_t)(u >> 16);
-}
-__device__ __forceinline__ float bf16_to_f(uint16_t h) { return __uint_as_float(((uint32_t)h) << 16); }
-
-// x = h1 + h2 + h3 in BF16 (each remainder is exact in FP32)
-__device__ __forceinline__ void split3(float x, uint16_t &h1, uint16_t &h2, uint16_t &h3)
-{
-    h1 = bf16_rn(x);
-    const float r1 = x - bf16_to_f(h1);
-    h2 = bf16_rn(r1);
-    const float r2 = r1 - bf16_to_f(h2);
-    h3 = bf16_rn(r2);
-}
-
-// byte offset of element (row, k) in a K-major no-swizzle tile with 64 columns of K
-__device__ __forceinline__ uint32_t kmajor_off(int row, int k)
-{
-    return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
-}
-
-constexpr int kTileA = 128 * 64 * 2;   // 16384 B: 128 rows (60 used) x 64 K (60 used)
-constexpr int kTileB = 16 * 64 * 2;    // 2048 B: 16 load cases x 64 K
-constexpr int kTcSmem = 2 * 3 * kTileA + 2 * 3 * kTileB + 64;   // two operand sets
+// Tile geometry (BF16, K-major, no swizzle; 8-row x 16-byte core matrices,
+// LBO = 128 B between core matrices adjacent in K, SBO = 1024 B between
+// 8-row groups).  A term holds rows 0..63 of K_e (8 KB).  The MMA reads
+// M = 128 rows, so rows 64..127 of a term are the next 8 KB of shared
+// memory: they only feed accumulator rows 64..127, which nobody reads.
+constexpr int kTermA = 64 * 64 * 2;          // 8192
+constexpr int kBufA = 4 * kTermA;            // 3 terms + the 8 KB read as rows 64..127 of the last
+constexpr int kTermB = 16 * 64 * 2;          // 2048: 16 load cases x 64 K
+constexpr int kBufB = 3 * kTermB;
+constexpr int kStK = 7328;                   // packed-symmetric FP32 K_e (1830 + 2 pad floats)
+constexpr int kStP = 20 * 3 * KR * 8;        // P of the 20 nodes: 20 x 384 B
+constexpr int kStage = kStK + kStP;          // 15008 B, a multiple of 16
+constexpr int kNst = 4;                      // operand stages in flight per CTA
+constexpr int kTcThreads = 256;
+constexpr int kOffB = 2 * kBufA;
+constexpr int kOffSt = kOffB + 2 * kBufB;
+constexpr int kOffAux = kOffSt + kNst * kStage;
+constexpr int kTcSmem = kOffAux + 128;
+constexpr uint32_t kIdesc = idesc_bf16(128, 16);
+static_assert(kOffSt % 16 == 0 && kStage % 16 == 0 && kOffAux % 8 == 0, "bulk-copy alignment");
 
 }  // namespace
 
 // Block element products on the tensor cores: ut[e][i][j] = sum_c K_e(i,c) P(slot(c), j).
-// A persistent CTA of 128 threads works on a sequence of elements with two
-// sets of operand tiles and two TMEM accumulators: while the MMAs of element
-// t run on the tensor cores, the threads split and store the operands of
-// element t+1, then read back element t-1's accumulator.  Operands are
-// written 8 K-values (16 bytes) at a time.  64 TMEM columns per CTA.
-__global__ void __launch_bounds__(128)
-k_mr_elem_tc(int nels, const float *__restrict__ km32, const int *__restrict__ conn,
+//
+// One persistent CTA of 8 warps per SM walks the elements e = blockIdx.x +
+// t * gridDim.x.  Operands arrive by bulk copy (cp.async.bulk + mbarrier),
+// kNst elements ahead: the packed upper triangle of K_e (7,328 B) and the
+// 16-case P block of each of the element's 20 nodes (384 B each, contiguous
+// in the interleaved vector).  Per element the threads split K_e and P_e
+// into three BF16 terms each and write them into one of two tile sets;
+// thread 0 issues the six products of order <= 2^-16 (24 MMAs, M=128, N=16,
+// K=16) into one of two TMEM accumulators and commits them to an mbarrier;
+// while they run, warps 0-1 read back the previous element's accumulator.
+// Every wait is bounded: a wait that runs out sets the device error word to
+// 3, and the CTA waits (bounded) for its copies and MMAs in flight, frees
+// its TMEM and returns.
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ conn,
              const double *__restrict__ P, float *__restrict__ ut, int *__restrict__ err,
              const int *__restrict__ skip)
 {
     if (skip && *skip) return;   // a residual replacement is pending: nothing to compute
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char *A = sm;                             // [2 buffers][3 terms] tiles
-    unsigned char *B = sm + 2 * 3 * kTileA;            // [2][3]
-    unsigned char *aux = sm + 2 * 3 * kTileA + 2 * 3 * kTileB;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(aux);          // 2 mbarriers
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(aux + 16);
-    int &s_fail = *reinterpret_cast<int *>(aux + 32);
+    unsigned char *A = sm;
+    unsigned char *B = sm + kOffB;
+    unsigned char *stg = sm + kOffSt;
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + kOffAux);      // kNst
+    uint64_t *mbar = full + kNst;                                     // 2
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+    int *s_fail = reinterpret_cast<int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int nmine = blockIdx.x < nels ? (nels - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto elem = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
 
-    for (int i = tid; i < (2 * 3 * kTileA + 2 * 3 * kTileB) / 16; i += blockDim.x)
-        reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
+    for (int i = tid; i < kOffSt / 16; i += kTcThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;" ::"r"(smem_addr(tslot))
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        tmem_alloc(tslot, 32);
     }
     if (tid == 0) {
-        mbar_init1(&bar[0]);
-        mbar_init1(&bar[1]);
-        s_fail = 0;
+        for (int s = 0; s < kNst; ++s) mbar_init(&full[s], 1);
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_fence_init();
+        *s_fail = 0;
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    fence_proxy_async();   // zeroed tiles -> async proxy
+    tc_fence_before();
     __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tc_fence_after();
     const uint32_t tmem = *tslot;
-    uint32_t phase[2] = {0, 0};
 
-    // epilogue of the element whose MMAs went into accumulator `buf`
+    // producer (warp 0): element t's operands into stage t % kNst
+    auto issue = [&](int t, int nd) {
+        const int s = t % kNst;
+        unsigned char *dst = stg + s * kStage;
+        if (lane == 0) mbar_expect_tx(&full[s], kStage);
+        __syncwarp();
+        if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &full[s]);
+        if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * nd * KR, 384, &full[s]);
+    };
+    int conn_next = 0;   // warp 0, lanes 0..19: node of the next element to issue
+    if (warp == 0) {
+        for (int t = 0; t < kNst && t < nmine; ++t) {
+            const int nd = lane < 20 ? conn[(size_t)elem(t) * 20 + lane] : 0;
+            issue(t, nd);
+        }
+        if (kNst < nmine && lane < 20) conn_next = conn[(size_t)elem(kNst) * 20 + lane];
+    }
+
+    uint32_t mphase[2] = {0, 0};
     auto epilogue = [&](int e, int buf) {
-        if (!mbar_wait_bounded(&bar[buf], phase[buf])) atomicOr(&s_fail, 1);
-        phase[buf] ^= 1;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (warp < 2) {   // rows 0..63 live in TMEM lanes 0..63 (warps 0 and 1)
+            if (!mbar_wait(&mbar[buf], mphase[buf])) atomicOr(s_fail, 1);
+            tc_fence_after();
             float v[16];
             tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * buf), v);
             const int row = 32 * warp + lane;
@@ -195,99 +142,86 @@ k_mr_elem_tc(int nels, const float *__restrict__ km32, const int *__restrict__ c
                 o[3] = make_float4(v[12], v[13], v[14], v[15]);
             }
         }
+        mphase[buf] ^= 1;
     };
 
-    int t = 0, prev_e = -1;
-    for (int e = blockIdx.x; e < nels; e += gridDim.x, ++t) {
-        const int buf = t & 1;
-        unsigned char *Ab = A + buf * 3 * kTileA, *Bb = B + buf * 3 * kTileB;
-        // operands of element e: K rows i, 8 K-values (input dofs) per task
-        const float *ke = km32 + (size_t)e * 3600;
-        for (int task = tid; task < 60 * 8; task += blockDim.x) {
-            const int q = task / 60, i = task - 60 * q;
-            uint32_t w1[4], w2[4], w3[4];
+    int t = 0;
+    for (; t < nmine; ++t) {
+        const int s = t % kNst, buf = t & 1;
+        if (!mbar_wait(&full[s], (uint32_t)((t / kNst) & 1))) atomicOr(s_fail, 1);
+        const float *U = reinterpret_cast<const float *>(stg + s * kStage);
+        const double *Pe = reinterpret_cast<const double *>(stg + s * kStage + kStK);
+        unsigned char *Ab = A + buf * kBufA, *Bb = B + buf * kBufB;
+        // A: K_e rows i (0..63), 8 K-values per task; K(i,k) = U(min, max) at T(max) + min
 #pragma unroll
-            for (int r = 0; r < 8; r += 2) {
-                const int c0 = 8 * q + r, c1 = c0 + 1;
-                const float x0 = c0 < 60 ? ke[60 * c0 + i] : 0.f, x1 = c1 < 60 ? ke[60 * c1 + i] : 0.f;
-                uint16_t a1, a2, a3, b1, b2, b3;
-                split3(x0, a1, a2, a3);
-                split3(x1, b1, b2, b3);
-                w1[r / 2] = (uint32_t)a1 | ((uint32_t)b1 << 16);
-                w2[r / 2] = (uint32_t)a2 | ((uint32_t)b2 << 16);
-                w3[r / 2] = (uint32_t)a3 | ((uint32_t)b3 << 16);
+        for (int h = 0; h < 2; ++h) {
+            const int task = tid + kTcThreads * h;
+            const int i = task & 63, q = task >> 6;
+            float xv[8];
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                const int k = 8 * q + g;
+                const int lo = i < k ? i : k, hi = i < k ? k : i;
+                xv[g] = (i < 60 && k < 60) ? U[hi * (hi + 1) / 2 + lo] : 0.f;
             }
-            const uint32_t o = kmajor_off(i, 8 * q);
-            *reinterpret_cast<uint4 *>(Ab + o) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-            *reinterpret_cast<uint4 *>(Ab + kTileA + o) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
-            *reinterpret_cast<uint4 *>(Ab + 2 * kTileA + o) = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+            split3_store8(xv, Ab + kmajor_off(i, 8 * q), kTermA);
         }
-        {   // P_e: one task per thread, case j, 8 dofs
-            const int j = tid & (KR - 1), q = tid >> 4;   // 16 cases x 8 chunks = 128 tasks
-            uint32_t w1[4], w2[4], w3[4];
+        if (tid < 128) {   // B: P_e, case j, dofs 8q..8q+7; the stage holds P_e(c, j) at c*16 + j
+            const int j = tid & (KR - 1), q = tid >> 4;
+            float xv[8];
 #pragma unroll
-            for (int r = 0; r < 8; r += 2) {
-                float xv[2];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int c = 8 * q + r + h;
-                    xv[h] = 0.f;
-                    if (c < 60) {
-                        const int nd = conn[(size_t)e * 20 + c / 3];
-                        xv[h] = (float)P[((size_t)3 * nd + c % 3) * KR + j];
-                    }
-                }
-                uint16_t a1, a2, a3, b1, b2, b3;
-                split3(xv[0], a1, a2, a3);
-                split3(xv[1], b1, b2, b3);
-                w1[r / 2] = (uint32_t)a1 | ((uint32_t)b1 << 16);
-                w2[r / 2] = (uint32_t)a2 | ((uint32_t)b2 << 16);
-                w3[r / 2] = (uint32_t)a3 | ((uint32_t)b3 << 16);
+            for (int g = 0; g < 8; ++g) {
+                const int c = 8 * q + g;
+                xv[g] = c < 60 ? (float)Pe[c * KR + j] : 0.f;
             }
-            const uint32_t o = kmajor_off(j, 8 * q);
-            *reinterpret_cast<uint4 *>(Bb + o) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
-            *reinterpret_cast<uint4 *>(Bb + kTileB + o) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
-            *reinterpret_cast<uint4 *>(Bb + 2 * kTileB + o) = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+            split3_store8(xv, Bb + kmajor_off(j, 8 * q), kTermB);
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
+        fence_proxy_async();
+        __syncthreads();   // tiles complete; stage s consumed by every thread
+        if (*s_fail) break;
         if (tid == 0) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            tc_fence_after();
             // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
             const int ta[6] = {0, 0, 1, 0, 1, 2};
             const int tb[6] = {0, 1, 0, 2, 1, 0};
             uint32_t acc = 0;
             for (int tt = 0; tt < 6; ++tt) {
-                const uint32_t a0 = smem_addr(Ab + ta[tt] * kTileA), b0 = smem_addr(Bb + tb[tt] * kTileB);
+                const uint32_t a0 = smem_u32(Ab + ta[tt] * kTermA), b0 = smem_u32(Bb + tb[tt] * kTermB);
                 for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
                     mma_bf16(tmem + (uint32_t)(16 * buf), umma_desc(a0 + ks * 256, 128, 1024),
-                             umma_desc(b0 + ks * 256, 128, 1024), acc);
+                             umma_desc(b0 + ks * 256, 128, 1024), kIdesc, acc);
                     acc = 1;
                 }
             }
-            mma_commit(&bar[buf]);
+            mma_commit(&mbar[buf]);
         }
-        // meanwhile: the previous element's accumulator
-        if (prev_e >= 0) epilogue(prev_e, buf ^ 1);
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (s_fail) break;
-        prev_e = e;
-    }
-    if (prev_e >= 0 && !s_fail) {
-        epilogue(prev_e, (t - 1) & 1);
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        // refill stage s with element t + kNst
+        if (warp == 0 && t + kNst < nmine) {
+            fence_proxy_async();
+            issue(t + kNst, conn_next);
+            if (t + kNst + 1 < nmine && lane < 20) conn_next = conn[(size_t)elem(t + kNst + 1) * 20 + lane];
+        }
+        if (t > 0) epilogue(elem(t - 1), buf ^ 1);
+        tc_fence_before();
         __syncthreads();
     }
-    if (s_fail) {
-        if (tid == 0) atomicExch(err, 3);
-        // give outstanding MMAs a bounded chance to finish before TMEM goes back
-        mbar_wait_bounded(&bar[0], phase[0]);
-        mbar_wait_bounded(&bar[1], phase[1]);
+    if (!*s_fail && t > 0) {
+        epilogue(elem(t - 1), (t - 1) & 1);
+        tc_fence_before();
+        __syncthreads();
     }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;" ::"r"(tmem) : "memory");
+    if (*s_fail) {
+        if (tid == 0) {
+            atomicExch(err, 3);
+            // copies still in flight: stages t .. t+kNst-1; MMAs: both accumulators
+            for (int k = t; k < nmine && k < t + kNst; ++k) mbar_wait(&full[k % kNst], (uint32_t)((k / kNst) & 1));
+            mbar_wait(&mbar[0], mphase[0]);
+            mbar_wait(&mbar[1], mphase[1]);
+        }
+        __syncthreads();
+    }
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 32);
 }
 
 // Block element products on CUDA cores (FP32 or FP64): one warp per element,
@@ -388,10 +322,12 @@ k_mr_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list, 
 // per-case state
 struct MState {
     double up[KR], ff[KR], rr[KR], thr[KR];
+    double alpha[KR], beta[KR];   // this iteration's step lengths (0 for inactive cases)
     int active[KR];      // 1 until the case's true residual reaches tol
     int flag[KR];        // recursive residual reached thr (replacement wanted)
     int iters[KR];
     int any_flag;        // stop iterating: some active case wants a replacement
+    int pending;         // set by this iteration's k_mr_beta, moved to any_flag by k_mr_finish
     int err;
 };
 
@@ -401,6 +337,23 @@ __device__ __forceinline__ double case_sum(const double *part, int G, int j)
     double s = 0.0;
     for (int b = 0; b < G; ++b) s += part[(size_t)b * KR + j];
     return s;
+}
+
+// The same sums by one 256-thread block: thread (g, j) adds partials
+// g, g+16, ... of case j, then thread j adds the 16 group sums in order.
+// Fixed order, so the result is the same in every run.
+__device__ __forceinline__ double case_sum_block(const double *part, int G, double (*sh)[KR])
+{
+    const int j = threadIdx.x & (KR - 1), g = threadIdx.x >> 4;
+    double s = 0.0;
+    for (int b = g; b < G; b += 16) s += part[(size_t)b * KR + j];
+    sh[g][j] = s;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < KR)
+        for (int i = 0; i < 16; ++i) t += sh[i][threadIdx.x];
+    __syncthreads();
+    return t;   // valid in threads 0..15
 }
 
 template <int NV>
@@ -461,20 +414,29 @@ __global__ void k_mr_init2(MState *st, const double *__restrict__ part, int G, d
     st->iters[j] = 0;
     if (j == 0) {
         st->any_flag = 0;
+        st->pending = 0;
         st->err = 0;
     }
 }
 
+// alpha = up / (p.u) per case, from the scatter's partials (one block)
+__global__ void __launch_bounds__(256) k_mr_alpha(MState *st, const double *__restrict__ ps, int Gs)
+{
+    __shared__ double sh[16][KR];
+    if (st->any_flag) return;
+    const double pu = case_sum_block(ps, Gs, sh);
+    const int j = threadIdx.x;
+    if (j < KR) st->alpha[j] = st->active[j] ? st->up[j] / pu : 0.0;
+}
+
 __global__ void __launch_bounds__(256)
-k_mr_update1(int ns, const MState *__restrict__ st, const double *__restrict__ ps, int Gs,
-             double *__restrict__ pu_out, int G, double *__restrict__ X, double *__restrict__ R,
-             double *__restrict__ D, const double *__restrict__ P, const double *__restrict__ U,
-             const double *__restrict__ dinv)
+k_mr_update1(int ns, const MState *__restrict__ st, double *__restrict__ pu_out, int G, double *__restrict__ X,
+             double *__restrict__ R, double *__restrict__ D, const double *__restrict__ P,
+             const double *__restrict__ U, const double *__restrict__ dinv)
 {
     if (st->any_flag) return;
     const int j = threadIdx.x & (KR - 1);
-    const double pu = case_sum(ps, Gs, j);
-    const double alpha = st->active[j] ? st->up[j] / pu : 0.0;
+    const double alpha = st->alpha[j];
     double rd = 0.0, rr = 0.0;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
          t += (size_t)gridDim.x * blockDim.x) {
@@ -490,38 +452,54 @@ k_mr_update1(int ns, const MState *__restrict__ st, const double *__restrict__ p
     case_block_reduce<2>(v, 0u, pu_out, (size_t)G * KR);
 }
 
+// r.d and r.r per case; beta = (r.d)_new / up; the new up, rr and iteration
+// count; the stopping test (one block).  The flag raised here reaches
+// any_flag only in k_mr_finish, after this iteration's k_mr_update2.
+__global__ void __launch_bounds__(256) k_mr_beta(MState *st, const double *__restrict__ part, int G, int limit)
+{
+    __shared__ double sh[16][KR];
+    __shared__ int s_any;
+    if (st->any_flag) return;
+    if (threadIdx.x == 0) s_any = 0;
+    const double rd = case_sum_block(part, G, sh);
+    const double rr = case_sum_block(part + (size_t)G * KR, G, sh);
+    const int j = threadIdx.x;
+    if (j < KR) {
+        if (st->active[j]) {
+            st->beta[j] = rd / st->up[j];
+            st->up[j] = rd;
+            st->rr[j] = rr;
+            st->iters[j] += 1;
+            const bool f = sqrt(rr) / sqrt(st->ff[j]) <= st->thr[j] || st->iters[j] >= limit || !isfinite(rd);
+            st->flag[j] = f ? 1 : 0;
+            if (!isfinite(rd)) st->err = 1;
+            if (f) atomicOr(&s_any, 1);
+        } else {
+            st->beta[j] = 0.0;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_any) st->pending = 1;
+}
+
 __global__ void __launch_bounds__(256)
-k_mr_update2(int ns, const MState *__restrict__ st, const double *__restrict__ part, int G,
-             const double *__restrict__ D, double *__restrict__ P)
+k_mr_update2(int ns, const MState *__restrict__ st, const double *__restrict__ D, double *__restrict__ P)
 {
     if (st->any_flag) return;
     const int j = threadIdx.x & (KR - 1);
-    const double rd = case_sum(part, G, j);
-    const double beta = st->active[j] ? rd / st->up[j] : 0.0;
+    const double beta = st->beta[j];
+    const bool act = st->active[j] != 0;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
          t += (size_t)gridDim.x * blockDim.x)
-        if (st->active[j]) P[t] = fma(P[t], beta, D[t]);
+        if (act) P[t] = fma(P[t], beta, D[t]);
 }
 
-__global__ void k_mr_finish(MState *st, const double *__restrict__ part, int G, int limit)
+__global__ void k_mr_finish(MState *st)
 {
-    __shared__ int s_any;
-    if (threadIdx.x == 0) s_any = 0;
-    __syncthreads();
-    if (st->any_flag) return;
-    const int j = threadIdx.x;
-    if (j < KR && st->active[j]) {
-        const double rd = case_sum(part, G, j), rr = case_sum(part + (size_t)G * KR, G, j);
-        st->up[j] = rd;
-        st->rr[j] = rr;
-        st->iters[j] += 1;
-        const bool f = sqrt(rr) / sqrt(st->ff[j]) <= st->thr[j] || st->iters[j] >= limit || !isfinite(rd);
-        st->flag[j] = f ? 1 : 0;
-        if (!isfinite(rd)) st->err = 1;
-        if (f) atomicOr(&s_any, 1);
+    if (threadIdx.x == 0 && !st->any_flag && st->pending) {
+        st->any_flag = 1;
+        st->pending = 0;
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && s_any) st->any_flag = 1;
 }
 
 // residual replacement: R = RRES for active cases, D = dinv*R, partials r.d, r.r
@@ -553,7 +531,10 @@ __global__ void k_mr_replace2(MState *st, const double *__restrict__ part, int G
         st->rr[j] = case_sum(part + (size_t)G * KR, G, j);
         st->flag[j] = 0;
     }
-    if (j == 0) st->any_flag = 0;
+    if (j == 0) {
+        st->any_flag = 0;
+        st->pending = 0;
+    }
 }
 
 __global__ void k_mr_sums(const double *__restrict__ part, int G, double *__restrict__ out)
@@ -638,8 +619,8 @@ static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
     if (prec == 16) {
         const int smem = kTcSmem;
         MCK(cudaFuncSetAttribute(k_mr_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        const int grid = c.nels < c.nsm * 2 ? c.nels : c.nsm * 2;
-        k_mr_elem_tc<<<grid, 128, smem, c.stream>>>(c.nels, c.km32, c.conn, P, m.ut32, c.kerr, skip);
+        const int grid = c.nels < c.nsm ? c.nels : c.nsm;
+        k_mr_elem_tc<<<grid, kTcThreads, smem, c.stream>>>(c.nels, c.km32p, c.conn, P, m.ut32, c.kerr, skip);
         return mr_launched(c, "k_mr_elem_tc");
     }
     if (prec == 32) {
@@ -716,6 +697,10 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
         set_error("pf_solve_multi: k must be %d", KR);
         return PF_FAILURE;
     }
+    if (c.shared) {
+        set_error("pf_solve_multi: needs per-element storkm (the context uses a shared element matrix)");
+        return PF_FAILURE;
+    }
     if (!c.have_km || *limit < 1 || (*prec != 16 && *prec != 32)) {
         set_error("pf_solve_multi: needs storkm, limit >= 1 and prec 16 (tensor cores) or 32 (CUDA cores)");
         return PF_FAILURE;
@@ -752,12 +737,15 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
             MCK(cudaEventRecord(tev[3 * i + 1], c.stream));
             if (mr_scatter(c, *prec, 0, m.P, m.U, skip)) return PF_FAILURE;
             MCK(cudaEventRecord(tev[3 * i + 2], c.stream));
-            k_mr_update1<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.part, Gs, pu, G, m.X, m.R, m.D, m.P, m.U,
-                                                  c.dinv);
+            k_mr_alpha<<<1, 256, 0, c.stream>>>(m.st, m.part, Gs);
+            if (mr_launched(c, "k_mr_alpha")) return PF_FAILURE;
+            k_mr_update1<<<G, 256, 0, c.stream>>>(c.nslots, m.st, pu, G, m.X, m.R, m.D, m.P, m.U, c.dinv);
             if (mr_launched(c, "k_mr_update1")) return PF_FAILURE;
-            k_mr_update2<<<G, 256, 0, c.stream>>>(c.nslots, m.st, pu, G, m.D, m.P);
+            k_mr_beta<<<1, 256, 0, c.stream>>>(m.st, pu, G, *limit);
+            if (mr_launched(c, "k_mr_beta")) return PF_FAILURE;
+            k_mr_update2<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.D, m.P);
             if (mr_launched(c, "k_mr_update2")) return PF_FAILURE;
-            k_mr_finish<<<1, 32, 0, c.stream>>>(m.st, pu, G, *limit);
+            k_mr_finish<<<1, 32, 0, c.stream>>>(m.st);
             if (mr_launched(c, "k_mr_finish")) return PF_FAILURE;
         }
         total += chunk;
@@ -844,8 +832,8 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, co
     }
     Ctx &c = *(Ctx *)*ctx;
     MCK(cudaSetDevice(c.device));
-    if (*k != KR || !c.have_km || (*prec != 16 && *prec != 32 && *prec != 64)) {
-        set_error("pf_ebe_matvec_multi: k must be %d, prec 16/32/64, storkm formed", KR);
+    if (*k != KR || !c.have_km || c.shared || (*prec != 16 && *prec != 32 && *prec != 64)) {
+        set_error("pf_ebe_matvec_multi: k must be %d, prec 16/32/64, per-element storkm formed", KR);
         return PF_FAILURE;
     }
     if (mr_alloc(c)) return PF_FAILURE;

@@ -1,0 +1,298 @@
+// pf_shared.cu -- element products when every element has the same
+// stiffness matrix km (PCG_KM, src/modules/mpi/maths.f90:1152-1323, whose
+// iteration computes utemp = MATMUL(km, pmul) over all elements at once;
+// the uniform-mesh GPU experiment xx9, src/programs/dev/xx9/mathsgpu.f90).
+//
+// With one km the product is a true GEMM, U(60 x nels) = km(60 x 60) *
+// P(60 x nels), and no per-element matrix is streamed from HBM.
+//   k_elem_shared64   FP64 on CUDA cores: km in shared memory, one warp per
+//                     element (bound by FP64 FMA throughput, as k_elem<double>).
+//   k_elem_shared_tc  FP32-class on the tensor cores: km split once into
+//                     three BF16 terms held in shared memory for the whole
+//                     kernel; tiles of 128 elements' gathered p values are
+//                     split the same way; the six products of order <= 2^-16
+//                     accumulate in FP32 in TMEM (M = 128 with rows 60..127
+//                     unused, N = 128 elements, K = 64).  The gather of one
+//                     tile overlaps the MMAs of the previous one and the
+//                     read-back of the one before.  Results are written in
+//                     the node-padded FP32 layout the scatter reads.
+#include "pf_device.cuh"
+#include "pf_tc.cuh"
+
+namespace pf {
+
+using namespace tc;
+
+namespace {
+
+constexpr int kNT = 128;                    // elements per tile (MMA N)
+constexpr int kSTermA = 64 * 64 * 2;        // 8 KB: rows 0..63 of one km term
+constexpr int kSBufA = 4 * kSTermA;         // 3 terms + 8 KB read as rows 64..127 of the last
+constexpr int kSTermB = kNT * 64 * 2;       // 16 KB: 128 elements x 64 K
+constexpr int kSBufB = 3 * kSTermB;
+constexpr int kSConn = kNT * 20 * 4;        // 10 KB: connectivity of one tile
+constexpr int kSOffB = kSBufA;
+constexpr int kSOffC = kSOffB + 2 * kSBufB;
+constexpr int kSOffAux = kSOffC + 2 * kSConn;
+constexpr int kSSmem = kSOffAux + 128;
+constexpr int kSThreads = 256;
+constexpr uint32_t kSIdesc = idesc_bf16(128, kNT);
+static_assert(kSOffC % 16 == 0 && kSConn % 16 == 0 && kSOffAux % 8 == 0, "bulk-copy alignment");
+static_assert(kSSmem <= 227 * 1024, "shared memory per CTA");
+
+}  // namespace
+
+// u_e = km p_e in FP64 for every element (results utemp[e*60 + i]).
+__global__ void __launch_bounds__(256)
+k_elem_shared64(int nels, const double *__restrict__ km, const int *__restrict__ conn,
+                const double *__restrict__ p, double *__restrict__ ut, const PcgState *__restrict__ st)
+{
+    __shared__ __align__(16) double ks[3600];
+    if (block_stopped(st)) return;
+    for (int i = threadIdx.x; i < 3600; i += blockDim.x) ks[i] = km[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int j1 = lane + 32;
+    for (int e = warp; e < nels; e += nwarps) {
+        const int nd = (lane < 20) ? conn[(size_t)e * 20 + lane] : 0;
+        const int n0 = __shfl_sync(FULLMASK, nd, lane / 3);
+        const int n1 = __shfl_sync(FULLMASK, nd, j1 < 60 ? j1 / 3 : 0);
+        const double p0 = p[(size_t)3 * n0 + lane % 3];
+        const double p1 = (j1 < 60) ? p[(size_t)3 * n1 + j1 % 3] : 0.0;
+        double a0 = 0.0, a1 = 0.0;
+#pragma unroll 12
+        for (int j = 0; j < 60; ++j) {   // ascending column order, as k_elem<double>
+            const double pj = __shfl_sync(FULLMASK, j < 32 ? p0 : p1, j & 31);
+            if (lane < 30) {
+                const double2 k2 = *reinterpret_cast<const double2 *>(ks + 60 * j + 2 * lane);
+                a0 = fma(k2.x, pj, a0);
+                a1 = fma(k2.y, pj, a1);
+            }
+        }
+        if (lane < 30) reinterpret_cast<double2 *>(ut + (size_t)e * 60)[lane] = make_double2(a0, a1);
+    }
+}
+
+// u_e = km p_e on the tensor cores for every element (FP32 results,
+// node-padded: row i of element e at e*80 + (i/3)*4 + i%3).
+// One persistent CTA of 8 warps per SM walks the tiles T = blockIdx.x +
+// t * gridDim.x.  Every wait is bounded; a wait that runs out sets the
+// device error word to 3 and the CTA drains its copies and MMAs (bounded),
+// frees its TMEM and returns.
+__global__ void __launch_bounds__(kSThreads, 1)
+k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict__ conn,
+                 const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
+                 int *__restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char sm[];
+    int *s_stop = reinterpret_cast<int *>(sm + kSOffAux + 64);
+    if (threadIdx.x == 0) *s_stop = st ? st->stop : 0;
+    __syncthreads();
+    if (*s_stop) return;   // uniform: read once per block
+    unsigned char *A = sm;
+    unsigned char *B = sm + kSOffB;
+    int *cs = reinterpret_cast<int *>(sm + kSOffC);                  // [2][128*20]
+    uint64_t *cfull = reinterpret_cast<uint64_t *>(sm + kSOffAux);   // 2: connectivity copies
+    uint64_t *mbar = cfull + 2;                                      // 2: MMA completion
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+    int *s_fail = reinterpret_cast<int *>(tslot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ntiles = (nels + kNT - 1) / kNT;
+    const int nmine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    auto tile = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
+    auto tile_n = [&](int t) { const int r = nels - tile(t) * kNT; return r < kNT ? r : kNT; };
+
+    // km once: K(i,k) = km32[i + 60k], three BF16 terms, rows 0..63 x K 0..63
+    for (int i = tid; i < kSOffC / 16; i += kSThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
+    __syncthreads();
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int task = tid + kSThreads * h;
+        const int i = task & 63, q = task >> 6;
+        float xv[8];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const int k = 8 * q + g;
+            xv[g] = (i < 60 && k < 60) ? km32[i + 60 * k] : 0.f;
+        }
+        split3_store8(xv, A + kmajor_off(i, 8 * q), kSTermA);
+    }
+    if (warp == 0) tmem_alloc(tslot, 256);
+    if (tid == 0) {
+        mbar_init(&cfull[0], 1);
+        mbar_init(&cfull[1], 1);
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        mbar_fence_init();
+        *s_fail = 0;
+    }
+    fence_proxy_async();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    auto issue_conn = [&](int t) {   // thread 0: connectivity of tile t into buffer t & 1
+        const uint32_t bytes = (uint32_t)tile_n(t) * 80u;
+        mbar_expect_tx(&cfull[t & 1], bytes);
+        bulk_g2s(cs + (t & 1) * kNT * 20, conn + (size_t)tile(t) * kNT * 20, bytes, &cfull[t & 1]);
+    };
+    if (tid == 0 && nmine > 0) issue_conn(0);
+
+    uint32_t mphase[2] = {0, 0};
+    auto epilogue = [&](int t, int buf) {
+        // TMEM lanes 0..63 hold rows 0..63: warps 0, 1 (columns 0..63) and 4, 5 (64..127)
+        if ((warp & 3) < 2) {
+            if (!mbar_wait(&mbar[buf], mphase[buf])) atomicOr(s_fail, 1);
+            tc_fence_after();
+            const int row = 32 * (warp & 3) + lane;
+            const int n_here = tile_n(t);
+            const size_t e0 = (size_t)tile(t) * kNT;
+            const int col0 = (warp >> 2) * 64;
+            const size_t roff = (size_t)(row / 3) * 4 + row % 3;
+#pragma unroll 1
+            for (int ch = 0; ch < 4; ++ch) {
+                float v[16];
+                tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(buf * kNT + col0 + 16 * ch),
+                                   v);
+                if (row < 60) {
+#pragma unroll
+                    for (int x = 0; x < 16; ++x) {
+                        const int n = col0 + 16 * ch + x;
+                        if (n < n_here) ut[(e0 + n) * 80 + roff] = v[x];
+                    }
+                }
+            }
+        }
+        mphase[buf] ^= 1;
+    };
+
+    int t = 0;
+    for (; t < nmine; ++t) {
+        const int buf = t & 1;
+        if (tid == 0 && t + 1 < nmine) {
+            fence_proxy_async();
+            issue_conn(t + 1);   // its buffer was last read by tile t-1, before the last barrier
+        }
+        if (!mbar_wait(&cfull[buf], (uint32_t)((t >> 1) & 1))) atomicOr(s_fail, 1);
+        const int *ct = cs + buf * kNT * 20;
+        const int n_here = tile_n(t);
+        unsigned char *Bb = B + buf * kSBufB;
+        // B: element n of the tile, dofs 8q..8q+7 (4 tasks per thread; loads first)
+        float xv[4][8];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int task = tid + kSThreads * h;
+            const int n = task & (kNT - 1), q = task >> 7;
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                const int c = 8 * q + g;
+                xv[h][g] = 0.f;
+                if (c < 60 && n < n_here) xv[h][g] = (float)p[(size_t)3 * ct[n * 20 + c / 3] + c % 3];
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int task = tid + kSThreads * h;
+            const int n = task & (kNT - 1), q = task >> 7;
+            split3_store8(xv[h], Bb + kmajor_off(n, 8 * q), kSTermB);
+        }
+        fence_proxy_async();
+        __syncthreads();
+        if (*s_fail) break;
+        if (tid == 0) {
+            tc_fence_after();
+            // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
+            const int ta[6] = {0, 0, 1, 0, 1, 2};
+            const int tb[6] = {0, 1, 0, 2, 1, 0};
+            uint32_t acc = 0;
+            for (int tt = 0; tt < 6; ++tt) {
+                const uint32_t a0 = smem_u32(A + ta[tt] * kSTermA), b0 = smem_u32(Bb + tb[tt] * kSTermB);
+                for (int ks = 0; ks < 4; ++ks) {
+                    mma_bf16(tmem + (uint32_t)(buf * kNT), umma_desc(a0 + ks * 256, 128, 1024),
+                             umma_desc(b0 + ks * 256, 128, 1024), kSIdesc, acc);
+                    acc = 1;
+                }
+            }
+            mma_commit(&mbar[buf]);
+        }
+        if (t > 0) epilogue(t - 1, buf ^ 1);
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (!*s_fail && t > 0) {
+        epilogue(t - 1, (t - 1) & 1);
+        tc_fence_before();
+        __syncthreads();
+    }
+    if (*s_fail) {
+        if (tid == 0) {
+            atomicExch(err, 3);
+            if (t + 1 < nmine) mbar_wait(&cfull[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1));
+            mbar_wait(&mbar[0], mphase[0]);
+            mbar_wait(&mbar[1], mphase[1]);
+        }
+        __syncthreads();
+    }
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, 256);
+}
+
+// ediag[e*60 + i] = km(i,i) for every element
+__global__ void k_shared_ediag(int nels, const double *__restrict__ km, double *__restrict__ ediag)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)nels * 60;
+         t += (size_t)gridDim.x * blockDim.x)
+        ediag[t] = km[(t % 60) * 61];
+}
+
+int launch_shared_ediag(Ctx &c)
+{
+    k_shared_ediag<<<c.nsm * 8, 256, 0, c.stream>>>(c.nels, c.skm64, c.ediag);
+    c.launches++;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("k_shared_ediag: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+// u_e = km p_e for every element: prec 64 on CUDA cores in FP64, otherwise
+// on the tensor cores (FP32-class).  st: PCG state whose stop flag turns the
+// launch into a no-op (nullptr outside a PCG run).
+int launch_elem_shared(Ctx &c, int prec, const double *p, const PcgState *st)
+{
+    cudaError_t e;
+    if (prec == PREC_FP64) {
+        long long g = ((long long)c.nels + 7) / 8;
+        if (g > (long long)c.nsm * 8) g = (long long)c.nsm * 8;
+        if (g < 1) g = 1;
+        k_elem_shared64<<<(int)g, 256, 0, c.stream>>>(c.nels, c.skm64, c.conn, p, (double *)c.utemp, st);
+    } else {
+        if (!c.shared_attr) {   // set once, before any stream capture
+            e = cudaFuncSetAttribute(k_elem_shared_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSSmem);
+            if (e != cudaSuccess) {
+                set_error("k_elem_shared_tc: cannot reserve %d bytes of shared memory: %s", kSSmem,
+                          cudaGetErrorString(e));
+                return 1;
+            }
+            c.shared_attr = true;
+        }
+        const int ntiles = (c.nels + kNT - 1) / kNT;
+        const int grid = ntiles < c.nsm ? ntiles : c.nsm;
+        k_elem_shared_tc<<<grid, kSThreads, kSSmem, c.stream>>>(c.nels, c.skm32, c.conn, p, (float *)c.utemp, st,
+                                                                 c.kerr);
+    }
+    c.launches++;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("shared-km element product: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+}  // namespace pf

@@ -1,0 +1,187 @@
+// pf_tc.cuh -- inline-PTX helpers for the Blackwell asynchronous units:
+// mbarriers, bulk copies (cp.async.bulk, the TMA engine without a tensor
+// map), tcgen05 tensor-core MMAs with TMEM accumulators, and the BF16
+// three-term split used to reach FP32 accuracy on BF16 tensor cores.
+//
+// Every wait here is bounded: mbar_wait returns false after kSpinLimit polls
+// and the caller records an error and drains what it has in flight.
+#pragma once
+#include <cstdint>
+
+namespace pf {
+namespace tc {
+
+constexpr long long kSpinLimit = 1LL << 22;   // try_wait polls before giving up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// ---------------------------------------------------------------------------
+// mbarriers
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// arrive once and expect `bytes` of transaction (bulk-copy) completions
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase with the given parity: false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    for (long long i = 0; i < kSpinLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// bulk copies global -> shared (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// orders this thread's generic-proxy shared-memory accesses with the async proxy
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// tcgen05
+// Shared-memory matrix descriptor, K-major, no swizzle: core matrices of
+// 8 rows x 16 bytes stored contiguously; LBO = byte distance between core
+// matrices adjacent in K, SBO = between core matrices adjacent in M/N.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;   // descriptor version 1 (sm_100 family); base offset 0; no swizzle
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major.
+constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// the mbarrier completes when every MMA this thread issued so far has finished
+__device__ __forceinline__ void mma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+// whole-warp TMEM allocation of `ncols` columns (a power of two >= 32); the
+// base address is written to *slot
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tmem_dealloc(uint32_t base, uint32_t ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(base), "r"(ncols) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (lane = row)
+__device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---------------------------------------------------------------------------
+// BF16 three-term split
+__device__ __forceinline__ uint16_t bf16_rn(float x)
+{
+    uint32_t u = __float_as_uint(x);
+    u += 0x7FFFu + ((u >> 16) & 1u);   // round to nearest even (finite inputs)
+    return (uint16_t)(u >> 16);
+}
+__device__ __forceinline__ float bf16_to_f(uint16_t h) { return __uint_as_float(((uint32_t)h) << 16); }
+
+// x = h1 + h2 + h3 in BF16 (each remainder is exact in FP32)
+__device__ __forceinline__ void split3(float x, uint16_t &h1, uint16_t &h2, uint16_t &h3)
+{
+    h1 = bf16_rn(x);
+    const float r1 = x - bf16_to_f(h1);
+    h2 = bf16_rn(r1);
+    const float r2 = r1 - bf16_to_f(h2);
+    h3 = bf16_rn(r2);
+}
+
+// Splits 8 consecutive K-values and writes the three 16-byte chunks, one per
+// term tile (term t at dst + t * term_bytes).
+__device__ __forceinline__ void split3_store8(const float (&x)[8], unsigned char *dst, uint32_t term_bytes)
+{
+    uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+    for (int r = 0; r < 8; r += 2) {
+        uint16_t a1, a2, a3, b1, b2, b3;
+        split3(x[r], a1, a2, a3);
+        split3(x[r + 1], b1, b2, b3);
+        w1[r / 2] = (uint32_t)a1 | ((uint32_t)b1 << 16);
+        w2[r / 2] = (uint32_t)a2 | ((uint32_t)b2 << 16);
+        w3[r / 2] = (uint32_t)a3 | ((uint32_t)b3 << 16);
+    }
+    *reinterpret_cast<uint4 *>(dst) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+    *reinterpret_cast<uint4 *>(dst + term_bytes) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+    *reinterpret_cast<uint4 *>(dst + 2 * term_bytes) = make_uint4(w3[0], w3[1], w3[2], w3[3]);
+}
+
+// byte offset of (row, k) in a K-major no-swizzle tile with 64 K-columns:
+// 8-row groups 1024 B apart (SBO), 8-column core matrices 128 B apart (LBO)
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k)
+{
+    return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+}  // namespace tc
+}  // namespace pf

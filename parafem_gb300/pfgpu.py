@@ -48,6 +48,8 @@ _SIGS = {
     "pf_set_material": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_form_storkm": [_VPP, _IP, _IP],
     "pf_set_storkm": [_VPP, ctypes.c_void_p],
+    "pf_set_shared_km": [_VPP, ctypes.c_void_p],
+    "pf_form_km": [_VPP, _IP, _IP, _IP, ctypes.c_void_p],
     "pf_get_storkm": [_VPP, _IP, _IP, ctypes.c_void_p],
     "pf_get_diag": [_VPP, ctypes.c_void_p],
     "pf_ebe_matvec": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
@@ -248,6 +250,21 @@ class Solver:
     def set_storkm(self, km):
         km, pk = _arr(km, np.float64)
         _check(lib().pf_set_storkm(self._ref, pk), "pf_set_storkm")
+
+    def form_km(self, iel=1, nip=27, exact_weights=False):
+        """The (60, 60) stiffness matrix of element iel (1-based), formed on the GPU."""
+        km = np.zeros((60, 60))
+        _check(lib().pf_form_km(self._ref, _i(iel), _i(nip), _i(FORM_EXACT_WEIGHTS if exact_weights else 0),
+                                km.ctypes.data), "pf_form_km")
+        return km
+
+    def set_shared_km(self, km):
+        """One element matrix (60, 60) for every element (PCG_KM); see pf_set_shared_km."""
+        km = np.asarray(km, np.float64)
+        if km.shape != (60, 60):
+            raise ValueError("km must be 60 x 60")
+        km, pk = _arr(km, np.float64)
+        _check(lib().pf_set_shared_km(self._ref, pk), "pf_set_shared_km")
 
     def get_storkm(self, first=0, count=None):
         count = self.nels - first if count is None else count
