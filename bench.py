@@ -47,10 +47,11 @@ def parse_args():
     ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--workload", default="cube100",
-                    choices=["cube100", "hetero80", "serving", "multirhs60", "cube10", "shared100"],
+                    choices=["cube100", "hetero80", "serving", "multirhs60", "cube10", "shared100", "p123book"],
                     help="cube100: the headline; hetero80: per-element E and v, accuracy study; "
                          "serving: continuous batching of a Poisson request stream; shared100: one element "
-                         "matrix for every element (PCG_KM)")
+                         "matrix for every element (PCG_KM); p123book: p123's book run (Laplace, 200^3 8-node "
+                         "bricks)")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
     ap.add_argument("--rates", default="20", help="serving: comma-separated arrival rates (requests/s); "
                                                     "0 = all requests at t=0")
@@ -611,6 +612,56 @@ def run_shared(args, rank, world, local, dist):
     return 0
 
 
+def run_p123(args, rank, world, local, dist):
+    """p123's book run (examples/5th_ed/p123/book/p123.mg): 200^3 8-node
+    bricks of 0.005, kx = ky = kz = 2, box_bc8 restraints, load 10 at
+    freedom 39801, checon_par tol 1e-5.  The reference recorded 180
+    iterations and 52.4 s in the solver on 16 Cray XE6 cores."""
+    import parafem_gb300 as P
+    n = args.size if args.size != 100 else 200
+    t0 = time.perf_counter()
+    prob = P.box8_problem(n, n, n, .005, .005, .005)
+    t_host = time.perf_counter() - t0
+    s = P.Solver(local)
+    s.setup_scalar8(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+    t1 = time.perf_counter()
+    s.form_storkc(8, 2.0, 2.0, 2.0)
+    t_form = time.perf_counter() - t1
+    neq = prob["neq"]
+    s.solve(prob["r"], 1e-5, 10000, P.MODE_P121)        # warm-up
+    t2 = time.perf_counter()
+    x, it, rel = s.solve(prob["r"], 1e-5, 10000, P.MODE_P121)
+    t_solve = time.perf_counter() - t2
+    st = s.stats()
+    s.bench_iterations(64, max(args.warmup, 3))
+    clk = Clocks(local).start() if rank == 0 else None
+    l0 = s.launches()
+    ms_tot, ms_elem, ms_scat = s.bench_iterations(64, args.steps)
+    launches = s.launches() - l0
+    clocks = clk.stop() if clk else None
+    s.close()
+    nres = prob["nres"]
+    peak, peak_kind = measured_peaks()
+    b_launch = prob["g_num"].shape[0] * (512 + 32 + 64) + prob["nn"] * 8   # storkc, conn, results, gathered p
+    avg_s = ms_elem / args.steps / 1e3
+    line = {"metric": METRIC, "value": neq * args.steps / (ms_tot / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"p123 book run: {n}^3 8-node bricks (Laplace), kx=ky=kz=2, nip 8, checon tol "
+                                   f"1e-5", "nels": n ** 3, "neq": neq},
+            "solve": {"iters": it, "wall_s": t_solve, "device_s": st["solve_ms"] / 1e3,
+                      "dof_iter_per_s": neq * it / t_solve, "potentials": [float(v) for v in x[nres - 1:nres + 3]],
+                      "reference_book": {"iters": 180, "solver_s": 52.3833, "cores": 16}},
+            "roofline": {"kernel": "k_elem8 (FP64 storkc)", "bound": "hbm", "achieved": b_launch / avg_s / 1e9,
+                         "peak": peak, "unit": "GB/s", "frac": b_launch / avg_s / 1e9 / peak,
+                         "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": b_launch,
+                         "avg_launch_ms": avg_s * 1e3, "traffic": None, "scatter_avg_ms": ms_scat / args.steps},
+            "host_setup_s": t_host, "storkc_formation_s": t_form, "gpu_launches": int(launches), "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def run_cube10(args, rank, world, local, dist):
     """The reference's CPU-runnable case: 10^3 cube, nip 27, E 100, v 0.3,
     fixed base, top pressure (total -1), checon_par tol 1e-6, limit 5000.
@@ -668,6 +719,8 @@ def main():
             return run_cube10(args, rank, world, local, dist)
         if args.workload == "shared100":
             return run_shared(args, rank, world, local, dist)
+        if args.workload == "p123book":
+            return run_p123(args, rank, world, local, dist)
         return run_gb300(args, rank, world, local, dist)
     finally:
         if dist is not None:

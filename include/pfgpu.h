@@ -148,6 +148,11 @@ int pf_bench_iterations(void **ctx, const int *prec, const int *steps,
  * (p121.f90:112-123): sigma(6) = D . B(0,0,0) . u_e; iel is 1-based. */
 int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *sigma);
 
+/* Centroid stresses of elements first..first+count-1 (1-based) for the
+ * displacements xnew(neq): sigma(6, count), one thread per element (the
+ * post-solve stress recovery of p121.f90:112-123 for the whole mesh). */
+int pf_element_stresses(void **ctx, const double *xnew, const int *first, const int *count, double *sigma);
+
 /* The autotuner's choice for the packed-symmetric FP32 element kernel, made
  * at pf_form_storkm / pf_set_storkm by timing every configuration on this
  * mesh: warps per CTA, shared-memory stages per warp, and the measured
@@ -163,6 +168,23 @@ int pf_set_tuning(void **ctx, const int *config);
  * on first use per solve mode) when *on != 0, the default; *on == 0 launches
  * every kernel directly.  Both give bitwise the same iterates. */
 int pf_set_graphs(void **ctx, const int *on);
+
+/* ---- p123: 3-D Laplace with 8-node bricks (src/programs/5th_ed/p123/p123.f90) ----
+ * A context set up with pf_setup_scalar8 holds one freedom per node:
+ * g_num(8,nels), g_g(8,nels) (0 = restrained), g_coord(8,3,nels).  pf_solve
+ * (PF_MODE_P121 or PF_MODE_FP64_RES), pf_ebe_matvec (prec 64),
+ * pf_bench_iterations (prec 64), pf_get_diag and pf_solve_stats apply. */
+int pf_setup_scalar8(void **ctx, const int *nels, const int *nn, const int *neq,
+                     const int *g_num, const int *g_g, const double *g_coord);
+/* storkc = sum over the Gauss points of (kx dx dx' + ky dy dy' + kz dz dz')
+ * det w (p123.f90:70-85) and the Jacobi diagonal (:87-94). */
+int pf_form_storkc(void **ctx, const int *nip, const double *kx, const double *ky, const double *kz);
+int pf_get_storkc(void **ctx, const int *first, const int *count, double *storkc);
+/* Fixed freedoms by the penalty method (p123.f90:104-131): diag(eq) +=
+ * penalty for each listed equation, and every product then returns
+ * u(eq) = p(eq) * diag(eq).  The caller sets r(eq) = diag(eq) * value
+ * (pf_get_diag gives diag(eq) after this call).  pf_form_storkc clears them. */
+int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const double *penalty);
 
 /* Number of kernels this library launched since the context was created. */
 int pf_kernel_launches(void **ctx, long long *count);
@@ -238,8 +260,9 @@ int pf_ebe_matvec_noalloc(const int *nels, const int *neq, const double *storkm,
 /* ---------------------------------------------------------------------- */
 /* Host-side driver layer (C++, no GPU work): deck I/O and generators.     */
 
-/* p12meshgen's p121 case (src/tools/preprocessing/p12meshgen/p12meshgen.f90:118-323):
- * reads job.mg and writes job.dat, job.d, job.bnd, job.lds. */
+/* p12meshgen's p121 and p123 cases (src/tools/preprocessing/p12meshgen/
+ * p12meshgen.f90:118-323, 658-801): reads job.mg and writes job.dat, job.d,
+ * job.bnd, job.lds (and job.fix for p123 decks with fixed freedoms). */
 int pf_p12meshgen(const char *job);
 
 /* Runs the whole p121 job (p121.f90:1-141) on the GPU: reads job.dat/.d/
@@ -247,6 +270,21 @@ int pf_p12meshgen(const char *job);
  * mode: PF_MODE_*; iters and central (xnew(1)) are returned. */
 int pf_p121_run(const char *job, const int *device, const int *mode,
                 int *iters, double *central);
+
+/* Host side of p123: an nxe x nye x nze box of 8-node bricks numbered as
+ * GEOMETRY_8BXZ (geometry.f90:70-166): g_num(8,nels), g_coord(8,3,nels). */
+int pf_mesh_box8(const int *nxe, const int *nye, const int *nze, const double *aa, const double *bb,
+                 const double *cc, int *g_num, double *g_coord);
+/* box_bc8's restraints (geometry.f90:655-696): node_fix(nn) = 1 free, 0 fixed. */
+int pf_box8_restraints(const int *nxe, const int *nye, const int *nze, int *node_fix);
+/* One freedom per node: equation = free nodes up to and including the node
+ * (rearrange_2 + find_g4, new_library.f90:3118-3271). */
+int pf_number_equations1(const int *nels, const int *nn, const int *nod, const int *g_num,
+                         const int *node_fix, int *g_g, int *neq);
+/* The whole p123 job: reads job.dat/.d/.bnd/.lds/.fix, solves on the GPU,
+ * writes job.res and job.ensi.NDPTL-000001; returns the iterations and the
+ * four printed potentials (equations nres..nres+3). */
+int pf_p123_run(const char *job, const int *device, int *iters, double *potentials);
 
 /* Structured 20-node cube mesh in GEOMETRY_20BXZ numbering
  * (src/modules/shared/geometry.f90:172-290), nxe x nye x nze elements of

@@ -1,4 +1,4 @@
-"""CPU oracle for the p121 EBE-PCG path (TEST INFRASTRUCTURE ONLY).
+"""CPU oracle for the p121 and p123 EBE-PCG paths (TEST INFRASTRUCTURE ONLY).
 
 Wraps ``p121_oracle.c`` (a plain-C restatement of ParaFEM's p121 solve) and
 adds a numpy reader for p121 decks.  Only the tests, the smoke check and the
@@ -38,14 +38,14 @@ _PD = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 def build(force: bool = False) -> str:
     """Compile the C restatement into ``oracle/_build/liborc.so`` (gcc, OpenMP)."""
-    src = os.path.join(HERE, "p121_oracle.c")
+    srcs = [os.path.join(HERE, "p121_oracle.c"), os.path.join(HERE, "p123_oracle.c")]
     os.makedirs(BUILD_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src)):
+            and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs)):
         return LIB_PATH
     tmp = LIB_PATH + f".tmp{os.getpid()}"
     subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-fopenmp",
-                           "-ffp-contract=off", "-o", tmp, src, "-lm"])
+                           "-ffp-contract=off", "-o", tmp] + srcs + ["-lm"])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -77,6 +77,22 @@ def lib():
             L.orc_centroid_stress.argtypes = [_PD, _PD, _D, _D, _PD]
             L.orc_num_threads.restype = _I
             L.orc_set_num_threads.argtypes = [_I]
+            # p123 (p123_oracle.c)
+            L.orc_geometry_8bxz.argtypes = [_I, _I, _I, _D, _D, _D, _PD, _PI]
+            L.orc_box_bc8.argtypes = [_I, _I, _I, _PI]
+            L.orc_box_bc8.restype = _I
+            L.orc_rearrange_2.argtypes = [_I, _PI]
+            L.orc_find_g4.argtypes = [_PI, _I, _PI, _I, _PI]
+            L.orc_abaqus2sg8.argtypes = [_I, _PI]
+            L.orc_shape_der8.argtypes = [_PD, _D, _D, _D]
+            L.orc_form_storkc.argtypes = [_I, _I, _PD, _D, _D, _D, _PD]
+            L.orc_diag8.argtypes = [_I, _I, _PI, _PD, _I, _PD]
+            L.orc_pcg123.argtypes = [_I, _I, _PI, _PD, _I, _PD, _PD, _I, _PI, _PD, _D, _I, _PD,
+                                     ctypes.POINTER(ctypes.c_double)]
+            L.orc_pcg123.restype = _I
+            L.orc_ebe_matvec8.argtypes = [_I, _I, _PI, _PD, _I, _PD, _PD]
+            L.orc_mesh_box8.argtypes = [_I, _I, _I, _D, _D, _D, _PI, ctypes.c_void_p]
+            L.orc_steering8.argtypes = [_I, _PI, _I, _PI, _PI]
             _lib = L
     return _lib
 
@@ -265,3 +281,92 @@ def _seq_sum(a: np.ndarray) -> float:
     for val in a.tolist():
         s += val
     return s
+
+
+# ---------------------------------------------------------------------------
+# p123: 3-D Laplace with 8-node bricks (src/programs/5th_ed/p123/p123.f90),
+# restated in p123_oracle.c
+# ---------------------------------------------------------------------------
+def box8_mesh(nxe, nye, nze, aa, bb, cc, coords=True):
+    """GEOMETRY_8BXZ over the box: g_num (nels, 8) and, if asked, g_coord (nels, 3, 8)."""
+    nels = nxe * nye * nze
+    g_num = np.zeros((nels, 8), np.int32)
+    g_coord = np.zeros((nels, 3, 8)) if coords else None
+    lib().orc_mesh_box8(nxe, nye, nze, aa, bb, cc, g_num, g_coord.ctypes.data if coords else None)
+    return g_num, g_coord
+
+
+def box8_rest(nxe, nye, nze):
+    """box_bc8 rows (node, 0), sorted by node."""
+    nn = (nxe + 1) * (nye + 1) * (nze + 1)
+    rest = np.zeros(2 * nn, np.int32)
+    nr = lib().orc_box_bc8(nxe, nye, nze, rest)
+    return np.ascontiguousarray(rest[:2 * nr].reshape(nr, 2))
+
+
+def steering8(g_num, rest):
+    """rearrange_2 + find_g4 for every element -> g_g (nels, 8), and neq."""
+    rr = np.ascontiguousarray(rest, dtype=np.int32).copy()
+    lib().orc_rearrange_2(rr.shape[0], rr)
+    g_g = np.zeros(g_num.shape, np.int32)
+    lib().orc_steering8(g_num.shape[0], np.ascontiguousarray(g_num, dtype=np.int32), rr.shape[0], rr, g_g)
+    return g_g, int(g_g.max())
+
+
+def form_storkc(g_coord, nip, kx, ky, kz):
+    g_coord = np.ascontiguousarray(g_coord, dtype=np.float64)
+    nels = g_coord.shape[0]
+    kc = np.zeros((nels, 8, 8))
+    lib().orc_form_storkc(nels, nip, g_coord, kx, ky, kz, kc)
+    return kc
+
+
+def diag8(g_g, storkc, neq, shared=False):
+    out = np.zeros(neq)
+    lib().orc_diag8(g_g.shape[0], neq, np.ascontiguousarray(g_g, dtype=np.int32),
+                    np.ascontiguousarray(storkc, dtype=np.float64), 0 if shared else 64, out)
+    return out
+
+
+def pcg123(g_g, storkc, dg, rhs, tol, limit, fix_eq=(), fix_store=(), shared=False):
+    """p123's PCG with checon_par; dg already holds the penalties. Returns (iters, x, metric)."""
+    neq = dg.shape[0]
+    x = np.zeros(neq)
+    metric = ctypes.c_double(0.0)
+    fe = np.ascontiguousarray(np.asarray(fix_eq, dtype=np.int32))
+    fs = np.ascontiguousarray(np.asarray(fix_store, dtype=np.float64))
+    it = lib().orc_pcg123(g_g.shape[0], neq, np.ascontiguousarray(g_g, dtype=np.int32),
+                          np.ascontiguousarray(storkc, dtype=np.float64), 0 if shared else 64,
+                          np.ascontiguousarray(dg, dtype=np.float64), np.ascontiguousarray(rhs, dtype=np.float64),
+                          fe.size, fe if fe.size else np.zeros(1, np.int32), fs if fs.size else np.zeros(1),
+                          tol, limit, x, ctypes.byref(metric))
+    return it, x, metric.value
+
+
+def ebe_matvec8(g_g, storkc, p, shared=False):
+    u = np.zeros_like(p)
+    lib().orc_ebe_matvec8(g_g.shape[0], p.shape[0], np.ascontiguousarray(g_g, dtype=np.int32),
+                          np.ascontiguousarray(storkc, dtype=np.float64), 0 if shared else 64,
+                          np.ascontiguousarray(p, dtype=np.float64), u)
+    return u
+
+
+def run_p123_box(nxe, nye, nze, aa, bb, cc, kx, ky, kz, tol, limit, nip=8, load=10.0):
+    """The p123 job on p12meshgen's box (p12meshgen.f90:658-801 + p123.f90),
+    in memory: every element of the uniform box has element 1's storkc,
+    which the solve shares.  Returns dict(nn, nr, neq, iters, q, nres, x)."""
+    g_num, _ = box8_mesh(nxe, nye, nze, aa, bb, cc, coords=False)
+    co = np.zeros(24)
+    num = np.zeros(8, np.int32)
+    lib().orc_geometry_8bxz(1, nxe, nze, aa, bb, cc, co, num)
+    kc = form_storkc(co.reshape(1, 3, 8), nip, kx, ky, kz)
+    rest = box8_rest(nxe, nye, nze)
+    g_g, neq = steering8(g_num, rest)
+    del g_num
+    dg = diag8(g_g, kc, neq, shared=True)
+    nres = nxe * (nze - 1) + 1
+    r = np.zeros(neq)
+    r[nres - 1] = load                       # loaded freedom used as an equation (p123.f90:98-103)
+    it, x, _ = pcg123(g_g, kc, dg, r, tol, limit, shared=True)
+    return dict(nn=(nxe + 1) * (nye + 1) * (nze + 1), nr=rest.shape[0], neq=neq, iters=it, q=float(r.sum()),
+                nres=nres, x=x)

@@ -16,10 +16,12 @@ OUT = os.path.join(HERE, "_build")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(OUT, "libpfgpu.so")
 EXE = os.path.join(OUT, "p121")
+EXE123 = os.path.join(OUT, "p123")
+PROGRAMS = [("p121_main.cpp", EXE), ("p123_main.cpp", EXE123)]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["pf_kernels.cu", "pf_elem_sym.cu", "pf_shared.cu", "pf_batch.cu", "pf_multi.cu", "pf_abi.cu",
-                "pf_noalloc.cu"]
+CUDA_SOURCES = ["pf_kernels.cu", "pf_elem_sym.cu", "pf_shared.cu", "pf_scalar8.cu", "pf_batch.cu", "pf_multi.cu",
+                "pf_abi.cu", "pf_noalloc.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
 HEADERS = ["pf_internal.h", "pf_device.cuh", "pf_tc.cuh"]
 
@@ -34,7 +36,7 @@ def nvcc() -> str:
 
 
 def _sources():
-    return ([os.path.join(SRC, s) for s in CUDA_SOURCES + CXX_SOURCES + HEADERS + ["p121_main.cpp"]]
+    return ([os.path.join(SRC, s) for s in CUDA_SOURCES + CXX_SOURCES + HEADERS + [m for m, _ in PROGRAMS]]
             + [os.path.join(INCLUDE, "pfgpu.h"), os.path.abspath(__file__)])
 
 
@@ -48,7 +50,7 @@ def _stale(target: str) -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     """Compile everything if any source is newer than the library; return its path."""
     with _lock:
-        if not force and not _stale(LIB) and not _stale(EXE):
+        if not force and not _stale(LIB) and not any(_stale(x) for _, x in PROGRAMS):
             return LIB
         os.makedirs(OUT, exist_ok=True)
         cc = nvcc()
@@ -75,9 +77,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
         tmp = LIB + f".tmp{os.getpid()}"
         subprocess.check_call([cc] + ARCH + ["-shared", "-o", tmp] + objs)
         os.replace(tmp, LIB)
-        tmpx = EXE + f".tmp{os.getpid()}"
         cxx = shutil.which("g++") or shutil.which("c++") or "g++"
-        subprocess.check_call([cxx, "-O2", "-std=c++17", "-I", INCLUDE, os.path.join(SRC, "p121_main.cpp"),
-                               "-L", OUT, "-lpfgpu", "-Wl,-rpath,$ORIGIN", "-o", tmpx])
-        os.replace(tmpx, EXE)
+        for main, exe in PROGRAMS:
+            tmpx = exe + f".tmp{os.getpid()}"
+            subprocess.check_call([cxx, "-O2", "-std=c++17", "-I", INCLUDE, os.path.join(SRC, main),
+                                   "-L", OUT, "-lpfgpu", "-Wl,-rpath,$ORIGIN", "-o", tmpx])
+            os.replace(tmpx, exe)
         return LIB

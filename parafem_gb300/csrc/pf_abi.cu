@@ -94,8 +94,9 @@ static void free_mesh(Ctx &c)
     drop_graph(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
-    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32);
+    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore);
     c.shared = false;
+    c.kind = KIND_SOLID20;
     dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
     dfree(c.d); dfree(c.p); dfree(c.u); dfree(c.rres); dfree(c.eqbuf); dfree(c.utemp); dfree(c.part);
     c.nels = c.nn = c.neq = c.nslots = 0;
@@ -352,8 +353,10 @@ extern "C" int pf_ctx_destroy(void **ctx)
     return PF_SUCCESS;
 }
 
-extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const int *neq_p, const int *g_num,
-                        const int *g_g, const double *g_coord)
+// Mesh tables of a context: nod nodes per element (20 or 8) with nodof
+// freedoms per node (3 or 1).  Slots are node-major (nodof * node + dof).
+static int setup_mesh(void **ctx, const int *nels_p, const int *nn_p, const int *neq_p, const int *g_num,
+                      const int *g_g, const double *g_coord, const int nod, const int nodof)
 {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
@@ -362,32 +365,34 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
         set_error("pf_setup: null argument");
         return PF_FAILURE;
     }
+    const int ntot = nod * nodof;
     const int nels = *nels_p, nn = *nn_p, neq = *neq_p;
-    if (nels < 1 || nn < 1 || neq < 0 || (long long)nn * 3 > 0x7fffffffLL || (long long)nels * 20 > 0x7fffffffLL) {
+    if (nels < 1 || nn < 1 || neq < 0 || (long long)nn * nodof > 0x7fffffffLL ||
+        (long long)nels * 60 > 0x7fffffffLL) {
         set_error("pf_setup: invalid sizes nels=%d nn=%d neq=%d", nels, nn, neq);
         return PF_FAILURE;
     }
     CK(cudaStreamSynchronize(c.stream));
     free_mesh(c);
-    const int ns = 3 * nn;
-    std::vector<int> conn((size_t)nels * 20), slot_eq(ns, -1), eq_slot(neq > 0 ? neq : 1, -1);
+    const int ns = nodof * nn;
+    std::vector<int> conn((size_t)nels * nod), slot_eq(ns, -1), eq_slot(neq > 0 ? neq : 1, -1);
     std::vector<int> cnt(nn + 1, 0);
     for (size_t e = 0; e < (size_t)nels; ++e)
-        for (int a = 0; a < 20; ++a) {
-            const int nd = g_num[e * 20 + a];
+        for (int a = 0; a < nod; ++a) {
+            const int nd = g_num[e * nod + a];
             if (nd < 1 || nd > nn) {
                 set_error("pf_setup: g_num(%d,%zu)=%d outside 1..%d", a + 1, e + 1, nd, nn);
                 return PF_FAILURE;
             }
-            conn[e * 20 + a] = nd - 1;
+            conn[e * nod + a] = nd - 1;
             cnt[nd]++;
-            for (int d = 0; d < 3; ++d) {
-                const int q = g_g[e * 60 + 3 * a + d];
+            for (int d = 0; d < nodof; ++d) {
+                const int q = g_g[e * ntot + nodof * a + d];
                 if (q < 0 || q > neq) {
-                    set_error("pf_setup: g_g(%d,%zu)=%d outside 0..%d", 3 * a + d + 1, e + 1, q, neq);
+                    set_error("pf_setup: g_g(%d,%zu)=%d outside 0..%d", nodof * a + d + 1, e + 1, q, neq);
                     return PF_FAILURE;
                 }
-                int &se = slot_eq[3 * (nd - 1) + d];
+                int &se = slot_eq[nodof * (nd - 1) + d];
                 if (se < 0) se = q;
                 else if (se != q) {
                     set_error("pf_setup: node %d dof %d has equations %d and %d in different elements", nd,
@@ -406,7 +411,7 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
                 return PF_FAILURE;
             }
             eq_slot[q - 1] = s;
-            fm[s / 3] |= (uint8_t)(1u << (s % 3));
+            fm[s / nodof] |= (uint8_t)(1u << (s % nodof));
         }
     }
     for (int q = 0; q < neq; ++q)
@@ -417,14 +422,15 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
     // node -> (element, local node) table, ascending element order per node
     std::vector<int> ptr(nn + 1, 0);
     for (int n = 0; n < nn; ++n) ptr[n + 1] = ptr[n] + cnt[n + 1];
-    std::vector<int> fill(ptr.begin(), ptr.end() - 1), list((size_t)nels * 20);
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1), list((size_t)nels * nod);
     for (size_t e = 0; e < (size_t)nels; ++e)
-        for (int a = 0; a < 20; ++a) {
-            const int n = conn[e * 20 + a];
-            list[fill[n]++] = (int)(e * 20 + a);   // contribution index: element e, local node a
+        for (int a = 0; a < nod; ++a) {
+            const int n = conn[e * nod + a];
+            list[fill[n]++] = (int)(e * nod + a);   // contribution index: element e, local node a
         }
 
     c.nels = nels; c.nn = nn; c.neq = neq; c.nslots = ns;
+    c.kind = nod == 8 ? KIND_SCALAR8 : KIND_SOLID20;
     long long g = ((long long)ns + 255) / 256;
     if (g > (long long)c.nsm * 8) g = (long long)c.nsm * 8;
     c.G = (int)(g < 1 ? 1 : g);
@@ -432,14 +438,15 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
     if (gs > (long long)c.nsm * 16) gs = (long long)c.nsm * 16;
     c.Gs = (int)(gs < 1 ? 1 : gs);
     const size_t ne = (size_t)nels;
-    if (dalloc(&c.conn, ne * 20, "connectivity") || dalloc(&c.node_ptr, nn + 1, "node table") ||
-        dalloc(&c.node_list, ne * 20, "node table") || dalloc(&c.slot_eq, ns, "slot map") ||
+    if (dalloc(&c.conn, ne * nod, "connectivity") || dalloc(&c.node_ptr, nn + 1, "node table") ||
+        dalloc(&c.node_list, ne * nod, "node table") || dalloc(&c.slot_eq, ns, "slot map") ||
         dalloc(&c.eq_slot, neq, "equation map") || dalloc(&c.freemask, nn, "restraint mask") ||
-        dalloc(&c.coord, ne * 60, "coordinates") || dalloc(&c.ediag, ne * 60, "element diagonals") ||
+        dalloc(&c.coord, ne * nod * 3, "coordinates") || dalloc(&c.ediag, ne * ntot, "element diagonals") ||
+        (nodof == 1 && dalloc(&c.fstore, ns, "fixed freedoms")) ||
         dalloc(&c.diag, ns, "diag") || dalloc(&c.dinv, ns, "diag") || dalloc(&c.f, ns, "f") ||
         dalloc(&c.x, ns, "x") || dalloc(&c.c, ns, "c") || dalloc(&c.r, ns, "r") || dalloc(&c.d, ns, "d") ||
         dalloc(&c.p, ns, "p") || dalloc(&c.u, ns, "u") || dalloc(&c.rres, ns, "rres") ||
-        dalloc(&c.eqbuf, neq + 8, "equation buffer") || dalloc((double **)&c.utemp, ne * 60, "utemp") ||
+        dalloc(&c.eqbuf, neq + 8, "equation buffer") || dalloc((double **)&c.utemp, ne * ntot, "utemp") ||
         dalloc(&c.part, (size_t)c.Gs + 6 * (size_t)c.G + 16, "partials")) {
         free_mesh(c);
         return PF_FAILURE;
@@ -448,18 +455,108 @@ extern "C" int pf_setup(void **ctx, const int *nels_p, const int *nn_p, const in
     c.part_u = c.part_s + c.Gs;
     c.part_r = c.part_u + 4 * (size_t)c.G;
     c.scr = c.part_r + 2 * (size_t)c.G;
-    CK(cudaMemcpyAsync(c.conn, conn.data(), ne * 20 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.conn, conn.data(), ne * nod * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.node_ptr, ptr.data(), (nn + 1) * sizeof(int), cudaMemcpyHostToDevice, c.stream));
-    CK(cudaMemcpyAsync(c.node_list, list.data(), ne * 20 * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.node_list, list.data(), ne * nod * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.slot_eq, slot_eq.data(), ns * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     if (neq > 0)
         CK(cudaMemcpyAsync(c.eq_slot, eq_slot.data(), neq * sizeof(int), cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.freemask, fm.data(), nn, cudaMemcpyHostToDevice, c.stream));
-    CK(cudaMemcpyAsync(c.coord, g_coord, ne * 60 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.coord, g_coord, ne * nod * 3 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    if (c.fstore) CK(cudaMemsetAsync(c.fstore, 0, ns * sizeof(double), c.stream));
     CK(cudaMemsetAsync(c.x, 0, ns * sizeof(double), c.stream));
     CK(cudaMemsetAsync(c.f, 0, ns * sizeof(double), c.stream));
     CK(cudaStreamSynchronize(c.stream));
     return PF_SUCCESS;
+}
+
+extern "C" int pf_setup(void **ctx, const int *nels, const int *nn, const int *neq, const int *g_num,
+                        const int *g_g, const double *g_coord)
+{
+    return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 20, 3);
+}
+
+extern "C" int pf_setup_scalar8(void **ctx, const int *nels, const int *nn, const int *neq, const int *g_num,
+                                const int *g_g, const double *g_coord)
+{
+    return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 8, 1);
+}
+
+extern "C" int pf_form_storkc(void **ctx, const int *nip, const double *kx, const double *ky, const double *kz)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (c.kind != KIND_SCALAR8 || c.nels == 0) {
+        set_error("pf_form_storkc: call pf_setup_scalar8 first");
+        return PF_FAILURE;
+    }
+    if (!nip || !kx || !ky || !kz || (*nip != 8 && *nip != 27)) {
+        set_error("pf_form_storkc: nip must be 8 or 27");
+        return PF_FAILURE;
+    }
+    if (!c.km64 && dalloc(&c.km64, (size_t)c.nels * 64, "storkc")) return PF_FAILURE;
+    drop_graph(c);
+    TRY(launch_form_storkc(c, *nip, *kx, *ky, *kz));
+    TRY(launch_assemble_diag(c));
+    TRY(sync(c));
+    c.have_km = true;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_get_storkc(void **ctx, const int *first, const int *count, double *storkc)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (c.kind != KIND_SCALAR8 || !c.have_km || !first || !count || !storkc || *first < 0 || *count < 0 ||
+        *first + (long long)*count > c.nels) {
+        set_error("pf_get_storkc: invalid range or no storkc");
+        return PF_FAILURE;
+    }
+    CK(cudaMemcpyAsync(storkc, c.km64 + (size_t)*first * 64, (size_t)*count * 64 * sizeof(double),
+                       cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const double *penalty)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (c.kind != KIND_SCALAR8 || !c.have_km) {
+        set_error("pf_set_fixed: needs a scalar 8-node context with storkc formed");
+        return PF_FAILURE;
+    }
+    if (!nfix || *nfix < 0 || (*nfix > 0 && !eqs) || !penalty) {
+        set_error("pf_set_fixed: invalid arguments");
+        return PF_FAILURE;
+    }
+    if (*nfix == 0) return PF_SUCCESS;
+    std::vector<int> slot_eq(c.nslots), slots(*nfix);
+    CK(cudaMemcpy(slot_eq.data(), c.slot_eq, (size_t)c.nslots * sizeof(int), cudaMemcpyDeviceToHost));
+    std::vector<int> eq_slot(c.neq + 1, -1);
+    for (int s = 0; s < c.nslots; ++s)
+        if (slot_eq[s] > 0) eq_slot[slot_eq[s]] = s;
+    for (int i = 0; i < *nfix; ++i) {
+        if (eqs[i] < 1 || eqs[i] > c.neq) {
+            set_error("pf_set_fixed: equation %d outside 1..%d", eqs[i], c.neq);
+            return PF_FAILURE;
+        }
+        slots[i] = eq_slot[eqs[i]];
+    }
+    int *d_slots = nullptr;
+    if (dalloc(&d_slots, (size_t)*nfix, "fixed freedoms")) return PF_FAILURE;
+    cudaError_t e = cudaMemcpyAsync(d_slots, slots.data(), (size_t)*nfix * sizeof(int), cudaMemcpyHostToDevice,
+                                    c.stream);
+    int bad = e != cudaSuccess;
+    if (!bad) bad = launch_set_fixed(c, *nfix, d_slots, *penalty);
+    if (!bad) bad = sync(c);
+    cudaFree(d_slots);
+    if (bad && e != cudaSuccess) set_error("pf_set_fixed: %s", cudaGetErrorString(e));
+    drop_graph(c);
+    return bad ? PF_FAILURE : PF_SUCCESS;
 }
 
 extern "C" int pf_set_material(void **ctx, const int *n, const double *e, const double *v)
@@ -505,6 +602,10 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_form_storkm: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
     if (!nip || !flags || (*nip != 8 && *nip != 27)) {
         set_error("pf_form_storkm: nip must be 8 or 27");
         return PF_FAILURE;
@@ -529,6 +630,10 @@ extern "C" int pf_set_storkm(void **ctx, const double *storkm)
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_set_storkm: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
     if (!storkm || c.nels == 0) { set_error("pf_set_storkm: call pf_setup first"); return PF_FAILURE; }
     TRY(ensure_storkm(c));
     CK(cudaMemcpyAsync(c.km64, storkm, (size_t)c.nels * 3600 * sizeof(double), cudaMemcpyHostToDevice,
@@ -547,6 +652,10 @@ extern "C" int pf_form_km(void **ctx, const int *iel, const int *nip, const int 
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_form_km: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
     if (!iel || !nip || !flags || !km || (*nip != 8 && *nip != 27)) {
         set_error("pf_form_km: nip must be 8 or 27");
         return PF_FAILURE;
@@ -581,6 +690,10 @@ extern "C" int pf_set_shared_km(void **ctx, const double *km)
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_set_shared_km: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
     if (!km || c.nels == 0) {
         set_error("pf_set_shared_km: call pf_setup first");
         return PF_FAILURE;
@@ -610,6 +723,10 @@ extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, dou
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_get_storkm: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
     if (c.shared) {
         set_error("pf_get_storkm: the context uses one shared element matrix (pf_set_shared_km)");
         return PF_FAILURE;
@@ -641,8 +758,9 @@ extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, doubl
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32 && *prec != 31)) {
-        set_error("pf_ebe_matvec: invalid arguments or no storkm");
+    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32 && *prec != 31) ||
+        (c.kind == KIND_SCALAR8 && *prec != 64)) {
+        set_error("pf_ebe_matvec: invalid arguments or no storkm (8-node scalar contexts: prec 64)");
         return PF_FAILURE;
     }
     CK(cudaMemcpyAsync(c.eqbuf, p, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
@@ -735,6 +853,10 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
         set_error("pf_solve: invalid arguments or no storkm");
         return PF_FAILURE;
     }
+    if (c.kind == KIND_SCALAR8 && (*mode == PF_MODE_MIXED || *mode == PF_MODE_MIXED_RESTART)) {
+        set_error("pf_solve: the mixed modes need 20-node elements; 8-node scalar contexts solve in FP64");
+        return PF_FAILURE;
+    }
     for (int i = 0; i < 8; ++i) c.stats[i] = 0.0;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -796,8 +918,9 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (!prec || !steps || *steps < 1 || !c.have_km || (*prec != 32 && *prec != 31 && *prec != 64)) {
-        set_error("pf_bench_iterations: invalid arguments or no storkm");
+    if (!prec || !steps || *steps < 1 || !c.have_km || (*prec != 32 && *prec != 31 && *prec != 64) ||
+        (c.kind == KIND_SCALAR8 && *prec != 64)) {
+        set_error("pf_bench_iterations: invalid arguments or no storkm (8-node scalar contexts: prec 64)");
         return PF_FAILURE;
     }
     const int n = *steps;
@@ -844,6 +967,10 @@ extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_centroid_stress: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
     if (!iel || !xnew || !sigma || *iel < 1 || *iel > c.nels || c.nmat == 0) {
         set_error("pf_centroid_stress: invalid element or no material");
         return PF_FAILURE;
@@ -851,8 +978,33 @@ extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew
     double *sig = c.scr + 2;
     CK(cudaMemcpyAsync(c.eqbuf, xnew, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
-    TRY(launch_centroid_stress(c, *iel - 1, c.rres, sig));
+    TRY(launch_centroid_stress(c, *iel - 1, 1, c.rres, sig));
     CK(cudaMemcpyAsync(sigma, sig, 6 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    TRY(sync(c));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_element_stresses(void **ctx, const double *xnew, const int *first, const int *count,
+                                   double *sigma)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    Ctx &c = *cp;
+    if (c.kind != KIND_SOLID20) {
+        set_error("pf_element_stresses: needs a 20-node context (pf_setup)");
+        return PF_FAILURE;
+    }
+    if (!xnew || !first || !count || !sigma || *first < 1 || *count < 0 || *first - 1 + (long long)*count > c.nels ||
+        c.nmat == 0) {
+        set_error("pf_element_stresses: invalid element range or no material");
+        return PF_FAILURE;
+    }
+    if (*count == 0) return PF_SUCCESS;
+    double *sig = (double *)c.utemp;   // 6 x count <= 60 x nels doubles
+    CK(cudaMemcpyAsync(c.eqbuf, xnew, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
+    TRY(launch_centroid_stress(c, *first - 1, *count, c.rres, sig));
+    CK(cudaMemcpyAsync(sigma, sig, (size_t)6 * *count * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
 }

@@ -20,7 +20,9 @@
 //
 // The solve is p121's Jacobi-PCG (p121.f90:86-104) stopped at
 // ||r||_2/||f||_2 <= tol, with one of two element products chosen at
-// creation: FP64 storkm, or FP32 storkm with FP64 residual replacement per
+// creation: FP64 storkm, or the packed-symmetric FP32 storkm (products by
+// the bulk-copy kernel of the single-mesh path, through a map from active
+// element positions to arena elements) with FP64 residual replacement per
 // mesh (the PF_MODE_MIXED scheme: a mesh whose recursive residual has
 // dropped 10x pauses, the host computes its FP64 true residual at the next
 // sync and either retires it or replaces its residual and resumes it).
@@ -103,47 +105,19 @@ k_bt_elem(int nseg, const BSeg *__restrict__ segs, long long total, const double
     }
 }
 
-// FP32 element products of every active mesh (mixed precision): full FP32
-// storkm, node-padded float results
-__global__ void __launch_bounds__(256)
-k_bt_elem32(int nseg, const BSeg *__restrict__ segs, long long total, const float *__restrict__ km,
-            const int *__restrict__ conn, const double *__restrict__ p, float *__restrict__ ut,
-            const PcgState *__restrict__ st)
+// arena element of every active element position (the segment table in
+// element order), for the bulk-copy element kernel of the mixed engine
+__global__ void k_bt_emap(int nseg, const BSeg *__restrict__ segs, long long total, int *__restrict__ emap)
 {
-    const int lane = threadIdx.x & 31;
-    const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const int j1 = lane + 32;
-    for (long long g = warp; g < total; g += nwarps) {
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < total;
+         g += (long long)gridDim.x * blockDim.x) {
         int lo = 0, hi = nseg - 1;
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (segs[mid].el_cum <= g) lo = mid;
             else hi = mid - 1;
         }
-        if (st[segs[lo].sid].stop) continue;
-        const size_t e = (size_t)segs[lo].el0 + (size_t)(g - segs[lo].el_cum);
-        const int nd = (lane < 20) ? conn[e * 20 + lane] : 0;
-        const int n0 = __shfl_sync(FULLMASK, nd, lane / 3);
-        const int n1 = __shfl_sync(FULLMASK, nd, j1 < 60 ? j1 / 3 : 0);
-        const float p0 = (float)p[(size_t)3 * n0 + lane % 3];
-        const float p1 = (j1 < 60) ? (float)p[(size_t)3 * n1 + j1 % 3] : 0.f;
-        const float *ke = km + e * 3600 + 2 * lane;
-        float a0 = 0.f, a1 = 0.f;
-#pragma unroll 12
-        for (int j = 0; j < 60; ++j) {
-            const float pj = __shfl_sync(FULLMASK, j < 32 ? p0 : p1, j & 31);
-            if (lane < 30) {
-                const float2 k2 = __ldg(reinterpret_cast<const float2 *>(ke + 60 * j));
-                a0 = fmaf(k2.x, pj, a0);
-                a1 = fmaf(k2.y, pj, a1);
-            }
-        }
-        if (lane < 30) {
-            const int i0 = 2 * lane, i1 = 2 * lane + 1;
-            ut[e * 80 + (i0 / 3) * 4 + i0 % 3] = a0;
-            ut[e * 80 + (i1 / 3) * 4 + i1 % 3] = a1;
-        }
+        emap[g] = segs[lo].el0 + (int)(g - segs[lo].el_cum);
     }
 }
 
@@ -486,11 +460,13 @@ struct Batch {
     int device = 0, nsm = 1;
     int prec = 64;                   // 64: FP64 products; 32: FP32 products + FP64 residual replacement
     cudaStream_t stream = nullptr;
+    int *kerr = nullptr;             // bulk-copy wait timeouts of the element kernel
+    int *emap = nullptr;             // [cap_el] arena element of each active element (prec 32)
     long long cap_el = 0, cap_nodes = 0;
     int max_meshes = 0, capb_s = 0, capb_v = 0;
     // arenas
     double *km64 = nullptr, *coord = nullptr, *ediag = nullptr, *ut = nullptr, *mat_e = nullptr, *mat_v = nullptr;
-    float *km32 = nullptr;
+    float *km32p = nullptr;          // packed-symmetric FP32 storkm (prec 32): 1832 floats per element
     int *conn = nullptr, *list = nullptr;
     int2 *nptr = nullptr;
     uint8_t *fm = nullptr;
@@ -562,7 +538,7 @@ Batch *get_batch(void **h)
 
 void free_batch(Batch &B)
 {
-    void *ptrs[] = {B.km32, B.km64, B.coord, B.ediag, B.ut, B.mat_e, B.mat_v, B.conn, B.list, B.nptr, B.fm, B.f, B.x, B.r,
+    void *ptrs[] = {B.km32p, B.kerr, B.emap, B.km64, B.coord, B.ediag, B.ut, B.mat_e, B.mat_v, B.conn, B.list, B.nptr, B.fm, B.f, B.x, B.r,
                     B.d, B.p, B.u, B.dinv, B.rres, B.part_s, B.part_u, B.part_i, B.scr, B.gp, B.st, B.d_segs,
                     B.d_blk_s, B.d_blk_v};
     for (void *q : ptrs)
@@ -614,6 +590,12 @@ int rebuild_tables(Batch &B)
         BCK(cudaMemcpy(B.d_segs, segs.data(), segs.size() * sizeof(BSeg), cudaMemcpyHostToDevice));
         BCK(cudaMemcpy(B.d_blk_s, bs.data(), bs.size() * sizeof(int), cudaMemcpyHostToDevice));
         BCK(cudaMemcpy(B.d_blk_v, bv.data(), bv.size() * sizeof(int), cudaMemcpyHostToDevice));
+        if (B.prec == 32) {
+            long long g = (cum + 255) / 256;
+            if (g > (long long)B.nsm * 8) g = (long long)B.nsm * 8;
+            k_bt_emap<<<(int)g, 256, 0, B.stream>>>(B.nseg, B.d_segs, cum, B.emap);
+            if (launched(B, "k_bt_emap")) return 1;
+        }
     }
     B.dirty = false;
     ++B.version;
@@ -694,9 +676,10 @@ int batch_iterations(Batch &B, int n)
     if (ge < 1) ge = 1;
     for (int i = 0; i < n; ++i) {
         if (B.prec == 32) {
-            k_bt_elem32<<<(int)ge, 256, 0, B.stream>>>(B.nseg, B.d_segs, B.total_el, B.km32, B.conn, B.p,
-                                                       (float *)B.ut, B.st);
-            if (launched(B, "k_bt_elem32")) return 1;
+            if (launch_elem_sym32_mapped(B.stream, B.nsm, (int)B.total_el, B.km32p, B.conn, B.p, (float *)B.ut,
+                                         B.kerr, B.emap))
+                return 1;
+            B.launches++;
             k_bt_scatter<float><<<B.nblk_s, 256, 0, B.stream>>>(B.d_blk_s, B.d_segs, B.nptr, B.list,
                                                                 (const float *)B.ut, B.fm, B.p, B.u, B.part_s,
                                                                 B.st);
@@ -788,10 +771,11 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
     cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, B->device);
     if (B->nsm < 1) B->nsm = 1;
     B->max_meshes = *max_meshes;
-    // bytes per element slot: storkm 28800, coord 480, conn 80, element diag 480,
-    // results 480, node list 80, material 16; nodes: 7 per element slot at
+    // bytes per element slot: storkm 28800 (+ packed FP32 7328 and the element
+    // map 4 for prec 32), coord 480, conn 80, element diag 480, results 480,
+    // node list 80, material 16; nodes: 7 per element slot at
     // 8 (ptr) + 1 (mask) + 8 vectors x 24 bytes
-    const long long per_el = 28800 + (B->prec == 32 ? 14400 : 0) + 480 + 80 + 480 + 480 + 80 + 16 +
+    const long long per_el = 28800 + (B->prec == 32 ? 7328 + 4 : 0) + 480 + 80 + 480 + 480 + 80 + 16 +
                              7 * (8 + 1 + 8 * 24);
     B->cap_el = *budget_bytes / per_el;
     if (B->cap_el > 0x7fffffffLL / 60) B->cap_el = 0x7fffffffLL / 60;
@@ -804,7 +788,11 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
         if (ok && cudaMalloc(ptr, bytes ? bytes : 1) != cudaSuccess) ok = false;
     };
     al((void **)&B->km64, E * 3600 * 8);
-    if (B->prec == 32) al((void **)&B->km32, E * 3600 * 4);
+    if (B->prec == 32) {
+        al((void **)&B->km32p, E * 1832 * 4);
+        al((void **)&B->emap, E * 4);
+    }
+    al((void **)&B->kerr, 4);
     al((void **)&B->coord, E * 60 * 8);
     al((void **)&B->ediag, E * 60 * 8);
     al((void **)&B->ut, E * 60 * 8);
@@ -834,7 +822,13 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
         return PF_FAILURE;
     }
     cudaMemset(B->st, 0, (size_t)B->max_meshes * sizeof(PcgState));
+    cudaMemset(B->kerr, 0, sizeof(int));
     memset(B->hst, 0, (size_t)B->max_meshes * sizeof(PcgState));
+    if (B->prec == 32 && sym32_prepare()) {
+        free_batch(*B);
+        delete B;
+        return PF_FAILURE;
+    }
     B->el_free.init(B->cap_el);
     B->node_free.init(B->cap_nodes);
     for (int i = B->max_meshes - 1; i >= 0; --i) B->sid_free.push_back(i);
@@ -1022,11 +1016,15 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
         B.gp_nip = nip;
     }
     if (launch_form_storkm_raw(B.stream, B.nsm, nels, nip, B.gp, B.coord + (size_t)el0 * 60, B.mat_e + el0,
-                               B.mat_v + el0, nmat, B.km64 + (size_t)el0 * 3600,
-                               B.km32 ? B.km32 + (size_t)el0 * 3600 : nullptr,
+                               B.mat_v + el0, nmat, B.km64 + (size_t)el0 * 3600, nullptr,
                                B.ediag + (size_t)el0 * 60))
         return PF_FAILURE;
     B.launches++;
+    if (B.km32p) {
+        if (launch_pack_sym32_raw(B.stream, B.nsm, nels, B.km64 + (size_t)el0 * 3600, B.km32p + (size_t)el0 * 1832))
+            return PF_FAILURE;
+        B.launches++;
+    }
     k_bt_diag<<<(nn + 255) / 256, 256, 0, B.stream>>>(S, B.nptr, B.list, B.ediag, B.fm, B.dinv);
     if (launched(B, "k_bt_diag")) return PF_FAILURE;
     k_bt_init1<<<q.nbv, 256, 0, B.stream>>>(S, B.f, B.dinv, B.x, B.r, B.d, B.p, B.part_i, B.capb_v);
@@ -1063,7 +1061,14 @@ extern "C" int pf_batch_sync(void **batch, int *n_active, int *n_done)
     if (!Bp) return PF_FAILURE;
     Batch &B = *Bp;
     BCK(cudaMemcpyAsync(B.hst, B.st, (size_t)B.max_meshes * sizeof(PcgState), cudaMemcpyDeviceToHost, B.stream));
+    int kerr = 0;
+    BCK(cudaMemcpyAsync(&kerr, B.kerr, sizeof(int), cudaMemcpyDeviceToHost, B.stream));
     BCK(cudaStreamSynchronize(B.stream));
+    if (kerr) {
+        cudaMemsetAsync(B.kerr, 0, sizeof(int), B.stream);
+        set_error("pf_batch_sync: a shared-memory bulk-copy wait of the element kernel timed out");
+        return PF_FAILURE;
+    }
     std::vector<int> fin;
     for (int id : B.order)
         if (B.hst[B.active[id].sid].stop) fin.push_back(id);

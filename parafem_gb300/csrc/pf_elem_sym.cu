@@ -59,7 +59,7 @@ template <int kWarps, int kStages>
 __global__ void __launch_bounds__(kWarps * 32, 1)
 k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ conn,
              const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
-             int *__restrict__ err)
+             int *__restrict__ err, const int *__restrict__ emap)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -83,7 +83,9 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
     const int first = e0 + w;
     if (first >= e1) return;
     const int nmine = (e1 - first + kWarps - 1) / kWarps;   // elements of this warp
-    auto elem = [&](int k) { return first + k * kWarps; };
+    // the k-th element of this warp; emap (serving batches) maps the
+    // position among the active elements to the arena element
+    auto elem = [&](int k) { const int g = first + k * kWarps; return emap ? __ldg(emap + g) : g; };
 
     if (lane == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
@@ -196,7 +198,8 @@ static int launch_sym_cfg(Ctx &c, const double *p, const PcgState *st)
         c.sym_attr |= bit;
     }
     const int grid = c.nels < c.nsm * W ? (c.nels + W - 1) / W : c.nsm;
-    k_elem_sym32<W, S><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km32p, c.conn, p, (float *)c.utemp, st, c.kerr);
+    k_elem_sym32<W, S><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km32p, c.conn, p, (float *)c.utemp, st, c.kerr,
+                                                         nullptr);
     c.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -217,6 +220,47 @@ static int launch_sym_index(Ctx &c, int idx, const double *p, const PcgState *st
     case 2: return launch_sym_cfg<8, 3>(c, p, st);
     default: return launch_sym_cfg<14, 2>(c, p, st);
     }
+}
+
+// The serving engine's entry points: the (14, 2) configuration over n
+// active elements mapped to arena elements by emap.  sym32_prepare sets the
+// shared-memory attribute; call it once per device before any stream capture.
+int sym32_prepare()
+{
+    constexpr size_t smem = sym_smem_bytes<14, 2>();
+    const cudaError_t e = cudaFuncSetAttribute(k_elem_sym32<14, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+    if (e != cudaSuccess) {
+        set_error("k_elem_sym32: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+int launch_elem_sym32_mapped(cudaStream_t stream, int nsm, int n, const float *kp, const int *conn, const double *p,
+                             float *ut, int *err, const int *emap)
+{
+    if (n <= 0) return 0;
+    constexpr int W = 14;
+    const int grid = n < nsm * W ? (n + W - 1) / W : nsm;
+    k_elem_sym32<W, 2><<<grid, W * 32, sym_smem_bytes<W, 2>(), stream>>>(n, kp, conn, p, ut, nullptr, err, emap);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("k_elem_sym32: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+int launch_pack_sym32_raw(cudaStream_t stream, int nsm, int nels, const double *km, float *kp)
+{
+    k_pack_sym32<<<nsm * 8, 256, 0, stream>>>(nels, km, kp);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("k_pack_sym32: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
 }
 
 int launch_pack_sym32(Ctx &c)

@@ -479,6 +479,8 @@ extern "C" int pf_random_material(const int *nels, const long long *seed, const 
 }
 
 // ---------------------------------------------------------------------------
+static int p12meshgen_p123(const std::string &job, const std::vector<std::string> &t);
+
 extern "C" int pf_p12meshgen(const char *job_c)
 {
     if (!job_c) { set_error("pf_p12meshgen: null job name"); return PF_FAILURE; }
@@ -488,8 +490,9 @@ extern "C" int pf_p12meshgen(const char *job_c)
         set_error("cannot read %s.mg", job.c_str());
         return PF_FAILURE;
     }
+    if (t[0] == "p123") return p12meshgen_p123(job, t);
     if (t[0] != "p121") {
-        set_error("%s.mg: only the p121 case is supported (got %s)", job.c_str(), t[0].c_str());
+        set_error("%s.mg: the p121 and p123 cases are supported (got %s)", job.c_str(), t[0].c_str());
         return PF_FAILURE;
     }
     const std::string iotype = t[1];
@@ -662,5 +665,403 @@ extern "C" int pf_p121_run(const char *job_c, const int *device, const int *mode
     fclose(fr);
     if (iters_out) *iters_out = iters;
     if (central_out) *central_out = neq > 0 ? x[0] : 0.0;
+    return PF_SUCCESS;
+}
+
+// ===========================================================================
+// p123: 3-D Laplace with 8-node bricks (src/programs/5th_ed/p123/p123.f90).
+namespace {
+
+// Nodes (Smith-Griffiths order) and coordinates coord(8,3) of element iel
+// (1-based) of an nxe x nye x nze box of bricks numbered in x-z planes
+// marching in y (GEOMETRY_8BXZ, src/modules/shared/geometry.f90:70-166).
+void box8_element(int iel, int nxe, int nze, double aa, double bb, double cc, int num[8], double co[24])
+{
+    const int per_plane = nxe * nze;
+    const int iq = (iel - 1) / per_plane;          // y layer (0-based)
+    const int in = (iel - 1) % per_plane;
+    const int is = in / nxe;                       // z row from the top (0-based)
+    const int ip = in % nxe;                       // x column (0-based)
+    const long long plane = (long long)(nxe + 1) * (nze + 1);
+    // node (x column cx, z level lz from the top, y plane py), 1-based
+    auto node = [&](int cx, int lz, int py) { return (int)(py * plane + (long long)lz * (nxe + 1) + cx + 1); };
+    // corner signs of the Smith-Griffiths brick: (x: 0 left / 1 right, z: 0 bottom / 1 top, y: 0 front / 1 back)
+    static const int sx[8] = {0, 0, 1, 1, 0, 0, 1, 1}, sz[8] = {0, 1, 1, 0, 0, 1, 1, 0},
+                     sy[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+    for (int a = 0; a < 8; ++a) {
+        const int lz = is + 1 - sz[a];             // top of the element is level is, bottom is + 1
+        num[a] = node(ip + sx[a], lz, iq + sy[a]);
+        co[a] = (ip + sx[a]) * aa;
+        co[a + 8] = (iq + sy[a]) * bb;
+        co[a + 16] = -(double)lz * cc;
+    }
+}
+
+// box_bc8 (src/modules/shared/geometry.f90:655-696): node_fix[n] = 1 for a
+// free node, 0 for a restrained one.  Restrained: in every x-z plane but
+// the last, the last x column (x = nxe*aa) and the top level (z = 0); the
+// whole last plane.
+void box8_fix(int nxe, int nye, int nze, std::vector<int> &fix)
+{
+    const long long plane = (long long)(nxe + 1) * (nze + 1);
+    fix.assign((size_t)plane * (nye + 1), 1);
+    for (long long py = 0; py <= nye; ++py)
+        for (long long k = 0; k < plane; ++k) {
+            const long long lz = k / (nxe + 1), cx = k % (nxe + 1);
+            if (py == nye || cx == nxe || lz == 0) fix[(size_t)(py * plane + k)] = 0;
+        }
+}
+
+struct Deck8 {
+    int meshgen = 0, partitioner = 0, nels = 0, nn = 0, nr = 0, nip = 0, nod = 0, loaded = 0, fixed = 0;
+    int limit = 0, nres = 0;
+    double kx = 0, ky = 0, kz = 0, tol = 0;
+    std::vector<double> coords;   // (3, nn)
+    std::vector<int> g_num;       // (8, nels), Smith-Griffiths order
+    std::vector<int> rest;        // (2, nr): node, flag
+    std::vector<int> lno;         // loaded freedoms (used as equation numbers, p123.f90:98-103)
+    std::vector<double> lval;
+    std::vector<int> fnode, fsense;
+    std::vector<double> fval;
+};
+
+int read_deck8(const std::string &job, Deck8 &D)
+{
+    std::vector<std::string> t;
+    if (!read_tokens(job + ".dat", t) || t.size() < 16) {
+        set_error("cannot read %s.dat", job.c_str());
+        return 1;
+    }
+    // READ_P123 (src/modules/mpi/input.f90:3620-3806): element, mesh, partition,
+    // nels, nn, nr, nip, nod, loaded, fixed, kx, ky, kz, tol, limit, nres
+    D.meshgen = atoi(t[1].c_str());
+    D.partitioner = atoi(t[2].c_str());
+    D.nels = atoi(t[3].c_str());
+    D.nn = atoi(t[4].c_str());
+    D.nr = atoi(t[5].c_str());
+    D.nip = atoi(t[6].c_str());
+    D.nod = atoi(t[7].c_str());
+    D.loaded = atoi(t[8].c_str());
+    D.fixed = atoi(t[9].c_str());
+    D.kx = to_d(t[10]);
+    D.ky = to_d(t[11]);
+    D.kz = to_d(t[12]);
+    D.tol = to_d(t[13]);
+    D.limit = atoi(t[14].c_str());
+    D.nres = atoi(t[15].c_str());
+    if (t[0] != "hexahedron" || D.nod != 8 || D.nels < 1 || D.nn < 1) {
+        set_error("%s.dat: p123 decks of 8-node hexahedra only (got %s, nod=%d)", job.c_str(), t[0].c_str(), D.nod);
+        return 1;
+    }
+    std::ifstream f(job + ".d");
+    if (!f) {
+        set_error("cannot read %s.d", job.c_str());
+        return 1;
+    }
+    std::string line;
+    std::getline(f, line);
+    std::getline(f, line);
+    D.coords.assign((size_t)3 * D.nn, 0.0);
+    for (int i = 0; i < D.nn; ++i) {
+        if (!std::getline(f, line)) { set_error("%s.d: short node list", job.c_str()); return 1; }
+        std::istringstream ss(line);
+        std::string id, a, b, c;
+        ss >> id >> a >> b >> c;
+        D.coords[3 * (size_t)i] = to_d(a);
+        D.coords[3 * (size_t)i + 1] = to_d(b);
+        D.coords[3 * (size_t)i + 2] = to_d(c);
+    }
+    std::getline(f, line);   // *ELEMENTS
+    D.g_num.assign((size_t)8 * D.nels, 0);
+    for (int e = 0; e < D.nels; ++e) {
+        if (!std::getline(f, line)) { set_error("%s.d: short element list", job.c_str()); return 1; }
+        std::istringstream ss(line);
+        long long k;
+        ss >> k >> k >> k >> k;
+        for (int a = 0; a < 8; ++a) ss >> D.g_num[8 * (size_t)e + a];
+        if (!ss) { set_error("%s.d: bad element line %d", job.c_str(), e + 1); return 1; }
+    }
+    if (D.meshgen == 2) {   // ABAQUS2SG, 8-node (new_library.f90:3604-3618)
+        static const int from[8] = {1, 5, 6, 2, 4, 8, 7, 3};
+        int tmp[8];
+        for (int e = 0; e < D.nels; ++e) {
+            int *g = &D.g_num[8 * (size_t)e];
+            std::copy(g, g + 8, tmp);
+            for (int a = 0; a < 8; ++a) g[a] = tmp[from[a] - 1];
+        }
+    }
+    std::vector<std::string> tb;
+    if (!read_tokens(job + ".bnd", tb) || tb.size() < (size_t)2 * D.nr) {
+        set_error("cannot read %d restraints from %s.bnd", D.nr, job.c_str());
+        return 1;
+    }
+    D.rest.resize((size_t)2 * D.nr);
+    for (size_t i = 0; i < (size_t)2 * D.nr; ++i) D.rest[i] = atoi(tb[i].c_str());
+    if (D.loaded > 0) {   // READ_LOADS (input.f90:2350-2411), one value per freedom
+        std::vector<std::string> tl;
+        if (!read_tokens(job + ".lds", tl) || tl.size() < (size_t)2 * D.loaded) {
+            set_error("cannot read %d loads from %s.lds", D.loaded, job.c_str());
+            return 1;
+        }
+        for (int i = 0; i < D.loaded; ++i) {
+            D.lno.push_back(atoi(tl[2 * (size_t)i].c_str()));
+            D.lval.push_back(to_d(tl[2 * (size_t)i + 1]));
+        }
+    }
+    if (D.fixed > 0) {   // READ_FIXED (input.f90:2483-2564): node, sense, value
+        std::vector<std::string> tf;
+        if (!read_tokens(job + ".fix", tf) || tf.size() < (size_t)3 * D.fixed) {
+            set_error("cannot read %d fixed freedoms (node sense value) from %s.fix", D.fixed, job.c_str());
+            return 1;
+        }
+        for (int i = 0; i < D.fixed; ++i) {
+            D.fnode.push_back(atoi(tf[3 * (size_t)i].c_str()));
+            D.fsense.push_back(atoi(tf[3 * (size_t)i + 1].c_str()));
+            D.fval.push_back(to_d(tf[3 * (size_t)i + 2]));
+        }
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" int pf_mesh_box8(const int *nxe, const int *nye, const int *nze, const double *aa, const double *bb,
+                            const double *cc, int *g_num, double *g_coord)
+{
+    if (!nxe || !nye || !nze || !aa || !bb || !cc || !g_num || !g_coord || *nxe < 1 || *nye < 1 || *nze < 1) {
+        set_error("pf_mesh_box8: invalid arguments");
+        return PF_FAILURE;
+    }
+    const long long nels = (long long)*nxe * *nye * *nze;
+    for (long long iel = 1; iel <= nels; ++iel)
+        box8_element((int)iel, *nxe, *nze, *aa, *bb, *cc, g_num + 8 * (iel - 1), g_coord + 24 * (iel - 1));
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_box8_restraints(const int *nxe, const int *nye, const int *nze, int *node_fix)
+{
+    if (!nxe || !nye || !nze || !node_fix || *nxe < 1 || *nye < 1 || *nze < 1) {
+        set_error("pf_box8_restraints: invalid arguments");
+        return PF_FAILURE;
+    }
+    std::vector<int> fix;
+    box8_fix(*nxe, *nye, *nze, fix);
+    std::copy(fix.begin(), fix.end(), node_fix);
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_number_equations1(const int *nels, const int *nn, const int *nod, const int *g_num,
+                                    const int *node_fix, int *g_g, int *neq)
+{
+    if (!nels || !nn || !nod || !g_num || !node_fix || !g_g || !neq || *nels < 0 || *nn < 1 || *nod < 1) {
+        set_error("pf_number_equations1: invalid arguments");
+        return PF_FAILURE;
+    }
+    // equation of a free node = free nodes up to it (rearrange_2 + find_g4,
+    // new_library.f90:3118-3124, 3249-3271, for a restraint list sorted by node)
+    std::vector<int> eq((size_t)*nn, 0);
+    int q = 0;
+    for (int n = 0; n < *nn; ++n)
+        if (node_fix[n]) eq[n] = ++q;
+    for (size_t k = 0; k < (size_t)*nels * *nod; ++k) {
+        const int nd = g_num[k];
+        if (nd < 1 || nd > *nn) {
+            set_error("pf_number_equations1: node %d outside 1..%d", nd, *nn);
+            return PF_FAILURE;
+        }
+        g_g[k] = eq[nd - 1];
+    }
+    *neq = q;
+    return PF_SUCCESS;
+}
+
+// p12meshgen's p123 case (src/tools/preprocessing/p12meshgen/p12meshgen.f90:
+// 658-801).  The .fix file is written as READ_FIXED reads it (node, sense,
+// value); the reference's generator writes node and value only.
+static int p12meshgen_p123(const std::string &job, const std::vector<std::string> &t)
+{
+    if (t.size() < 15) {
+        set_error("%s.mg: the p123 case needs 14 values", job.c_str());
+        return PF_FAILURE;
+    }
+    const std::string iotype = t[1];
+    const int nels = atoi(t[2].c_str()), nxe = atoi(t[3].c_str()), nze = atoi(t[4].c_str());
+    const int nip = atoi(t[5].c_str());
+    const double aa = to_d(t[6]), bb = to_d(t[7]), cc = to_d(t[8]), kx = to_d(t[9]), ky = to_d(t[10]),
+                 kz = to_d(t[11]), tol = to_d(t[12]);
+    const int limit = atoi(t[13].c_str()), loaded = atoi(t[14].c_str());
+    const int fixed = t.size() > 15 ? atoi(t[15].c_str()) : 0;
+    if (iotype != "parafem" || nxe < 1 || nze < 1 || nels % (nxe * nze) != 0) {
+        set_error("%s.mg: supported: 'parafem' decks (nels divisible by nxe*nze)", job.c_str());
+        return PF_FAILURE;
+    }
+    const int nye = nels / nxe / nze;
+    const long long nn = (long long)(nxe + 1) * (nye + 1) * (nze + 1);
+    const long long nr = (long long)(nxe + 1) * (nye + 1) + (long long)(nxe + 1) * nze + (long long)nye * nze;
+    const int nres = nxe * (nze - 1) + 1;
+    std::vector<double> gc((size_t)3 * nn, 0.0);
+    std::vector<int> gnum((size_t)8 * nels);
+    for (int iel = 1; iel <= nels; ++iel) {
+        double co[24];
+        int *num = &gnum[8 * (size_t)(iel - 1)];
+        box8_element(iel, nxe, nze, aa, bb, cc, num, co);
+        for (int a = 0; a < 8; ++a)
+            for (int d = 0; d < 3; ++d) gc[3 * (size_t)(num[a] - 1) + d] = co[a + 8 * d];
+    }
+    FILE *fd = fopen((job + ".d").c_str(), "w");
+    if (!fd) { set_error("cannot write %s.d", job.c_str()); return PF_FAILURE; }
+    fprintf(fd, "*THREE_DIMENSIONAL\n*NODES\n");
+    for (long long i = 0; i < nn; ++i)
+        fprintf(fd, "%s%s%s%s\n", fmt_I(i + 1, 12).c_str(), fmt_E(gc[3 * i], 14, 6).c_str(),
+                fmt_E(gc[3 * i + 1], 14, 6).c_str(), fmt_E(gc[3 * i + 2], 14, 6).c_str());
+    fprintf(fd, "*ELEMENTS\n");
+    static const int abq[8] = {1, 4, 8, 5, 2, 3, 7, 6};   // Abaqus order of the written nodes
+    for (int iel = 0; iel < nels; ++iel) {
+        std::string s = fmt_I(iel + 1, 12) + " 3 8 1 ";
+        for (int a = 0; a < 8; ++a) s += fmt_I(gnum[8 * (size_t)iel + abq[a] - 1], 10);
+        fprintf(fd, "%s 1\n", s.c_str());
+    }
+    fclose(fd);
+    std::vector<int> fix;
+    box8_fix(nxe, nye, nze, fix);
+    FILE *fb = fopen((job + ".bnd").c_str(), "w");
+    if (!fb) { set_error("cannot write %s.bnd", job.c_str()); return PF_FAILURE; }
+    long long written = 0;
+    for (long long i = 0; i < nn; ++i)
+        if (!fix[(size_t)i]) {
+            fprintf(fb, "%s%s\n", fmt_I(i + 1, 8).c_str(), fmt_I(0, 6).c_str());
+            ++written;
+        }
+    fclose(fb);
+    if (written != nr) {
+        set_error("p12meshgen p123: %lld restrained nodes, expected %lld", written, nr);
+        return PF_FAILURE;
+    }
+    if (loaded > 0) {
+        FILE *fl = fopen((job + ".lds").c_str(), "w");
+        if (!fl) { set_error("cannot write %s.lds", job.c_str()); return PF_FAILURE; }
+        for (int i = 0; i < loaded; ++i) fprintf(fl, "%s%s\n", fmt_I(nres, 10).c_str(), fmt_E(10.0, 16, 8).c_str());
+        fclose(fl);
+    }
+    if (fixed > 0) {
+        FILE *ff = fopen((job + ".fix").c_str(), "w");
+        if (!ff) { set_error("cannot write %s.fix", job.c_str()); return PF_FAILURE; }
+        for (int i = 0; i < fixed; ++i)
+            fprintf(ff, "%s%s%s\n", fmt_I(nres, 10).c_str(), fmt_I(1, 6).c_str(), fmt_E(100.0, 16, 8).c_str());
+        fclose(ff);
+    }
+    FILE *ft = fopen((job + ".dat").c_str(), "w");
+    if (!ft) { set_error("cannot write %s.dat", job.c_str()); return PF_FAILURE; }
+    fprintf(ft, "'hexahedron'\n2\n1\n%s%s%s%s%s%s%s\n", fmt_I(nels, 12).c_str(), fmt_I(nn, 12).c_str(),
+            fmt_I(nr, 12).c_str(), fmt_I(nip, 6).c_str(), fmt_I(8, 6).c_str(), fmt_I(loaded, 6).c_str(),
+            fmt_I(fixed, 6).c_str());
+    fprintf(ft, "%s%s%s%s%s%s\n", fmt_E(kx, 12, 4).c_str(), fmt_E(ky, 12, 4).c_str(), fmt_E(kz, 12, 4).c_str(),
+            fmt_E(tol, 12, 4).c_str(), fmt_I(limit, 8).c_str(), fmt_I(nres, 8).c_str());
+    fclose(ft);
+    return PF_SUCCESS;
+}
+
+// The p123 job (p123.f90:1-182) with the solve on the GPU.
+extern "C" int pf_p123_run(const char *job_c, const int *device, int *iters_out, double *potentials_out)
+{
+    if (!job_c || !device) { set_error("pf_p123_run: null argument"); return PF_FAILURE; }
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto secs = [&](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    const std::string job(job_c);
+    Deck8 D;
+    if (read_deck8(job, D)) return PF_FAILURE;
+    std::vector<int> fix((size_t)D.nn, 1);
+    int last = 0;
+    for (int i = 0; i < D.nr; ++i) {
+        const int nd = D.rest[2 * (size_t)i];
+        if (nd < 1 || nd > D.nn || nd <= last) {
+            set_error("%s.bnd: restraint row %d (node %d) out of range or not sorted", job.c_str(), i + 1, nd);
+            return PF_FAILURE;
+        }
+        last = nd;
+        fix[(size_t)nd - 1] = D.rest[2 * (size_t)i + 1] != 0 ? 1 : 0;
+    }
+    std::vector<int> g_g((size_t)8 * D.nels);
+    int neq = 0, nod = 8;
+    if (pf_number_equations1(&D.nels, &D.nn, &nod, D.g_num.data(), fix.data(), g_g.data(), &neq)) return PF_FAILURE;
+    std::vector<double> gcoord((size_t)24 * D.nels);
+    for (size_t e = 0; e < (size_t)D.nels; ++e)
+        for (int a = 0; a < 8; ++a)
+            for (int d = 0; d < 3; ++d)
+                gcoord[24 * e + a + 8 * d] = D.coords[3 * (size_t)(D.g_num[8 * e + a] - 1) + d];
+    void *ctx = nullptr;
+    int rc = PF_FAILURE;
+    std::vector<double> r(neq > 0 ? neq : 1, 0.0), x(neq > 0 ? neq : 1, 0.0), dg(neq > 0 ? neq : 1, 0.0);
+    double q = 0.0, relres = 0.0, t_setup = 0, t_solve = 0;
+    int iters = 0, mode = PF_MODE_P121;
+    do {
+        if (pf_ctx_create(device, &ctx)) break;
+        if (pf_setup_scalar8(&ctx, &D.nels, &D.nn, &neq, D.g_num.data(), g_g.data(), gcoord.data())) break;
+        if (pf_form_storkc(&ctx, &D.nip, &D.kx, &D.ky, &D.kz)) break;
+        // loads: the listed numbers are equations (p123.f90:98-103)
+        bool bad = false;
+        for (int i = 0; i < D.loaded; ++i) {
+            if (D.lno[i] < 1 || D.lno[i] > neq) { bad = true; break; }
+            r[D.lno[i] - 1] = D.lval[i];
+        }
+        if (bad) { set_error("%s.lds: a loaded freedom is outside 1..%d", job.c_str(), neq); break; }
+        for (int i = 0; i < neq; ++i) q += r[i];
+        // fixed freedoms by the penalty method (p123.f90:104-118; FIND_NO2, loading.f90:742-828)
+        std::vector<int> feq;
+        for (int i = 0; i < D.fixed; ++i) {
+            const int nd = D.fnode[i];
+            if (nd < 1 || nd > D.nn || D.fsense[i] != 1 || !fix[(size_t)nd - 1]) { bad = true; break; }
+            int e = 0;
+            for (int n = 0; n < nd; ++n) e += fix[(size_t)n];
+            feq.push_back(e);
+        }
+        if (bad) { set_error("%s.fix: a fixed freedom is not a free node with sense 1", job.c_str()); break; }
+        const double penalty = 1.0e20;
+        int nfix = (int)feq.size();
+        if (pf_set_fixed(&ctx, &nfix, feq.data(), &penalty)) break;
+        if (nfix > 0) {
+            if (pf_get_diag(&ctx, dg.data())) break;
+            for (int i = 0; i < nfix; ++i) r[feq[i] - 1] = dg[feq[i] - 1] * D.fval[i];
+        }
+        t_setup = secs(t0);
+        const auto ts = clk::now();
+        if (pf_solve(&ctx, r.data(), &D.tol, &D.limit, &mode, x.data(), &iters, &relres)) break;
+        t_solve = secs(ts);
+        rc = PF_SUCCESS;
+    } while (0);
+    if (ctx) pf_ctx_destroy(&ctx);
+    if (rc) return PF_FAILURE;
+
+    FILE *fr = fopen((job + ".res").c_str(), "w");
+    if (!fr) { set_error("cannot write %s.res", job.c_str()); return PF_FAILURE; }
+    fprintf(fr, "This job ran on %s  processes\n", fmt_I(1, 5).c_str());
+    fprintf(fr, "There are %s nodes%s restrained and   %s equations\n", fmt_I(D.nn, 12).c_str(),
+            fmt_I(D.nr, 12).c_str(), fmt_I(neq, 12).c_str());
+    fprintf(fr, "Time after setup is %s\n", fmt_F(t_setup, 10, 4).c_str());
+    fprintf(fr, "The number of iterations to convergence was %s\n", fmt_I(iters, 5).c_str());
+    fprintf(fr, "The total load is %s\n", fmt_E(q, 12, 4).c_str());
+    fprintf(fr, "The potentials are:\n Freedom       Potential\n");
+    for (int i = 0; i < 4; ++i) {
+        const int fq = D.nres + i;
+        const double v = (fq >= 1 && fq <= neq) ? x[fq - 1] : 0.0;
+        fprintf(fr, "%s     %s\n", fmt_I(fq, 8).c_str(), fmt_E(v, 12, 4).c_str());
+        if (potentials_out) potentials_out[i] = v;
+    }
+    fprintf(fr, "Integration, preconditioning and loading took %s\n", fmt_F(t_setup, 10, 4).c_str());
+    fprintf(fr, "Time spent in the solver was %s\n", fmt_F(t_solve, 10, 4).c_str());
+    // Ensight Gold per-node scalar file (p123.f90:160-173)
+    FILE *fe = fopen((job + ".ensi.NDPTL-000001").c_str(), "w");
+    if (!fe) { fclose(fr); set_error("cannot write the potential file"); return PF_FAILURE; }
+    fprintf(fe, "Alya Ensight Gold --- Scalar per-node variable file\npart\n    1\ncoordinates\n");
+    int e = 0;
+    for (int nd = 0; nd < D.nn; ++nd) {
+        const int eq = fix[(size_t)nd] ? ++e : 0;
+        fprintf(fe, "%s\n", fmt_E(eq > 0 ? x[eq - 1] : 0.0, 12, 5).c_str());
+    }
+    fclose(fe);
+    fprintf(fr, "This analysis took %s\n", fmt_F(secs(t0), 10, 4).c_str());
+    fclose(fr);
+    if (iters_out) *iters_out = iters;
     return PF_SUCCESS;
 }

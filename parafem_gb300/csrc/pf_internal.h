@@ -28,6 +28,7 @@ struct PcgState {
 };
 
 enum { STOP_CHECON = 0, STOP_RELRES = 1 };
+enum { KIND_SOLID20 = 0, KIND_SCALAR8 = 1 };   // 20-node elasticity (p121), 8-node scalar (p123)
 
 struct Ctx {
     int device = 0;
@@ -70,6 +71,8 @@ struct Ctx {
     double *it_xsol = nullptr;
     long long it_launches = 0;  // kernels in one replay
     bool use_graphs = true;
+    int kind = 0;               // KIND_SOLID20 (p121) or KIND_SCALAR8 (p123)
+    double *fstore = nullptr;   // [nn] KIND_SCALAR8: penalty store of fixed freedoms, 0 = free
     // one element matrix shared by every element (PCG_KM); per-element storkm unused
     bool shared = false;
     double *skm64 = nullptr;    // [3600] column-major
@@ -120,14 +123,24 @@ int launch_pcg_iteration(Ctx &c, int prec, double *xsol);
 int launch_axpy(Ctx &c, double *y, const double *xv);          // y += x
 int launch_replace(Ctx &c, double tol);   // r = rres, d = diag*r, up = r.d; p kept
 int launch_sum_partials(Ctx &c, int nvals, double *out_dev);   // out[0] = sum of part_s
-int launch_centroid_stress(Ctx &c, int iel, const double *xslot, double *sig_dev);
+int launch_centroid_stress(Ctx &c, int e0, int count, const double *xslot, double *sig_dev);
 // prec codes of the element products: 64 FP64 storkm, 32 packed-symmetric
 // FP32 storkm (bulk-copy staged), 31 full FP32 storkm
 enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31 };
 int launch_pack_sym32(Ctx &c);
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);
+int sym32_prepare();   // shared-memory attribute of the mapped launch (once per device, outside capture)
+int launch_elem_sym32_mapped(cudaStream_t stream, int nsm, int n, const float *kp, const int *conn, const double *p,
+                             float *ut, int *err, const int *emap);
+int launch_pack_sym32_raw(cudaStream_t stream, int nsm, int nels, const double *km, float *kp);
 int autotune_sym32(Ctx &c, const double *p);   // picks c.sym_cfg by timing on this mesh
 int launch_elem_shared(Ctx &c, int prec, const double *p, const PcgState *st);   // shared km
+// 8-node scalar (p123) kernels; km64 holds storkc(8,8,e) in such a context
+int launch_form_storkc(Ctx &c, int nip, double kx, double ky, double kz);
+int launch_elem8(Ctx &c, const double *p, const PcgState *st);
+int launch_scatter1(Ctx &c, int mode, const double *xin, const double *pf, double *out, const PcgState *st);
+int launch_assemble_diag1(Ctx &c);
+int launch_set_fixed(Ctx &c, int nfix, const int *slots_dev, double penalty);
 int launch_shared_ediag(Ctx &c);
 void set_sym_config(Ctx &c, int idx);           // 0: 14 warps x 2 stages, 1: 12 x 2, 2: 8 x 3
 int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs,

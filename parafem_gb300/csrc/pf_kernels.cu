@@ -542,50 +542,56 @@ __global__ void k_axpy(int ns, double *__restrict__ y, const double *__restrict_
         y[s] += x[s];
 }
 
-// Centroid stress of one element (p121.f90:112-123): nip=1 at the origin.
-__global__ void k_centroid_stress(int e, const int *__restrict__ conn, const double *__restrict__ coord,
-                                  const double *__restrict__ me, const double *__restrict__ mv,
-                                  int nmat, const double *__restrict__ x, double *__restrict__ sig)
+// Centroid stresses (p121.f90:112-123: nip=1 at the origin) of elements
+// e0 .. e0+count-1, one thread per element; sig[6*k + c] for element e0+k.
+// The shape-function derivatives at the centroid are the same for every
+// element; the Jacobian, its inverse and the strains follow p121's order.
+__global__ void __launch_bounds__(128)
+k_centroid_stress(int e0, int count, const int *__restrict__ conn, const double *__restrict__ coord,
+                  const double *__restrict__ me, const double *__restrict__ mv, int nmat,
+                  const double *__restrict__ x, double *__restrict__ sig)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double der[60], jac[9], deriv[60], eld[60], eps[6];
-    const double *co = coord + (size_t)e * 60;
-    for (int l = 0; l < 20; ++l) shape_der20(l, 0.0, 0.0, 0.0, &der[3 * l]);
-    for (int a = 0; a < 3; ++a)
-        for (int b = 0; b < 3; ++b) {
-            double s = 0.0;
-            for (int k = 0; k < 20; ++k) s += der[a + 3 * k] * co[k + 20 * b];
-            jac[a + 3 * b] = s;
-        }
-    det_invert3(jac);
-    for (int l = 0; l < 20; ++l)
+    __shared__ double der[60];
+    if (threadIdx.x < 20) shape_der20(threadIdx.x, 0.0, 0.0, 0.0, &der[3 * threadIdx.x]);
+    __syncthreads();
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int e = e0 + k;
+        const double *co = coord + (size_t)e * 60;
+        double jac[9];
         for (int a = 0; a < 3; ++a)
-            deriv[a + 3 * l] = jac[a] * der[3 * l] + jac[a + 3] * der[1 + 3 * l] + jac[a + 6] * der[2 + 3 * l];
-    for (int l = 0; l < 20; ++l) {
-        const int nd = conn[(size_t)e * 20 + l];
-        for (int d = 0; d < 3; ++d) eld[3 * l + d] = x[(size_t)3 * nd + d];
+            for (int b = 0; b < 3; ++b) {
+                double s = 0.0;
+                for (int m = 0; m < 20; ++m) s += der[a + 3 * m] * co[m + 20 * b];
+                jac[a + 3 * b] = s;
+            }
+        det_invert3(jac);
+        // eps = bee . eld (BEEMAT rows ex, ey, ez, gxy, gyz, gzx), deriv = jac^-1 der
+        double eps[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int m = 0; m < 20; ++m) {
+            const double d0 = der[3 * m], d1 = der[3 * m + 1], d2 = der[3 * m + 2];
+            const double gx = jac[0] * d0 + jac[3] * d1 + jac[6] * d2;
+            const double gy = jac[1] * d0 + jac[4] * d1 + jac[7] * d2;
+            const double gz = jac[2] * d0 + jac[5] * d1 + jac[8] * d2;
+            const int nd = conn[(size_t)e * 20 + m];
+            const double ux = x[(size_t)3 * nd], uy = x[(size_t)3 * nd + 1], uz = x[(size_t)3 * nd + 2];
+            eps[0] += gx * ux;
+            eps[1] += gy * uy;
+            eps[2] += gz * uz;
+            eps[3] += gy * ux + gx * uy;
+            eps[4] += gz * uy + gy * uz;
+            eps[5] += gz * ux + gx * uz;
+        }
+        double d11, d12, d44;
+        const int mi = nmat == 1 ? 0 : e;
+        deemat3(me[mi], mv[mi], d11, d12, d44);
+        double *o = sig + (size_t)6 * k;
+        o[0] = d11 * eps[0] + d12 * eps[1] + d12 * eps[2];
+        o[1] = d12 * eps[0] + d11 * eps[1] + d12 * eps[2];
+        o[2] = d12 * eps[0] + d12 * eps[1] + d11 * eps[2];
+        o[3] = d44 * eps[3];
+        o[4] = d44 * eps[4];
+        o[5] = d44 * eps[5];
     }
-    // eps = bee . eld (BEEMAT rows ex, ey, ez, gxy, gyz, gzx)
-    for (int k = 0; k < 6; ++k) eps[k] = 0.0;
-    for (int m = 0; m < 20; ++m) {
-        const double gx = deriv[3 * m], gy = deriv[3 * m + 1], gz = deriv[3 * m + 2];
-        const double ux = eld[3 * m], uy = eld[3 * m + 1], uz = eld[3 * m + 2];
-        eps[0] += gx * ux;
-        eps[1] += gy * uy;
-        eps[2] += gz * uz;
-        eps[3] += gy * ux + gx * uy;
-        eps[4] += gz * uy + gy * uz;
-        eps[5] += gz * ux + gx * uz;
-    }
-    double d11, d12, d44;
-    const int mi = nmat == 1 ? 0 : e;
-    deemat3(me[mi], mv[mi], d11, d12, d44);
-    sig[0] = d11 * eps[0] + d12 * eps[1] + d12 * eps[2];
-    sig[1] = d12 * eps[0] + d11 * eps[1] + d12 * eps[2];
-    sig[2] = d12 * eps[0] + d12 * eps[1] + d11 * eps[2];
-    sig[3] = d44 * eps[3];
-    sig[4] = d44 * eps[4];
-    sig[5] = d44 * eps[5];
 }
 
 // Generic batched product of the xx3 layer (cuda_helpers.cu:144-177 semantics):
@@ -669,6 +675,7 @@ int launch_cast_km32(Ctx &c)
 
 int launch_assemble_diag(Ctx &c)
 {
+    if (c.kind == KIND_SCALAR8) return launch_assemble_diag1(c);
     k_assemble_diag<<<grid_for(c, c.nn, 256, 8), 256, 0, c.stream>>>(
         c.nn, c.node_ptr, c.node_list, c.ediag, c.freemask, c.diag, c.dinv);
     return check_launch(c, "k_assemble_diag");
@@ -688,6 +695,7 @@ int launch_slot_to_eq(Ctx &c, const double *slot, double *eq)
 
 int launch_elem(Ctx &c, int prec, const double *p)
 {
+    if (c.kind == KIND_SCALAR8) return launch_elem8(c, p, c.st);
     if (c.shared) return launch_elem_shared(c, prec, p, c.st);
     if (prec == PREC_FP32_SYM) return launch_elem_sym32(c, p, c.st);
     const int grid = grid_for(c, c.nels, 8, 8);
@@ -701,6 +709,7 @@ int launch_elem(Ctx &c, int prec, const double *p)
 
 int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
 {
+    if (c.kind == KIND_SCALAR8) return launch_scatter1(c, mode, pf, pf, out, mode == 0 ? c.st : nullptr);
     const PcgState *st = mode == 0 ? c.st : nullptr;
     if (prec != PREC_FP64) {
         if (mode == 0)
@@ -723,6 +732,10 @@ int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
 // u = K p outside a PCG run (state-independent).
 int launch_matvec(Ctx &c, int prec, const double *p, double *u)
 {
+    if (c.kind == KIND_SCALAR8) {
+        if (launch_elem8(c, p, nullptr)) return 1;
+        return launch_scatter1(c, 0, p, p, u, nullptr);
+    }
     const int grid = grid_for(c, c.nels, 8, 8);
     if (c.shared) {
         if (launch_elem_shared(c, prec, p, nullptr)) return 1;
@@ -746,6 +759,10 @@ int launch_matvec(Ctx &c, int prec, const double *p, double *u)
 
 int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
 {
+    if (c.kind == KIND_SCALAR8) {
+        if (launch_elem8(c, x, nullptr)) return 1;
+        return launch_scatter1(c, 1, x, f, rres, nullptr);
+    }
     const int grid = grid_for(c, c.nels, 8, 8);
     if (c.shared) {
         if (launch_elem_shared(c, PREC_FP64, x, nullptr)) return 1;
@@ -814,9 +831,11 @@ int launch_sum_partials(Ctx &c, int nvals, double *out_dev)
     return check_launch(c, "k_sum_partials");
 }
 
-int launch_centroid_stress(Ctx &c, int iel, const double *xslot, double *sig_dev)
+int launch_centroid_stress(Ctx &c, int e0, int count, const double *xslot, double *sig_dev)
 {
-    k_centroid_stress<<<1, 1, 0, c.stream>>>(iel, c.conn, c.coord, c.mat_e, c.mat_v, c.nmat, xslot, sig_dev);
+    const int grid = grid_for(c, count, 128, 8);
+    k_centroid_stress<<<grid, 128, 0, c.stream>>>(e0, count, c.conn, c.coord, c.mat_e, c.mat_v, c.nmat, xslot,
+                                                  sig_dev);
     return check_launch(c, "k_centroid_stress");
 }
 

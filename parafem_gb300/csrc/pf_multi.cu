@@ -48,31 +48,52 @@ constexpr int kBufB = 3 * kTermB;
 constexpr int kStK = 7328;                   // packed-symmetric FP32 K_e (1830 + 2 pad floats)
 constexpr int kStP = 20 * 3 * KR * 8;        // P of the 20 nodes: 20 x 384 B
 constexpr int kStage = kStK + kStP;          // 15008 B, a multiple of 16
-constexpr int kNst = 4;                      // operand stages in flight per CTA
-constexpr int kTcThreads = 256;
-constexpr int kOffB = 2 * kBufA;
-constexpr int kOffSt = kOffB + 2 * kBufB;
+constexpr int kNst = 4;                      // operand stages (bulk copies in flight)
+constexpr int kNTile = 3;                    // BF16 tile sets (A + B)
+constexpr int kNAcc = 4;                     // TMEM accumulators (16 columns each)
+constexpr int kBuildWarps = 16;              // warps 0-15 split K_e and P_e (one A task per thread)
+constexpr int kEpiWarp0 = 16;                // warps 16-17 read TMEM lanes 0..63 back
+constexpr int kProdWarp = 18;                // warp 18 issues the bulk copies
+constexpr int kMmaWarp = 19;                 // warp 19, lane 0 issues the MMAs
+constexpr int kTcThreads = 20 * 32;
+static_assert(kBuildWarps * 32 == 8 * 64, "one A task (row i, 8 K-values) per builder thread");
+constexpr int kOffB = kNTile * kBufA;
+constexpr int kOffSt = kOffB + kNTile * kBufB;
 constexpr int kOffAux = kOffSt + kNst * kStage;
-constexpr int kTcSmem = kOffAux + 128;
+constexpr int kTcSmem = kOffAux + 256;
 constexpr uint32_t kIdesc = idesc_bf16(128, 16);
 static_assert(kOffSt % 16 == 0 && kStage % 16 == 0 && kOffAux % 8 == 0, "bulk-copy alignment");
+static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
+static_assert(kEpiWarp0 % 4 == 0, "epilogue warps must reach TMEM lanes 0..63");
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
 }  // namespace
 
 // Block element products on the tensor cores: ut[e][i][j] = sum_c K_e(i,c) P(slot(c), j).
 //
-// One persistent CTA of 8 warps per SM walks the elements e = blockIdx.x +
-// t * gridDim.x.  Operands arrive by bulk copy (cp.async.bulk + mbarrier),
-// kNst elements ahead: the packed upper triangle of K_e (7,328 B) and the
-// 16-case P block of each of the element's 20 nodes (384 B each, contiguous
-// in the interleaved vector).  Per element the threads split K_e and P_e
-// into three BF16 terms each and write them into one of two tile sets;
-// thread 0 issues the six products of order <= 2^-16 (24 MMAs, M=128, N=16,
-// K=16) into one of two TMEM accumulators and commits them to an mbarrier;
-// while they run, warps 0-1 read back the previous element's accumulator.
-// Every wait is bounded: a wait that runs out sets the device error word to
-// 3, and the CTA waits (bounded) for its copies and MMAs in flight, frees
-// its TMEM and returns.
+// One persistent CTA of 20 warps per SM walks the elements e = blockIdx.x +
+// t * gridDim.x with warp-specialised roles linked by mbarriers:
+//   warp 18      bulk copies (cp.async.bulk) of the packed upper triangle of
+//                K_e (7,328 B) and of the 16-case P blocks of the element's
+//                20 nodes (384 B each, contiguous in the interleaved vector)
+//                into a ring of kNst stages;
+//   warps 0-15   split K_e and P_e into three BF16 terms each and write them
+//                into a ring of kNTile tile sets (one 8-value row segment of
+//                K_e per thread, its shared-memory offsets computed once);
+//   warp 19      one thread issues the six products of order <= 2^-16
+//                (24 MMAs, M=128, N=16, K=16) into a ring of kNAcc TMEM
+//                accumulators and commits them to mbarriers that free the
+//                tile set and fill the accumulator;
+//   warps 16-17  read the accumulators back (TMEM lanes 0..63) and store
+//                the 60 x 16 results.
+// Every wait is bounded.  A wait that runs out sets a shared failure flag
+// that every role checks before its next wait, writes 3 to the device error
+// word, and the CTA waits (bounded) for the copies and MMAs it has in flight
+// before it frees its TMEM and returns.
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ conn,
              const double *__restrict__ P, float *__restrict__ ut, int *__restrict__ err,
@@ -83,145 +104,169 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
     unsigned char *A = sm;
     unsigned char *B = sm + kOffB;
     unsigned char *stg = sm + kOffSt;
-    uint64_t *full = reinterpret_cast<uint64_t *>(sm + kOffAux);      // kNst
-    uint64_t *mbar = full + kNst;                                     // 2
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
-    int *s_fail = reinterpret_cast<int *>(tslot + 1);
+    uint64_t *st_full = reinterpret_cast<uint64_t *>(sm + kOffAux);
+    uint64_t *st_empty = st_full + kNst;
+    uint64_t *tl_full = st_empty + kNst;
+    uint64_t *tl_empty = tl_full + kNTile;
+    uint64_t *ac_full = tl_empty + kNTile;
+    uint64_t *ac_empty = ac_full + kNAcc;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(ac_empty + kNAcc);
+    volatile int *s_fail = reinterpret_cast<volatile int *>(tslot + 1);
+    int *s_count = reinterpret_cast<int *>(tslot + 2);   // [0] copies issued, [1] MMA groups committed
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nmine = blockIdx.x < nels ? (nels - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto elem = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
 
     for (int i = tid; i < kOffSt / 16; i += kTcThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
-    if (warp == 0) {
-        tmem_alloc(tslot, 32);
-    }
+    if (warp == 0) tmem_alloc(tslot, 64);
     if (tid == 0) {
-        for (int s = 0; s < kNst; ++s) mbar_init(&full[s], 1);
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int i = 0; i < kNst; ++i) {
+            mbar_init(&st_full[i], 1);
+            mbar_init(&st_empty[i], kBuildWarps);
+        }
+        for (int i = 0; i < kNTile; ++i) {
+            mbar_init(&tl_full[i], kBuildWarps);
+            mbar_init(&tl_empty[i], 1);
+        }
+        for (int i = 0; i < kNAcc; ++i) {
+            mbar_init(&ac_full[i], 1);
+            mbar_init(&ac_empty[i], 2);
+        }
         mbar_fence_init();
         *s_fail = 0;
+        s_count[0] = s_count[1] = 0;
     }
-    fence_proxy_async();   // zeroed tiles -> async proxy
+    fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-
-    // producer (warp 0): element t's operands into stage t % kNst
-    auto issue = [&](int t, int nd) {
-        const int s = t % kNst;
-        unsigned char *dst = stg + s * kStage;
-        if (lane == 0) mbar_expect_tx(&full[s], kStage);
-        __syncwarp();
-        if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &full[s]);
-        if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * nd * KR, 384, &full[s]);
+    // bounded wait that also gives up at once when another role has failed
+    auto wait = [&](uint64_t *bar, uint32_t parity) {
+        if (*s_fail) return false;
+        if (mbar_wait(bar, parity)) return true;
+        *s_fail = 1;
+        return false;
     };
-    int conn_next = 0;   // warp 0, lanes 0..19: node of the next element to issue
-    if (warp == 0) {
-        for (int t = 0; t < kNst && t < nmine; ++t) {
-            const int nd = lane < 20 ? conn[(size_t)elem(t) * 20 + lane] : 0;
-            issue(t, nd);
-        }
-        if (kNst < nmine && lane < 20) conn_next = conn[(size_t)elem(kNst) * 20 + lane];
-    }
 
-    uint32_t mphase[2] = {0, 0};
-    auto epilogue = [&](int e, int buf) {
-        if (warp < 2) {   // rows 0..63 live in TMEM lanes 0..63 (warps 0 and 1)
-            if (!mbar_wait(&mbar[buf], mphase[buf])) atomicOr(s_fail, 1);
+    if (warp == kProdWarp) {
+        int nd = lane < 20 && nmine > 0 ? conn[(size_t)elem(0) * 20 + lane] : 0;
+        int t = 0;
+        for (; t < nmine; ++t) {
+            const int s = t % kNst;
+            if (t >= kNst && !wait(&st_empty[s], (uint32_t)((t / kNst - 1) & 1))) break;
+            unsigned char *dst = stg + s * kStage;
+            if (lane == 0) mbar_expect_tx(&st_full[s], kStage);
+            __syncwarp();
+            if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &st_full[s]);
+            if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * nd * KR, 384, &st_full[s]);
+            if (t + 1 < nmine && lane < 20) nd = conn[(size_t)elem(t + 1) * 20 + lane];
+        }
+        if (lane == 0) s_count[0] = t;
+    } else if (warp < kBuildWarps) {
+        // this thread's A task: row i, K-values 8q..8q+7; K(i,k) = U(min, max)
+        // at T(max) + min, and entries outside 60 x 60 read the zero pad at 1830
+        const int i = tid & 63, q = tid >> 6;
+        int off[8];
+#pragma unroll
+        for (int g = 0; g < 8; ++g) {
+            const int k = 8 * q + g;
+            const int lo = i < k ? i : k, hi = i < k ? k : i;
+            off[g] = (i < 60 && k < 60) ? hi * (hi + 1) / 2 + lo : 1830;
+        }
+        const uint32_t a_off = kmajor_off(i, 8 * q);
+        for (int t = 0; t < nmine; ++t) {
+            const int s = t % kNst, b = t % kNTile;
+            if (!wait(&st_full[s], (uint32_t)((t / kNst) & 1))) break;
+            if (t >= kNTile && !wait(&tl_empty[b], (uint32_t)((t / kNTile - 1) & 1))) break;
+            const float *U = reinterpret_cast<const float *>(stg + s * kStage);
+            const double *Pe = reinterpret_cast<const double *>(stg + s * kStage + kStK);
+            unsigned char *Ab = A + b * kBufA, *Bb = B + b * kBufB;
+            {
+                float xv[8];
+#pragma unroll
+                for (int g = 0; g < 8; ++g) xv[g] = U[off[g]];
+                split3_store8(xv, Ab + a_off, kTermA);
+            }
+            if (tid < 128) {   // B: P_e, case j, dofs 8qb..8qb+7; the stage holds P_e(c, j) at c*16 + j
+                const int j = tid & (KR - 1), qb = tid >> 4;
+                float xv[8];
+#pragma unroll
+                for (int g = 0; g < 8; ++g) {
+                    const int c = 8 * qb + g;
+                    xv[g] = c < 60 ? (float)Pe[c * KR + j] : 0.f;
+                }
+                split3_store8(xv, Bb + kmajor_off(j, 8 * qb), kTermB);
+            }
+            fence_proxy_async();   // this thread's tile writes -> the tensor cores
+            __syncwarp();
+            if (lane == 0) {
+                mbar_arrive(&st_empty[s]);
+                mbar_arrive(&tl_full[b]);
+            }
+        }
+    } else if (warp == kMmaWarp) {
+        int t = 0;
+        if (lane == 0) {
+            for (; t < nmine; ++t) {
+                const int b = t % kNTile, a = t % kNAcc;
+                if (!wait(&tl_full[b], (uint32_t)((t / kNTile) & 1))) break;
+                if (t >= kNAcc && !wait(&ac_empty[a], (uint32_t)((t / kNAcc - 1) & 1))) break;
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(A + b * kBufA), b0 = smem_u32(B + b * kBufB);
+                // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
+                const int ta[6] = {0, 0, 1, 0, 1, 2};
+                const int tb[6] = {0, 1, 0, 2, 1, 0};
+                uint32_t acc = 0;
+#pragma unroll
+                for (int tt = 0; tt < 6; ++tt)
+#pragma unroll
+                    for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
+                        mma_bf16(tmem + (uint32_t)(16 * a), umma_desc(a0 + ta[tt] * kTermA + ks * 256, 128, 1024),
+                                 umma_desc(b0 + tb[tt] * kTermB + ks * 256, 128, 1024), kIdesc, acc);
+                        acc = 1;
+                    }
+                mma_commit(&tl_empty[b]);
+                mma_commit(&ac_full[a]);
+            }
+            s_count[1] = t;
+        }
+        __syncwarp();
+    } else if (warp == kEpiWarp0 || warp == kEpiWarp0 + 1) {
+        const int row = 32 * (warp - kEpiWarp0) + lane;   // TMEM lanes 0..63 = rows
+        for (int t = 0; t < nmine; ++t) {
+            const int a = t % kNAcc;
+            if (!wait(&ac_full[a], (uint32_t)((t / kNAcc) & 1))) break;
             tc_fence_after();
             float v[16];
-            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * buf), v);
-            const int row = 32 * warp + lane;
+            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * (warp - kEpiWarp0)) << 16) + (uint32_t)(16 * a), v);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ac_empty[a]);
             if (row < 60) {
-                float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)e * 60 + row) * KR);
+                float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)elem(t) * 60 + row) * KR);
                 o[0] = make_float4(v[0], v[1], v[2], v[3]);
                 o[1] = make_float4(v[4], v[5], v[6], v[7]);
                 o[2] = make_float4(v[8], v[9], v[10], v[11]);
                 o[3] = make_float4(v[12], v[13], v[14], v[15]);
             }
         }
-        mphase[buf] ^= 1;
-    };
-
-    int t = 0;
-    for (; t < nmine; ++t) {
-        const int s = t % kNst, buf = t & 1;
-        if (!mbar_wait(&full[s], (uint32_t)((t / kNst) & 1))) atomicOr(s_fail, 1);
-        const float *U = reinterpret_cast<const float *>(stg + s * kStage);
-        const double *Pe = reinterpret_cast<const double *>(stg + s * kStage + kStK);
-        unsigned char *Ab = A + buf * kBufA, *Bb = B + buf * kBufB;
-        // A: K_e rows i (0..63), 8 K-values per task; K(i,k) = U(min, max) at T(max) + min
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int task = tid + kTcThreads * h;
-            const int i = task & 63, q = task >> 6;
-            float xv[8];
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                const int k = 8 * q + g;
-                const int lo = i < k ? i : k, hi = i < k ? k : i;
-                xv[g] = (i < 60 && k < 60) ? U[hi * (hi + 1) / 2 + lo] : 0.f;
-            }
-            split3_store8(xv, Ab + kmajor_off(i, 8 * q), kTermA);
-        }
-        if (tid < 128) {   // B: P_e, case j, dofs 8q..8q+7; the stage holds P_e(c, j) at c*16 + j
-            const int j = tid & (KR - 1), q = tid >> 4;
-            float xv[8];
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                const int c = 8 * q + g;
-                xv[g] = c < 60 ? (float)Pe[c * KR + j] : 0.f;
-            }
-            split3_store8(xv, Bb + kmajor_off(j, 8 * q), kTermB);
-        }
-        fence_proxy_async();
-        __syncthreads();   // tiles complete; stage s consumed by every thread
-        if (*s_fail) break;
-        if (tid == 0) {
-            tc_fence_after();
-            // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
-            const int ta[6] = {0, 0, 1, 0, 1, 2};
-            const int tb[6] = {0, 1, 0, 2, 1, 0};
-            uint32_t acc = 0;
-            for (int tt = 0; tt < 6; ++tt) {
-                const uint32_t a0 = smem_u32(Ab + ta[tt] * kTermA), b0 = smem_u32(Bb + tb[tt] * kTermB);
-                for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
-                    mma_bf16(tmem + (uint32_t)(16 * buf), umma_desc(a0 + ks * 256, 128, 1024),
-                             umma_desc(b0 + ks * 256, 128, 1024), kIdesc, acc);
-                    acc = 1;
-                }
-            }
-            mma_commit(&mbar[buf]);
-        }
-        // refill stage s with element t + kNst
-        if (warp == 0 && t + kNst < nmine) {
-            fence_proxy_async();
-            issue(t + kNst, conn_next);
-            if (t + kNst + 1 < nmine && lane < 20) conn_next = conn[(size_t)elem(t + kNst + 1) * 20 + lane];
-        }
-        if (t > 0) epilogue(elem(t - 1), buf ^ 1);
-        tc_fence_before();
-        __syncthreads();
     }
-    if (!*s_fail && t > 0) {
-        epilogue(elem(t - 1), (t - 1) & 1);
-        tc_fence_before();
-        __syncthreads();
-    }
+    __syncthreads();
     if (*s_fail) {
         if (tid == 0) {
             atomicExch(err, 3);
-            // copies still in flight: stages t .. t+kNst-1; MMAs: both accumulators
-            for (int k = t; k < nmine && k < t + kNst; ++k) mbar_wait(&full[k % kNst], (uint32_t)((k / kNst) & 1));
-            mbar_wait(&mbar[0], mphase[0]);
-            mbar_wait(&mbar[1], mphase[1]);
+            // copies issued: elements 0 .. s_count[0]-1; MMA groups committed: 0 .. s_count[1]-1.
+            // Wait (bounded) for the last phase of every stage and accumulator still owed.
+            for (int t = s_count[0] - kNst; t < s_count[0]; ++t)
+                if (t >= 0) mbar_wait(&st_full[t % kNst], (uint32_t)((t / kNst) & 1));
+            for (int t = s_count[1] - kNAcc; t < s_count[1]; ++t)
+                if (t >= 0) mbar_wait(&ac_full[t % kNAcc], (uint32_t)((t / kNAcc) & 1));
         }
         __syncthreads();
     }
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 32);
+    if (warp == 0) tmem_dealloc(tmem, 64);
 }
 
 // Block element products on CUDA cores (FP32 or FP64): one warp per element,
@@ -697,8 +742,8 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
         set_error("pf_solve_multi: k must be %d", KR);
         return PF_FAILURE;
     }
-    if (c.shared) {
-        set_error("pf_solve_multi: needs per-element storkm (the context uses a shared element matrix)");
+    if (c.shared || c.kind != KIND_SOLID20) {
+        set_error("pf_solve_multi: needs per-element 20-node storkm");
         return PF_FAILURE;
     }
     if (!c.have_km || *limit < 1 || (*prec != 16 && *prec != 32)) {
@@ -832,7 +877,7 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, co
     }
     Ctx &c = *(Ctx *)*ctx;
     MCK(cudaSetDevice(c.device));
-    if (*k != KR || !c.have_km || c.shared || (*prec != 16 && *prec != 32 && *prec != 64)) {
+    if (*k != KR || !c.have_km || c.shared || c.kind != KIND_SOLID20 || (*prec != 16 && *prec != 32 && *prec != 64)) {
         set_error("pf_ebe_matvec_multi: k must be %d, prec 16/32/64, per-element storkm formed", KR);
         return PF_FAILURE;
     }

@@ -12,10 +12,12 @@
 //                     kernel; tiles of 128 elements' gathered p values are
 //                     split the same way; the six products of order <= 2^-16
 //                     accumulate in FP32 in TMEM (M = 128 with rows 60..127
-//                     unused, N = 128 elements, K = 64).  The gather of one
-//                     tile overlaps the MMAs of the previous one and the
-//                     read-back of the one before.  Results are written in
-//                     the node-padded FP32 layout the scatter reads.
+//                     unused, N = 128 elements, K = 64).  The p values of
+//                     tile t+1 are loaded into registers while tile t's MMAs
+//                     run and tile t-1's accumulator is read back; the
+//                     connectivity arrives by bulk copy two tiles ahead.
+//                     Results are written in the node-padded FP32 layout the
+//                     scatter reads.
 #include "pf_device.cuh"
 #include "pf_tc.cuh"
 
@@ -31,9 +33,10 @@ constexpr int kSBufA = 4 * kSTermA;         // 3 terms + 8 KB read as rows 64..1
 constexpr int kSTermB = kNT * 64 * 2;       // 16 KB: 128 elements x 64 K
 constexpr int kSBufB = 3 * kSTermB;
 constexpr int kSConn = kNT * 20 * 4;        // 10 KB: connectivity of one tile
+constexpr int kSNC = 3;                     // connectivity buffers: tiles t, t+1, t+2
 constexpr int kSOffB = kSBufA;
 constexpr int kSOffC = kSOffB + 2 * kSBufB;
-constexpr int kSOffAux = kSOffC + 2 * kSConn;
+constexpr int kSOffAux = kSOffC + kSNC * kSConn;
 constexpr int kSSmem = kSOffAux + 128;
 constexpr int kSThreads = 256;
 constexpr uint32_t kSIdesc = idesc_bf16(128, kNT);
@@ -93,9 +96,9 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     if (*s_stop) return;   // uniform: read once per block
     unsigned char *A = sm;
     unsigned char *B = sm + kSOffB;
-    int *cs = reinterpret_cast<int *>(sm + kSOffC);                  // [2][128*20]
-    uint64_t *cfull = reinterpret_cast<uint64_t *>(sm + kSOffAux);   // 2: connectivity copies
-    uint64_t *mbar = cfull + 2;                                      // 2: MMA completion
+    int *cs = reinterpret_cast<int *>(sm + kSOffC);                  // [3][128*20]
+    uint64_t *cfull = reinterpret_cast<uint64_t *>(sm + kSOffAux);   // 3: connectivity copies
+    uint64_t *mbar = cfull + kSNC;                                   // 2: MMA completion
     uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
     int *s_fail = reinterpret_cast<int *>(tslot + 1);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -121,8 +124,7 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     }
     if (warp == 0) tmem_alloc(tslot, 256);
     if (tid == 0) {
-        mbar_init(&cfull[0], 1);
-        mbar_init(&cfull[1], 1);
+        for (int b = 0; b < kSNC; ++b) mbar_init(&cfull[b], 1);
         mbar_init(&mbar[0], 1);
         mbar_init(&mbar[1], 1);
         mbar_fence_init();
@@ -134,12 +136,33 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     tc_fence_after();
     const uint32_t tmem = *tslot;
 
-    auto issue_conn = [&](int t) {   // thread 0: connectivity of tile t into buffer t & 1
+    auto issue_conn = [&](int t) {   // thread 0: connectivity of tile t into buffer t % kSNC
+        const int b = t % kSNC;
         const uint32_t bytes = (uint32_t)tile_n(t) * 80u;
-        mbar_expect_tx(&cfull[t & 1], bytes);
-        bulk_g2s(cs + (t & 1) * kNT * 20, conn + (size_t)tile(t) * kNT * 20, bytes, &cfull[t & 1]);
+        mbar_expect_tx(&cfull[b], bytes);
+        bulk_g2s(cs + b * kNT * 20, conn + (size_t)tile(t) * kNT * 20, bytes, &cfull[b]);
     };
-    if (tid == 0 && nmine > 0) issue_conn(0);
+    // p values of tile t into registers: element n = task & 127, dofs 8q..8q+7
+    float xv[4][8];
+    auto load_tile = [&](int t) {
+        if (!mbar_wait(&cfull[t % kSNC], (uint32_t)((t / kSNC) & 1))) atomicOr(s_fail, 1);
+        const int *ct = cs + (t % kSNC) * kNT * 20;
+        const int n_here = tile_n(t);
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const int task = tid + kSThreads * h;
+            const int n = task & (kNT - 1), q = task >> 7;
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                const int c = 8 * q + g;
+                xv[h][g] = 0.f;
+                if (c < 60 && n < n_here) xv[h][g] = (float)p[(size_t)3 * ct[n * 20 + c / 3] + c % 3];
+            }
+        }
+    };
+    if (tid == 0)
+        for (int t = 0; t < 2 && t < nmine; ++t) issue_conn(t);
+    if (nmine > 0) load_tile(0);
 
     uint32_t mphase[2] = {0, 0};
     auto epilogue = [&](int t, int buf) {
@@ -172,27 +195,8 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     int t = 0;
     for (; t < nmine; ++t) {
         const int buf = t & 1;
-        if (tid == 0 && t + 1 < nmine) {
-            fence_proxy_async();
-            issue_conn(t + 1);   // its buffer was last read by tile t-1, before the last barrier
-        }
-        if (!mbar_wait(&cfull[buf], (uint32_t)((t >> 1) & 1))) atomicOr(s_fail, 1);
-        const int *ct = cs + buf * kNT * 20;
-        const int n_here = tile_n(t);
         unsigned char *Bb = B + buf * kSBufB;
-        // B: element n of the tile, dofs 8q..8q+7 (4 tasks per thread; loads first)
-        float xv[4][8];
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            const int task = tid + kSThreads * h;
-            const int n = task & (kNT - 1), q = task >> 7;
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                const int c = 8 * q + g;
-                xv[h][g] = 0.f;
-                if (c < 60 && n < n_here) xv[h][g] = (float)p[(size_t)3 * ct[n * 20 + c / 3] + c % 3];
-            }
-        }
+        // B: the p values of tile t (loaded during the previous iteration), split into three terms
 #pragma unroll
         for (int h = 0; h < 4; ++h) {
             const int task = tid + kSThreads * h;
@@ -217,7 +221,13 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
                 }
             }
             mma_commit(&mbar[buf]);
+            // connectivity of tile t+2 into the buffer tile t-1 used (read before the last barrier)
+            if (t + 2 < nmine) {
+                fence_proxy_async();
+                issue_conn(t + 2);
+            }
         }
+        if (t + 1 < nmine) load_tile(t + 1);   // in flight during the read-back below
         if (t > 0) epilogue(t - 1, buf ^ 1);
         tc_fence_before();
         __syncthreads();
@@ -230,7 +240,7 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     if (*s_fail) {
         if (tid == 0) {
             atomicExch(err, 3);
-            if (t + 1 < nmine) mbar_wait(&cfull[(t + 1) & 1], (uint32_t)(((t + 1) >> 1) & 1));
+            for (int k = t + 1; k < nmine && k < t + 3; ++k) mbar_wait(&cfull[k % kSNC], (uint32_t)((k / kSNC) & 1));
             mbar_wait(&mbar[0], mphase[0]);
             mbar_wait(&mbar[1], mphase[1]);
         }

@@ -139,37 +139,30 @@ __device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, float (&v)[16
 
 // ---------------------------------------------------------------------------
 // BF16 three-term split
-__device__ __forceinline__ uint16_t bf16_rn(float x)
+// Two floats rounded to nearest-even BF16 in one instruction: lo in bits
+// 0..15, hi in bits 16..31.
+__device__ __forceinline__ uint32_t cvt_bf16x2(float lo, float hi)
 {
-    uint32_t u = __float_as_uint(x);
-    u += 0x7FFFu + ((u >> 16) & 1u);   // round to nearest even (finite inputs)
-    return (uint16_t)(u >> 16);
-}
-__device__ __forceinline__ float bf16_to_f(uint16_t h) { return __uint_as_float(((uint32_t)h) << 16); }
-
-// x = h1 + h2 + h3 in BF16 (each remainder is exact in FP32)
-__device__ __forceinline__ void split3(float x, uint16_t &h1, uint16_t &h2, uint16_t &h3)
-{
-    h1 = bf16_rn(x);
-    const float r1 = x - bf16_to_f(h1);
-    h2 = bf16_rn(r1);
-    const float r2 = r1 - bf16_to_f(h2);
-    h3 = bf16_rn(r2);
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
 }
 
-// Splits 8 consecutive K-values and writes the three 16-byte chunks, one per
-// term tile (term t at dst + t * term_bytes).
+// Splits 8 consecutive K-values into three BF16 terms (x = h1 + h2 + h3;
+// each remainder is exact in FP32) and writes the three 16-byte chunks, one
+// per term tile (term t at dst + t * term_bytes).  Each term is the
+// nearest-even BF16 of the remainder left by the terms before it.
 __device__ __forceinline__ void split3_store8(const float (&x)[8], unsigned char *dst, uint32_t term_bytes)
 {
     uint32_t w1[4], w2[4], w3[4];
 #pragma unroll
-    for (int r = 0; r < 8; r += 2) {
-        uint16_t a1, a2, a3, b1, b2, b3;
-        split3(x[r], a1, a2, a3);
-        split3(x[r + 1], b1, b2, b3);
-        w1[r / 2] = (uint32_t)a1 | ((uint32_t)b1 << 16);
-        w2[r / 2] = (uint32_t)a2 | ((uint32_t)b2 << 16);
-        w3[r / 2] = (uint32_t)a3 | ((uint32_t)b3 << 16);
+    for (int r = 0; r < 4; ++r) {
+        const float a = x[2 * r], b = x[2 * r + 1];
+        w1[r] = cvt_bf16x2(a, b);
+        const float ra = a - __uint_as_float(w1[r] << 16), rb = b - __uint_as_float(w1[r] & 0xFFFF0000u);
+        w2[r] = cvt_bf16x2(ra, rb);
+        const float sa = ra - __uint_as_float(w2[r] << 16), sb = rb - __uint_as_float(w2[r] & 0xFFFF0000u);
+        w3[r] = cvt_bf16x2(sa, sb);
     }
     *reinterpret_cast<uint4 *>(dst) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
     *reinterpret_cast<uint4 *>(dst + term_bytes) = make_uint4(w2[0], w2[1], w2[2], w2[3]);

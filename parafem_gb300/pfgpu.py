@@ -57,6 +57,7 @@ _SIGS = {
     "pf_solve_stats": [_VPP, ctypes.c_void_p, _IP],
     "pf_bench_iterations": [_VPP, _IP, _IP, _DP, _DP, _DP],
     "pf_centroid_stress": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_element_stresses": [_VPP, ctypes.c_void_p, _IP, _IP, ctypes.c_void_p],
     "pf_kernel_launches": [_VPP, _LLP],
     "pf_tuning": [_VPP, _IP, _IP, ctypes.c_void_p],
     "pf_set_tuning": [_VPP, _IP],
@@ -79,6 +80,14 @@ _SIGS = {
     "pf_batch_set_graphs": [_VPP, _IP],
     "pf_p12meshgen": [ctypes.c_char_p],
     "pf_p121_run": [ctypes.c_char_p, _IP, _IP, _IP, _DP],
+    "pf_p123_run": [ctypes.c_char_p, _IP, _IP, ctypes.c_void_p],
+    "pf_mesh_box8": [_IP, _IP, _IP, _DP, _DP, _DP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_box8_restraints": [_IP, _IP, _IP, ctypes.c_void_p],
+    "pf_number_equations1": [_IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
+    "pf_setup_scalar8": [_VPP, _IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_form_storkc": [_VPP, _IP, _DP, _DP, _DP],
+    "pf_get_storkc": [_VPP, _IP, _IP, ctypes.c_void_p],
+    "pf_set_fixed": [_VPP, _IP, ctypes.c_void_p, _DP],
     "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_cube_restraints": [_IP, _IP, _IP, _IP, ctypes.c_void_p],
     "pf_number_equations": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
@@ -238,6 +247,30 @@ class Solver:
         _check(lib().pf_setup(self._ref, _i(nels), _i(nn), _i(neq), pn, pg, pc), "pf_setup")
         self.nels, self.nn, self.neq = nels, int(nn), int(neq)
 
+    def setup_scalar8(self, g_num, g_g, g_coord, nn, neq):
+        """8-node bricks with one freedom per node (p123)."""
+        g_num, pn = _arr(g_num, np.int32)
+        g_g, pg = _arr(g_g, np.int32)
+        g_coord, pc = _arr(g_coord, np.float64)
+        nels = g_num.shape[0]
+        if g_num.shape != (nels, 8) or g_g.shape != (nels, 8) or g_coord.shape != (nels, 3, 8):
+            raise ValueError("g_num (nels,8), g_g (nels,8), g_coord (nels,3,8) expected")
+        _check(lib().pf_setup_scalar8(self._ref, _i(nels), _i(nn), _i(neq), pn, pg, pc), "pf_setup_scalar8")
+        self.nels, self.nn, self.neq = nels, int(nn), int(neq)
+
+    def form_storkc(self, nip, kx, ky, kz):
+        _check(lib().pf_form_storkc(self._ref, _i(nip), _d(kx), _d(ky), _d(kz)), "pf_form_storkc")
+
+    def get_storkc(self, first=0, count=None):
+        count = self.nels - first if count is None else count
+        out = np.zeros((max(count, 1), 8, 8))
+        _check(lib().pf_get_storkc(self._ref, _i(first), _i(count), out.ctypes.data), "pf_get_storkc")
+        return out[:count]
+
+    def set_fixed(self, eqs, penalty=1.0e20):
+        eqs, pe = _arr(np.atleast_1d(eqs), np.int32)
+        _check(lib().pf_set_fixed(self._ref, _i(eqs.size), pe, _d(penalty)), "pf_set_fixed")
+
     def set_material(self, e, v):
         e, pe = _arr(np.atleast_1d(e), np.float64)
         v, pv = _arr(np.atleast_1d(v), np.float64)
@@ -334,6 +367,15 @@ class Solver:
         x, px = _arr(x, np.float64)
         s = np.zeros(6)
         _check(lib().pf_centroid_stress(self._ref, _i(iel), px, s.ctypes.data), "pf_centroid_stress")
+        return s
+
+    def element_stresses(self, x, first: int = 1, count=None):
+        """Centroid stresses of elements first..first+count-1 (1-based): (count, 6)."""
+        x, px = _arr(x, np.float64)
+        count = self.nels - first + 1 if count is None else count
+        s = np.zeros((max(count, 1), 6))
+        _check(lib().pf_element_stresses(self._ref, px, _i(first), _i(count), s.ctypes.data),
+               "pf_element_stresses")
         return s
 
     def launches(self) -> int:
@@ -469,6 +511,54 @@ def random_top_loads(g_g, nxe, nze, neq, k, seed):
     R = np.zeros((neq, k), order="F")
     R[eqs - 1, :] = rng.standard_normal((eqs.size, k))
     return R
+
+
+def mesh_box8(nxe, nye, nze, aa=1.0, bb=1.0, cc=1.0):
+    """GEOMETRY_8BXZ box of 8-node bricks: (g_num (nels,8), g_coord (nels,3,8), nn)."""
+    nels = nxe * nye * nze
+    g_num = np.zeros((nels, 8), np.int32)
+    g_coord = np.zeros((nels, 3, 8), np.float64)
+    _check(lib().pf_mesh_box8(_i(nxe), _i(nye), _i(nze), _d(aa), _d(bb), _d(cc), g_num.ctypes.data,
+                              g_coord.ctypes.data), "pf_mesh_box8")
+    return g_num, g_coord, (nxe + 1) * (nye + 1) * (nze + 1)
+
+
+def box8_restraints(nxe, nye, nze):
+    """box_bc8: per node 1 = free, 0 = restrained."""
+    fix = np.zeros((nxe + 1) * (nye + 1) * (nze + 1), np.int32)
+    _check(lib().pf_box8_restraints(_i(nxe), _i(nye), _i(nze), fix.ctypes.data), "pf_box8_restraints")
+    return fix
+
+
+def number_equations1(g_num, node_fix):
+    """One freedom per node: g_g (nels, nod), 0 = restrained, and neq."""
+    g_num, pn = _arr(g_num, np.int32)
+    node_fix, pf = _arr(node_fix, np.int32)
+    g_g = np.zeros(g_num.shape, np.int32)
+    neq = ctypes.c_int(0)
+    _check(lib().pf_number_equations1(_i(g_num.shape[0]), _i(node_fix.shape[0]), _i(g_num.shape[1]), pn, pf,
+                                      g_g.ctypes.data, ctypes.byref(neq)), "pf_number_equations1")
+    return g_g, neq.value
+
+
+def box8_problem(nxe, nye, nze, aa=1.0, bb=1.0, cc=1.0, load=10.0):
+    """p123's box: 8-node bricks, box_bc8 restraints, a load at equation
+    nres = nxe*(nze-1)+1 (the freedom p12meshgen loads).  Host only."""
+    g_num, g_coord, nn = mesh_box8(nxe, nye, nze, aa, bb, cc)
+    fix = box8_restraints(nxe, nye, nze)
+    g_g, neq = number_equations1(g_num, fix)
+    nres = nxe * (nze - 1) + 1
+    r = np.zeros(neq)
+    r[nres - 1] = load
+    return dict(g_num=g_num, g_coord=g_coord, nn=nn, g_g=g_g, neq=neq, r=r, fix=fix, nres=nres,
+                nxe=nxe, nye=nye, nze=nze)
+
+
+def p123_run(job: str, device: int = 0):
+    it = ctypes.c_int(0)
+    pot = np.zeros(4)
+    _check(lib().pf_p123_run(os.fsencode(job), _i(device), ctypes.byref(it), pot.ctypes.data), "pf_p123_run")
+    return it.value, pot
 
 
 def cube_problem(nxe, nye, nze, bc=1, pressure=None, aa=1.0, bb=1.0, cc=1.0):

@@ -2,10 +2,11 @@
 
 Usage: python tests/golden/make_golden.py /path/to/parafem
 
-Reads the reference's own recorded runs (examples/5th_ed/p121) and writes
+Reads the reference's own recorded runs (examples/5th_ed/p121, p123) and writes
   p121_golden.json      .res figures of the demo and book runs, the .mg
                         inputs, and sha256 of the demo deck files
   p121_demo_displ.npz   the demo displacement field (p121_demo.ensi.DISPL-000001)
+  p123_golden.json      .res figures of the p123 book run and its .mg input
 The fixtures let the tests run where the reference tree is absent.
 """
 from __future__ import annotations
@@ -76,5 +77,32 @@ def main(root):
     print("wrote", os.path.join(HERE, "p121_golden.json"), disp.shape)
 
 
+def parse_res123(path):
+    txt = open(path).read()
+    lines = txt.splitlines()
+    out = {}
+    m = re.search(r"There are\s+(\d+) nodes\s+(\d+) restrained and\s+(\d+) equations", txt)
+    out["nn"], out["nr"], out["neq"] = (int(g) for g in m.groups())
+    out["processes"] = int(re.search(r"This job ran on\s+(\d+)\s+processes", txt).group(1))
+    out["iterations"] = int(re.search(r"The number of iterations to convergence was\s+(\d+)", txt).group(1))
+    out["total_load_text"] = re.search(r"The total load is\s+(\S+)", txt).group(1)
+    i = next(k for k, ln in enumerate(lines) if ln.strip().startswith("Freedom"))
+    out["potentials"] = [[int(ln.split()[0]), ln.split()[1]] for ln in lines[i + 1:i + 5]]
+    out["lines"] = {"potentials": lines[i + 1:i + 5],
+                    "total_load": next(ln for ln in lines if ln.startswith("The total load"))}
+    return out
+
+
+def main123(root):
+    ex = os.path.join(root, "examples", "5th_ed", "p123", "book")
+    gold = {"source": "examples/5th_ed/p123/book of the ParaFEM tree",
+            "book": parse_res123(os.path.join(ex, "p123.res")),
+            "book_mg": open(os.path.join(ex, "p123.mg")).read()}
+    with open(os.path.join(HERE, "p123_golden.json"), "w") as f:
+        json.dump(gold, f, indent=1, sort_keys=True)
+    print("wrote", os.path.join(HERE, "p123_golden.json"))
+
+
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
+    main123(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")

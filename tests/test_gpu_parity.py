@@ -136,6 +136,24 @@ def test_demo_stresses_via_gpu_at_golden_iteration(demo_problem, golden):
     assert normal == golden["demo"]["lines"]["stress"][:36]
 
 
+def test_element_stresses_of_every_element_match_oracle():
+    g_num, g_coord, nn, g_g, neq = distorted_cube(4, 3, 3)
+    nels = g_num.shape[0]
+    e, v = P.random_material(nels, 5, 1.0, 1000.0, 0.2, 0.35)
+    x = np.random.default_rng(12).standard_normal(neq)
+    x0 = np.concatenate([[0.0], x])
+    ref = np.array([O.centroid_stress(g_coord[k], x0[g_g[k]], e[k], v[k]) for k in range(nels)])
+    with P.Solver() as s:
+        s.setup(g_num, g_g, g_coord, nn, neq)
+        s.set_material(e, v)
+        sig = s.element_stresses(x)
+        part = s.element_stresses(x, 7, 5)
+        one = s.centroid_stress(x, 9)
+    assert np.abs(sig - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.array_equal(part, sig[6:11])
+    assert np.array_equal(one, sig[8])
+
+
 def test_config1_fp64_drop_in_matches_oracle():
     """10^3 cube, nip=27, E=100, v=0.3, fixed base, top pressure, checon tol 1e-6."""
     prob = P.cube_problem(10, 10, 10)
