@@ -47,11 +47,13 @@ def parse_args():
     ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--workload", default="cube100",
-                    choices=["cube100", "hetero80", "serving", "multirhs60", "cube10", "shared100", "p123book"],
+                    choices=["cube100", "hetero80", "serving", "multirhs60", "cube10", "shared100", "p123book",
+                             "p122book"],
                     help="cube100: the headline; hetero80: per-element E and v, accuracy study; "
                          "serving: continuous batching of a Poisson request stream; shared100: one element "
                          "matrix for every element (PCG_KM); p123book: p123's book run (Laplace, 200^3 8-node "
-                         "bricks)")
+                         "bricks); p122book: p122's book run (Mohr-Coulomb viscoplasticity, 20^3 20-node bricks, "
+                         "12 load increments)")
     ap.add_argument("--requests", type=int, default=2000, help="serving: number of requests")
     ap.add_argument("--rates", default="20", help="serving: comma-separated arrival rates (requests/s); "
                                                     "0 = all requests at t=0")
@@ -662,6 +664,44 @@ def run_p123(args, rank, world, local, dist):
     return 0
 
 
+def run_p122(args, rank, world, local, dist):
+    """p122's book run (examples/5th_ed/p122/book/p122.mg): 20^3 20-node
+    bricks of 0.5, E 1e4, v 0.3, Mohr-Coulomb c 100, phi = psi = 0, 12 load
+    increments under load control, plastic tolerance 1e-4, PCG tolerance
+    1e-5.  The reference recorded 409 s on 16 Cray XE6 cores.  The mesh,
+    restraints and loads are p12meshgen's p122 case (host side)."""
+    import parafem_gb300 as P
+    nxe = nze = 20
+    nels, aa = 8000, 0.5
+    qinc = [200.0, 100.0, 50.0, 50.0, 50.0, 30.0, 20.0, 10.0, 10.0, 5.0, 5.0, 5.0]
+    prob = P.cube_problem(nxe, nels // nxe // nze, nze, bc=0, pressure=0.0, aa=aa, bb=aa, cc=aa)
+    ld0 = P.patch_loads(nxe, nze, prob["g_num"], prob["g_g"], prob["neq"], -aa * aa / 12.0)
+    s = P.Solver(local)
+    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+    s.set_material(1.0e4, 0.3)
+    s.form_storkm(8)
+    l0 = s.launches()
+    t0 = time.perf_counter()
+    res, _ = s.p122_solve(8, 0.0, 100.0, 0.0, qinc, 1000, 1000, 1e-4, 1e-5, ld0)
+    wall = time.perf_counter() - t0
+    launches = s.launches() - l0
+    s.close()
+    cj = float(res[:, 4].sum())
+    line = {"metric": METRIC, "value": prob["neq"] * cj / wall, "unit": UNIT, "n_gpus": world, "steps": int(cj),
+            "warmup": 0, "ms_per_step": 1e3 * wall / cj, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "p122 book run: 20^3 20-node bricks, Mohr-Coulomb (c 100, phi 0, psi 0), E 1e4, "
+                                   "v 0.3, 12 load increments", "nels": nels, "neq": prob["neq"]},
+            "p122": {"wall_s": wall, "increments": [
+                {"displacement": float(r[0]), "sigma_z": float(r[1]), "sigma_x": float(r[2]), "sigma_y": float(r[3]),
+                 "cj_iterations": int(r[4]), "plastic_iterations": int(r[5])} for r in res],
+                "reference_book": {"wall_s": 409.0, "cores": 16}},
+            "gpu_launches": int(launches)}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def run_cube10(args, rank, world, local, dist):
     """The reference's CPU-runnable case: 10^3 cube, nip 27, E 100, v 0.3,
     fixed base, top pressure (total -1), checon_par tol 1e-6, limit 5000.
@@ -721,6 +761,8 @@ def main():
             return run_shared(args, rank, world, local, dist)
         if args.workload == "p123book":
             return run_p123(args, rank, world, local, dist)
+        if args.workload == "p122book":
+            return run_p122(args, rank, world, local, dist)
         return run_gb300(args, rank, world, local, dist)
     finally:
         if dist is not None:

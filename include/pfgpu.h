@@ -186,6 +186,23 @@ int pf_get_storkc(void **ctx, const int *first, const int *count, double *storkc
  * (pf_get_diag gives diag(eq) after this call).  pf_form_storkc clears them. */
 int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const double *penalty);
 
+/* ---- p122: elastic-plastic (Mohr-Coulomb) solid, viscoplastic strain method ----
+ * The solve of src/programs/5th_ed/p122/p122.f90:78-225 for 20-node bricks
+ * under load control, on a context with storkm formed (pf_form_storkm with
+ * nip and one material E, v).  For each load increment iy (qinc(iy) times
+ * the nodal loads ld0(neq)), plastic iterations of a warm-started PCG
+ * (tolerance cjtol, at most cjits iterations, checon_par) and a Gauss-point
+ * pass (INVAR, MOCOUF, MOCOUQ, FORMM, the viscoplastic strains and body
+ * loads) until checon_par of the displacements meets plastol or plasits
+ * iterations.  results(6, incs) per increment: totd(1), sigma z, sigma x,
+ * sigma y at element 1 Gauss point 1, PCG iterations, plastic iterations.
+ * totd(neq, incs) (may be NULL): the total displacements after each increment.
+ * phi, c, psi: friction angle, cohesion, dilation angle (degrees). */
+int pf_p122_solve(void **ctx, const int *nip, const double *phi, const double *c, const double *psi,
+                  const int *incs, const double *qinc, const int *plasits, const int *cjits,
+                  const double *plastol, const double *cjtol, const double *ld0, double *results,
+                  double *totd, int *incs_done);
+
 /* Number of kernels this library launched since the context was created. */
 int pf_kernel_launches(void **ctx, long long *count);
 
@@ -270,6 +287,19 @@ int pf_p12meshgen(const char *job);
  * mode: PF_MODE_*; iters and central (xnew(1)) are returned. */
 int pf_p121_run(const char *job, const int *device, const int *mode,
                 int *iters, double *central);
+
+/* load_p121's patch load on the top face of a 20-node cube (loading.f90:
+ * 386-480), nle = nxe/5: r(z equation of each patch node) = factor x the
+ * pattern multiplier (LOAD + SCATTER_NOADD semantics: assignment).  p122's
+ * decks use factor = -aa*bb/12 (p12meshgen.f90:420). */
+int pf_patch_loads(const int *nxe, const int *nze, const double *factor, const int *nels, const int *g_num,
+                   const int *g_g, const int *neq, double *r);
+
+/* The whole p122 job (p122.f90:1-233) for 20-node bricks under load
+ * control: reads job.dat (READ_P122's record and the qinc values), .d,
+ * .bnd, .lds; solves every increment on the GPU (pf_p122_solve); writes
+ * job.res and job.ensi.DISPL-0000nn per increment. */
+int pf_p122_run(const char *job, const int *device, int *incs_done);
 
 /* Host side of p123: an nxe x nye x nze box of 8-node bricks numbered as
  * GEOMETRY_8BXZ (geometry.f90:70-166): g_num(8,nels), g_coord(8,3,nels). */

@@ -38,7 +38,8 @@ _PD = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 
 def build(force: bool = False) -> str:
     """Compile the C restatement into ``oracle/_build/liborc.so`` (gcc, OpenMP)."""
-    srcs = [os.path.join(HERE, "p121_oracle.c"), os.path.join(HERE, "p123_oracle.c")]
+    srcs = [os.path.join(HERE, "p121_oracle.c"), os.path.join(HERE, "p123_oracle.c"),
+            os.path.join(HERE, "p122_oracle.c")]
     os.makedirs(BUILD_DIR, exist_ok=True)
     if (not force and os.path.exists(LIB_PATH)
             and os.path.getmtime(LIB_PATH) >= max(os.path.getmtime(s) for s in srcs)):
@@ -93,6 +94,15 @@ def lib():
             L.orc_ebe_matvec8.argtypes = [_I, _I, _PI, _PD, _I, _PD, _PD]
             L.orc_mesh_box8.argtypes = [_I, _I, _I, _D, _D, _D, _PI, ctypes.c_void_p]
             L.orc_steering8.argtypes = [_I, _PI, _I, _PI, _PI]
+            # p122 (p122_oracle.c)
+            L.orc_p122.argtypes = [_I, _I, _PI, _PD, _I, _D, _D, _D, _D, _D, _I, _PD, _I, _I, _D, _D, _PD, _PD,
+                                   ctypes.c_void_p]
+            L.orc_p122.restype = _I
+            L.orc_invar.argtypes = [_PD, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]
+            L.orc_mocouf.argtypes = [_D, _D, _D, _D, _D]
+            L.orc_mocouf.restype = _D
+            L.orc_mocouq.argtypes = [_D, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]
+            L.orc_formm.argtypes = [_PD, _PD, _PD, _PD]
             _lib = L
     return _lib
 
@@ -370,3 +380,51 @@ def run_p123_box(nxe, nye, nze, aa, bb, cc, kx, ky, kz, tol, limit, nip=8, load=
     it, x, _ = pcg123(g_g, kc, dg, r, tol, limit, shared=True)
     return dict(nn=(nxe + 1) * (nye + 1) * (nze + 1), nr=rest.shape[0], neq=neq, iters=it, q=float(r.sum()),
                 nres=nres, x=x)
+
+
+# ---------------------------------------------------------------------------
+# p122: elastic-plastic (Mohr-Coulomb) solid, viscoplastic strain method,
+# 20-node bricks (src/programs/5th_ed/p122/p122.f90), restated in p122_oracle.c
+# ---------------------------------------------------------------------------
+def cube20_problem(nels, nxe, nze, aa, bb, cc, load_factor):
+    """p12meshgen's p121/p122 box of 20-node bricks (GEOMETRY_20BXZ,
+    cube_bc20, load_p121 with val = val * load_factor): returns
+    dict(g_num, g_coord, g_g, neq, nn, nr, ld0)."""
+    L = lib()
+    nye = nels // nxe // nze
+    g_num = np.zeros((nels, 20), np.int32)
+    g_coord = np.zeros((nels, 3, 20))
+    co = np.zeros(60)
+    num = np.zeros(20, np.int32)
+    for iel in range(1, nels + 1):
+        L.orc_geometry_20bxz(iel, nxe, nze, aa, bb, cc, co, num)
+        g_num[iel - 1] = num
+        g_coord[iel - 1] = co.reshape(3, 20)
+    nn = int(g_num.max())
+    rest = np.zeros(4 * nn, np.int32)
+    nr = L.orc_cube_bc20(nxe, nye, nze, rest)
+    rest = np.ascontiguousarray(rest[:4 * nr].reshape(nr, 4))
+    g_g = steering(g_num, rest)
+    neq = int(g_g.max())
+    nle = nxe // 5
+    node = np.zeros(4 * (nle + 1) ** 2 + 8, np.int32)
+    val = np.zeros(node.size)
+    nl = L.orc_load_p121(nle, nxe, nze, node, val)
+    lv = np.zeros((nl, 3))
+    lv[:, 2] = val[:nl] * load_factor
+    ld0 = load_vector(g_num, g_g, np.ascontiguousarray(node[:nl]), lv, neq)
+    return dict(g_num=g_num, g_coord=g_coord, g_g=g_g, neq=neq, nn=nn, nr=nr, ld0=ld0)
+
+
+def run_p122(prob, nip, phi, c, psi, e, v, qinc, plasits, cjits, plastol, cjtol, keep_totd=False):
+    """The p122 solve: per increment (totd(1), sigma z, sigma x, sigma y of
+    element 1 Gauss point 1, cj iterations, plastic iterations)."""
+    qinc = np.ascontiguousarray(qinc, dtype=np.float64)
+    incs = qinc.size
+    out = np.zeros((incs, 6))
+    totd = np.zeros((incs, prob["neq"])) if keep_totd else None
+    n = lib().orc_p122(prob["g_num"].shape[0], prob["neq"], np.ascontiguousarray(prob["g_g"]),
+                       np.ascontiguousarray(prob["g_coord"]), nip, phi, c, psi, e, v, incs, qinc, plasits, cjits,
+                       plastol, cjtol, np.ascontiguousarray(prob["ld0"]), out,
+                       totd.ctypes.data if keep_totd else None)
+    return out[:n], (totd[:n] if keep_totd else None)

@@ -207,6 +207,8 @@ static int run_pcg(Ctx &c, int prec, double *xsol, int limit)
     return 0;
 }
 
+int run_pcg_public(Ctx &c, int prec, double *xsol, int limit) { return run_pcg(c, prec, xsol, limit); }
+
 // ||f - K64 x||_2 / ||f||_2 on the device (fills c.rres).
 static int true_relres(Ctx &c, const double *x, double ff, double *out, double *dev2)
 {

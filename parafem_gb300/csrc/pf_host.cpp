@@ -240,6 +240,8 @@ struct Deck {
     std::vector<double> lval;     // (3, loaded)
 };
 
+int read_mesh_files(const std::string &job, Deck &D);
+
 int read_deck(const std::string &job, Deck &D)
 {
     std::vector<std::string> t;
@@ -265,6 +267,14 @@ int read_deck(const std::string &job, Deck &D)
                   D.element.c_str(), D.nod);
         return 1;
     }
+    return read_mesh_files(job, D);
+}
+
+// job.d (nodes, 20-node elements), job.bnd and job.lds of a deck whose
+// .dat record is already in D (READ_G_NUM_PP, READ_G_COORD_PP, READ_REST,
+// READ_LOADS of src/modules/mpi/input.f90)
+int read_mesh_files(const std::string &job, Deck &D)
+{
     std::ifstream f(job + ".d");
     if (!f) {
         set_error("cannot read %s.d", job.c_str());
@@ -480,6 +490,7 @@ extern "C" int pf_random_material(const int *nels, const long long *seed, const 
 
 // ---------------------------------------------------------------------------
 static int p12meshgen_p123(const std::string &job, const std::vector<std::string> &t);
+static int p12meshgen_p122(const std::string &job, const std::vector<std::string> &t);
 
 extern "C" int pf_p12meshgen(const char *job_c)
 {
@@ -491,8 +502,9 @@ extern "C" int pf_p12meshgen(const char *job_c)
         return PF_FAILURE;
     }
     if (t[0] == "p123") return p12meshgen_p123(job, t);
+    if (t[0] == "p122") return p12meshgen_p122(job, t);
     if (t[0] != "p121") {
-        set_error("%s.mg: the p121 and p123 cases are supported (got %s)", job.c_str(), t[0].c_str());
+        set_error("%s.mg: the p121, p122 and p123 cases are supported (got %s)", job.c_str(), t[0].c_str());
         return PF_FAILURE;
     }
     const std::string iotype = t[1];
@@ -665,6 +677,33 @@ extern "C" int pf_p121_run(const char *job_c, const int *device, const int *mode
     fclose(fr);
     if (iters_out) *iters_out = iters;
     if (central_out) *central_out = neq > 0 ? x[0] : 0.0;
+    return PF_SUCCESS;
+}
+
+// load_p121's patch on the top face (loading.f90:386-480) as a load vector:
+// r(z-equation of each listed node) = factor * multiplier, by LOAD +
+// SCATTER_NOADD (loading.f90:36-146): assignment, the last entry wins.
+extern "C" int pf_patch_loads(const int *nxe, const int *nze, const double *factor, const int *nels,
+                              const int *g_num, const int *g_g, const int *neq, double *r)
+{
+    if (!nxe || !nze || !factor || !nels || !g_num || !g_g || !neq || !r || *nxe < 5 || *nze < 1) {
+        set_error("pf_patch_loads: invalid arguments (nxe >= 5)");
+        return PF_FAILURE;
+    }
+    std::vector<int> node;
+    std::vector<double> mult;
+    load_p121_pattern(*nxe / 5, *nxe, *nze, node, mult);
+    int maxnode = 0;
+    for (int nd : node) maxnode = nd > maxnode ? nd : maxnode;
+    std::vector<int> which((size_t)maxnode + 1, -1);
+    for (size_t i = 0; i < node.size(); ++i) which[node[i]] = (int)i;
+    for (size_t e = 0; e < (size_t)*nels; ++e)
+        for (int a = 0; a < 20; ++a) {
+            const int nd = g_num[20 * e + a];
+            if (nd < 1 || nd > maxnode || which[nd] < 0) continue;
+            const int q = g_g[60 * e + 3 * a + 2];
+            if (q > 0 && q <= *neq) r[q - 1] = *factor * mult[which[nd]];
+        }
     return PF_SUCCESS;
 }
 
@@ -1063,5 +1102,213 @@ extern "C" int pf_p123_run(const char *job_c, const int *device, int *iters_out,
     fprintf(fr, "This analysis took %s\n", fmt_F(secs(t0), 10, 4).c_str());
     fclose(fr);
     if (iters_out) *iters_out = iters;
+    return PF_SUCCESS;
+}
+
+// ===========================================================================
+// p122: elastic-plastic (Mohr-Coulomb) solid, 20-node bricks, load control
+// (src/programs/5th_ed/p122/p122.f90).
+
+// p12meshgen's p122 case for 20-node bricks (p12meshgen.f90:372-590).
+static int p12meshgen_p122(const std::string &job, const std::vector<std::string> &t)
+{
+    if (t.size() < 20) {
+        set_error("%s.mg: the p122 case needs at least 19 values", job.c_str());
+        return PF_FAILURE;
+    }
+    const std::string iotype = t[1];
+    const int nels = atoi(t[2].c_str()), nxe = atoi(t[3].c_str()), nze = atoi(t[4].c_str());
+    const int nod = atoi(t[5].c_str()), nip = atoi(t[6].c_str());
+    const double aa = to_d(t[7]), bb = to_d(t[8]), cc = to_d(t[9]);
+    const int incs = atoi(t[10].c_str());
+    const double phi = to_d(t[11]), c = to_d(t[12]), psi = to_d(t[13]), e = to_d(t[14]), v = to_d(t[15]);
+    const int plasits = atoi(t[16].c_str()), cjits = atoi(t[17].c_str());
+    const double plastol = to_d(t[18]), cjtol = to_d(t[19]);
+    if (nod != 20 || iotype != "parafem" || nxe < 5 || nze < 1 || nels % (nxe * nze) != 0 || incs < 1 ||
+        t.size() < (size_t)20 + incs) {
+        set_error("%s.mg: supported: 'parafem' p122 decks of 20-node cubes (nxe >= 5) with incs qinc values",
+                  job.c_str());
+        return PF_FAILURE;
+    }
+    const int nye = nels / nxe / nze;
+    const long long nn = cube_nn(nxe, nye, nze);
+    std::vector<double> gc((size_t)3 * nn, 0.0);
+    std::vector<int> gnum((size_t)20 * nels);
+    for (int iel = 1; iel <= nels; ++iel) {
+        double co[60];
+        int *num = &gnum[20 * (size_t)(iel - 1)];
+        cube_element(iel, nxe, nze, aa, bb, cc, num, co);
+        for (int a = 0; a < 20; ++a)
+            for (int d = 0; d < 3; ++d) gc[3 * (size_t)(num[a] - 1) + d] = co[a + 20 * d];
+    }
+    std::vector<int> fix;
+    cube_fix(nxe, nye, nze, 0, fix);
+    std::vector<int> lnode;
+    std::vector<double> mult;
+    load_p121_pattern(nxe / 5, nxe, nze, lnode, mult);
+    FILE *fd = fopen((job + ".d").c_str(), "w");
+    if (!fd) { set_error("cannot write %s.d", job.c_str()); return PF_FAILURE; }
+    fprintf(fd, "*THREE_DIMENSIONAL\n*NODES\n");
+    for (long long i = 0; i < nn; ++i)
+        fprintf(fd, "%s%s%s%s\n", fmt_I(i + 1, 12).c_str(), fmt_E(gc[3 * i], 14, 6).c_str(),
+                fmt_E(gc[3 * i + 1], 14, 6).c_str(), fmt_E(gc[3 * i + 2], 14, 6).c_str());
+    fprintf(fd, "*ELEMENTS\n");
+    static const int abq[20] = {3, 5, 7, 1, 15, 17, 19, 13, 4, 6, 8, 2, 16, 18, 20, 14, 10, 11, 12, 9};
+    for (int iel = 0; iel < nels; ++iel) {
+        std::string s = fmt_I(iel + 1, 12) + " 3 20 1 ";
+        for (int a = 0; a < 20; ++a) s += fmt_I(gnum[20 * (size_t)iel + abq[a] - 1], 12);
+        fprintf(fd, "%s 1\n", s.c_str());
+    }
+    fclose(fd);
+    FILE *fb = fopen((job + ".bnd").c_str(), "w");
+    if (!fb) { set_error("cannot write %s.bnd", job.c_str()); return PF_FAILURE; }
+    long long nr = 0;
+    for (long long i = 0; i < nn; ++i) {
+        const int *f = &fix[3 * (size_t)i];
+        if (f[0] && f[1] && f[2]) continue;
+        fprintf(fb, "%s%s%s%s\n", fmt_I(i + 1, 8).c_str(), fmt_I(f[0], 6).c_str(), fmt_I(f[1], 6).c_str(),
+                fmt_I(f[2], 6).c_str());
+        ++nr;
+    }
+    fclose(fb);
+    FILE *fl = fopen((job + ".lds").c_str(), "w");
+    if (!fl) { set_error("cannot write %s.lds", job.c_str()); return PF_FAILURE; }
+    for (size_t i = 0; i < lnode.size(); ++i)
+        fprintf(fl, "%s  0.00000000E+00  0.00000000E+00%s\n", fmt_I(lnode[i], 12).c_str(),
+                fmt_E(-mult[i] * aa * bb / 12.0, 16, 8).c_str());
+    fclose(fl);
+    FILE *ft = fopen((job + ".dat").c_str(), "w");
+    if (!ft) { set_error("cannot write %s.dat", job.c_str()); return PF_FAILURE; }
+    fprintf(ft, "'hexahedron'\n2\n1\n%s%s%s%s%s  0  %s\n", fmt_I(nels, 9).c_str(), fmt_I(nn, 9).c_str(),
+            fmt_I(nr, 9).c_str(), fmt_I(nip, 9).c_str(), fmt_I(nod, 9).c_str(),
+            fmt_I((long long)lnode.size(), 9).c_str());
+    fprintf(ft, "%s%s%s%s%s\n", fmt_E(phi, 12, 4).c_str(), fmt_E(c, 12, 4).c_str(), fmt_E(psi, 12, 4).c_str(),
+            fmt_E(e, 12, 4).c_str(), fmt_E(v, 12, 4).c_str());
+    fprintf(ft, "%s%s%s%s%s\n", fmt_I(incs, 6).c_str(), fmt_I(plasits, 6).c_str(), fmt_I(cjits, 6).c_str(),
+            fmt_E(plastol, 12, 4).c_str(), fmt_E(cjtol, 12, 4).c_str());
+    for (int i = 0; i < incs; ++i) fprintf(ft, "%s\n", fmt_E(to_d(t[20 + i]), 12, 4).c_str());
+    fclose(ft);
+    return PF_SUCCESS;
+}
+
+// The p122 job (p122.f90:1-233) with the solve on the GPU: reads job.dat
+// (READ_P122, input.f90, and the qinc values that follow), .d, .bnd, .lds;
+// writes job.res and job.ensi.DISPL-0000nn for every increment.
+extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
+{
+    if (!job_c || !device) { set_error("pf_p122_run: null argument"); return PF_FAILURE; }
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    auto secs = [&](clk::time_point a) { return std::chrono::duration<double>(clk::now() - a).count(); };
+    const std::string job(job_c);
+    std::vector<std::string> t;
+    if (!read_tokens(job + ".dat", t) || t.size() < 21) {
+        set_error("cannot read %s.dat", job.c_str());
+        return PF_FAILURE;
+    }
+    // element, mesh, partition, nels, nn, nr, nip, nod, fixed, loaded, phi, c, psi, e, v,
+    // incs, plasits, cjits, plastol, cjtol, qinc(incs)
+    Deck D;
+    D.element = t[0];
+    D.meshgen = atoi(t[1].c_str());
+    D.partitioner = atoi(t[2].c_str());
+    D.nels = atoi(t[3].c_str());
+    D.nn = atoi(t[4].c_str());
+    D.nr = atoi(t[5].c_str());
+    D.nip = atoi(t[6].c_str());
+    D.nod = atoi(t[7].c_str());
+    const int fixed = atoi(t[8].c_str());
+    D.loaded = atoi(t[9].c_str());
+    const double phi = to_d(t[10]), coh = to_d(t[11]), psi = to_d(t[12]);
+    D.e = to_d(t[13]);
+    D.v = to_d(t[14]);
+    const int incs = atoi(t[15].c_str()), plasits = atoi(t[16].c_str()), cjits = atoi(t[17].c_str());
+    const double plastol = to_d(t[18]), cjtol = to_d(t[19]);
+    if (D.element != "hexahedron" || D.nod != 20 || fixed != 0 || incs < 1 || t.size() < (size_t)20 + incs) {
+        set_error("%s.dat: p122 decks of 20-node hexahedra under load control only (nod=%d, fixed freedoms %d)",
+                  job.c_str(), D.nod, fixed);
+        return PF_FAILURE;
+    }
+    std::vector<double> qinc(incs);
+    for (int i = 0; i < incs; ++i) qinc[i] = to_d(t[20 + i]);
+    if (read_mesh_files(job, D)) return PF_FAILURE;
+    std::vector<int> fix;
+    if (rest_to_fix(D.nn, D.nr, D.rest.data(), fix)) return PF_FAILURE;
+    std::vector<int> g_g((size_t)60 * D.nels);
+    int neq = 0;
+    if (pf_number_equations(&D.nels, &D.nn, D.g_num.data(), fix.data(), g_g.data(), &neq)) return PF_FAILURE;
+    std::vector<double> gcoord((size_t)60 * D.nels);
+    for (size_t e = 0; e < (size_t)D.nels; ++e)
+        for (int a = 0; a < 20; ++a)
+            for (int d = 0; d < 3; ++d)
+                gcoord[60 * e + a + 20 * d] = D.coords[3 * (size_t)(D.g_num[20 * e + a] - 1) + d];
+    std::vector<int> node_eq;
+    number_nodes(D.nn, fix.data(), node_eq);
+    std::vector<double> ld0(neq > 0 ? neq : 1, 0.0);
+    {   // LOAD + SCATTER_NOADD (loading.f90:36-146): assignment, the last node entry wins
+        std::vector<int> node_slot((size_t)D.nn + 1, -1);
+        for (int i = 0; i < D.loaded; ++i)
+            if (D.lnode[i] >= 1 && D.lnode[i] <= D.nn) node_slot[D.lnode[i]] = i;
+        for (int nd = 1; nd <= D.nn; ++nd) {
+            const int i = node_slot[nd];
+            if (i < 0) continue;
+            for (int d = 0; d < 3; ++d) {
+                const int eq = node_eq[(size_t)(nd - 1) * 3 + d];
+                if (eq > 0) ld0[eq - 1] = D.lval[3 * (size_t)i + d];
+            }
+        }
+    }
+    void *ctx = nullptr;
+    int rc = PF_FAILURE, done = 0, one = 1, flags = 0;
+    std::vector<double> res((size_t)6 * incs, 0.0), totd((size_t)(neq > 0 ? neq : 1) * incs, 0.0);
+    double t_setup = 0.0;
+    do {
+        if (pf_ctx_create(device, &ctx)) break;
+        if (pf_setup(&ctx, &D.nels, &D.nn, &neq, D.g_num.data(), g_g.data(), gcoord.data())) break;
+        if (pf_set_material(&ctx, &one, &D.e, &D.v)) break;
+        if (pf_form_storkm(&ctx, &D.nip, &flags)) break;
+        t_setup = secs(t0);
+        int incs_i = incs;
+        if (pf_p122_solve(&ctx, &D.nip, &phi, &coh, &psi, &incs_i, qinc.data(), &plasits, &cjits, &plastol, &cjtol,
+                          ld0.data(), res.data(), totd.data(), &done))
+            break;
+        rc = PF_SUCCESS;
+    } while (0);
+    if (ctx) pf_ctx_destroy(&ctx);
+    if (rc) return PF_FAILURE;
+    const double pi = std::acos(-1.0), snph = std::sin(phi * pi / 180.0);
+    const double dt = 4.0 * (1.0 + D.v) * (1.0 - 2.0 * D.v) / (D.e * (1.0 - 2.0 * D.v + snph * snph));
+    FILE *fr = fopen((job + ".res").c_str(), "w");
+    if (!fr) { set_error("cannot write %s.res", job.c_str()); return PF_FAILURE; }
+    fprintf(fr, "This job ran on %s  processes\n", fmt_I(1, 5).c_str());
+    fprintf(fr, "There are %s nodes%s restrained and   %s equations\n", fmt_I(D.nn, 7).c_str(),
+            fmt_I(D.nr, 7).c_str(), fmt_I(neq, 7).c_str());
+    fprintf(fr, "Time after setup is:%s\n", fmt_F(t_setup, 10, 4).c_str());
+    fprintf(fr, "The critical timestep is   %s\n", fmt_E(dt, 12, 4).c_str());
+    for (int iy = 1; iy <= done; ++iy) {
+        const double *o = &res[6 * (size_t)(iy - 1)];
+        fprintf(fr, "\nLoad Increment   %s\n", fmt_I(iy, 5).c_str());
+        fprintf(fr, "The displacement is  %s\n", fmt_E(o[0], 12, 4).c_str());
+        fprintf(fr, "  sigma z    sigma x     sigma y\n%s%s%s\n", fmt_E(o[1], 12, 4).c_str(),
+                fmt_E(o[2], 12, 4).c_str(), fmt_E(o[3], 12, 4).c_str());
+        fprintf(fr, "The total number of cj iterations was  %s\n", fmt_I((long long)o[4], 12).c_str());
+        fprintf(fr, "The number of plastic iterations was  %s\n", fmt_I((long long)o[5], 12).c_str());
+        fprintf(fr, "cj iterations per plastic iteration were %s\n", fmt_F(o[4] / o[5], 11, 2).c_str());
+        char name[64];
+        snprintf(name, sizeof name, ".ensi.DISPL-%06d", iy);
+        FILE *fe = fopen((job + name).c_str(), "w");
+        if (!fe) { fclose(fr); set_error("cannot write the displacement file"); return PF_FAILURE; }
+        fprintf(fe, "Alya Ensight Gold --- Vector per-node variable file\npart\n    1\ncoordinates\n");
+        const double *x = &totd[(size_t)neq * (iy - 1)];
+        for (int d = 0; d < 3; ++d)
+            for (int nd = 0; nd < D.nn; ++nd) {
+                const int eq = node_eq[(size_t)nd * 3 + d];
+                fprintf(fe, "%s\n", fmt_E(eq > 0 ? x[eq - 1] : 0.0, 12, 5).c_str());
+            }
+        fclose(fe);
+    }
+    fprintf(fr, "This analysis took: %s\n", fmt_F(secs(t0), 10, 4).c_str());
+    fclose(fr);
+    if (incs_out) *incs_out = done;
     return PF_SUCCESS;
 }

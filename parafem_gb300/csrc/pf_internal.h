@@ -115,8 +115,9 @@ int launch_elem(Ctx &c, int prec, const double *p);
 int launch_scatter(Ctx &c, int prec, int mode, const double *p_or_f, double *out);
 int launch_matvec(Ctx &c, int prec, const double *p, double *u);
 int launch_residual(Ctx &c, const double *f, const double *x, double *rres);
-int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol,
-                    int limit);
+int launch_scatter_add64(Ctx &c, double *out);   // out += scatter of the FP64 element results in utemp
+int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit,
+                    bool keep_x = false);
 int launch_update1(Ctx &c, double *xsol);
 int launch_update2(Ctx &c);   // update2 + the one-block finish kernel
 int launch_pcg_iteration(Ctx &c, int prec, double *xsol);

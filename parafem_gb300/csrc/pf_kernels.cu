@@ -275,6 +275,7 @@ k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
 // flight together.
 //   MODE 0: out = u (restrained 0), partial p.u       (pf = p)
 //   MODE 1: out = f - u (restrained 0), partial out.out (pf = f)
+//   MODE 2: out += u at free dofs, no partials          (pf unused)
 template <typename UT, int MODE>
 __global__ void __launch_bounds__(256)
 k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
@@ -331,13 +332,16 @@ k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
                 const double uv = fr ? a[d] : 0.0;
                 out[s] = uv;
                 loc = fma(pf[s], uv, loc);
-            } else {
+            } else if (MODE == 1) {
                 const double rv = fr ? pf[s] - a[d] : 0.0;
                 out[s] = rv;
                 loc = fma(rv, rv, loc);
+            } else {   // MODE 2: out += sum (SCATTER's accumulation into an existing vector)
+                if (fr) out[s] = out[s] + a[d];
             }
         }
     }
+    if (MODE == 2) return;   // no partial sums (the kernel has no block barrier after this point)
     double v[1] = {loc};
     block_reduce<1>(v, 0u);
     if (threadIdx.x == 0) part[blockIdx.x] = v[0];
@@ -349,13 +353,13 @@ k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
 __global__ void __launch_bounds__(256)
 k_pcg_init(int ns, const double *__restrict__ rhs, const double *__restrict__ dinv,
            double *__restrict__ x, double *__restrict__ r, double *__restrict__ d,
-           double *__restrict__ p, double *__restrict__ part, int G)
+           double *__restrict__ p, double *__restrict__ part, int G, int keep_x)
 {
     double rd = 0.0, rr = 0.0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
         const double rv = rhs[s];
         const double dv = dinv[s] * rv;
-        x[s] = 0.0;
+        if (!keep_x) x[s] = 0.0;
         r[s] = rv;
         d[s] = dv;
         p[s] = dv;
@@ -757,6 +761,14 @@ int launch_matvec(Ctx &c, int prec, const double *p, double *u)
     return check_launch(c, "k_scatter");
 }
 
+// out += K x (FP64 storkm) at the free dofs: SCATTER accumulating into out
+int launch_scatter_add64(Ctx &c, double *out)
+{
+    k_scatter<double, 2><<<c.Gs, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, (const double *)c.utemp,
+                                                     c.freemask, nullptr, out, c.part_s, nullptr);
+    return check_launch(c, "k_scatter");
+}
+
 int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
 {
     if (c.kind == KIND_SCALAR8) {
@@ -775,10 +787,10 @@ int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
     return check_launch(c, "k_scatter");
 }
 
-int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit)
+int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit, bool keep_x)
 {
     c.stop_mode = stop_mode;
-    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G);
+    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G, keep_x ? 1 : 0);
     if (check_launch(c, "k_pcg_init")) return 1;
     k_pcg_init2<<<1, 256, 0, c.stream>>>(c.st, c.part_u, c.G, stop_mode, tol, limit);
     return check_launch(c, "k_pcg_init2");

@@ -150,19 +150,34 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
     };
 
     if (warp == kProdWarp) {
-        int nd = lane < 20 && nmine > 0 ? conn[(size_t)elem(0) * 20 + lane] : 0;
-        int t = 0;
-        for (; t < nmine; ++t) {
-            const int s = t % kNst;
-            if (t >= kNst && !wait(&st_empty[s], (uint32_t)((t / kNst - 1) & 1))) break;
-            unsigned char *dst = stg + s * kStage;
-            if (lane == 0) mbar_expect_tx(&st_full[s], kStage);
-            __syncwarp();
-            if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &st_full[s]);
-            if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * nd * KR, 384, &st_full[s]);
-            if (t + 1 < nmine && lane < 20) nd = conn[(size_t)elem(t + 1) * 20 + lane];
+        // the connectivity (lane a: node a of the element) is loaded kCD
+        // elements ahead, so its latency is not paid once per element
+        constexpr int kCD = 8;
+        int ndr[kCD];
+#pragma unroll
+        for (int j = 0; j < kCD; ++j) ndr[j] = (lane < 20 && j < nmine) ? conn[(size_t)elem(j) * 20 + lane] : 0;
+        int issued = 0;   // elements whose copies are in flight or done
+        bool stop = false;
+        for (int t0 = 0; t0 < nmine && !stop; t0 += kCD) {
+#pragma unroll
+            for (int j = 0; j < kCD; ++j) {
+                const int t = t0 + j;
+                if (t >= nmine) break;
+                const int s = t % kNst;
+                if (t >= kNst && !wait(&st_empty[s], (uint32_t)((t / kNst - 1) & 1))) {
+                    stop = true;
+                    break;
+                }
+                unsigned char *dst = stg + s * kStage;
+                if (lane == 0) mbar_expect_tx(&st_full[s], kStage);
+                __syncwarp();
+                if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &st_full[s]);
+                if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * ndr[j] * KR, 384, &st_full[s]);
+                ndr[j] = (lane < 20 && t + kCD < nmine) ? conn[(size_t)elem(t + kCD) * 20 + lane] : 0;
+                issued = t + 1;
+            }
         }
-        if (lane == 0) s_count[0] = t;
+        if (lane == 0) s_count[0] = issued;
     } else if (warp < kBuildWarps) {
         // this thread's A task: row i, K-values 8q..8q+7; K(i,k) = U(min, max)
         // at T(max) + min, and entries outside 60 x 60 read the zero pad at 1830

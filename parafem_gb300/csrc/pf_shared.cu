@@ -12,12 +12,11 @@
 //                     kernel; tiles of 128 elements' gathered p values are
 //                     split the same way; the six products of order <= 2^-16
 //                     accumulate in FP32 in TMEM (M = 128 with rows 60..127
-//                     unused, N = 128 elements, K = 64).  The p values of
-//                     tile t+1 are loaded into registers while tile t's MMAs
-//                     run and tile t-1's accumulator is read back; the
-//                     connectivity arrives by bulk copy two tiles ahead.
-//                     Results are written in the node-padded FP32 layout the
-//                     scatter reads.
+//                     unused, N = 128 elements, K = 64).  Warp-specialised:
+//                     connectivity copies, gather + split, MMA issue and the
+//                     TMEM read-back overlap across tiles through mbarrier
+//                     rings.  Results are written in the node-padded FP32
+//                     layout the scatter reads.
 #include "pf_device.cuh"
 #include "pf_tc.cuh"
 
@@ -33,15 +32,28 @@ constexpr int kSBufA = 4 * kSTermA;         // 3 terms + 8 KB read as rows 64..1
 constexpr int kSTermB = kNT * 64 * 2;       // 16 KB: 128 elements x 64 K
 constexpr int kSBufB = 3 * kSTermB;
 constexpr int kSConn = kNT * 20 * 4;        // 10 KB: connectivity of one tile
-constexpr int kSNC = 3;                     // connectivity buffers: tiles t, t+1, t+2
+constexpr int kSNB = 3;                     // B tile sets in flight
+constexpr int kSNC = 4;                     // connectivity buffers in flight
+constexpr int kSNA = 4;                     // TMEM accumulators (128 columns each, all 512)
+constexpr int kSGather = 16;                // warps 0-15 gather p and split it (two tasks per thread)
+constexpr int kSEpi0 = 16;                  // warps 16-17 read TMEM lanes 0..63 back
+constexpr int kSProd = 18;                  // warp 18 copies the connectivity
+constexpr int kSMma = 19;                   // warp 19, lane 0 issues the MMAs
+constexpr int kSThreads = 20 * 32;
 constexpr int kSOffB = kSBufA;
-constexpr int kSOffC = kSOffB + 2 * kSBufB;
+constexpr int kSOffC = kSOffB + kSNB * kSBufB;
 constexpr int kSOffAux = kSOffC + kSNC * kSConn;
-constexpr int kSSmem = kSOffAux + 128;
-constexpr int kSThreads = 256;
+constexpr int kSSmem = kSOffAux + 256;
 constexpr uint32_t kSIdesc = idesc_bf16(128, kNT);
 static_assert(kSOffC % 16 == 0 && kSConn % 16 == 0 && kSOffAux % 8 == 0, "bulk-copy alignment");
 static_assert(kSSmem <= 227 * 1024, "shared memory per CTA");
+static_assert(kSGather * 32 * 2 == kNT * 8, "two B tasks (element, 8 dofs) per gather thread");
+static_assert(kSEpi0 % 4 == 0, "epilogue warps must reach TMEM lanes 0..63");
+
+__device__ __forceinline__ void mbar_arrive1(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 
 }  // namespace
 
@@ -80,28 +92,42 @@ k_elem_shared64(int nels, const double *__restrict__ km, const int *__restrict__
 
 // u_e = km p_e on the tensor cores for every element (FP32 results,
 // node-padded: row i of element e at e*80 + (i/3)*4 + i%3).
-// One persistent CTA of 8 warps per SM walks the tiles T = blockIdx.x +
-// t * gridDim.x.  Every wait is bounded; a wait that runs out sets the
-// device error word to 3 and the CTA drains its copies and MMAs (bounded),
-// frees its TMEM and returns.
+// One persistent CTA of 20 warps per SM walks the tiles T = blockIdx.x +
+// t * gridDim.x with warp-specialised roles linked by mbarriers:
+//   warp 18      bulk-copies each tile's connectivity into a ring of kSNC;
+//   warps 0-15   gather the tile's p values (two 8-dof tasks per thread),
+//                split them into three BF16 terms and write a ring of kSNB
+//                B tile sets;
+//   warp 19      one thread issues the six products (24 MMAs, M=128, N=128,
+//                K=16) into a ring of kSNA TMEM accumulators;
+//   warps 16-17  read TMEM lanes 0..63 back and store the results.
+// Every wait is bounded.  A wait that runs out sets a shared failure flag
+// that every role checks before its next wait, writes 3 to the device error
+// word, and the CTA waits (bounded) for the copies and MMAs it has in flight
+// before it frees its TMEM and returns.
 __global__ void __launch_bounds__(kSThreads, 1)
 k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict__ conn,
                  const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
                  int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
-    int *s_stop = reinterpret_cast<int *>(sm + kSOffAux + 64);
-    if (threadIdx.x == 0) *s_stop = st ? st->stop : 0;
-    __syncthreads();
-    if (*s_stop) return;   // uniform: read once per block
     unsigned char *A = sm;
     unsigned char *B = sm + kSOffB;
-    int *cs = reinterpret_cast<int *>(sm + kSOffC);                  // [3][128*20]
-    uint64_t *cfull = reinterpret_cast<uint64_t *>(sm + kSOffAux);   // 3: connectivity copies
-    uint64_t *mbar = cfull + kSNC;                                   // 2: MMA completion
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
-    int *s_fail = reinterpret_cast<int *>(tslot + 1);
+    int *cs = reinterpret_cast<int *>(sm + kSOffC);                   // [kSNC][128*20]
+    uint64_t *c_full = reinterpret_cast<uint64_t *>(sm + kSOffAux);
+    uint64_t *c_empty = c_full + kSNC;
+    uint64_t *b_full = c_empty + kSNC;
+    uint64_t *b_empty = b_full + kSNB;
+    uint64_t *a_full = b_empty + kSNB;
+    uint64_t *a_empty = a_full + kSNA;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(a_empty + kSNA);
+    volatile int *s_fail = reinterpret_cast<volatile int *>(tslot + 1);
+    int *s_count = reinterpret_cast<int *>(tslot + 2);   // [0] copies issued, [1] MMA groups committed
+    int *s_stop = s_count + 2;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) *s_stop = st ? st->stop : 0;
+    __syncthreads();
+    if (*s_stop) return;   // uniform: read once per block
     const int ntiles = (nels + kNT - 1) / kNT;
     const int nmine = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto tile = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
@@ -110,10 +136,8 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     // km once: K(i,k) = km32[i + 60k], three BF16 terms, rows 0..63 x K 0..63
     for (int i = tid; i < kSOffC / 16; i += kSThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int task = tid + kSThreads * h;
-        const int i = task & 63, q = task >> 6;
+    if (tid < 512) {
+        const int i = tid & 63, q = tid >> 6;
         float xv[8];
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
@@ -122,132 +146,146 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
         }
         split3_store8(xv, A + kmajor_off(i, 8 * q), kSTermA);
     }
-    if (warp == 0) tmem_alloc(tslot, 256);
+    if (warp == 0) tmem_alloc(tslot, 512);
     if (tid == 0) {
-        for (int b = 0; b < kSNC; ++b) mbar_init(&cfull[b], 1);
-        mbar_init(&mbar[0], 1);
-        mbar_init(&mbar[1], 1);
+        for (int i = 0; i < kSNC; ++i) {
+            mbar_init(&c_full[i], 1);
+            mbar_init(&c_empty[i], kSGather);
+        }
+        for (int i = 0; i < kSNB; ++i) {
+            mbar_init(&b_full[i], kSGather);
+            mbar_init(&b_empty[i], 1);
+        }
+        for (int i = 0; i < kSNA; ++i) {
+            mbar_init(&a_full[i], 1);
+            mbar_init(&a_empty[i], 2);
+        }
         mbar_fence_init();
         *s_fail = 0;
+        s_count[0] = s_count[1] = 0;
     }
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-
-    auto issue_conn = [&](int t) {   // thread 0: connectivity of tile t into buffer t % kSNC
-        const int b = t % kSNC;
-        const uint32_t bytes = (uint32_t)tile_n(t) * 80u;
-        mbar_expect_tx(&cfull[b], bytes);
-        bulk_g2s(cs + b * kNT * 20, conn + (size_t)tile(t) * kNT * 20, bytes, &cfull[b]);
+    auto wait = [&](uint64_t *bar, uint32_t parity) {
+        if (*s_fail) return false;
+        if (mbar_wait(bar, parity)) return true;
+        *s_fail = 1;
+        return false;
     };
-    // p values of tile t into registers: element n = task & 127, dofs 8q..8q+7
-    float xv[4][8];
-    auto load_tile = [&](int t) {
-        if (!mbar_wait(&cfull[t % kSNC], (uint32_t)((t / kSNC) & 1))) atomicOr(s_fail, 1);
-        const int *ct = cs + (t % kSNC) * kNT * 20;
-        const int n_here = tile_n(t);
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            const int task = tid + kSThreads * h;
-            const int n = task & (kNT - 1), q = task >> 7;
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                const int c = 8 * q + g;
-                xv[h][g] = 0.f;
-                if (c < 60 && n < n_here) xv[h][g] = (float)p[(size_t)3 * ct[n * 20 + c / 3] + c % 3];
+
+    if (warp == kSProd) {
+        int t = 0;
+        if (lane == 0) {
+            for (; t < nmine; ++t) {
+                const int b = t % kSNC;
+                if (t >= kSNC && !wait(&c_empty[b], (uint32_t)((t / kSNC - 1) & 1))) break;
+                const uint32_t bytes = (uint32_t)tile_n(t) * 80u;
+                mbar_expect_tx(&c_full[b], bytes);
+                bulk_g2s(cs + b * kNT * 20, conn + (size_t)tile(t) * kNT * 20, bytes, &c_full[b]);
             }
+            s_count[0] = t;
         }
-    };
-    if (tid == 0)
-        for (int t = 0; t < 2 && t < nmine; ++t) issue_conn(t);
-    if (nmine > 0) load_tile(0);
-
-    uint32_t mphase[2] = {0, 0};
-    auto epilogue = [&](int t, int buf) {
-        // TMEM lanes 0..63 hold rows 0..63: warps 0, 1 (columns 0..63) and 4, 5 (64..127)
-        if ((warp & 3) < 2) {
-            if (!mbar_wait(&mbar[buf], mphase[buf])) atomicOr(s_fail, 1);
+        __syncwarp();
+    } else if (warp < kSGather) {
+        for (int t = 0; t < nmine; ++t) {
+            const int cb = t % kSNC, bb = t % kSNB;
+            if (!wait(&c_full[cb], (uint32_t)((t / kSNC) & 1))) break;
+            if (t >= kSNB && !wait(&b_empty[bb], (uint32_t)((t / kSNB - 1) & 1))) break;
+            const int *ct = cs + cb * kNT * 20;
+            const int n_here = tile_n(t);
+            float xv[2][8];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int task = tid + kSGather * 32 * h;
+                const int n = task & (kNT - 1), q = task >> 7;
+#pragma unroll
+                for (int g = 0; g < 8; ++g) {
+                    const int c = 8 * q + g;
+                    xv[h][g] = (c < 60 && n < n_here) ? (float)p[(size_t)3 * ct[n * 20 + c / 3] + c % 3] : 0.f;
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&c_empty[cb]);   // connectivity read
+            unsigned char *Bb = B + bb * kSBufB;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int task = tid + kSGather * 32 * h;
+                const int n = task & (kNT - 1), q = task >> 7;
+                split3_store8(xv[h], Bb + kmajor_off(n, 8 * q), kSTermB);
+            }
+            fence_proxy_async();   // this thread's tile writes -> the tensor cores
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&b_full[bb]);
+        }
+    } else if (warp == kSMma) {
+        int t = 0;
+        if (lane == 0) {
+            for (; t < nmine; ++t) {
+                const int bb = t % kSNB, a = t % kSNA;
+                if (!wait(&b_full[bb], (uint32_t)((t / kSNB) & 1))) break;
+                if (t >= kSNA && !wait(&a_empty[a], (uint32_t)((t / kSNA - 1) & 1))) break;
+                tc_fence_after();
+                const uint32_t b0 = smem_u32(B + bb * kSBufB), a0 = smem_u32(A);
+                // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
+                const int ta[6] = {0, 0, 1, 0, 1, 2};
+                const int tb[6] = {0, 1, 0, 2, 1, 0};
+                uint32_t acc = 0;
+#pragma unroll
+                for (int tt = 0; tt < 6; ++tt)
+#pragma unroll
+                    for (int ks = 0; ks < 4; ++ks) {
+                        mma_bf16(tmem + (uint32_t)(a * kNT), umma_desc(a0 + ta[tt] * kSTermA + ks * 256, 128, 1024),
+                                 umma_desc(b0 + tb[tt] * kSTermB + ks * 256, 128, 1024), kSIdesc, acc);
+                        acc = 1;
+                    }
+                mma_commit(&b_empty[bb]);
+                mma_commit(&a_full[a]);
+            }
+            s_count[1] = t;
+        }
+        __syncwarp();
+    } else if (warp == kSEpi0 || warp == kSEpi0 + 1) {
+        const int row = 32 * (warp - kSEpi0) + lane;   // TMEM lanes 0..63 = rows
+        const size_t roff = (size_t)(row / 3) * 4 + row % 3;
+        for (int t = 0; t < nmine; ++t) {
+            const int a = t % kSNA;
+            if (!wait(&a_full[a], (uint32_t)((t / kSNA) & 1))) break;
             tc_fence_after();
-            const int row = 32 * (warp & 3) + lane;
             const int n_here = tile_n(t);
             const size_t e0 = (size_t)tile(t) * kNT;
-            const int col0 = (warp >> 2) * 64;
-            const size_t roff = (size_t)(row / 3) * 4 + row % 3;
 #pragma unroll 1
-            for (int ch = 0; ch < 4; ++ch) {
+            for (int ch = 0; ch < kNT / 16; ++ch) {
                 float v[16];
-                tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(buf * kNT + col0 + 16 * ch),
-                                   v);
+                tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * (warp - kSEpi0)) << 16) + (uint32_t)(a * kNT + 16 * ch), v);
                 if (row < 60) {
 #pragma unroll
                     for (int x = 0; x < 16; ++x) {
-                        const int n = col0 + 16 * ch + x;
+                        const int n = 16 * ch + x;
                         if (n < n_here) ut[(e0 + n) * 80 + roff] = v[x];
                     }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&a_empty[a]);
         }
-        mphase[buf] ^= 1;
-    };
-
-    int t = 0;
-    for (; t < nmine; ++t) {
-        const int buf = t & 1;
-        unsigned char *Bb = B + buf * kSBufB;
-        // B: the p values of tile t (loaded during the previous iteration), split into three terms
-#pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            const int task = tid + kSThreads * h;
-            const int n = task & (kNT - 1), q = task >> 7;
-            split3_store8(xv[h], Bb + kmajor_off(n, 8 * q), kSTermB);
-        }
-        fence_proxy_async();
-        __syncthreads();
-        if (*s_fail) break;
-        if (tid == 0) {
-            tc_fence_after();
-            // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
-            const int ta[6] = {0, 0, 1, 0, 1, 2};
-            const int tb[6] = {0, 1, 0, 2, 1, 0};
-            uint32_t acc = 0;
-            for (int tt = 0; tt < 6; ++tt) {
-                const uint32_t a0 = smem_u32(A + ta[tt] * kSTermA), b0 = smem_u32(Bb + tb[tt] * kSTermB);
-                for (int ks = 0; ks < 4; ++ks) {
-                    mma_bf16(tmem + (uint32_t)(buf * kNT), umma_desc(a0 + ks * 256, 128, 1024),
-                             umma_desc(b0 + ks * 256, 128, 1024), kSIdesc, acc);
-                    acc = 1;
-                }
-            }
-            mma_commit(&mbar[buf]);
-            // connectivity of tile t+2 into the buffer tile t-1 used (read before the last barrier)
-            if (t + 2 < nmine) {
-                fence_proxy_async();
-                issue_conn(t + 2);
-            }
-        }
-        if (t + 1 < nmine) load_tile(t + 1);   // in flight during the read-back below
-        if (t > 0) epilogue(t - 1, buf ^ 1);
-        tc_fence_before();
-        __syncthreads();
     }
-    if (!*s_fail && t > 0) {
-        epilogue(t - 1, (t - 1) & 1);
-        tc_fence_before();
-        __syncthreads();
-    }
+    __syncthreads();
     if (*s_fail) {
         if (tid == 0) {
             atomicExch(err, 3);
-            for (int k = t + 1; k < nmine && k < t + 3; ++k) mbar_wait(&cfull[k % kSNC], (uint32_t)((k / kSNC) & 1));
-            mbar_wait(&mbar[0], mphase[0]);
-            mbar_wait(&mbar[1], mphase[1]);
+            for (int t = s_count[0] - kSNC; t < s_count[0]; ++t)
+                if (t >= 0) mbar_wait(&c_full[t % kSNC], (uint32_t)((t / kSNC) & 1));
+            for (int t = s_count[1] - kSNA; t < s_count[1]; ++t)
+                if (t >= 0) mbar_wait(&a_full[t % kSNA], (uint32_t)((t / kSNA) & 1));
         }
         __syncthreads();
     }
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 256);
+    if (warp == 0) tmem_dealloc(tmem, 512);
 }
 
 // ediag[e*60 + i] = km(i,i) for every element

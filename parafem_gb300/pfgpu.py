@@ -81,6 +81,7 @@ _SIGS = {
     "pf_p12meshgen": [ctypes.c_char_p],
     "pf_p121_run": [ctypes.c_char_p, _IP, _IP, _IP, _DP],
     "pf_p123_run": [ctypes.c_char_p, _IP, _IP, ctypes.c_void_p],
+    "pf_p122_run": [ctypes.c_char_p, _IP, _IP],
     "pf_mesh_box8": [_IP, _IP, _IP, _DP, _DP, _DP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_box8_restraints": [_IP, _IP, _IP, ctypes.c_void_p],
     "pf_number_equations1": [_IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
@@ -88,10 +89,13 @@ _SIGS = {
     "pf_form_storkc": [_VPP, _IP, _DP, _DP, _DP],
     "pf_get_storkc": [_VPP, _IP, _IP, ctypes.c_void_p],
     "pf_set_fixed": [_VPP, _IP, ctypes.c_void_p, _DP],
+    "pf_p122_solve": [_VPP, _IP, _DP, _DP, _DP, _IP, ctypes.c_void_p, _IP, _IP, _DP, _DP, ctypes.c_void_p,
+                      ctypes.c_void_p, ctypes.c_void_p, _IP],
     "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_cube_restraints": [_IP, _IP, _IP, _IP, ctypes.c_void_p],
     "pf_number_equations": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
     "pf_cube_top_pressure": [_IP, _IP, _IP, _DP, _DP, _DP, ctypes.c_void_p, _IP, ctypes.c_void_p],
+    "pf_patch_loads": [_IP, _IP, _DP, _IP, ctypes.c_void_p, ctypes.c_void_p, _IP, ctypes.c_void_p],
     "pf_random_material": [_IP, _LLP, _DP, _DP, _DP, _DP, ctypes.c_void_p, ctypes.c_void_p],
 }
 
@@ -187,6 +191,16 @@ def cube_top_pressure(nxe, nze, g_g, neq, p, aa=1.0, bb=1.0, r=None):
     return r
 
 
+def patch_loads(nxe, nze, g_num, g_g, neq, factor):
+    """load_p121's top-face patch as a load vector (see pf_patch_loads)."""
+    g_num, pn = _arr(g_num, np.int32)
+    g_g, pg = _arr(g_g, np.int32)
+    r = np.zeros(neq)
+    _check(lib().pf_patch_loads(_i(nxe), _i(nze), _d(factor), _i(g_num.shape[0]), pn, pg, _i(neq), r.ctypes.data),
+           "pf_patch_loads")
+    return r
+
+
 def random_material(nels, seed, e_lo, e_hi, v_lo, v_hi):
     e = np.zeros(nels)
     v = np.zeros(nels)
@@ -270,6 +284,19 @@ class Solver:
     def set_fixed(self, eqs, penalty=1.0e20):
         eqs, pe = _arr(np.atleast_1d(eqs), np.int32)
         _check(lib().pf_set_fixed(self._ref, _i(eqs.size), pe, _d(penalty)), "pf_set_fixed")
+
+    def p122_solve(self, nip, phi, c, psi, qinc, plasits, cjits, plastol, cjtol, ld0, keep_totd=False):
+        """p122's load increments (see pf_p122_solve): results (incs_done, 6), totd (incs_done, neq) or None."""
+        qinc = np.ascontiguousarray(np.atleast_1d(qinc), dtype=np.float64)
+        ld0 = np.ascontiguousarray(ld0, dtype=np.float64)
+        res = np.zeros((qinc.size, 6))
+        totd = np.zeros((qinc.size, self.neq)) if keep_totd else None
+        done = ctypes.c_int(0)
+        _check(lib().pf_p122_solve(self._ref, _i(nip), _d(phi), _d(c), _d(psi), _i(qinc.size), qinc.ctypes.data,
+                                   _i(plasits), _i(cjits), _d(plastol), _d(cjtol), ld0.ctypes.data, res.ctypes.data,
+                                   totd.ctypes.data if keep_totd else None, ctypes.byref(done)), "pf_p122_solve")
+        n = done.value
+        return res[:n], (totd[:n] if keep_totd else None)
 
     def set_material(self, e, v):
         e, pe = _arr(np.atleast_1d(e), np.float64)
@@ -559,6 +586,12 @@ def p123_run(job: str, device: int = 0):
     pot = np.zeros(4)
     _check(lib().pf_p123_run(os.fsencode(job), _i(device), ctypes.byref(it), pot.ctypes.data), "pf_p123_run")
     return it.value, pot
+
+
+def p122_run(job: str, device: int = 0):
+    incs = ctypes.c_int(0)
+    _check(lib().pf_p122_run(os.fsencode(job), _i(device), ctypes.byref(incs)), "pf_p122_run")
+    return incs.value
 
 
 def cube_problem(nxe, nye, nze, bc=1, pressure=None, aa=1.0, bb=1.0, cc=1.0):

@@ -7,6 +7,7 @@ Reads the reference's own recorded runs (examples/5th_ed/p121, p123) and writes
                         inputs, and sha256 of the demo deck files
   p121_demo_displ.npz   the demo displacement field (p121_demo.ensi.DISPL-000001)
   p123_golden.json      .res figures of the p123 book run and its .mg input
+  p122_golden.json      per-increment .res figures of the p122 book run and its .mg input
 The fixtures let the tests run where the reference tree is absent.
 """
 from __future__ import annotations
@@ -103,6 +104,38 @@ def main123(root):
     print("wrote", os.path.join(HERE, "p123_golden.json"))
 
 
+def parse_res122(path):
+    txt = open(path).read()
+    lines = txt.splitlines()
+    out = {}
+    m = re.search(r"There are\s+(\d+) nodes\s+(\d+) restrained and\s+(\d+) equations", txt)
+    out["nn"], out["nr"], out["neq"] = (int(g) for g in m.groups())
+    out["processes"] = int(re.search(r"This job ran on\s+(\d+)\s+processes", txt).group(1))
+    out["dt_text"] = re.search(r"The critical timestep is\s+(\S+)", txt).group(1)
+    incs = []
+    for k, ln in enumerate(lines):
+        if ln.startswith("Load Increment"):
+            inc = {"increment": int(ln.split()[-1])}
+            inc["displacement_text"] = lines[k + 1].split()[-1]
+            inc["stress_text"] = lines[k + 3].split()
+            inc["cj_iterations"] = int(lines[k + 4].split()[-1])
+            inc["plastic_iterations"] = int(lines[k + 5].split()[-1])
+            incs.append(inc)
+    out["increments"] = incs
+    return out
+
+
+def main122(root):
+    ex = os.path.join(root, "examples", "5th_ed", "p122", "book")
+    gold = {"source": "examples/5th_ed/p122/book of the ParaFEM tree",
+            "book": parse_res122(os.path.join(ex, "p122.res")),
+            "book_mg": open(os.path.join(ex, "p122.mg")).read()}
+    with open(os.path.join(HERE, "p122_golden.json"), "w") as f:
+        json.dump(gold, f, indent=1, sort_keys=True)
+    print("wrote", os.path.join(HERE, "p122_golden.json"))
+
+
 if __name__ == "__main__":
     main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
     main123(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
+    main122(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
