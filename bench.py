@@ -63,6 +63,9 @@ def parse_args():
                     help="serving: 32 = FP32 products with FP64 residual replacement, 64 = FP64")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--limit", type=int, default=50000, help="multirhs60: PCG iteration limit of the block solves")
+    ap.add_argument("--tuning", type=int, default=-1, choices=[-1, 0, 1, 2],
+                    help="cube100: force the packed-symmetric kernel configuration (0: 14x2, 1: 12x2, 2: 8x3); "
+                         "-1 keeps the autotuner's choice")
     return ap.parse_args()
 
 
@@ -280,6 +283,9 @@ def run_gb300(args, rank, world, local, dist):
     nels = n ** 3
     r = prob["r"]
     extra = {"host_setup_s": t_host, "storkm_formation_s": t_form, "autotune": s.tuning()}
+    if args.tuning >= 0:
+        s.set_tuning(args.tuning)
+        extra["forced_tuning"] = args.tuning
 
     # e2e: one full mixed solve through the C-ABI with host buffers
     solves = {}
@@ -304,6 +310,13 @@ def run_gb300(args, rank, world, local, dist):
                           "relres": rel_64}
         solves["mixed_over_fp64_time"] = t_mixed / t_64
         solves["mixed_vs_fp64_rel_err_2"] = float(np.linalg.norm(x - x64) / np.linalg.norm(x64))
+        # accuracy: both solutions against FP64 converged to relres 1e-12
+        xr, it_r, rel_r = s.solve(r, 1e-12, 50000, P.MODE_FP64_RES)
+        nr_ = np.linalg.norm(xr)
+        solves["fp64_1e-12"] = {"iters": it_r, "relres": rel_r, "device_s": s.stats()["solve_ms"] / 1e3}
+        solves["mixed_vs_fp64_1e-12_rel_err_2"] = float(np.linalg.norm(x - xr) / nr_)
+        solves["mixed_vs_fp64_1e-12_rel_err_inf"] = float(np.abs(x - xr).max() / np.abs(xr).max())
+        solves["fp64_1e-8_vs_fp64_1e-12_rel_err_2"] = float(np.linalg.norm(x64 - xr) / nr_)
 
     # timed steps: K iterations of the FP32-storkm PCG, device resident
     s.bench_iterations(32, max(args.warmup, 3))
