@@ -63,7 +63,8 @@ def test_p122_job_writes_res_and_displacements(tmp_path):
     ref, tref = O.run_p122(prob, 8, 20.0, 30.0, 5.0, 1.0e4, 0.3, [200.0, 100.0], 200, 1000, 1e-4, 1e-6,
                            keep_totd=True)
     res = open(job + ".res").read().splitlines()
-    assert res[1] == "There are    4961 nodes   1541 restrained and     %7d equations" % prob["neq"]
+    # p122.f90:62-63 writes '(A,3(I7,A))' with " restrained and   " before neq.
+    assert res[1] == "There are    4961 nodes   1541 restrained and   %7d equations" % prob["neq"]
     incs = [k for k, ln in enumerate(res) if ln.startswith("Load Increment")]
     assert len(incs) == 2
     for i, k in enumerate(incs):
