@@ -2,22 +2,30 @@
 // staged through shared memory by the bulk-copy (TMA) engine.
 //
 // storkm(60,60,e) is symmetric (B'DB), so the inner PCG of the mixed solver
-// keeps only its upper triangle: U(i,j), i <= j, column-major,
-// offset T(j)+i with T(j) = j(j+1)/2 -- 1,830 floats, padded to 1,832
-// (7,328 bytes, a multiple of 16) per element.  That halves the dominant
-// HBM stream of an iteration (the idea of xx16's packed DSPMV storage,
-// src/programs/dev/xx16/xx16.f90:393-459).
+// keeps each entry once, in FP32: 1,830 floats, padded to 1,832 (7,328
+// bytes, a multiple of 16) per element.  That halves the dominant HBM stream
+// of an iteration (the idea of xx16's packed DSPMV storage,
+// src/programs/dev/xx16/xx16.f90:393-459).  The entries are stored by cyclic
+// diagonals (packed_off): D[s][i] = K(i, (i+s) mod 60).
 //
-// Kernel structure (one persistent CTA of 14 warps per SM):
+// Kernel structure (one persistent CTA of 12-14 warps per SM):
 //   * every warp owns a ring of NSTAGE shared-memory stages with one
 //     mbarrier each; lane 0 issues cp.async.bulk of the next elements'
 //     packed blocks into the ring (complete_tx on the stage's mbarrier);
-//   * the warp gathers p for the element two positions ahead in registers,
-//     so the global gather overlaps the current element's arithmetic;
-//   * lanes 0..29 own rows l and 59-l and walk the 60 columns, reading
-//     U(min(i,j), max(i,j)) from shared memory (at most 2-way bank conflicts)
-//     with p(j) broadcast from a per-warp slot.  Each row is summed in
-//     ascending column order with FMA, as the full-storage kernel does.
+//   * the warp gathers p for the next element in registers, so the global
+//     gather overlaps the current element's arithmetic;
+//   * lane l < 30 owns rows l and l+30.  Forward distance d and backward
+//     distance 30-d of both rows read D[d][l], D[d][l+30], D[30-d][l+d] and
+//     D[30-d][(l+d+30) mod 60] with the p values l+d and l+d+30, so every
+//     shared-memory address is the lane plus a compile-time constant and
+//     each p load feeds two FMAs;
+//   * the product is P K_e P p_e, P removing the element's mean translation
+//     (an identity in exact arithmetic, since K_e annihilates rigid
+//     translations).  It keeps the rounding of FP32 away from the smooth,
+//     low-energy part of p, which otherwise slows the mixed solver's
+//     convergence more the finer the mesh.  Rows l and l+30 share a
+//     direction, so each mean is one reduction over the lanes of a class
+//     mod 3.
 // Every wait on an mbarrier is bounded; a wait that runs out writes 2 to
 // the context's device error word and the warp drains its in-flight copies
 // (again with a bound) before it returns.
@@ -34,10 +42,39 @@ namespace {
 
 constexpr int kPacked = 1832;                 // floats per element (1830 + 2 pad)
 constexpr int kPackedBytes = kPacked * 4;     // 7328
+constexpr int kPSlot = 120;                   // floats of p per warp (p_e twice)
 constexpr unsigned kFull = 0xffffffffu;
+
+// v = hi + lo with hi = v truncated to FP32 and lo the FP32 remainder
+// (rounded to 23 bits), by integer operations on the bits of v.  GB300's FP64
+// rate is about 1/60 of its FP32 rate, so the kernel does no FP64 arithmetic
+// and no FP64 conversion.  |hi + lo - v| <= 2^-46 |v| for 2^-103 <= |v| <
+// 2^128; below that lo is 0 (hi alone is accurate to 2^-23), |v| >= 2^128
+// gives hi = +-inf and a NaN gives a NaN.
+__device__ __forceinline__ void split_f64(double v, float &hi, float &lo)
+{
+    const uint32_t bh = (uint32_t)__double2hiint(v), bl = (uint32_t)__double2loint(v);
+    const uint32_t sign = bh & 0x80000000u;
+    const int e = (int)((bh >> 20) & 0x7ffu);          // biased FP64 exponent
+    const int fe = e - 1023 + 127;                      // biased FP32 exponent
+    const uint32_t mant = ((bh & 0xfffffu) << 3) | (bl >> 29);
+    if (fe >= 1 && fe <= 254)
+        hi = __uint_as_float(sign | ((uint32_t)fe << 23) | mant);
+    else if (fe > 254)
+        hi = __uint_as_float(sign | 0x7f800000u | ((e == 0x7ff && ((bh & 0xfffffu) | bl)) ? 0x400000u : 0u));
+    else
+        hi = __uint_as_float(sign);
+    // the low 29 mantissa bits, top 23 of them: (rem >> 6) * 2^(e - 1069)
+    const float m = __uint_as_float(0x3f800000u | ((bl & 0x1fffffffu) >> 6)) - 1.0f;   // (rem >> 6) * 2^-23
+    const int se = e - 1046 + 127;                                                     // 2^(e - 1046)
+    lo = (fe >= 1 && se >= 1 && se <= 254)
+             ? __uint_as_float(__float_as_uint(m * __uint_as_float((uint32_t)se << 23)) | sign)
+             : 0.0f;
+}
 }  // namespace
 
-// Packs the upper triangle of the FP64 storkm into FP32 (one warp per element).
+// Packs the FP64 storkm into the cyclic-diagonal FP32 layout of
+// packed_off (one warp per element).
 __global__ void k_pack_sym32(int nels, const double *__restrict__ km, float *__restrict__ kp)
 {
     const int lane = threadIdx.x & 31;
@@ -46,13 +83,27 @@ __global__ void k_pack_sym32(int nels, const double *__restrict__ km, float *__r
     for (int e = warp; e < nels; e += nwarps) {
         const double *ke = km + (size_t)e * 3600;
         float *out = kp + (size_t)e * kPacked;
-        for (int j = 0; j < 60; ++j)
-            for (int i = lane; i <= j; i += 32) out[j * (j + 1) / 2 + i] = (float)ke[60 * j + i];
-        if (lane < 2) out[1830 + lane] = 0.0f;
+        for (int pos = lane; pos < kPacked; pos += 32) {
+            const int sd = pos < 1800 ? pos / 60 : 30, i = pos < 1800 ? pos % 60 : pos - 1800;
+            out[pos] = pos < 1830 ? (float)ke[60 * ((i + sd) % 60) + i] : 0.0f;   // K(i, i+s)
+        }
     }
 }
 
-// u_e = K_e p_e for every element, K_e from the packed FP32 triangle.
+// Sums v over each class of lanes with equal index mod 3 (lanes 0..29 hold
+// the values, lanes 30 and 31 hold 0) and returns to every lane the sum of
+// its class, the same bits on every lane of the class.
+__device__ __forceinline__ float sum_mod3(float v, int lane)
+{
+#pragma unroll
+    for (int off = 3; off < 32; off <<= 1) {   // 3, 6, 12, 24
+        const float w = __shfl_down_sync(kFull, v, off);
+        v += (lane + off < 32) ? w : 0.0f;
+    }
+    return __shfl_sync(kFull, v, lane % 3);
+}
+
+// u_e = P K_e P p_e for every element, K_e from the packed FP32 diagonals.
 // kWarps warps per CTA, kStages shared-memory stages per warp (tuned at
 // run time among the instantiations below).
 template <int kWarps, int kStages>
@@ -65,10 +116,11 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     float *stage = reinterpret_cast<float *>(smem) + (size_t)w * kStages * kPacked;
-    float *pslot = reinterpret_cast<float *>(smem + (size_t)kWarps * kStages * kPackedBytes) + w * 64;
+    // p_e twice over (120 floats), so that (i + s) mod 60 needs no wrap
+    float *pp = reinterpret_cast<float *>(smem + (size_t)kWarps * kStages * kPackedBytes) + w * kPSlot;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kWarps * kStages * kPackedBytes +
-                                                 kWarps * 64 * 4) + w * kStages;
-    static_assert((kWarps * kStages * kPackedBytes + kWarps * 64 * 4) % 8 == 0, "mbarrier alignment");
+                                                 kWarps * kPSlot * 4) + w * kStages;
+    static_assert((kWarps * kStages * kPackedBytes + kWarps * kPSlot * 4) % 8 == 0, "mbarrier alignment");
 
     // stop flag: uniform per warp (no block barrier after this point)
     int stopped = 0;
@@ -99,62 +151,98 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
         }
     }
 
-    // gather pipeline: p values of element k (two floats per lane: dofs lane,
-    // lane+32) and the connectivity of element k+1
-    const int j1 = lane + 32;
-    auto gather = [&](int e, int nd, float &a, float &b) {
+    // Lane l < 30 owns dofs and rows l and l+30 (node l/3 and node l/3+10,
+    // both in direction l%3).  Gather pipeline: p of element k in registers
+    // (FP64), connectivity of element k+1.
+    const bool active = lane < 30;
+    auto gather = [&](int nd, double &a, double &b) {
         const int n0 = __shfl_sync(kFull, nd, lane / 3);
-        const int n1 = __shfl_sync(kFull, nd, j1 < 60 ? j1 / 3 : 0);
-        a = (float)p[(size_t)3 * n0 + lane % 3];
-        b = j1 < 60 ? (float)p[(size_t)3 * n1 + j1 % 3] : 0.0f;
+        const int n1 = __shfl_sync(kFull, nd, active ? lane / 3 + 10 : 0);
+        a = active ? p[(size_t)3 * n0 + lane % 3] : 0.0;
+        b = active ? p[(size_t)3 * n1 + lane % 3] : 0.0;
     };
     int conn_next = 0;
-    float pa = 0.f, pb = 0.f;
+    double pa = 0.0, pb = 0.0;
     {
         const int nd0 = lane < 20 ? conn[(size_t)elem(0) * 20 + lane] : 0;
-        gather(elem(0), nd0, pa, pb);
+        gather(nd0, pa, pb);
         if (nmine > 1 && lane < 20) conn_next = conn[(size_t)elem(1) * 20 + lane];
     }
 
-    // rows owned by this lane and the running offsets of U(min,max) in column j
-    const int ra = lane, rb = 59 - lane;
-    const bool active = lane < 30;
     bool failed = false;
     int k = 0;
     for (; k < nmine; ++k) {
         const int s = k % kStages;
         const uint32_t parity = (uint32_t)((k / kStages) & 1);
         // prefetch: p of element k+1, connectivity of element k+2
-        float na = 0.f, nb = 0.f;
-        if (k + 1 < nmine) gather(elem(k + 1), conn_next, na, nb);
+        double na = 0.0, nb = 0.0;
+        if (k + 1 < nmine) gather(conn_next, na, nb);
         int conn_next2 = 0;
         if (k + 2 < nmine && lane < 20) conn_next2 = conn[(size_t)elem(k + 2) * 20 + lane];
 
-        // p of element k into the warp's slot
-        pslot[lane] = pa;
-        if (j1 < 60) pslot[j1] = pb;
+        // p of element k, less its mean translation, into the warp's slot.
+        // K_e t = 0 for a rigid translation t, so the subtraction changes
+        // nothing in exact arithmetic; in FP32 it keeps the translation of
+        // a smooth p out of the rounding of p, of storkm's entries and of
+        // the sums (errors that grow with the square of the mesh size on
+        // the lowest modes).  The mean is formed from the FP32 high parts --
+        // any translation serves -- and (hi - t) + lo recovers p - t to FP32
+        // accuracy relative to p - t.
+        {
+            float ha, la, hb, lb;
+            split_f64(pa, ha, la);
+            split_f64(pb, hb, lb);
+            const float t = 0.05f * sum_mod3(ha + hb, lane);
+            if (active) {
+                const float qa = (ha - t) + la, qb = (hb - t) + lb;
+                pp[lane] = qa;
+                pp[lane + 60] = qa;
+                pp[lane + 30] = qb;
+                pp[lane + 90] = qb;
+            }
+        }
         const bool ok = __all_sync(kFull, mbar_wait(&bar[s], parity));
         if (!ok) {
             failed = true;
             break;
         }
         __syncwarp();
-        const float *U = stage + s * kPacked;
+        // Row l and row l+30 as four running sums over the diagonals: step
+        // d pairs forward distance d (K(l, l+d), K(l+30, l+30+d)) with
+        // backward distance 30-d (K(l+30, l+d), K(l, l+30+d)), which use
+        // the same two p values.  Every address is the lane plus a constant.
+        const float *D = stage + s * kPacked;
         float acc_a = 0.f, acc_b = 0.f;
         if (active) {
-            int ia = ra * (ra + 1) / 2;   // U(min(ra,0), max(ra,0)) = T(ra) + 0
-            int ib = rb * (rb + 1) / 2;
-#pragma unroll 4
-            for (int j = 0; j < 60; ++j) {
-                const float pj = pslot[j];
-                acc_a = fmaf(U[ia], pj, acc_a);
-                acc_b = fmaf(U[ib], pj, acc_b);
-                ia += (j < ra) ? 1 : j + 1;   // T(ra)+j -> T(ra)+j+1, then T(j)+ra -> T(j+1)+ra
-                ib += (j < rb) ? 1 : j + 1;
+            const float *Dl = D + lane, *Dw = D + lane + 60;   // Dw: entries (l - t) mod 60 for t > l
+            const float *pl = pp + lane;
+            float f0 = Dl[0] * pl[0], f1 = Dl[30] * pl[30], g0 = 0.f, g1 = 0.f;
+#pragma unroll
+            for (int d = 1; d < 30; ++d) {
+                const int t = 30 - d;
+                const float p0 = pl[d], p1 = pl[30 + d];
+                f0 = fmaf(Dl[60 * d], p0, f0);                              // K(l, l+d)
+                f1 = fmaf(Dl[60 * d + 30], p1, f1);                         // K(l+30, l+30+d)
+                g1 = fmaf(Dl[60 * t + d], p0, g1);                          // K(l+30, l+d) = D[t][l+d]
+                g0 = fmaf((lane < t ? Dw : Dl)[59 * t], p1, g0);            // K(l, l-t) = D[t][(l-t) mod 60]
             }
+            const float d30 = Dl[1800];                                     // K(l, l+30)
+            f0 = fmaf(d30, pl[30], f0);
+            f1 = fmaf(d30, pl[0], f1);
+            acc_a = f0 + g0;
+            acc_b = f1 + g1;
+        }
+        // the same projection on the result (t'K_e = 0 as well), so that
+        // the product stays symmetric: u_e = P K_e P p_e
+        {
+            const float t = 0.05f * sum_mod3(acc_a + acc_b, lane);
+            acc_a -= t;
+            acc_b -= t;
+        }
+        if (active) {
             float *o = ut + (size_t)elem(k) * 80;   // node-padded: row i at (i/3)*4 + i%3
-            o[(ra / 3) * 4 + ra % 3] = acc_a;
-            o[(rb / 3) * 4 + rb % 3] = acc_b;
+            o[(lane / 3) * 4 + lane % 3] = acc_a;
+            o[(lane / 3 + 10) * 4 + lane % 3] = acc_b;
         }
         __syncwarp();   // every lane is done with stage s and the p slot
         if (lane == 0 && k + kStages < nmine) {
@@ -177,7 +265,7 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
 template <int W, int S>
 constexpr size_t sym_smem_bytes()
 {
-    return (size_t)W * S * kPackedBytes + W * 64 * 4 + W * S * 8;
+    return (size_t)W * S * kPackedBytes + W * kPSlot * 4 + W * S * 8;
 }
 
 template <int W, int S>

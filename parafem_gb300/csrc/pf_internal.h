@@ -7,6 +7,17 @@
 
 namespace pf {
 
+// Packed-symmetric FP32 storkm (1,830 floats + 2 zero pads per element), by
+// cyclic diagonals: D[s][i] = K(i, (i+s) mod 60) at 60 s + i for s = 0..29,
+// i = 0..59, and the 30 distinct entries of diagonal 30, K(i, i+30) for
+// i = 0..29, at 1800 + i.  Every entry of the symmetric 60 x 60 matrix is
+// stored once.  Returns the position of K(i, k), i, k in 0..59.
+__host__ __device__ constexpr int packed_off(int i, int k)
+{
+    const int s = (k - i + 60) % 60;
+    return s < 30 ? 60 * s + i : s == 30 ? 1800 + (i < 30 ? i : i - 30) : 60 * (60 - s) + k;
+}
+
 // Records a formatted error message for pf_last_error (thread local).
 void set_error(const char *fmt, ...);
 
@@ -50,7 +61,7 @@ struct Ctx {
 
     double *km64 = nullptr;     // [nels*3600] storkm(60,60,e)
     float *km32 = nullptr;      // [nels*3600] full FP32 copy
-    float *km32p = nullptr;     // [nels*1832] packed upper triangle, FP32
+    float *km32p = nullptr;     // [nels*1832] packed symmetric storkm (packed_off), FP32
     int *kerr = nullptr;        // device error word of the bulk-copy kernels (2 = wait timed out)
     bool have_km = false;
 

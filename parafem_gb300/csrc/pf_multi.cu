@@ -77,7 +77,7 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 //
 // One persistent CTA of 20 warps per SM walks the elements e = blockIdx.x +
 // t * gridDim.x with warp-specialised roles linked by mbarriers:
-//   warp 18      bulk copies (cp.async.bulk) of the packed upper triangle of
+//   warp 18      bulk copies (cp.async.bulk) of the packed symmetric storkm of
 //                K_e (7,328 B) and of the 16-case P blocks of the element's
 //                20 nodes (384 B each, contiguous in the interleaved vector)
 //                into a ring of kNst stages;
@@ -179,15 +179,14 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
         }
         if (lane == 0) s_count[0] = issued;
     } else if (warp < kBuildWarps) {
-        // this thread's A task: row i, K-values 8q..8q+7; K(i,k) = U(min, max)
-        // at T(max) + min, and entries outside 60 x 60 read the zero pad at 1830
+        // this thread's A task: row i, K-values 8q..8q+7; K(i,k) is at
+        // packed_off(i, k), and entries outside 60 x 60 read the zero pad at 1830
         const int i = tid & 63, q = tid >> 6;
         int off[8];
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const int k = 8 * q + g;
-            const int lo = i < k ? i : k, hi = i < k ? k : i;
-            off[g] = (i < 60 && k < 60) ? hi * (hi + 1) / 2 + lo : 1830;
+            off[g] = (i < 60 && k < 60) ? packed_off(i, k) : 1830;
         }
         const uint32_t a_off = kmajor_off(i, 8 * q);
         for (int t = 0; t < nmine; ++t) {

@@ -213,6 +213,33 @@ def test_packed_symmetric_product_is_symmetric_and_deterministic(demo_problem):
     assert abs(b @ ka - a @ kb) <= 1e-6 * abs(b @ ka)
 
 
+def test_packed_product_keeps_rigid_translations_out_of_the_rounding():
+    """K_e t = 0 for a translation t; the packed FP32 product subtracts each
+    element's mean translation in FP64 before rounding, so on a nearly rigid
+    p its error away from the restrained elements is set by the small
+    non-rigid part, while the full-FP32 product (no projection) errs by the
+    rounding of the translation itself."""
+    prob = P.cube_problem(8, 8, 8)
+    g_g, neq = prob["g_g"], prob["neq"]
+    rng = np.random.default_rng(12)
+    x = 1.0 + 1e-4 * rng.standard_normal(neq)
+    with P.Solver() as s:
+        s.setup(prob["g_num"], g_g, prob["g_coord"], prob["nn"], prob["neq"])
+        s.set_material(100.0, 0.3)
+        s.form_storkm(27)
+        u64, u32, u31 = s.ebe_matvec(x, 64), s.ebe_matvec(x, 32), s.ebe_matvec(x, 31)
+    # equations of elements with no restrained freedom, minus every equation
+    # that also belongs to an element with one
+    touched = np.zeros(neq + 1, bool)
+    touched[g_g[(g_g == 0).any(axis=1)].ravel()] = True
+    inner = ~touched[1:]
+    assert inner.sum() > neq // 2
+    e32 = np.abs(u32 - u64)[inner].max()
+    e31 = np.abs(u31 - u64)[inner].max()
+    assert e31 > 0.0
+    assert e32 <= 1e-2 * e31, (e32, e31)
+
+
 def test_autotuned_configurations_give_bitwise_equal_products(demo_problem):
     p = demo_problem
     d = p["deck"]
