@@ -45,32 +45,6 @@ constexpr int kPackedBytes = kPacked * 4;     // 7328
 constexpr int kPSlot = 120;                   // floats of p per warp (p_e twice)
 constexpr unsigned kFull = 0xffffffffu;
 
-// v = hi + lo with hi = v truncated to FP32 and lo the FP32 remainder
-// (rounded to 23 bits), by integer operations on the bits of v.  GB300's FP64
-// rate is about 1/60 of its FP32 rate, so the kernel does no FP64 arithmetic
-// and no FP64 conversion.  |hi + lo - v| <= 2^-46 |v| for 2^-103 <= |v| <
-// 2^128; below that lo is 0 (hi alone is accurate to 2^-23), |v| >= 2^128
-// gives hi = +-inf and a NaN gives a NaN.
-__device__ __forceinline__ void split_f64(double v, float &hi, float &lo)
-{
-    const uint32_t bh = (uint32_t)__double2hiint(v), bl = (uint32_t)__double2loint(v);
-    const uint32_t sign = bh & 0x80000000u;
-    const int e = (int)((bh >> 20) & 0x7ffu);          // biased FP64 exponent
-    const int fe = e - 1023 + 127;                      // biased FP32 exponent
-    const uint32_t mant = ((bh & 0xfffffu) << 3) | (bl >> 29);
-    if (fe >= 1 && fe <= 254)
-        hi = __uint_as_float(sign | ((uint32_t)fe << 23) | mant);
-    else if (fe > 254)
-        hi = __uint_as_float(sign | 0x7f800000u | ((e == 0x7ff && ((bh & 0xfffffu) | bl)) ? 0x400000u : 0u));
-    else
-        hi = __uint_as_float(sign);
-    // the low 29 mantissa bits, top 23 of them: (rem >> 6) * 2^(e - 1069)
-    const float m = __uint_as_float(0x3f800000u | ((bl & 0x1fffffffu) >> 6)) - 1.0f;   // (rem >> 6) * 2^-23
-    const int se = e - 1046 + 127;                                                     // 2^(e - 1046)
-    lo = (fe >= 1 && se >= 1 && se <= 254)
-             ? __uint_as_float(__float_as_uint(m * __uint_as_float((uint32_t)se << 23)) | sign)
-             : 0.0f;
-}
 }  // namespace
 
 // Packs the FP64 storkm into the cyclic-diagonal FP32 layout of

@@ -11,8 +11,12 @@
 //                     three BF16 terms held in shared memory for the whole
 //                     kernel; tiles of 128 elements' gathered p values are
 //                     split the same way; the six products of order <= 2^-16
-//                     accumulate in FP32 in TMEM (M = 128 with rows 60..127
-//                     unused, N = 128 elements, K = 64).  Warp-specialised:
+//                     accumulate in FP32 in TMEM (M = 128: km's rows in four
+//                     blocks of five nodes, each block with the three
+//                     direction sums of km's rows; N = 128 elements,
+//                     K = 64).  The product is P km P p_e, P removing the
+//                     element's mean translation, as in the packed per-element
+//                     kernel.  Warp-specialised:
 //                     connectivity copies, gather + split, MMA issue and the
 //                     TMEM read-back overlap across tiles through mbarrier
 //                     rings.  Results are written in the node-padded FP32
@@ -27,19 +31,21 @@ using namespace tc;
 namespace {
 
 constexpr int kNT = 128;                    // elements per tile (MMA N)
-constexpr int kSTermA = 64 * 64 * 2;        // 8 KB: rows 0..63 of one km term
-constexpr int kSBufA = 4 * kSTermA;         // 3 terms + 8 KB read as rows 64..127 of the last
+constexpr int kSRowsA = 128;                // A rows: 4 blocks of 32 (15 node rows, 3 sum rows, 14 zero rows)
+constexpr int kSTermA = kSRowsA * 64 * 2;   // 16 KB: one km term, K = 64
+constexpr int kSBufA = 3 * kSTermA;
 constexpr int kSTermB = kNT * 64 * 2;       // 16 KB: 128 elements x 64 K
 constexpr int kSBufB = 3 * kSTermB;
 constexpr int kSConn = kNT * 20 * 4;        // 10 KB: connectivity of one tile
 constexpr int kSNB = 3;                     // B tile sets in flight
-constexpr int kSNC = 4;                     // connectivity buffers in flight
+constexpr int kSNC = 3;                     // connectivity buffers in flight
 constexpr int kSNA = 4;                     // TMEM accumulators (128 columns each, all 512)
 constexpr int kSGather = 16;                // warps 0-15 gather p and split it (two tasks per thread)
-constexpr int kSEpi0 = 16;                  // warps 16-17 read TMEM lanes 0..63 back
-constexpr int kSProd = 18;                  // warp 18 copies the connectivity
-constexpr int kSMma = 19;                   // warp 19, lane 0 issues the MMAs
-constexpr int kSThreads = 20 * 32;
+constexpr int kSEpi0 = 16;                  // warps 16-19 read TMEM lanes 32w..32w+31 back, five nodes each
+constexpr int kSNEpi = 4;
+constexpr int kSProd = 20;                  // warp 20 copies the connectivity
+constexpr int kSMma = 21;                   // warp 21, lane 0 issues the MMAs
+constexpr int kSThreads = 22 * 32;
 constexpr int kSOffB = kSBufA;
 constexpr int kSOffC = kSOffB + kSNB * kSBufB;
 constexpr int kSOffAux = kSOffC + kSNC * kSConn;
@@ -48,7 +54,7 @@ constexpr uint32_t kSIdesc = idesc_bf16(128, kNT);
 static_assert(kSOffC % 16 == 0 && kSConn % 16 == 0 && kSOffAux % 8 == 0, "bulk-copy alignment");
 static_assert(kSSmem <= 227 * 1024, "shared memory per CTA");
 static_assert(kSGather * 32 * 2 == kNT * 8, "two B tasks (element, 8 dofs) per gather thread");
-static_assert(kSEpi0 % 4 == 0, "epilogue warps must reach TMEM lanes 0..63");
+static_assert(kSEpi0 % 4 == 0, "epilogue warp kSEpi0 + w must reach TMEM lanes 32w..32w+31");
 
 __device__ __forceinline__ void mbar_arrive1(uint64_t *bar)
 {
@@ -90,17 +96,18 @@ k_elem_shared64(int nels, const double *__restrict__ km, const int *__restrict__
     }
 }
 
-// u_e = km p_e on the tensor cores for every element (FP32 results,
+// u_e = P km P p_e on the tensor cores for every element (FP32 results,
 // node-padded: row i of element e at e*80 + (i/3)*4 + i%3).
-// One persistent CTA of 20 warps per SM walks the tiles T = blockIdx.x +
+// One persistent CTA of 22 warps per SM walks the tiles T = blockIdx.x +
 // t * gridDim.x with warp-specialised roles linked by mbarriers:
-//   warp 18      bulk-copies each tile's connectivity into a ring of kSNC;
+//   warp 20      bulk-copies each tile's connectivity into a ring of kSNC;
 //   warps 0-15   gather the tile's p values (two 8-dof tasks per thread),
-//                split them into three BF16 terms and write a ring of kSNB
-//                B tile sets;
-//   warp 19      one thread issues the six products (24 MMAs, M=128, N=128,
+//                remove each element's mean translation, split the values
+//                into three BF16 terms and write a ring of kSNB B tile sets;
+//   warp 21      one thread issues the six products (24 MMAs, M=128, N=128,
 //                K=16) into a ring of kSNA TMEM accumulators;
-//   warps 16-17  read TMEM lanes 0..63 back and store the results.
+//   warps 16-19  read TMEM lanes 0..127 back (five nodes each), remove
+//                each element's mean translation and store the results.
 // Every wait is bounded.  A wait that runs out sets a shared failure flag
 // that every role checks before its next wait, writes 3 to the device error
 // word, and the CTA waits (bounded) for the copies and MMAs it has in flight
@@ -133,18 +140,32 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     auto tile = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
     auto tile_n = [&](int t) { const int r = nels - tile(t) * kNT; return r < kNT ? r : kNT; };
 
-    // km once: K(i,k) = km32[i + 60k], three BF16 terms, rows 0..63 x K 0..63
+    // km once, three BF16 terms.  A row 32w + i is K row 3(5w + i/3) + i%3
+    // for i < 15 (nodes 5w..5w+4), the sum of K's 20 rows of direction
+    // i - 15 for i = 15..17, zero otherwise.  The sums are zero in exact
+    // arithmetic (K annihilates rigid translations); they carry the rounding
+    // of the FP32 km and put each element's per-direction sum of results
+    // beside its rows in the accumulator.  K(i,k) = km32[i + 60k].
     for (int i = tid; i < kSOffC / 16; i += kSThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
-    if (tid < 512) {
-        const int i = tid & 63, q = tid >> 6;
+    for (int task = tid; task < kSRowsA * 8; task += kSThreads) {
+        const int row = task % kSRowsA, q = task / kSRowsA;
+        const int w = row >> 5, i = row & 31;
         float xv[8];
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const int k = 8 * q + g;
-            xv[g] = (i < 60 && k < 60) ? km32[i + 60 * k] : 0.f;
+            float v = 0.f;
+            if (k < 60 && i < 15) {
+                v = km32[3 * (5 * w + i / 3) + i % 3 + 60 * k];
+            } else if (k < 60 && i < 18) {
+                double sum = 0.0;
+                for (int a = 0; a < 20; ++a) sum += (double)km32[3 * a + (i - 15) + 60 * k];
+                v = (float)sum;
+            }
+            xv[g] = v;
         }
-        split3_store8(xv, A + kmajor_off(i, 8 * q), kSTermA);
+        split3_store8(xv, A + kmajor_off(row, 8 * q), kSTermA);
     }
     if (warp == 0) tmem_alloc(tslot, 512);
     if (tid == 0) {
@@ -158,7 +179,7 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
         }
         for (int i = 0; i < kSNA; ++i) {
             mbar_init(&a_full[i], 1);
-            mbar_init(&a_empty[i], 2);
+            mbar_init(&a_empty[i], kSNEpi);
         }
         mbar_fence_init();
         *s_fail = 0;
@@ -196,25 +217,59 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
             if (t >= kSNB && !wait(&b_empty[bb], (uint32_t)((t / kSNB - 1) & 1))) break;
             const int *ct = cs + cb * kNT * 20;
             const int n_here = tile_n(t);
+            // Lane j + 4 qq of warp w holds dofs 8qq..8qq+7 of elements
+            // 8w + j (pass 0) and 8w + 4 + j (pass 1), so an element's eight
+            // chunks are the lanes j, j+4, ..., j+28.  Each element's mean
+            // translation is removed before the BF16 split (K t = 0 for a
+            // rigid translation t, so the product is unchanged in exact
+            // arithmetic and the rounding acts only on p - t).
+            const int j = lane & 3, qq = lane >> 2;
+            const int r = (2 * qq) % 3;   // direction of dof 8qq; dof 8qq+g has (r + g) % 3
+            double pv[2][8];   // both passes' loads in flight together
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int n = 8 * warp + 4 * h + j;
+#pragma unroll
+                for (int g = 0; g < 8; ++g) {
+                    const int c = 8 * qq + g;
+                    pv[h][g] = (c < 60 && n < n_here) ? p[(size_t)3 * ct[n * 20 + c / 3] + c % 3] : 0.0;
+                }
+            }
             float xv[2][8];
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int task = tid + kSGather * 32 * h;
-                const int n = task & (kNT - 1), q = task >> 7;
+                float hi[8], lo[8];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) {
-                    const int c = 8 * q + g;
-                    xv[h][g] = (c < 60 && n < n_here) ? (float)p[(size_t)3 * ct[n * 20 + c / 3] + c % 3] : 0.f;
+                for (int g = 0; g < 8; ++g) split_f64(pv[h][g], hi[g], lo[g]);
+                // sums of this chunk by direction, then over the element's chunks
+                const float u0 = hi[0] + hi[3] + hi[6], u1 = hi[1] + hi[4] + hi[7], u2 = hi[2] + hi[5];
+                float s0 = r == 0 ? u0 : r == 1 ? u2 : u1;
+                float s1 = r == 0 ? u1 : r == 1 ? u0 : u2;
+                float s2 = r == 0 ? u2 : r == 1 ? u1 : u0;
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) {
+                    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+                    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+                    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
                 }
+                const float t0 = 0.05f * s0, t1 = 0.05f * s1, t2 = 0.05f * s2;
+                const float tr[3] = {r == 0 ? t0 : r == 1 ? t1 : t2, r == 0 ? t1 : r == 1 ? t2 : t0,
+                                     r == 0 ? t2 : r == 1 ? t0 : t1};
+#pragma unroll
+                for (int g = 0; g < 8; ++g) xv[h][g] = (8 * qq + g < 60) ? (hi[g] - tr[g % 3]) + lo[g] : 0.f;
             }
             __syncwarp();
             if (lane == 0) mbar_arrive1(&c_empty[cb]);   // connectivity read
             unsigned char *Bb = B + bb * kSBufB;
+            // even chunks store pass 0 first, odd chunks pass 1: each quarter
+            // warp then writes eight different 16-byte bank groups
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int task = tid + kSGather * 32 * h;
-                const int n = task & (kNT - 1), q = task >> 7;
-                split3_store8(xv[h], Bb + kmajor_off(n, 8 * q), kSTermB);
+            for (int k = 0; k < 2; ++k) {
+                const int h = (qq & 1) ^ k;
+                float y[8];
+#pragma unroll
+                for (int g = 0; g < 8; ++g) y[g] = h ? xv[1][g] : xv[0][g];
+                split3_store8(y, Bb + kmajor_off(8 * warp + 4 * h + j, 8 * qq), kSTermB);
             }
             fence_proxy_async();   // this thread's tile writes -> the tensor cores
             __syncwarp();
@@ -247,9 +302,14 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
             s_count[1] = t;
         }
         __syncwarp();
-    } else if (warp == kSEpi0 || warp == kSEpi0 + 1) {
-        const int row = 32 * (warp - kSEpi0) + lane;   // TMEM lanes 0..63 = rows
-        const size_t roff = (size_t)(row / 3) * 4 + row % 3;
+    } else if (warp >= kSEpi0 && warp < kSEpi0 + kSNEpi) {
+        // TMEM lanes 32w + i: i < 15 row 3(5w + i/3) + i%3, i = 15..17 the
+        // sums of direction i - 15.  Subtracting a twentieth of the sum of
+        // the row's direction removes the result's mean translation (u_e =
+        // P km P p_e); the five nodes' results are 80 contiguous bytes.
+        const int w = warp - kSEpi0;
+        const int src = lane < 15 ? 15 + lane % 3 : lane;
+        const int roff = (5 * w + lane / 3) * 4 + lane % 3;
         for (int t = 0; t < nmine; ++t) {
             const int a = t % kSNA;
             if (!wait(&a_full[a], (uint32_t)((t / kSNA) & 1))) break;
@@ -259,8 +319,10 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
 #pragma unroll 1
             for (int ch = 0; ch < kNT / 16; ++ch) {
                 float v[16];
-                tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * (warp - kSEpi0)) << 16) + (uint32_t)(a * kNT + 16 * ch), v);
-                if (row < 60) {
+                tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)(a * kNT + 16 * ch), v);
+#pragma unroll
+                for (int x = 0; x < 16; ++x) v[x] -= 0.05f * __shfl_sync(0xffffffffu, v[x], src);
+                if (lane < 15) {
 #pragma unroll
                     for (int x = 0; x < 16; ++x) {
                         const int n = 16 * ch + x;
