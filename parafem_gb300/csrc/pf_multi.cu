@@ -38,33 +38,41 @@ constexpr unsigned kFullMask = 0xffffffffu;
 
 // Tile geometry (BF16, K-major, no swizzle; 8-row x 16-byte core matrices,
 // LBO = 128 B between core matrices adjacent in K, SBO = 1024 B between
-// 8-row groups).  A term holds rows 0..63 of K_e (8 KB).  The MMA reads
-// M = 128 rows, so rows 64..127 of a term are the next 8 KB of shared
-// memory: they only feed accumulator rows 64..127, which nobody reads.
-constexpr int kTermA = 64 * 64 * 2;          // 8192
-constexpr int kBufA = 4 * kTermA;            // 3 terms + the 8 KB read as rows 64..127 of the last
+// 8-row groups).  A term holds 96 rows: for direction d, rows 32d + i
+// (i < 20) are K_e's rows 3i + d, row 32d + 20 is the sum of those rows, rows
+// 32d + 21..31 stay zero.  The MMA reads M = 128 rows, so rows 96..127 of a
+// term are the next 4 KB of shared memory: they only feed accumulator rows
+// 96..127, which nobody reads.
+constexpr int kRowsA = 96;
+constexpr int kTermA = kRowsA * 64 * 2;      // 12288
+constexpr int kBufA = 3 * kTermA + 4096;     // 3 terms + the 4 KB read as rows 96..127 of the last
 constexpr int kTermB = 16 * 64 * 2;          // 2048: 16 load cases x 64 K
 constexpr int kBufB = 3 * kTermB;
 constexpr int kStK = 7328;                   // packed-symmetric FP32 K_e (1830 + 2 pad floats)
 constexpr int kStP = 20 * 3 * KR * 8;        // P of the 20 nodes: 20 x 384 B
-constexpr int kStage = kStK + kStP;          // 15008 B, a multiple of 16
+constexpr int kStC = 3 * 64 * 4;             // direction sums of K_e's rows (3 x 64 FP32)
+constexpr int kStage = kStK + kStP + kStC;   // 15776 B, a multiple of 16
 constexpr int kNst = 4;                      // operand stages (bulk copies in flight)
 constexpr int kNTile = 3;                    // BF16 tile sets (A + B)
 constexpr int kNAcc = 4;                     // TMEM accumulators (16 columns each)
 constexpr int kBuildWarps = 16;              // warps 0-15 split K_e and P_e (one A task per thread)
-constexpr int kEpiWarp0 = 16;                // warps 16-17 read TMEM lanes 0..63 back
-constexpr int kProdWarp = 18;                // warp 18 issues the bulk copies
-constexpr int kMmaWarp = 19;                 // warp 19, lane 0 issues the MMAs
-constexpr int kTcThreads = 20 * 32;
-static_assert(kBuildWarps * 32 == 8 * 64, "one A task (row i, 8 K-values) per builder thread");
+constexpr int kBWarps = 4;                   // warps 0-3 also split P_e (one B task per thread)
+constexpr int kEpiWarp0 = 16;                // warps 16-18 read TMEM lanes 32d..32d+31 back (direction d)
+constexpr int kNEpi = 3;
+constexpr int kProdWarp = 19;                // warp 19 issues the bulk copies
+constexpr int kMmaWarp = 20;                 // warp 20, lane 0 issues the MMAs
+constexpr int kTcThreads = 21 * 32;
+static_assert(kBuildWarps * 32 >= 63 * 8, "one A task (row, 8 K-values) per builder thread");
+static_assert(kBWarps * 32 == KR * 8, "one B task (load case, 8 dofs) per thread of warps 0-3");
 constexpr int kOffB = kNTile * kBufA;
 constexpr int kOffSt = kOffB + kNTile * kBufB;
 constexpr int kOffAux = kOffSt + kNst * kStage;
-constexpr int kTcSmem = kOffAux + 256;
+constexpr int kOffSum = kOffAux + 256;       // [2][8][KR][3] partial direction sums of P_e
+constexpr int kTcSmem = kOffSum + 2 * 8 * KR * 3 * 4;
 constexpr uint32_t kIdesc = idesc_bf16(128, 16);
 static_assert(kOffSt % 16 == 0 && kStage % 16 == 0 && kOffAux % 8 == 0, "bulk-copy alignment");
 static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
-static_assert(kEpiWarp0 % 4 == 0, "epilogue warps must reach TMEM lanes 0..63");
+static_assert(kEpiWarp0 % 4 == 0, "epilogue warp kEpiWarp0 + d must reach TMEM lanes 32d..32d+31");
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
@@ -75,27 +83,37 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 
 // Block element products on the tensor cores: ut[e][i][j] = sum_c K_e(i,c) P(slot(c), j).
 //
-// One persistent CTA of 20 warps per SM walks the elements e = blockIdx.x +
+// The product is P K_e P P_e, P removing each load case's mean translation
+// over the element's 20 nodes (an identity in exact arithmetic, since K_e
+// annihilates rigid translations; in FP32-class arithmetic it keeps the
+// rounding away from the smooth part of P, as the single-case kernels do).
+//
+// One persistent CTA of 21 warps per SM walks the elements e = blockIdx.x +
 // t * gridDim.x with warp-specialised roles linked by mbarriers:
-//   warp 18      bulk copies (cp.async.bulk) of the packed symmetric storkm of
-//                K_e (7,328 B) and of the 16-case P blocks of the element's
+//   warp 19      bulk copies (cp.async.bulk) of the packed symmetric storkm of
+//                K_e (7,328 B), of the 16-case P blocks of the element's
 //                20 nodes (384 B each, contiguous in the interleaved vector)
-//                into a ring of kNst stages;
-//   warps 0-15   split K_e and P_e into three BF16 terms each and write them
-//                into a ring of kNTile tile sets (one 8-value row segment of
-//                K_e per thread, its shared-memory offsets computed once);
-//   warp 19      one thread issues the six products of order <= 2^-16
+//                and of the direction sums of K_e's rows (768 B) into a ring
+//                of kNst stages;
+//   warps 0-15   split K_e (rows by direction, with the row sums) and P_e
+//                less its mean translations into three BF16 terms each and
+//                write them into a ring of kNTile tile sets (one 8-value row
+//                segment of K_e per thread, its shared-memory offsets
+//                computed once; warps 0-3 also one 8-dof segment of P_e,
+//                exchanging their partial sums through shared memory);
+//   warp 20      one thread issues the six products of order <= 2^-16
 //                (24 MMAs, M=128, N=16, K=16) into a ring of kNAcc TMEM
 //                accumulators and commits them to mbarriers that free the
 //                tile set and fill the accumulator;
-//   warps 16-17  read the accumulators back (TMEM lanes 0..63) and store
-//                the 60 x 16 results.
+//   warps 16-18  read the accumulators back (TMEM lanes 32d..32d+20,
+//                direction d), subtract the mean of the direction's rows and
+//                store the 60 x 16 results.
 // Every wait is bounded.  A wait that runs out sets a shared failure flag
 // that every role checks before its next wait, writes 3 to the device error
 // word, and the CTA waits (bounded) for the copies and MMAs it has in flight
 // before it frees its TMEM and returns.
 __global__ void __launch_bounds__(kTcThreads, 1)
-k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ conn,
+k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ ksum, const int *__restrict__ conn,
              const double *__restrict__ P, float *__restrict__ ut, int *__restrict__ err,
              const int *__restrict__ skip)
 {
@@ -110,7 +128,9 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
     uint64_t *tl_empty = tl_full + kNTile;
     uint64_t *ac_full = tl_empty + kNTile;
     uint64_t *ac_empty = ac_full + kNAcc;
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(ac_empty + kNAcc);
+    uint64_t *sum_bar = ac_empty + kNAcc;   // the four B warps' partial sums of an element are written
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sum_bar + 1);
+    float *psum = reinterpret_cast<float *>(sm + kOffSum);   // [t & 1][chunk][case][direction]
     volatile int *s_fail = reinterpret_cast<volatile int *>(tslot + 1);
     int *s_count = reinterpret_cast<int *>(tslot + 2);   // [0] copies issued, [1] MMA groups committed
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -130,8 +150,9 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
         }
         for (int i = 0; i < kNAcc; ++i) {
             mbar_init(&ac_full[i], 1);
-            mbar_init(&ac_empty[i], 2);
+            mbar_init(&ac_empty[i], kNEpi);
         }
+        mbar_init(sum_bar, kBWarps);
         mbar_fence_init();
         *s_fail = 0;
         s_count[0] = s_count[1] = 0;
@@ -173,22 +194,32 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
                 __syncwarp();
                 if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &st_full[s]);
                 if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * ndr[j] * KR, 384, &st_full[s]);
+                if (lane == 20) bulk_g2s(dst + kStK + kStP, ksum + (size_t)elem(t) * 192, kStC, &st_full[s]);
                 ndr[j] = (lane < 20 && t + kCD < nmine) ? conn[(size_t)elem(t + kCD) * 20 + lane] : 0;
                 issued = t + 1;
             }
         }
         if (lane == 0) s_count[0] = issued;
     } else if (warp < kBuildWarps) {
-        // this thread's A task: row i, K-values 8q..8q+7; K(i,k) is at
-        // packed_off(i, k), and entries outside 60 x 60 read the zero pad at 1830
-        const int i = tid & 63, q = tid >> 6;
+        // this thread's A task (tid < 504): A row 32d + i, K-values 8q..8q+7.
+        // i < 20: K(3i + d, k) at packed_off; i = 20: the sum of direction
+        // d's rows, after the P blocks in the stage; K-values past 59 read
+        // the zero pad at 1830.
+        const bool a_task = tid < 63 * 8;
+        const int r63 = tid % 63, q = tid / 63;
+        const int d = r63 / 21, i = r63 % 21;
         int off[8];
 #pragma unroll
         for (int g = 0; g < 8; ++g) {
             const int k = 8 * q + g;
-            off[g] = (i < 60 && k < 60) ? packed_off(i, k) : 1830;
+            off[g] = (!a_task || k >= 60) ? 1830 : i < 20 ? packed_off(3 * i + d, k) : (kStK + kStP) / 4 + 64 * d + k;
         }
-        const uint32_t a_off = kmajor_off(i, 8 * q);
+        const uint32_t a_off = a_task ? kmajor_off(32 * d + i, 8 * q) : 0u;
+        // B task (warps 0-3): load case j, dofs 8qb..8qb+7 (dof c has
+        // direction (rb + c - 8qb) % 3)
+        const int j = tid & (KR - 1), qb = tid >> 4;
+        const int rb = (2 * qb) % 3;
+        const bool b_task = warp < kBWarps;
         for (int t = 0; t < nmine; ++t) {
             const int s = t % kNst, b = t % kNTile;
             if (!wait(&st_full[s], (uint32_t)((t / kNst) & 1))) break;
@@ -196,20 +227,48 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
             const float *U = reinterpret_cast<const float *>(stg + s * kStage);
             const double *Pe = reinterpret_cast<const double *>(stg + s * kStage + kStK);
             unsigned char *Ab = A + b * kBufA, *Bb = B + b * kBufB;
-            {
+            float *ps = psum + (t & 1) * (8 * KR * 3);
+            float hi[8], lo[8];
+            if (b_task) {
+                // P_e(c, j) at c*16 + j: FP32 high and low parts, and this
+                // segment's sums by direction for the case's mean translation
+#pragma unroll
+                for (int g = 0; g < 8; ++g) {
+                    const int c = 8 * qb + g;
+                    split_f64(c < 60 ? Pe[c * KR + j] : 0.0, hi[g], lo[g]);
+                }
+                const float u0 = hi[0] + hi[3] + hi[6], u1 = hi[1] + hi[4] + hi[7], u2 = hi[2] + hi[5];
+                ps[(qb * KR + j) * 3 + 0] = rb == 0 ? u0 : rb == 1 ? u2 : u1;
+                ps[(qb * KR + j) * 3 + 1] = rb == 0 ? u1 : rb == 1 ? u0 : u2;
+                ps[(qb * KR + j) * 3 + 2] = rb == 0 ? u2 : rb == 1 ? u1 : u0;
+                __syncwarp();
+                if (lane == 0) mbar_arrive(sum_bar);
+            }
+            if (a_task) {
                 float xv[8];
 #pragma unroll
                 for (int g = 0; g < 8; ++g) xv[g] = U[off[g]];
                 split3_store8(xv, Ab + a_off, kTermA);
             }
-            if (tid < 128) {   // B: P_e, case j, dofs 8qb..8qb+7; the stage holds P_e(c, j) at c*16 + j
-                const int j = tid & (KR - 1), qb = tid >> 4;
+            if (b_task) {
+                // the four B warps' partial sums are in (bounded wait; the
+                // double buffer is safe because no warp passes element t+1's
+                // wait before every warp has arrived for it)
+                if (!wait(sum_bar, (uint32_t)(t & 1))) break;
+                float tdir[3];
+#pragma unroll
+                for (int dd = 0; dd < 3; ++dd) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int c8 = 0; c8 < 8; ++c8) acc += ps[(c8 * KR + j) * 3 + dd];
+                    tdir[dd] = 0.05f * acc;
+                }
+                const float t0 = tdir[0], t1 = tdir[1], t2 = tdir[2];
+                const float tr[3] = {rb == 0 ? t0 : rb == 1 ? t1 : t2, rb == 0 ? t1 : rb == 1 ? t2 : t0,
+                                     rb == 0 ? t2 : rb == 1 ? t0 : t1};
                 float xv[8];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) {
-                    const int c = 8 * qb + g;
-                    xv[g] = c < 60 ? (float)Pe[c * KR + j] : 0.f;
-                }
+                for (int g = 0; g < 8; ++g) xv[g] = (8 * qb + g < 60) ? (hi[g] - tr[g % 3]) + lo[g] : 0.f;
                 split3_store8(xv, Bb + kmajor_off(j, 8 * qb), kTermB);
             }
             fence_proxy_async();   // this thread's tile writes -> the tensor cores
@@ -246,19 +305,24 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const int *__restrict__ con
             s_count[1] = t;
         }
         __syncwarp();
-    } else if (warp == kEpiWarp0 || warp == kEpiWarp0 + 1) {
-        const int row = 32 * (warp - kEpiWarp0) + lane;   // TMEM lanes 0..63 = rows
+    } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + kNEpi) {
+        // direction dn: TMEM lane i < 20 holds row 3i + dn for the 16 cases,
+        // lane 20 the sum of those rows; subtracting a twentieth of it
+        // removes each case's mean translation from the result
+        const int dn = warp - kEpiWarp0;
         for (int t = 0; t < nmine; ++t) {
             const int a = t % kNAcc;
             if (!wait(&ac_full[a], (uint32_t)((t / kNAcc) & 1))) break;
             tc_fence_after();
             float v[16];
-            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * (warp - kEpiWarp0)) << 16) + (uint32_t)(16 * a), v);
+            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * dn) << 16) + (uint32_t)(16 * a), v);
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ac_empty[a]);
-            if (row < 60) {
-                float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)elem(t) * 60 + row) * KR);
+#pragma unroll
+            for (int x = 0; x < 16; ++x) v[x] -= 0.05f * __shfl_sync(kFullMask, v[x], 20);
+            if (lane < 20) {
+                float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)elem(t) * 60 + 3 * lane + dn) * KR);
                 o[0] = make_float4(v[0], v[1], v[2], v[3]);
                 o[1] = make_float4(v[4], v[5], v[6], v[7]);
                 o[2] = make_float4(v[8], v[9], v[10], v[11]);
@@ -596,6 +660,27 @@ __global__ void k_mr_replace2(MState *st, const double *__restrict__ part, int G
     }
 }
 
+// ksum[e][d][k] = sum over the 20 nodes a of K_e(3a + d, k) from the packed
+// FP32 storkm (summed in FP64), 0 for k = 60..63: the direction sums of
+// K_e's rows that the tensor-core block product adds to its A operand.
+__global__ void k_mr_rowsums(int nels, const float *__restrict__ kp, float *__restrict__ ksum)
+{
+    const size_t total = (size_t)nels * 192;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t e = idx / 192;
+        const int r = (int)(idx - e * 192), d = r / 64, k = r % 64;
+        float v = 0.f;
+        if (k < 60) {
+            const float *ke = kp + e * 1832;
+            double sum = 0.0;
+            for (int a = 0; a < 20; ++a) sum += (double)ke[packed_off(3 * a + d, k)];
+            v = (float)sum;
+        }
+        ksum[idx] = v;
+    }
+}
+
 __global__ void k_mr_sums(const double *__restrict__ part, int G, double *__restrict__ out)
 {
     if (threadIdx.x < KR) out[threadIdx.x] = case_sum(part, G, threadIdx.x);
@@ -628,7 +713,9 @@ struct MultiBufs {
     int ns = 0;
     double *F = nullptr, *X = nullptr, *R = nullptr, *D = nullptr, *P = nullptr, *U = nullptr, *RR = nullptr,
            *eq = nullptr;
+    int ne = 0;
     float *ut32 = nullptr;
+    float *ksum = nullptr;   // [nels][3][64] direction sums of K_e's rows (tensor-core products)
     double *ut64 = nullptr, *part = nullptr, *sums = nullptr;
     MState *st = nullptr;
     MState *hst = nullptr;
@@ -637,8 +724,8 @@ MultiBufs g_mb;   // one block solve at a time per process
 
 void mb_free()
 {
-    void *p[] = {g_mb.F, g_mb.X, g_mb.R, g_mb.D, g_mb.P, g_mb.U, g_mb.RR, g_mb.eq, g_mb.ut32, g_mb.ut64, g_mb.part,
-                 g_mb.sums, g_mb.st};
+    void *p[] = {g_mb.F, g_mb.X, g_mb.R, g_mb.D, g_mb.P, g_mb.U, g_mb.RR, g_mb.eq, g_mb.ut32, g_mb.ksum, g_mb.ut64,
+                 g_mb.part, g_mb.sums, g_mb.st};
     for (void *q : p)
         if (q) cudaFree(q);
     if (g_mb.hst) cudaFreeHost(g_mb.hst);
@@ -679,7 +766,7 @@ static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
         const int smem = kTcSmem;
         MCK(cudaFuncSetAttribute(k_mr_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         const int grid = c.nels < c.nsm ? c.nels : c.nsm;
-        k_mr_elem_tc<<<grid, kTcThreads, smem, c.stream>>>(c.nels, c.km32p, c.conn, P, m.ut32, c.kerr, skip);
+        k_mr_elem_tc<<<grid, kTcThreads, smem, c.stream>>>(c.nels, c.km32p, m.ksum, c.conn, P, m.ut32, c.kerr, skip);
         return mr_launched(c, "k_mr_elem_tc");
     }
     if (prec == 32) {
@@ -708,7 +795,7 @@ static int mr_scatter(Ctx &c, int prec, int mode, const double *pf, double *out,
 
 static int mr_alloc(Ctx &c)
 {
-    if (g_mb.ns == c.nslots && g_mb.F) return 0;
+    if (g_mb.ns == c.nslots && g_mb.ne == c.nels && g_mb.F) return 0;
     mb_free();
     const size_t n = (size_t)c.nslots * KR;
     const size_t parts = (size_t)(c.Gs > c.G ? c.Gs : c.G) * KR * 4 + 64;
@@ -717,17 +804,28 @@ static int mr_alloc(Ctx &c)
         if (cudaMalloc((void **)q, n * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&g_mb.eq, (size_t)(c.neq > 0 ? c.neq : 1) * KR * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&g_mb.ut32, (size_t)c.nels * 60 * KR * 4) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&g_mb.ksum, (size_t)c.nels * 192 * 4) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&g_mb.ut64, (size_t)c.nels * 60 * KR * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&g_mb.part, parts * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&g_mb.sums, 64 * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&g_mb.st, sizeof(MState)) != cudaSuccess) goto fail;
     if (cudaMallocHost((void **)&g_mb.hst, sizeof(MState)) != cudaSuccess) goto fail;
     g_mb.ns = c.nslots;
+    g_mb.ne = c.nels;
     return 0;
 fail:
     mb_free();
     set_error("pf_solve_multi: cannot allocate the block vectors (%zu slots x %d cases)", (size_t)c.nslots, KR);
     return 1;
+}
+
+// direction sums of the packed storkm's rows for the tensor-core block
+// product (once per solve or product call: storkm may have changed)
+static int mr_rowsums(Ctx &c)
+{
+    const int grid = c.nsm * 8;
+    k_mr_rowsums<<<grid, 256, 0, c.stream>>>(c.nels, c.km32p, g_mb.ksum);
+    return mr_launched(c, "k_mr_rowsums");
 }
 
 // FP64 true residuals of all cases; returns per-case ||f - K x||^2 in rr_out
@@ -765,6 +863,7 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
         return PF_FAILURE;
     }
     if (mr_alloc(c)) return PF_FAILURE;
+    if (*prec == 16 && mr_rowsums(c)) return PF_FAILURE;
     MultiBufs &m = g_mb;
     const int G = c.G, Gs = c.Gs;
     // load cases: r(neq, k) column-major
@@ -896,6 +995,7 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, co
         return PF_FAILURE;
     }
     if (mr_alloc(c)) return PF_FAILURE;
+    if (*prec == 16 && mr_rowsums(c)) return PF_FAILURE;
     MultiBufs &m = g_mb;
     MCK(cudaMemcpyAsync(m.eq, p, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
     k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, c.slot_eq, c.neq, m.eq, m.P);
