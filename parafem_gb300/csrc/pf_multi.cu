@@ -55,20 +55,22 @@ constexpr int kStage = kStK + kStP + kStC;   // 15776 B, a multiple of 16
 constexpr int kNst = 4;                      // operand stages (bulk copies in flight)
 constexpr int kNTile = 3;                    // BF16 tile sets (A + B)
 constexpr int kNAcc = 4;                     // TMEM accumulators (16 columns each)
-constexpr int kBuildWarps = 16;              // warps 0-15 split K_e and P_e (one A task per thread)
-constexpr int kBWarps = 4;                   // warps 0-3 also split P_e (one B task per thread)
+constexpr int kBuildWarps = 16;              // warps 0-15 split K_e and P_e
+constexpr int kGroups = 2;                   // builder groups: warps 8g..8g+7 build the elements t = g mod 2
+constexpr int kGroupWarps = kBuildWarps / kGroups;
+constexpr int kBWarps = 4;                   // warps 8g..8g+3 also split P_e (one B task per thread)
 constexpr int kEpiWarp0 = 16;                // warps 16-18 read TMEM lanes 32d..32d+31 back (direction d)
 constexpr int kNEpi = 3;
 constexpr int kProdWarp = 19;                // warp 19 issues the bulk copies
 constexpr int kMmaWarp = 20;                 // warp 20, lane 0 issues the MMAs
 constexpr int kTcThreads = 21 * 32;
-static_assert(kBuildWarps * 32 >= 63 * 8, "one A task (row, 8 K-values) per builder thread");
-static_assert(kBWarps * 32 == KR * 8, "one B task (load case, 8 dofs) per thread of warps 0-3");
+static_assert(kGroupWarps * 32 * 2 >= 63 * 8, "two A tasks (row, 8 K-values) per builder thread");
+static_assert(kBWarps * 32 == KR * 8, "one B task (load case, 8 dofs) per thread of a group's first four warps");
 constexpr int kOffB = kNTile * kBufA;
 constexpr int kOffSt = kOffB + kNTile * kBufB;
 constexpr int kOffAux = kOffSt + kNst * kStage;
-constexpr int kOffSum = kOffAux + 256;       // [2][8][KR][3] partial direction sums of P_e
-constexpr int kTcSmem = kOffSum + 2 * 8 * KR * 3 * 4;
+constexpr int kOffSum = kOffAux + 256;       // [group][2][8][KR][3] partial direction sums of P_e
+constexpr int kTcSmem = kOffSum + kGroups * 2 * 8 * KR * 3 * 4;
 constexpr uint32_t kIdesc = idesc_bf16(128, 16);
 static_assert(kOffSt % 16 == 0 && kStage % 16 == 0 && kOffAux % 8 == 0, "bulk-copy alignment");
 static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
@@ -97,10 +99,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 //                of kNst stages;
 //   warps 0-15   split K_e (rows by direction, with the row sums) and P_e
 //                less its mean translations into three BF16 terms each and
-//                write them into a ring of kNTile tile sets (one 8-value row
-//                segment of K_e per thread, its shared-memory offsets
-//                computed once; warps 0-3 also one 8-dof segment of P_e,
-//                exchanging their partial sums through shared memory);
+//                write them into a ring of kNTile tile sets.  Two groups of
+//                eight warps take alternate elements; a thread has two
+//                8-value row segments of K_e (shared-memory offsets computed
+//                once), and a group's warps 0-3 also one 8-dof segment of
+//                P_e each, exchanging partial sums through shared memory;
 //   warp 20      one thread issues the six products of order <= 2^-16
 //                (24 MMAs, M=128, N=16, K=16) into a ring of kNAcc TMEM
 //                accumulators and commits them to mbarriers that free the
@@ -128,9 +131,9 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
     uint64_t *tl_empty = tl_full + kNTile;
     uint64_t *ac_full = tl_empty + kNTile;
     uint64_t *ac_empty = ac_full + kNAcc;
-    uint64_t *sum_bar = ac_empty + kNAcc;   // the four B warps' partial sums of an element are written
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sum_bar + 1);
-    float *psum = reinterpret_cast<float *>(sm + kOffSum);   // [t & 1][chunk][case][direction]
+    uint64_t *sum_bar = ac_empty + kNAcc;   // [group]: its four B warps' partial sums of an element are written
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sum_bar + kGroups);
+    float *psum = reinterpret_cast<float *>(sm + kOffSum);   // [group][k & 1][chunk][case][direction]
     volatile int *s_fail = reinterpret_cast<volatile int *>(tslot + 1);
     int *s_count = reinterpret_cast<int *>(tslot + 2);   // [0] copies issued, [1] MMA groups committed
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -142,17 +145,17 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
     if (tid == 0) {
         for (int i = 0; i < kNst; ++i) {
             mbar_init(&st_full[i], 1);
-            mbar_init(&st_empty[i], kBuildWarps);
+            mbar_init(&st_empty[i], kGroupWarps);
         }
         for (int i = 0; i < kNTile; ++i) {
-            mbar_init(&tl_full[i], kBuildWarps);
+            mbar_init(&tl_full[i], kGroupWarps);
             mbar_init(&tl_empty[i], 1);
         }
         for (int i = 0; i < kNAcc; ++i) {
             mbar_init(&ac_full[i], 1);
             mbar_init(&ac_empty[i], kNEpi);
         }
-        mbar_init(sum_bar, kBWarps);
+        for (int g = 0; g < kGroups; ++g) mbar_init(&sum_bar[g], kBWarps);
         mbar_fence_init();
         *s_fail = 0;
         s_count[0] = s_count[1] = 0;
@@ -201,33 +204,45 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
         }
         if (lane == 0) s_count[0] = issued;
     } else if (warp < kBuildWarps) {
-        // this thread's A task (tid < 504): A row 32d + i, K-values 8q..8q+7.
-        // i < 20: K(3i + d, k) at packed_off; i = 20: the sum of direction
-        // d's rows, after the P blocks in the stage; K-values past 59 read
-        // the zero pad at 1830.
-        const bool a_task = tid < 63 * 8;
-        const int r63 = tid % 63, q = tid / 63;
-        const int d = r63 / 21, i = r63 % 21;
-        int off[8];
+        // Two groups of eight warps build alternate elements, so two
+        // elements are in the build stage at once.  A thread of a group has
+        // two A tasks (of 504): A row 32d + i, K-values 8q..8q+7.  i < 20:
+        // K(3i + d, k) at packed_off; i = 20: the sum of direction d's rows,
+        // after the P blocks in the stage; K-values past 59 read the zero
+        // pad at 1830.
+        const int grp = warp / kGroupWarps, gw = warp % kGroupWarps, gtid = tid % (kGroupWarps * 32);
+        int off[2][8];
+        uint32_t a_off[2];
+        bool a_task[2];
 #pragma unroll
-        for (int g = 0; g < 8; ++g) {
-            const int k = 8 * q + g;
-            off[g] = (!a_task || k >= 60) ? 1830 : i < 20 ? packed_off(3 * i + d, k) : (kStK + kStP) / 4 + 64 * d + k;
+        for (int h = 0; h < 2; ++h) {
+            const int task = gtid + h * kGroupWarps * 32;
+            a_task[h] = task < 63 * 8;
+            const int r63 = task % 63, q = task / 63;
+            const int d = r63 / 21, i = r63 % 21;
+#pragma unroll
+            for (int g = 0; g < 8; ++g) {
+                const int k = 8 * q + g;
+                off[h][g] = (!a_task[h] || k >= 60) ? 1830
+                            : i < 20                ? packed_off(3 * i + d, k)
+                                                    : (kStK + kStP) / 4 + 64 * d + k;
+            }
+            a_off[h] = a_task[h] ? kmajor_off(32 * d + i, 8 * q) : 0u;
         }
-        const uint32_t a_off = a_task ? kmajor_off(32 * d + i, 8 * q) : 0u;
-        // B task (warps 0-3): load case j, dofs 8qb..8qb+7 (dof c has
-        // direction (rb + c - 8qb) % 3)
-        const int j = tid & (KR - 1), qb = tid >> 4;
+        // B task (the group's warps 0-3): load case j, dofs 8qb..8qb+7 (dof c
+        // has direction (rb + c - 8qb) % 3)
+        const int j = gtid & (KR - 1), qb = gtid >> 4;
         const int rb = (2 * qb) % 3;
-        const bool b_task = warp < kBWarps;
-        for (int t = 0; t < nmine; ++t) {
-            const int s = t % kNst, b = t % kNTile;
+        const bool b_task = gw < kBWarps;
+        uint64_t *my_sum = &sum_bar[grp];
+        for (int t = grp; t < nmine; t += kGroups) {
+            const int s = t % kNst, b = t % kNTile, kk = t / kGroups;
             if (!wait(&st_full[s], (uint32_t)((t / kNst) & 1))) break;
             if (t >= kNTile && !wait(&tl_empty[b], (uint32_t)((t / kNTile - 1) & 1))) break;
             const float *U = reinterpret_cast<const float *>(stg + s * kStage);
             const double *Pe = reinterpret_cast<const double *>(stg + s * kStage + kStK);
             unsigned char *Ab = A + b * kBufA, *Bb = B + b * kBufB;
-            float *ps = psum + (t & 1) * (8 * KR * 3);
+            float *ps = psum + (grp * 2 + (kk & 1)) * (8 * KR * 3);
             float hi[8], lo[8];
             if (b_task) {
                 // P_e(c, j) at c*16 + j: FP32 high and low parts, and this
@@ -242,19 +257,23 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
                 ps[(qb * KR + j) * 3 + 1] = rb == 0 ? u1 : rb == 1 ? u0 : u2;
                 ps[(qb * KR + j) * 3 + 2] = rb == 0 ? u2 : rb == 1 ? u1 : u0;
                 __syncwarp();
-                if (lane == 0) mbar_arrive(sum_bar);
+                if (lane == 0) mbar_arrive(my_sum);
             }
-            if (a_task) {
-                float xv[8];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) xv[g] = U[off[g]];
-                split3_store8(xv, Ab + a_off, kTermA);
+            for (int h = 0; h < 2; ++h) {
+                if (a_task[h]) {
+                    float xv[8];
+#pragma unroll
+                    for (int g = 0; g < 8; ++g) xv[g] = U[off[h][g]];
+                    split3_store8(xv, Ab + a_off[h], kTermA);
+                }
             }
             if (b_task) {
                 // the four B warps' partial sums are in (bounded wait; the
-                // double buffer is safe because no warp passes element t+1's
-                // wait before every warp has arrived for it)
-                if (!wait(sum_bar, (uint32_t)(t & 1))) break;
+                // double buffer is safe because no warp of the group passes
+                // the wait for its next element before every one of them has
+                // arrived for it)
+                if (!wait(my_sum, (uint32_t)(kk & 1))) break;
                 float tdir[3];
 #pragma unroll
                 for (int dd = 0; dd < 3; ++dd) {
