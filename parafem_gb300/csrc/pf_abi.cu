@@ -94,7 +94,7 @@ static void free_mesh(Ctx &c)
     drop_graph(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
-    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore);
+    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.psplit);
     c.shared = false;
     c.kind = KIND_SOLID20;
     dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
@@ -707,6 +707,7 @@ extern "C" int pf_set_shared_km(void **ctx, const double *km)
         }
     if (!c.skm64 && dalloc(&c.skm64, 3600, "shared km")) return PF_FAILURE;
     if (!c.skm32 && dalloc(&c.skm32, 3600, "shared km")) return PF_FAILURE;
+    if (!c.psplit && dalloc(&c.psplit, (size_t)c.nslots, "split search direction")) return PF_FAILURE;
     std::vector<float> k32(3600);
     for (int i = 0; i < 3600; ++i) k32[i] = (float)km[i];
     CK(cudaMemcpyAsync(c.skm64, km, 3600 * sizeof(double), cudaMemcpyHostToDevice, c.stream));

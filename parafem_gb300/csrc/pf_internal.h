@@ -89,6 +89,7 @@ struct Ctx {
     double *skm64 = nullptr;    // [3600] column-major
     float *skm32 = nullptr;     // [3600]
     bool shared_attr = false;   // shared-memory attribute of the tensor-core kernel set
+    float2 *psplit = nullptr;   // [nslots] FP32 high and low parts of p (shared km): written with p
     int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel
     int sym_warps = 14, sym_stages = 2;
     unsigned long long sym_attr = 0;   // configurations whose shared-memory attribute is set

@@ -9,6 +9,7 @@
 // Reductions are deterministic: fixed per-thread assignment, xor-shuffle
 // trees, per-block partials summed in a fixed order by the consumer kernel.
 #include "pf_device.cuh"
+#include "pf_tc.cuh"
 
 #include <cmath>
 #include <cstdio>
@@ -349,11 +350,13 @@ k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
 
 // ---------------------------------------------------------------------------
 // PCG (p121.f90:86-104).
-// init: x = 0, r = rhs, d = dinv*r, p = d; partials r.d and r.r
+// init: x = 0, r = rhs, d = dinv*r, p = d; partials r.d and r.r.  ps
+// (shared-km contexts): the FP32 high and low parts of p, which the
+// tensor-core product gathers instead of p.
 __global__ void __launch_bounds__(256)
 k_pcg_init(int ns, const double *__restrict__ rhs, const double *__restrict__ dinv,
            double *__restrict__ x, double *__restrict__ r, double *__restrict__ d,
-           double *__restrict__ p, double *__restrict__ part, int G, int keep_x)
+           double *__restrict__ p, double *__restrict__ part, int G, int keep_x, float2 *__restrict__ ps)
 {
     double rd = 0.0, rr = 0.0;
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
@@ -363,6 +366,11 @@ k_pcg_init(int ns, const double *__restrict__ rhs, const double *__restrict__ di
         r[s] = rv;
         d[s] = dv;
         p[s] = dv;
+        if (ps) {
+            float h, l;
+            tc::split_f64(dv, h, l);
+            ps[s] = make_float2(h, l);
+        }
         rd = fma(rv, dv, rd);
         rr = fma(rv, rv, rr);
     }
@@ -438,16 +446,24 @@ k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict_
     }
 }
 
-// update2: beta = (r.d)/up; p = d + p*beta.  Reads st->up only.
+// update2: beta = (r.d)/up; p = d + p*beta (and its FP32 high and low
+// parts into ps, shared-km contexts).  Reads st->up only.
 __global__ void __launch_bounds__(256)
 k_pcg_update2(int ns, const PcgState *__restrict__ st, const double *__restrict__ part, int G,
-              const double *__restrict__ d, double *__restrict__ p)
+              const double *__restrict__ d, double *__restrict__ p, float2 *__restrict__ ps)
 {
     if (block_stopped(st)) return;
     const double rd = reduce_partials(part, G, false);
     const double beta = rd / st->up;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x)
-        p[s] = fma(p[s], beta, d[s]);
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const double pn = fma(p[s], beta, d[s]);
+        p[s] = pn;
+        if (ps) {
+            float h, l;
+            tc::split_f64(pn, h, l);
+            ps[s] = make_float2(h, l);
+        }
+    }
 }
 
 // finish (one block): the iteration's bookkeeping -- up for the next
@@ -790,7 +806,8 @@ int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
 int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit, bool keep_x)
 {
     c.stop_mode = stop_mode;
-    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G, keep_x ? 1 : 0);
+    k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G, keep_x ? 1 : 0,
+                                          c.shared ? c.psplit : nullptr);
     if (check_launch(c, "k_pcg_init")) return 1;
     k_pcg_init2<<<1, 256, 0, c.stream>>>(c.st, c.part_u, c.G, stop_mode, tol, limit);
     return check_launch(c, "k_pcg_init2");
@@ -809,7 +826,7 @@ int launch_update1(Ctx &c, double *xsol)
 
 int launch_update2(Ctx &c)
 {
-    k_pcg_update2<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_u, c.G, c.d, c.p);
+    k_pcg_update2<<<c.G, 256, 0, c.stream>>>(c.nslots, c.st, c.part_u, c.G, c.d, c.p, c.shared ? c.psplit : nullptr);
     if (check_launch(c, "k_pcg_update2")) return 1;
     k_pcg_finish<<<1, 256, 0, c.stream>>>(c.st, c.part_u, c.G);
     return check_launch(c, "k_pcg_finish");

@@ -114,7 +114,7 @@ k_elem_shared64(int nels, const double *__restrict__ km, const int *__restrict__
 // before it frees its TMEM and returns.
 __global__ void __launch_bounds__(kSThreads, 1)
 k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict__ conn,
-                 const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
+                 const float2 *__restrict__ ps, float *__restrict__ ut, const PcgState *__restrict__ st,
                  int *__restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char sm[];
@@ -225,14 +225,14 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
             // arithmetic and the rounding acts only on p - t).
             const int j = lane & 3, qq = lane >> 2;
             const int r = (2 * qq) % 3;   // direction of dof 8qq; dof 8qq+g has (r + g) % 3
-            double pv[2][8];   // both passes' loads in flight together
+            float2 pv[2][8];   // p's FP32 high and low parts; both passes' loads in flight together
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int n = 8 * warp + 4 * h + j;
 #pragma unroll
                 for (int g = 0; g < 8; ++g) {
                     const int c = 8 * qq + g;
-                    pv[h][g] = (c < 60 && n < n_here) ? p[(size_t)3 * ct[n * 20 + c / 3] + c % 3] : 0.0;
+                    pv[h][g] = (c < 60 && n < n_here) ? ps[(size_t)3 * ct[n * 20 + c / 3] + c % 3] : make_float2(0.f, 0.f);
                 }
             }
             float xv[2][8];
@@ -240,7 +240,10 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
             for (int h = 0; h < 2; ++h) {
                 float hi[8], lo[8];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) split_f64(pv[h][g], hi[g], lo[g]);
+                for (int g = 0; g < 8; ++g) {
+                    hi[g] = pv[h][g].x;
+                    lo[g] = pv[h][g].y;
+                }
                 // sums of this chunk by direction, then over the element's chunks
                 const float u0 = hi[0] + hi[3] + hi[6], u1 = hi[1] + hi[4] + hi[7], u2 = hi[2] + hi[5];
                 float s0 = r == 0 ? u0 : r == 1 ? u2 : u1;
@@ -373,6 +376,16 @@ int launch_shared_ediag(Ctx &c)
 // u_e = km p_e for every element: prec 64 on CUDA cores in FP64, otherwise
 // on the tensor cores (FP32-class).  st: PCG state whose stop flag turns the
 // launch into a no-op (nullptr outside a PCG run).
+// ps[s] = FP32 high and low parts of p[s]
+__global__ void k_split_p(int ns, const double *__restrict__ p, float2 *__restrict__ ps)
+{
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        float h, l;
+        split_f64(p[s], h, l);
+        ps[s] = make_float2(h, l);
+    }
+}
+
 int launch_elem_shared(Ctx &c, int prec, const double *p, const PcgState *st)
 {
     cudaError_t e;
@@ -391,10 +404,16 @@ int launch_elem_shared(Ctx &c, int prec, const double *p, const PcgState *st)
             }
             c.shared_attr = true;
         }
+        // the kernel gathers p's FP32 high and low parts: the PCG kernels
+        // keep them with c.p; any other vector is split here first
+        if (p != c.p) {
+            k_split_p<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, p, c.psplit);
+            c.launches++;
+        }
         const int ntiles = (c.nels + kNT - 1) / kNT;
         const int grid = ntiles < c.nsm ? ntiles : c.nsm;
-        k_elem_shared_tc<<<grid, kSThreads, kSSmem, c.stream>>>(c.nels, c.skm32, c.conn, p, (float *)c.utemp, st,
-                                                                 c.kerr);
+        k_elem_shared_tc<<<grid, kSThreads, kSSmem, c.stream>>>(c.nels, c.skm32, c.conn, c.psplit, (float *)c.utemp,
+                                                                 st, c.kerr);
     }
     c.launches++;
     e = cudaGetLastError();
