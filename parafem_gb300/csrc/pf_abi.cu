@@ -706,12 +706,21 @@ extern "C" int pf_set_shared_km(void **ctx, const double *km)
             return PF_FAILURE;
         }
     if (!c.skm64 && dalloc(&c.skm64, 3600, "shared km")) return PF_FAILURE;
-    if (!c.skm32 && dalloc(&c.skm32, 3600, "shared km")) return PF_FAILURE;
+    if (!c.skm32 && dalloc(&c.skm32, 3600 + 192, "shared km")) return PF_FAILURE;
     if (!c.psplit && dalloc(&c.psplit, (size_t)c.nslots, "split search direction")) return PF_FAILURE;
-    std::vector<float> k32(3600);
+    // FP32 km, then the direction sums of its rows, sum over a of K(3a + d, k)
+    // at 3600 + 64d + k (summed in FP64, zero for k = 60..63): the tensor-core
+    // product's A operand carries them to remove the results' mean translation
+    std::vector<float> k32(3600 + 192, 0.0f);
     for (int i = 0; i < 3600; ++i) k32[i] = (float)km[i];
+    for (int d = 0; d < 3; ++d)
+        for (int k = 0; k < 60; ++k) {
+            double sum = 0.0;
+            for (int a = 0; a < 20; ++a) sum += (double)k32[3 * a + d + 60 * k];
+            k32[3600 + 64 * d + k] = (float)sum;
+        }
     CK(cudaMemcpyAsync(c.skm64, km, 3600 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    CK(cudaMemcpyAsync(c.skm32, k32.data(), 3600 * sizeof(float), cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.skm32, k32.data(), (3600 + 192) * sizeof(float), cudaMemcpyHostToDevice, c.stream));
     c.shared = true;
     drop_graph(c);
     TRY(launch_shared_ediag(c));

@@ -87,7 +87,7 @@ struct Ctx {
     // one element matrix shared by every element (PCG_KM); per-element storkm unused
     bool shared = false;
     double *skm64 = nullptr;    // [3600] column-major
-    float *skm32 = nullptr;     // [3600]
+    float *skm32 = nullptr;     // [3600 + 192]: km, then the direction sums of its rows ([3][64])
     bool shared_attr = false;   // shared-memory attribute of the tensor-core kernel set
     float2 *psplit = nullptr;   // [nslots] FP32 high and low parts of p (shared km): written with p
     int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel

@@ -145,7 +145,8 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
     // i - 15 for i = 15..17, zero otherwise.  The sums are zero in exact
     // arithmetic (K annihilates rigid translations); they carry the rounding
     // of the FP32 km and put each element's per-direction sum of results
-    // beside its rows in the accumulator.  K(i,k) = km32[i + 60k].
+    // beside its rows in the accumulator.  K(i,k) = km32[i + 60k]; the sums
+    // follow km (km32[3600 + 64d + k]), so the prologue has no FP64 work.
     for (int i = tid; i < kSOffC / 16; i += kSThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
     __syncthreads();
     for (int task = tid; task < kSRowsA * 8; task += kSThreads) {
@@ -159,9 +160,7 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
             if (k < 60 && i < 15) {
                 v = km32[3 * (5 * w + i / 3) + i % 3 + 60 * k];
             } else if (k < 60 && i < 18) {
-                double sum = 0.0;
-                for (int a = 0; a < 20; ++a) sum += (double)km32[3 * a + (i - 15) + 60 * k];
-                v = (float)sum;
+                v = km32[3600 + 64 * (i - 15) + k];   // formed on the host with km
             }
             xv[g] = v;
         }
@@ -320,15 +319,15 @@ k_elem_shared_tc(int nels, const float *__restrict__ km32, const int *__restrict
             const int n_here = tile_n(t);
             const size_t e0 = (size_t)tile(t) * kNT;
 #pragma unroll 1
-            for (int ch = 0; ch < kNT / 16; ++ch) {
-                float v[16];
-                tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)(a * kNT + 16 * ch), v);
+            for (int ch = 0; ch < kNT / 32; ++ch) {   // 32 columns per TMEM round trip
+                float v[32];
+                tmem_ld_32x32b_x32(tmem + ((uint32_t)(32 * w) << 16) + (uint32_t)(a * kNT + 32 * ch), v);
 #pragma unroll
-                for (int x = 0; x < 16; ++x) v[x] -= 0.05f * __shfl_sync(0xffffffffu, v[x], src);
+                for (int x = 0; x < 32; ++x) v[x] -= 0.05f * __shfl_sync(0xffffffffu, v[x], src);
                 if (lane < 15) {
 #pragma unroll
-                    for (int x = 0; x < 16; ++x) {
-                        const int n = 16 * ch + x;
+                    for (int x = 0; x < 32; ++x) {
+                        const int n = 32 * ch + x;
                         if (n < n_here) ut[(e0 + n) * 80 + roff] = v[x];
                     }
                 }
