@@ -222,8 +222,10 @@ int pf_solve_multi(void **ctx, const int *k, const double *r, const double *tol,
 /* Block product U = K P for k = 16 cases (equation order, (neq,k)
  * column-major); prec 16 (tensor cores), 32 (FP32 CUDA cores), 64 (FP64). */
 int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, const double *p, double *u);
-/* Releases the block solver's device buffers. */
-int pf_multi_free(void);
+/* Releases the context's block-solve buffers (allocated by the first
+ * pf_solve_multi or pf_ebe_matvec_multi; also released with the mesh and by
+ * pf_ctx_destroy). */
+int pf_multi_free(void **ctx);
 
 /* ---------------------------------------------------------------------- */
 /* Serving layer: continuous batching of many independent solves.  No

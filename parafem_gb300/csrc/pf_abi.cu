@@ -92,6 +92,7 @@ static void drop_graph(Ctx &c)
 static void free_mesh(Ctx &c)
 {
     drop_graph(c);
+    multi_release(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
     dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.psplit);

@@ -7,6 +7,8 @@
 
 namespace pf {
 
+struct MultiBufs;   // block-solve buffers (pf_multi.cu)
+
 // Packed-symmetric FP32 storkm (1,830 floats + 2 zero pads per element), by
 // cyclic diagonals: D[s][i] = K(i, (i+s) mod 60) at 60 s + i for s = 0..29,
 // i = 0..59, and the 30 distinct entries of diagonal 30, K(i, i+30) for
@@ -90,6 +92,7 @@ struct Ctx {
     float *skm32 = nullptr;     // [3600 + 192]: km, then the direction sums of its rows ([3][64])
     bool shared_attr = false;   // shared-memory attribute of the tensor-core kernel set
     float2 *psplit = nullptr;   // [nslots] FP32 high and low parts of p (shared km): written with p
+    MultiBufs *multi = nullptr; // block-solve vectors, allocated on the first block solve or product
     int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel
     int sym_warps = 14, sym_stages = 2;
     unsigned long long sym_attr = 0;   // configurations whose shared-memory attribute is set
@@ -141,6 +144,7 @@ int launch_centroid_stress(Ctx &c, int e0, int count, const double *xslot, doubl
 // FP32 storkm (bulk-copy staged), 31 full FP32 storkm
 enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31 };
 int launch_pack_sym32(Ctx &c);
+void multi_release(Ctx &c);   // frees the context's block-solve buffers (pf_multi.cu)
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);
 int sym32_prepare();   // shared-memory attribute of the mapped launch (once per device, outside capture)
 int launch_elem_sym32_mapped(cudaStream_t stream, int nsm, int n, const float *kp, const int *conn, const double *p,

@@ -727,7 +727,8 @@ __global__ void k_mr_slot_to_eq(int neq, const int *__restrict__ eq_slot, const 
 }
 
 // ---------------------------------------------------------------------------
-namespace {
+// Block-solve buffers of one context (Ctx::multi), allocated on the first
+// block solve or product and kept while the mesh is unchanged.
 struct MultiBufs {
     int ns = 0;
     double *F = nullptr, *X = nullptr, *R = nullptr, *D = nullptr, *P = nullptr, *U = nullptr, *RR = nullptr,
@@ -739,18 +740,24 @@ struct MultiBufs {
     MState *st = nullptr;
     MState *hst = nullptr;
 };
-MultiBufs g_mb;   // one block solve at a time per process
-
-void mb_free()
+namespace {
+void mb_free(MultiBufs &m)
 {
-    void *p[] = {g_mb.F, g_mb.X, g_mb.R, g_mb.D, g_mb.P, g_mb.U, g_mb.RR, g_mb.eq, g_mb.ut32, g_mb.ksum, g_mb.ut64,
-                 g_mb.part, g_mb.sums, g_mb.st};
+    void *p[] = {m.F, m.X, m.R, m.D, m.P, m.U, m.RR, m.eq, m.ut32, m.ksum, m.ut64, m.part, m.sums, m.st};
     for (void *q : p)
         if (q) cudaFree(q);
-    if (g_mb.hst) cudaFreeHost(g_mb.hst);
-    g_mb = MultiBufs();
+    if (m.hst) cudaFreeHost(m.hst);
+    m = MultiBufs();
 }
 }  // namespace
+
+void multi_release(Ctx &c)
+{
+    if (!c.multi) return;
+    mb_free(*c.multi);
+    delete c.multi;
+    c.multi = nullptr;
+}
 
 }  // namespace pf
 
@@ -780,7 +787,7 @@ static int mr_launched(Ctx &c, const char *name)
 // into ut64).  skip: device flag that turns the launch into a no-op.
 static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
 {
-    MultiBufs &m = g_mb;
+    MultiBufs &m = *c.multi;
     if (prec == 16) {
         const int smem = kTcSmem;
         MCK(cudaFuncSetAttribute(k_mr_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
@@ -800,7 +807,7 @@ static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
 
 static int mr_scatter(Ctx &c, int prec, int mode, const double *pf, double *out, const int *skip)
 {
-    MultiBufs &m = g_mb;
+    MultiBufs &m = *c.multi;
     const int G = c.Gs;
     if (prec == 64) {
         if (mode == 0) k_mr_scatter<double, 0><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut64, c.freemask, pf, out, m.part, skip);
@@ -814,26 +821,28 @@ static int mr_scatter(Ctx &c, int prec, int mode, const double *pf, double *out,
 
 static int mr_alloc(Ctx &c)
 {
-    if (g_mb.ns == c.nslots && g_mb.ne == c.nels && g_mb.F) return 0;
-    mb_free();
+    if (!c.multi) c.multi = new MultiBufs();
+    MultiBufs &m = *c.multi;
+    if (m.ns == c.nslots && m.ne == c.nels && m.F) return 0;
+    mb_free(m);
     const size_t n = (size_t)c.nslots * KR;
     const size_t parts = (size_t)(c.Gs > c.G ? c.Gs : c.G) * KR * 4 + 64;
-    double **v[] = {&g_mb.F, &g_mb.X, &g_mb.R, &g_mb.D, &g_mb.P, &g_mb.U, &g_mb.RR};
+    double **v[] = {&m.F, &m.X, &m.R, &m.D, &m.P, &m.U, &m.RR};
     for (double **q : v)
         if (cudaMalloc((void **)q, n * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.eq, (size_t)(c.neq > 0 ? c.neq : 1) * KR * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.ut32, (size_t)c.nels * 60 * KR * 4) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.ksum, (size_t)c.nels * 192 * 4) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.ut64, (size_t)c.nels * 60 * KR * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.part, parts * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.sums, 64 * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&g_mb.st, sizeof(MState)) != cudaSuccess) goto fail;
-    if (cudaMallocHost((void **)&g_mb.hst, sizeof(MState)) != cudaSuccess) goto fail;
-    g_mb.ns = c.nslots;
-    g_mb.ne = c.nels;
+    if (cudaMalloc((void **)&m.eq, (size_t)(c.neq > 0 ? c.neq : 1) * KR * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.ut32, (size_t)c.nels * 60 * KR * 4) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.ksum, (size_t)c.nels * 192 * 4) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.ut64, (size_t)c.nels * 60 * KR * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.part, parts * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.sums, 64 * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.st, sizeof(MState)) != cudaSuccess) goto fail;
+    if (cudaMallocHost((void **)&m.hst, sizeof(MState)) != cudaSuccess) goto fail;
+    m.ns = c.nslots;
+    m.ne = c.nels;
     return 0;
 fail:
-    mb_free();
+    mb_free(m);
     set_error("pf_solve_multi: cannot allocate the block vectors (%zu slots x %d cases)", (size_t)c.nslots, KR);
     return 1;
 }
@@ -843,14 +852,14 @@ fail:
 static int mr_rowsums(Ctx &c)
 {
     const int grid = c.nsm * 8;
-    k_mr_rowsums<<<grid, 256, 0, c.stream>>>(c.nels, c.km32p, g_mb.ksum);
+    k_mr_rowsums<<<grid, 256, 0, c.stream>>>(c.nels, c.km32p, c.multi->ksum);
     return mr_launched(c, "k_mr_rowsums");
 }
 
 // FP64 true residuals of all cases; returns per-case ||f - K x||^2 in rr_out
 static int mr_true_residual(Ctx &c, double *rr_out)
 {
-    MultiBufs &m = g_mb;
+    MultiBufs &m = *c.multi;
     if (mr_elem(c, 64, m.X, nullptr)) return 1;
     if (mr_scatter(c, 64, 1, m.F, m.RR, nullptr)) return 1;
     k_mr_sums<<<1, 32, 0, c.stream>>>(m.part, c.Gs, m.sums);
@@ -883,7 +892,7 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
     }
     if (mr_alloc(c)) return PF_FAILURE;
     if (*prec == 16 && mr_rowsums(c)) return PF_FAILURE;
-    MultiBufs &m = g_mb;
+    MultiBufs &m = *c.multi;
     const int G = c.G, Gs = c.Gs;
     // load cases: r(neq, k) column-major
     MCK(cudaMemcpyAsync(m.eq, r, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
@@ -1015,7 +1024,7 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, co
     }
     if (mr_alloc(c)) return PF_FAILURE;
     if (*prec == 16 && mr_rowsums(c)) return PF_FAILURE;
-    MultiBufs &m = g_mb;
+    MultiBufs &m = *c.multi;
     MCK(cudaMemcpyAsync(m.eq, p, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
     k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, c.slot_eq, c.neq, m.eq, m.P);
     if (mr_launched(c, "k_mr_eq_to_slot")) return PF_FAILURE;
@@ -1035,8 +1044,12 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, co
     return PF_SUCCESS;
 }
 
-extern "C" int pf_multi_free(void)
+extern "C" int pf_multi_free(void **ctx)
 {
-    mb_free();
+    if (!ctx || !*ctx) return PF_SUCCESS;
+    Ctx &c = *(Ctx *)*ctx;
+    cudaSetDevice(c.device);
+    cudaStreamSynchronize(c.stream);
+    multi_release(c);
     return PF_SUCCESS;
 }

@@ -67,7 +67,7 @@ _SIGS = {
     "pf_solve_multi": [_VPP, _IP, ctypes.c_void_p, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p,
                        ctypes.c_void_p],
     "pf_ebe_matvec_multi": [_VPP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
-    "pf_multi_free": [],
+    "pf_multi_free": [_VPP],
     "pf_batch_create": [_IP, _LLP, _IP, _IP, _VPP],
     "pf_batch_destroy": [_VPP],
     "pf_batch_capacity": [_VPP, _LLP, _LLP],
@@ -370,6 +370,11 @@ class Solver:
         _check(lib().pf_bench_iterations(self._ref, _i(prec), _i(steps), ctypes.byref(a), ctypes.byref(b),
                                          ctypes.byref(c)), "pf_bench_iterations")
         return a.value, b.value, c.value
+
+    def multi_free(self):
+        """Releases this context's block-solve buffers (pf_multi_free); the
+        next block solve or product allocates them again."""
+        _check(lib().pf_multi_free(self._ref), "pf_multi_free")
 
     def solve_multi(self, R, tol, limit, prec=16):
         """k = 16 load cases together: R (neq, 16) -> X (neq, 16), iters (16,), relres (16,)."""

@@ -71,3 +71,26 @@ def test_tensor_core_block_product_keeps_translations_out_of_the_rounding():
     e32 = np.abs(u32 - u64)[inner].max()
     assert e32 > 0.0
     assert e16 <= 1e-2 * e32, (e16, e32)
+
+
+def test_block_buffers_belong_to_the_context():
+    """Each context keeps its own block-solve buffers: products of two
+    meshes interleave, and pf_multi_free releases one context's buffers
+    without touching the other's."""
+    s1, p1 = setup_solver(4, 3, 3)
+    s2, p2 = setup_solver(5, 4, 3, seed=4)
+    try:
+        rng = np.random.default_rng(15)
+        X1 = rng.standard_normal((p1["neq"], 16))
+        X2 = rng.standard_normal((p2["neq"], 16))
+        a1 = s1.ebe_matvec_multi(X1, 16)
+        a2 = s2.ebe_matvec_multi(X2, 16)
+        b1 = s1.ebe_matvec_multi(X1, 16)
+        s2.multi_free()
+        b2 = s2.ebe_matvec_multi(X2, 16)
+        c1 = s1.ebe_matvec_multi(X1, 16)
+    finally:
+        s1.close()
+        s2.close()
+    assert np.array_equal(a1, b1) and np.array_equal(a1, c1)
+    assert np.array_equal(a2, b2)
