@@ -69,99 +69,115 @@ __global__ void k_sample(int nip, int exact, double *gp)
 }
 
 // ---------------------------------------------------------------------------
-// storkm integration (p121.f90:54-64).  One 128-thread CTA per element;
-// thread t owns node pairs (a,b) = t, t+128, t+256, t+384 of the 20x20 block
-// grid and accumulates their 3x3 blocks of B'DB*det*w over the Gauss points.
-// The 3x3 block of B'DB for nodes a,b with gradients ga, gb is
+// storkm integration (p121.f90:54-64): sum over the Gauss points of
+// B'DB*det*w.  For isotropic D and nodes a, b with gradients ga, gb the 3x3
+// block of B'DB is
 //   (i,i): D11 ga_i gb_i + D44 sum_{k!=i} ga_k gb_k
 //   (i,j): D12 ga_i gb_j + D44 ga_j gb_i
-// which is the dense MATMUL(MATMUL(TRANSPOSE(bee),dee),bee) of p121.f90:61-62
-// with the zero entries of bee (BEEMAT, new_library.f90:976-993) skipped.
-__global__ void __launch_bounds__(128)
+// -- the dense MATMUL(MATMUL(TRANSPOSE(bee),dee),bee) of p121.f90:61-62 with
+// the zero entries of bee (BEEMAT, new_library.f90:976-993) skipped.  Both
+// are linear in M_ab(i,j) = sum_gp det*w ga_i gb_j, so each node pair
+// accumulates M_ab (9 FMA per point) and forms its block once.
+//
+// One CTA of kFormThreads threads per element (grid-stride): the shape
+// derivatives at the Gauss points are computed once per CTA; per element the
+// 27 Jacobians, their inverses and the 27 x 20 gradients are formed in four
+// phases, then thread t < 210 owns node pair (a, b), a <= b, and writes the
+// blocks (a, b) and (b, a) = (a, b)'.  GB300's FP64 rate is about 1/60 of its
+// FP32 rate; this order needs about 64k FP64 operations per element at
+// nip = 27 instead of the 486k of a per-point B'DB.
+constexpr int kFormThreads = 224;
+__global__ void __launch_bounds__(kFormThreads)
 k_form_storkm(int nels, int nip, const double *__restrict__ gp, const double *__restrict__ coord,
               const double *__restrict__ me, const double *__restrict__ mv, int nmat,
               double *__restrict__ km64, float *__restrict__ km32, double *__restrict__ ediag)
 {
-    __shared__ double s_coord[60];  // coord(20,3)
-    __shared__ double s_der[60];    // der(3,20)
-    __shared__ double s_jac[9];
-    __shared__ double s_deriv[60];  // deriv(3,20)
-    __shared__ double s_det;
+    __shared__ double s_der[27][60];   // der(3,20) at each point
+    __shared__ double s_w[27];
+    __shared__ double s_coord[60];     // coord(20,3)
+    __shared__ double s_jac[27][9];    // jac, then its inverse
+    __shared__ double s_wd[27];        // det * w
+    __shared__ double s_g[27][60];     // deriv(3,20) = jac^-1 der
+    __shared__ double s_h[27][60];     // det * w * deriv
     __shared__ double s_D[3];
     const int t = threadIdx.x;
+    for (int k = t; k < nip * 20; k += kFormThreads) {
+        const int ig = k / 20, l = k % 20;
+        shape_der20(l, gp[4 * ig], gp[4 * ig + 1], gp[4 * ig + 2], &s_der[ig][3 * l]);
+        if (l == 0) s_w[ig] = gp[4 * ig + 3];
+    }
+    // this thread's node pair: t = b(b+1)/2 + a, a <= b
+    int pa = 0, pb = 0;
+    if (t < 210) {
+        while ((pb + 1) * (pb + 2) / 2 <= t) ++pb;
+        pa = t - pb * (pb + 1) / 2;
+    }
     for (int e = blockIdx.x; e < nels; e += gridDim.x) {
         if (t < 60) s_coord[t] = coord[(size_t)e * 60 + t];
         if (t == 0) {
             const int m = nmat == 1 ? 0 : e;
             deemat3(me[m], mv[m], s_D[0], s_D[1], s_D[2]);
         }
-        double acc[4][9];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int k = 0; k < 9; ++k) acc[q][k] = 0.0;
         __syncthreads();
-        for (int ig = 0; ig < nip; ++ig) {
-            const double xi = gp[4 * ig], eta = gp[4 * ig + 1], zeta = gp[4 * ig + 2];
-            const double w = gp[4 * ig + 3];
-            if (t < 20) shape_der20(t, xi, eta, zeta, &s_der[3 * t]);
-            __syncthreads();
-            if (t < 9) {   // jac = MATMUL(der, coord)
-                const int a = t % 3, b = t / 3;
-                double s = 0.0;
-                for (int k = 0; k < 20; ++k) s += s_der[a + 3 * k] * s_coord[k + 20 * b];
-                s_jac[a + 3 * b] = s;
-            }
-            __syncthreads();
-            if (t == 0) s_det = det_invert3(s_jac);
-            __syncthreads();
-            if (t < 60) {  // deriv = MATMUL(jac^-1, der)
-                const int a = t % 3, l = t / 3;
-                s_deriv[a + 3 * l] = s_jac[a] * s_der[3 * l] + s_jac[a + 3] * s_der[1 + 3 * l] +
-                                     s_jac[a + 6] * s_der[2 + 3 * l];
-            }
-            __syncthreads();
-            const double det = s_det, D11 = s_D[0], D12 = s_D[1], D44 = s_D[2];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int pr = t + 128 * q;
-                if (pr < 400) {
-                    const int a = pr % 20, b = pr / 20;
-                    const double ga[3] = {s_deriv[3 * a], s_deriv[3 * a + 1], s_deriv[3 * a + 2]};
-                    const double gb[3] = {s_deriv[3 * b], s_deriv[3 * b + 1], s_deriv[3 * b + 2]};
-#pragma unroll
-                    for (int j = 0; j < 3; ++j)
-#pragma unroll
-                        for (int i = 0; i < 3; ++i) {
-                            double s;
-                            if (i == j) {
-                                const int k1 = (i + 1) % 3, k2 = (i + 2) % 3;
-                                s = D11 * ga[i] * gb[i] + D44 * (ga[k1] * gb[k1] + ga[k2] * gb[k2]);
-                            } else {
-                                s = D12 * ga[i] * gb[j] + D44 * ga[j] * gb[i];
-                            }
-                            acc[q][i + 3 * j] += s * det * w;
-                        }
-                }
-            }
-            __syncthreads();
+        for (int k = t; k < nip * 9; k += kFormThreads) {   // jac = MATMUL(der, coord)
+            const int ig = k / 9, a = k % 3, b = (k / 3) % 3;
+            double s = 0.0;
+            for (int n = 0; n < 20; ++n) s += s_der[ig][a + 3 * n] * s_coord[n + 20 * b];
+            s_jac[ig][a + 3 * b] = s;
         }
+        __syncthreads();
+        if (t < nip) s_wd[t] = det_invert3(s_jac[t]) * s_w[t];
+        __syncthreads();
+        for (int k = t; k < nip * 60; k += kFormThreads) {   // deriv = MATMUL(jac^-1, der)
+            const int ig = k / 60, a = k % 3, l = (k / 3) % 20;
+            const double *j = s_jac[ig];
+            const double g = j[a] * s_der[ig][3 * l] + j[a + 3] * s_der[ig][1 + 3 * l] + j[a + 6] * s_der[ig][2 + 3 * l];
+            s_g[ig][a + 3 * l] = g;
+            s_h[ig][a + 3 * l] = s_wd[ig] * g;
+        }
+        __syncthreads();
+        if (t < 210) {
+            double M[9];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int pr = t + 128 * q;
-            if (pr < 400) {
-                const int a = pr % 20, b = pr / 20;
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) {
-                        const double val = acc[q][i + 3 * j];
-                        const size_t idx = (size_t)e * 3600 + (size_t)(3 * b + j) * 60 + 3 * a + i;
-                        if (km64) km64[idx] = val;
-                        if (km32) km32[idx] = (float)val;
-                        if (a == b && i == j) ediag[(size_t)e * 60 + 3 * a + i] = val;
-                    }
+            for (int k = 0; k < 9; ++k) M[k] = 0.0;
+            for (int ig = 0; ig < nip; ++ig) {
+                const double ha0 = s_h[ig][3 * pa], ha1 = s_h[ig][3 * pa + 1], ha2 = s_h[ig][3 * pa + 2];
+                const double gb0 = s_g[ig][3 * pb], gb1 = s_g[ig][3 * pb + 1], gb2 = s_g[ig][3 * pb + 2];
+                M[0] = fma(ha0, gb0, M[0]); M[1] = fma(ha1, gb0, M[1]); M[2] = fma(ha2, gb0, M[2]);
+                M[3] = fma(ha0, gb1, M[3]); M[4] = fma(ha1, gb1, M[4]); M[5] = fma(ha2, gb1, M[5]);
+                M[6] = fma(ha0, gb2, M[6]); M[7] = fma(ha1, gb2, M[7]); M[8] = fma(ha2, gb2, M[8]);
             }
+            const double D11 = s_D[0], D12 = s_D[1], D44 = s_D[2];
+            double K[9];   // K(i + 3j) of block (a, b); M(i + 3j) = sum det w ga_i gb_j
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    if (i == j) {
+                        const int k1 = (i + 1) % 3, k2 = (i + 2) % 3;
+                        K[i + 3 * j] = D11 * M[i + 3 * i] + D44 * (M[k1 + 3 * k1] + M[k2 + 3 * k2]);
+                    } else {
+                        K[i + 3 * j] = D12 * M[i + 3 * j] + D44 * M[j + 3 * i];
+                    }
+                }
+            double *ke = km64 ? km64 + (size_t)e * 3600 : nullptr;
+            float *kf = km32 ? km32 + (size_t)e * 3600 : nullptr;
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const double v = K[i + 3 * j];
+                    const int ab = (3 * pb + j) * 60 + 3 * pa + i, ba = (3 * pa + i) * 60 + 3 * pb + j;
+                    if (ke) {
+                        ke[ab] = v;
+                        if (pa != pb) ke[ba] = v;
+                    }
+                    if (kf) {
+                        kf[ab] = (float)v;
+                        if (pa != pb) kf[ba] = (float)v;
+                    }
+                    if (pa == pb && i == j) ediag[(size_t)e * 60 + 3 * pa + i] = v;
+                }
         }
         __syncthreads();
     }
@@ -651,9 +667,9 @@ int launch_form_storkm(Ctx &c, int nip, bool exact_weights, bool keep32)
     }
     k_sample<<<1, 1, 0, c.stream>>>(nip, exact_weights ? 1 : 0, gp);
     if (check_launch(c, "k_sample")) return 1;
-    const int grid = c.nels < c.nsm * 64 ? c.nels : c.nsm * 64;
-    k_form_storkm<<<grid, 128, 0, c.stream>>>(c.nels, nip, gp, c.coord, c.mat_e, c.mat_v, c.nmat,
-                                              c.km64, keep32 ? c.km32 : nullptr, c.ediag);
+    const int grid = c.nels < c.nsm * 16 ? c.nels : c.nsm * 16;
+    k_form_storkm<<<grid, kFormThreads, 0, c.stream>>>(c.nels, nip, gp, c.coord, c.mat_e, c.mat_v, c.nmat,
+                                                       c.km64, keep32 ? c.km32 : nullptr, c.ediag);
     if (check_launch(c, "k_form_storkm")) return 1;
     cudaFreeAsync(gp, c.stream);
     return 0;
@@ -674,8 +690,8 @@ int launch_form_storkm_raw(cudaStream_t stream, int nsm, int nels, int nip, cons
                            const double *coord, const double *me, const double *mv, int nmat, double *km64,
                            float *km32, double *ediag)
 {
-    const int grid = nels < nsm * 64 ? nels : nsm * 64;
-    k_form_storkm<<<grid, 128, 0, stream>>>(nels, nip, gp, coord, me, mv, nmat, km64, km32, ediag);
+    const int grid = nels < nsm * 16 ? nels : nsm * 16;
+    k_form_storkm<<<grid, kFormThreads, 0, stream>>>(nels, nip, gp, coord, me, mv, nmat, km64, km32, ediag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("k_form_storkm: launch failed: %s", cudaGetErrorString(e));
