@@ -51,7 +51,7 @@ struct BSeg {
 };
 
 constexpr int kScatterNodes = 256;   // nodes per scatter block
-constexpr int kVectorSlots = 1024;   // slots per vector block
+constexpr int kVectorSlots = 2048;   // slots per vector block (8 per thread)
 
 __device__ __forceinline__ void elem_product(size_t e, int lane, const double *__restrict__ km,
                                              const int *__restrict__ conn, const double *__restrict__ p,
@@ -325,26 +325,36 @@ __global__ void k_bt_init2(BSeg S, const double *__restrict__ part, int cap, Pcg
     }
 }
 
+// one block per active mesh: alpha = (r.d)/(p.u) from the scatter's partials,
+// formed once per mesh (not once per vector block: the FP64 reduction of a
+// large mesh's partials in every block costs more than the update itself)
+__global__ void __launch_bounds__(256)
+k_bt_alpha(const BSeg *__restrict__ segs, PcgState *__restrict__ st, const double *__restrict__ part_s)
+{
+    const BSeg &S = segs[blockIdx.x];
+    if (st[S.sid].stop) return;
+    const double pu = reduce_partials(part_s + S.pbs, S.nbs, false);
+    if (threadIdx.x == 0) st[S.sid].alpha = st[S.sid].up / pu;
+}
+
 __global__ void __launch_bounds__(256)
 k_bt_update1(const int *__restrict__ blk, const BSeg *__restrict__ segs, const PcgState *__restrict__ st,
-             const double *__restrict__ part_s, double *__restrict__ part_u, int capv, double *__restrict__ x,
-             double *__restrict__ r, double *__restrict__ d, const double *__restrict__ p,
-             const double *__restrict__ u, const double *__restrict__ dinv)
+             double *__restrict__ part_u, int capv, double *__restrict__ x, double *__restrict__ r,
+             double *__restrict__ d, const double *__restrict__ p, const double *__restrict__ u,
+             const double *__restrict__ dinv)
 {
     const int b = blockIdx.x;
     const BSeg &S = segs[blk[b]];
     if (st[S.sid].stop) return;
-    const double pu = reduce_partials(part_s + S.pbs, S.nbs, false);
-    const double alpha = st[S.sid].up / pu;
+    const double alpha = st[S.sid].alpha;
     const size_t s0 = (size_t)3 * S.node0 + (size_t)(b - S.pbv) * kVectorSlots;
     const size_t s1 = min(s0 + kVectorSlots, (size_t)3 * (S.node0 + S.nn));
-    double rd = 0.0, rr = 0.0, mx = 0.0, md = 0.0;
+    // batched solves stop on the relative residual, so checon_par's max|x|
+    // and max|dx| (three FP64 operations per slot on GB300's slow FP64
+    // unit) are not formed
+    double rd = 0.0, rr = 0.0;
     for (size_t s = s0 + threadIdx.x; s < s1; s += blockDim.x) {
-        const double xo = x[s];
-        const double xn = fma(p[s], alpha, xo);
-        x[s] = xn;
-        mx = fmax(mx, fabs(xn));
-        md = fmax(md, fabs(xn - xo));
+        x[s] = fma(p[s], alpha, x[s]);
         const double rn = fma(-u[s], alpha, r[s]);
         r[s] = rn;
         const double dn = dinv[s] * rn;
@@ -352,13 +362,11 @@ k_bt_update1(const int *__restrict__ blk, const BSeg *__restrict__ segs, const P
         rd = fma(rn, dn, rd);
         rr = fma(rn, rn, rr);
     }
-    double v[4] = {rd, rr, mx, md};
-    block_reduce<4>(v, 0xCu);
+    double v[2] = {rd, rr};
+    block_reduce<2>(v, 0u);
     if (threadIdx.x == 0) {
         part_u[0 * (size_t)capv + b] = v[0];
         part_u[1 * (size_t)capv + b] = v[1];
-        part_u[2 * (size_t)capv + b] = v[2];
-        part_u[3 * (size_t)capv + b] = v[3];
     }
 }
 
@@ -384,19 +392,17 @@ k_bt_finish(const BSeg *__restrict__ segs, PcgState *__restrict__ st, const doub
     if (st[S.sid].stop) return;
     const double rd = reduce_partials(part_u + S.pbv, S.nbv, false);
     const double rr = reduce_partials(part_u + capv + S.pbv, S.nbv, false);
-    const double mx = reduce_partials(part_u + 2 * (size_t)capv + S.pbv, S.nbv, true);
-    const double md = reduce_partials(part_u + 3 * (size_t)capv + S.pbv, S.nbv, true);
     if (threadIdx.x == 0) {
         PcgState &T = st[S.sid];
         const int k = T.iters + 1;
-        const double metric = T.stop_mode == STOP_CHECON ? md / mx : sqrt(rr) / sqrt(T.ff);
+        const double metric = sqrt(rr) / sqrt(T.ff);   // batched solves: relative residual
         const bool conv = metric <= T.tol;
         T.up = rd;
         T.iters = k;
         T.rr = rr;
         T.metric = metric;
         T.converged = conv ? 1 : 0;
-        if (!isfinite(rd) || !isfinite(mx)) T.err = 1;
+        if (!isfinite(rd) || !isfinite(rr)) T.err = 1;
         if (conv || k >= T.limit || T.err) T.stop = 1;
     }
 }
@@ -691,8 +697,10 @@ int batch_iterations(Batch &B, int n)
                                                                  B.p, B.u, B.part_s, B.st);
         }
         if (launched(B, "k_bt_scatter")) return 1;
-        k_bt_update1<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_s, B.part_u, B.capb_v, B.x,
-                                                      B.r, B.d, B.p, B.u, B.dinv);
+        k_bt_alpha<<<B.nseg, 256, 0, B.stream>>>(B.d_segs, B.st, B.part_s);
+        if (launched(B, "k_bt_alpha")) return 1;
+        k_bt_update1<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_u, B.capb_v, B.x, B.r, B.d,
+                                                      B.p, B.u, B.dinv);
         if (launched(B, "k_bt_update1")) return 1;
         k_bt_update2<<<B.nblk_v, 256, 0, B.stream>>>(B.d_blk_v, B.d_segs, B.st, B.part_u, B.d, B.p);
         if (launched(B, "k_bt_update2")) return 1;
@@ -805,7 +813,7 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
     double **vecs[] = {&B->f, &B->x, &B->r, &B->d, &B->p, &B->u, &B->dinv, &B->rres};
     for (double **v : vecs) al((void **)v, N * 3 * 8);
     al((void **)&B->part_s, (size_t)B->capb_s * 8);
-    al((void **)&B->part_u, (size_t)4 * B->capb_v * 8);
+    al((void **)&B->part_u, (size_t)2 * B->capb_v * 8);   // r.d and r.r partials
     al((void **)&B->part_i, (size_t)2 * B->capb_v * 8);
     al((void **)&B->scr, 64);
     al((void **)&B->gp, 27 * 4 * 8);

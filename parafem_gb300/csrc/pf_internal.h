@@ -31,6 +31,7 @@ struct PcgState {
     double ff;         // f.f (relative-residual denominator)
     double metric;     // last stopping metric
     double rr;         // last r.r
+    double alpha;      // batched solves: the iteration's step length, formed once per mesh
     double tol;        // stopping tolerance
     int iters;         // iterations completed
     int stop;          // 1 once converged or at the limit: later kernels return
