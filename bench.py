@@ -302,6 +302,16 @@ def run_gb300(args, rank, world, local, dist):
         e2e_val = dist_sum(dist, local, neq * it_m) / t_mixed
         solves["mixed"] = {"wall_s": t_mixed, "device_s": st_m["solve_ms"] / 1e3, "inner_iters": it_m,
                            "corrections": st_m["outer"], "relres": rel_m}
+        # FP16 storkm in the inner products (PF_MODE_MIXED16); the FP16 copy is
+        # packed once, before the timed solve, as a caller would after forming storkm
+        s.bench_iterations(16, 1)
+        barrier(dist)
+        t5 = time.perf_counter()
+        x16, it_16, rel_16 = s.solve(r, 1e-8, 40000, P.MODE_MIXED16)
+        t_16 = dist_max(dist, local, time.perf_counter() - t5)
+        st_16 = s.stats()
+        solves["mixed16"] = {"wall_s": t_16, "device_s": st_16["solve_ms"] / 1e3, "inner_iters": it_16,
+                             "corrections": st_16["outer"], "relres": rel_16}
         t3 = time.perf_counter()
         x64, it_64, rel_64 = s.solve(r, 1e-8, 20000, P.MODE_FP64_RES)
         t_64 = dist_max(dist, local, time.perf_counter() - t3)
@@ -309,6 +319,7 @@ def run_gb300(args, rank, world, local, dist):
         solves["fp64"] = {"wall_s": t_64, "device_s": st_64["solve_ms"] / 1e3, "iters": it_64,
                           "relres": rel_64}
         solves["mixed_over_fp64_time"] = t_mixed / t_64
+        solves["mixed16_over_fp64_time"] = t_16 / t_64
         solves["mixed_vs_fp64_rel_err_2"] = float(np.linalg.norm(x - x64) / np.linalg.norm(x64))
         # accuracy: both solutions against FP64 converged to relres 1e-12
         xr, it_r, rel_r = s.solve(r, 1e-12, 50000, P.MODE_FP64_RES)
@@ -317,6 +328,8 @@ def run_gb300(args, rank, world, local, dist):
         solves["mixed_vs_fp64_1e-12_rel_err_2"] = float(np.linalg.norm(x - xr) / nr_)
         solves["mixed_vs_fp64_1e-12_rel_err_inf"] = float(np.abs(x - xr).max() / np.abs(xr).max())
         solves["fp64_1e-8_vs_fp64_1e-12_rel_err_2"] = float(np.linalg.norm(x64 - xr) / nr_)
+        solves["mixed16_vs_fp64_1e-12_rel_err_2"] = float(np.linalg.norm(x16 - xr) / nr_)
+        solves["mixed16_vs_fp64_1e-12_rel_err_inf"] = float(np.abs(x16 - xr).max() / np.abs(xr).max())
 
     # timed steps: K iterations of the FP32-storkm PCG, device resident
     s.bench_iterations(32, max(args.warmup, 3))
@@ -338,6 +351,11 @@ def run_gb300(args, rank, world, local, dist):
     ms31, ms31_elem, _ = s.bench_iterations(31, k2)
     extra["fp32_full_dof_iter_s"] = neq * k2 / (ms31 / 1e3)
     extra["fp32_full_elem_ms"] = ms31_elem / k2
+    s.bench_iterations(16, 3)
+    ms16, ms16_elem, _ = s.bench_iterations(16, args.steps)
+    extra["fp16_dof_iter_s"] = neq * args.steps / (ms16 / 1e3)
+    extra["fp16_step_ms"] = ms16 / args.steps
+    extra["fp16_elem_ms"] = ms16_elem / args.steps
 
     peak, peak_kind = measured_peaks()
     nslots = 3 * prob["nn"]
@@ -351,6 +369,7 @@ def run_gb300(args, rank, world, local, dist):
             "scatter_avg_ms": ms_scat / args.steps}
     extra["fp64_elem_hbm_frac"] = elem_bytes(nels, nslots, 28800, 8) / (ms64_elem / k2 / 1e3) / 1e9 / peak
     extra["fp32_full_elem_hbm_frac"] = elem_bytes(nels, nslots, 14400, 4) / (ms31_elem / k2 / 1e3) / 1e9 / peak
+    extra["fp16_elem_hbm_frac"] = elem_bytes(nels, nslots, 3664, 4) / (ms16_elem / args.steps / 1e3) / 1e9 / peak
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -40,6 +40,9 @@ extern "C" {
                               stop at the FP64 true ||f-Ku||2/||f||2 <= tol        */
 #define PF_MODE_MIXED_RESTART 3 /* FP32-storkm inner PCG restarted on each FP64
                               defect f-Ku (classic iterative refinement)           */
+#define PF_MODE_MIXED16  4 /* as PF_MODE_MIXED with FP16 storkm (scaled per
+                              element) in the inner products: half the bytes per
+                              iteration, more inner iterations; same FP64 stop    */
 
 /* pf_form_storkm flags */
 #define PF_FORM_EXACT_WEIGHTS 1 /* exact 5/9, 8/9 Gauss factors instead of
@@ -121,8 +124,10 @@ int pf_get_diag(void **ctx, double *diag);
 
 /* One element-by-element product u = K p in equation order (GATHER,
  * element MATMUL, SCATTER of p121.f90:92-97).  prec 64: FP64 storkm;
- * 32: packed-symmetric FP32 storkm (the upper triangle, used by
- * PF_MODE_MIXED); 31: full FP32 storkm. */
+ * 32: packed-symmetric FP32 storkm (used by PF_MODE_MIXED); 31: full FP32
+ * storkm; 16: packed-symmetric FP16 storkm scaled per element (used by
+ * PF_MODE_MIXED16).  The packed products are P K_e P p_e, P removing each
+ * element's mean translation (equal to K_e p_e in exact arithmetic). */
 int pf_ebe_matvec(void **ctx, const int *prec, const double *p, double *u);
 
 /* The PCG solve (p121.f90:86-104).  r: loads (neq); xnew: result (neq);
@@ -137,7 +142,7 @@ int pf_solve(void **ctx, const double *r, const double *tol, const int *limit,
  *  [6] true relative residual */
 int pf_solve_stats(void **ctx, double *stats, const int *n);
 
-/* Times `steps` PCG iterations on the resident state (prec 64, 32 or 31) with
+/* Times `steps` PCG iterations on the resident state (prec 64, 32, 31 or 16) with
  * CUDA events on the library stream.  ms_total: all steps; ms_elem: summed
  * duration of the element-product kernel launches; ms_scatter: summed
  * duration of the node-scatter kernel launches. */

@@ -95,7 +95,8 @@ static void free_mesh(Ctx &c)
     multi_release(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
-    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.psplit);
+    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.psplit); dfree(c.km16p);
+    c.km16_ok = false;
     c.shared = false;
     c.kind = KIND_SOLID20;
     dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
@@ -595,6 +596,7 @@ static int ensure_storkm(Ctx &c)
     if (!c.km64 && dalloc(&c.km64, ne * 3600, "FP64 storkm")) return 1;
     if (!c.km32 && dalloc(&c.km32, ne * 3600, "FP32 storkm")) return 1;
     if (!c.km32p && dalloc(&c.km32p, ne * 1832, "packed FP32 storkm")) return 1;
+    c.km16_ok = false;   // repacked on the next FP16 use
     c.shared = false;
     drop_graph(c);
     return 0;
@@ -771,11 +773,13 @@ extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, doubl
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32 && *prec != 31) ||
-        (c.kind == KIND_SCALAR8 && *prec != 64)) {
-        set_error("pf_ebe_matvec: invalid arguments or no storkm (8-node scalar contexts: prec 64)");
+    if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32 && *prec != 31 && *prec != 16) ||
+        (c.kind == KIND_SCALAR8 && *prec != 64) || (c.shared && *prec == 16)) {
+        set_error("pf_ebe_matvec: invalid arguments or no storkm (8-node scalar contexts: prec 64; "
+                  "prec 16 needs per-element storkm)");
         return PF_FAILURE;
     }
+    if (*prec == 16) TRY(ensure_km16(c));
     CK(cudaMemcpyAsync(c.eqbuf, p, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     TRY(launch_eq_to_slot(c, c.eqbuf, c.rres));
     TRY(launch_matvec(c, *prec, c.rres, c.u));
@@ -825,7 +829,7 @@ static int solve_mixed_restart(Ctx &c, double tol, int limit, double ff, double 
 // (defect correction) and the search direction is kept, so the Krylov space
 // built so far is not thrown away.  The solve ends when the TRUE relative
 // residual reaches tol.
-static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2)
+static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2, int inner_prec)
 {
     const double drop = 0.1;
     const int max_corrections = 200;
@@ -837,7 +841,7 @@ static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2)
     for (;;) {
         TRY(pull_state(c));
         const int done = c.hst->iters;
-        if (!c.hst->stop) TRY(run_pcg(c, 32, c.x, limit - done));
+        if (!c.hst->stop) TRY(run_pcg(c, inner_prec, c.x, limit - done));
         TRY(true_relres(c, c.x, ff, &rel, dev2));
         ++mv64;
         if (rel <= tol || c.hst->iters >= limit || corrections >= max_corrections) break;
@@ -862,14 +866,20 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
     Ctx &c = *cp;
     if (!r || !tol || !limit || !mode || !xnew || !iters || !c.have_km || *limit < 1 ||
         (*mode != PF_MODE_P121 && *mode != PF_MODE_FP64_RES && *mode != PF_MODE_MIXED &&
-         *mode != PF_MODE_MIXED_RESTART)) {
+         *mode != PF_MODE_MIXED_RESTART && *mode != PF_MODE_MIXED16)) {
         set_error("pf_solve: invalid arguments or no storkm");
         return PF_FAILURE;
     }
-    if (c.kind == KIND_SCALAR8 && (*mode == PF_MODE_MIXED || *mode == PF_MODE_MIXED_RESTART)) {
+    if (c.kind == KIND_SCALAR8 &&
+        (*mode == PF_MODE_MIXED || *mode == PF_MODE_MIXED_RESTART || *mode == PF_MODE_MIXED16)) {
         set_error("pf_solve: the mixed modes need 20-node elements; 8-node scalar contexts solve in FP64");
         return PF_FAILURE;
     }
+    if (*mode == PF_MODE_MIXED16 && c.shared) {
+        set_error("pf_solve: PF_MODE_MIXED16 needs per-element storkm (a shared km solves mixed with PF_MODE_MIXED)");
+        return PF_FAILURE;
+    }
+    if (*mode == PF_MODE_MIXED16) TRY(ensure_km16(c));
     for (int i = 0; i < 8; ++i) c.stats[i] = 0.0;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -886,8 +896,8 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
         TRY(pull_state(c));
         ff = c.hst->ff;
     }
-    if (*mode == PF_MODE_MIXED) {
-        rc = solve_mixed(c, *tol, *limit, ff, dev2);
+    if (*mode == PF_MODE_MIXED || *mode == PF_MODE_MIXED16) {
+        rc = solve_mixed(c, *tol, *limit, ff, dev2, *mode == PF_MODE_MIXED16 ? PREC_FP16_SYM : PREC_FP32_SYM);
     } else if (*mode == PF_MODE_MIXED_RESTART) {
         rc = solve_mixed_restart(c, *tol, *limit, ff, dev2);
     } else {
@@ -931,11 +941,14 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (!prec || !steps || *steps < 1 || !c.have_km || (*prec != 32 && *prec != 31 && *prec != 64) ||
-        (c.kind == KIND_SCALAR8 && *prec != 64)) {
-        set_error("pf_bench_iterations: invalid arguments or no storkm (8-node scalar contexts: prec 64)");
+    if (!prec || !steps || *steps < 1 || !c.have_km ||
+        (*prec != 32 && *prec != 31 && *prec != 64 && *prec != 16) || (c.kind == KIND_SCALAR8 && *prec != 64) ||
+        (c.shared && *prec == 16)) {
+        set_error("pf_bench_iterations: invalid arguments or no storkm (8-node scalar contexts: prec 64; "
+                  "prec 16 needs per-element storkm)");
         return PF_FAILURE;
     }
+    if (*prec == 16) TRY(ensure_km16(c));
     const int n = *steps;
     // never-converging run on the resident load vector (tol 0, no limit hit)
     TRY(launch_pcg_init(c, c.f, c.c, STOP_RELRES, 0.0, n + 1));

@@ -64,19 +64,6 @@ __global__ void k_pack_sym32(int nels, const double *__restrict__ km, float *__r
     }
 }
 
-// Sums v over each class of lanes with equal index mod 3 (lanes 0..29 hold
-// the values, lanes 30 and 31 hold 0) and returns to every lane the sum of
-// its class, the same bits on every lane of the class.
-__device__ __forceinline__ float sum_mod3(float v, int lane)
-{
-#pragma unroll
-    for (int off = 3; off < 32; off <<= 1) {   // 3, 6, 12, 24
-        const float w = __shfl_down_sync(kFull, v, off);
-        v += (lane + off < 32) ? w : 0.0f;
-    }
-    return __shfl_sync(kFull, v, lane % 3);
-}
-
 // u_e = P K_e P p_e for every element, K_e from the packed FP32 diagonals.
 // kWarps warps per CTA, kStages shared-memory stages per warp (tuned at
 // run time among the instantiations below).

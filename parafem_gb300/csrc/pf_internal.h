@@ -93,6 +93,11 @@ struct Ctx {
     float *skm32 = nullptr;     // [3600 + 192]: km, then the direction sums of its rows ([3][64])
     bool shared_attr = false;   // shared-memory attribute of the tensor-core kernel set
     float2 *psplit = nullptr;   // [nslots] FP32 high and low parts of p (shared km): written with p
+    uint32_t *km16p = nullptr;  // [nels*916] packed FP16 storkm (pf_elem_h16.cu), packed on first use
+    bool km16_ok = false;       // km16p holds the current storkm
+    int h16_cfg = 0;            // autotuned configuration of the FP16 kernel
+    unsigned h16_attr = 0;      // FP16 configurations whose shared-memory attribute is set
+    float tune16_ms[3] = {0, 0, 0};
     MultiBufs *multi = nullptr; // block-solve vectors, allocated on the first block solve or product
     int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel
     int sym_warps = 14, sym_stages = 2;
@@ -143,7 +148,10 @@ int launch_sum_partials(Ctx &c, int nvals, double *out_dev);   // out[0] = sum o
 int launch_centroid_stress(Ctx &c, int e0, int count, const double *xslot, double *sig_dev);
 // prec codes of the element products: 64 FP64 storkm, 32 packed-symmetric
 // FP32 storkm (bulk-copy staged), 31 full FP32 storkm
-enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31 };
+enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31, PREC_FP16_SYM = 16 };
+int ensure_km16(Ctx &c);   // packs (and autotunes) the FP16 storkm if storkm changed; outside stream capture
+int launch_elem_sym16(Ctx &c, const double *p, const PcgState *st);
+int h16_config(int idx, int *warps, int *stages);
 int launch_pack_sym32(Ctx &c);
 void multi_release(Ctx &c);   // frees the context's block-solve buffers (pf_multi.cu)
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);

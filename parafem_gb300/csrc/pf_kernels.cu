@@ -734,6 +734,7 @@ int launch_elem(Ctx &c, int prec, const double *p)
     if (c.kind == KIND_SCALAR8) return launch_elem8(c, p, c.st);
     if (c.shared) return launch_elem_shared(c, prec, p, c.st);
     if (prec == PREC_FP32_SYM) return launch_elem_sym32(c, p, c.st);
+    if (prec == PREC_FP16_SYM) return launch_elem_sym16(c, p, c.st);
     const int grid = grid_for(c, c.nels, 8, 8);
     if (prec == PREC_FP32_FULL) {
         k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, c.st);
@@ -777,6 +778,8 @@ int launch_matvec(Ctx &c, int prec, const double *p, double *u)
         if (launch_elem_shared(c, prec, p, nullptr)) return 1;
     } else if (prec == PREC_FP32_SYM) {
         if (launch_elem_sym32(c, p, nullptr)) return 1;
+    } else if (prec == PREC_FP16_SYM) {
+        if (launch_elem_sym16(c, p, nullptr)) return 1;
     } else {
         if (prec == PREC_FP32_FULL)
             k_elem<float, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, p, (float *)c.utemp, nullptr);

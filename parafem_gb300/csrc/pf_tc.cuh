@@ -184,6 +184,19 @@ __device__ __forceinline__ void split_f64(double v, float &hi, float &lo)
              : 0.0f;
 }
 
+// Sums v over each class of lanes with equal index mod 3 (lanes 0..29 hold
+// the values, lanes 30 and 31 hold 0) and returns to every lane the sum of
+// its class, the same bits on every lane of the class.
+__device__ __forceinline__ float sum_mod3(float v, int lane)
+{
+#pragma unroll
+    for (int off = 3; off < 32; off <<= 1) {   // 3, 6, 12, 24
+        const float w = __shfl_down_sync(0xffffffffu, v, off);
+        v += (lane + off < 32) ? w : 0.0f;
+    }
+    return __shfl_sync(0xffffffffu, v, lane % 3);
+}
+
 // ---------------------------------------------------------------------------
 // BF16 three-term split
 // Two floats rounded to nearest-even BF16 in one instruction: lo in bits

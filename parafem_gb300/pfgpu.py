@@ -23,6 +23,7 @@ MODE_P121 = 0
 MODE_FP64_RES = 1
 MODE_MIXED = 2
 MODE_MIXED_RESTART = 3
+MODE_MIXED16 = 4
 FORM_EXACT_WEIGHTS = 1
 
 _I = ctypes.c_int
