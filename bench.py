@@ -356,6 +356,7 @@ def run_gb300(args, rank, world, local, dist):
     extra["fp16_dof_iter_s"] = neq * args.steps / (ms16 / 1e3)
     extra["fp16_step_ms"] = ms16 / args.steps
     extra["fp16_elem_ms"] = ms16_elem / args.steps
+    extra["fp16_autotune"] = s.tuning16()
 
     peak, peak_kind = measured_peaks()
     nslots = 3 * prob["nn"]
@@ -412,7 +413,9 @@ def run_hetero(args, rank, world, local, dist):
     xr, itr, relr = s.solve(r, 1e-12, 50000, P.MODE_FP64_RES)
     out["oracle_fp64_1e-12"] = {"iters": itr, "relres": relr, "device_s": s.stats()["solve_ms"] / 1e3}
     nr = np.linalg.norm(xr)
-    for name, mode in (("mixed", P.MODE_MIXED), ("fp64", P.MODE_FP64_RES), ("mixed_restart", P.MODE_MIXED_RESTART)):
+    s.ebe_matvec(np.zeros(neq), 16)   # packs the FP16 storkm once, outside the timed solves
+    for name, mode in (("mixed", P.MODE_MIXED), ("mixed16", P.MODE_MIXED16), ("fp64", P.MODE_FP64_RES),
+                       ("mixed_restart", P.MODE_MIXED_RESTART)):
         t0 = time.perf_counter()
         x, it, rel = s.solve(r, 1e-8, 50000, mode)
         wall = time.perf_counter() - t0
@@ -429,7 +432,8 @@ def run_hetero(args, rank, world, local, dist):
             "config": {"workload": f"heterogeneous {n}^3 hex20 cube, E log-uniform [1,1000], v uniform "
                                    f"[0.2,0.35], Philox4x32-10 seed {args.seed}, nip 27, fixed base, top "
                                    f"pressure, tol 1e-8", "nels": nels, "neq": neq},
-            "solves": out, "mixed_over_fp64_time": out["mixed"]["wall_s"] / out["fp64"]["wall_s"]}
+            "solves": out, "mixed_over_fp64_time": out["mixed"]["wall_s"] / out["fp64"]["wall_s"],
+            "mixed16_over_fp64_time": out["mixed16"]["wall_s"] / out["fp64"]["wall_s"]}
     if rank == 0:
         print(json.dumps(line))
     return 0

@@ -164,6 +164,11 @@ int pf_element_stresses(void **ctx, const double *xnew, const int *first, const 
  * milliseconds per launch of the configurations (14,2), (12,2), (8,3). */
 int pf_tuning(void **ctx, int *warps, int *stages, float *ms);
 
+/* The same for the packed FP16 element kernel (PF_MODE_MIXED16, pf_ebe_matvec
+ * prec 16), tuned when the FP16 storkm is packed on its first use:
+ * configurations (20,2), (24,2), (16,3).  Fails before that first use. */
+int pf_tuning16(void **ctx, int *warps, int *stages, float *ms);
+
 /* Force configuration *config (0: 14x2, 1: 12x2, 2: 8x3) of that kernel, or
  * re-run the autotuner (*config = -1).  Every configuration gives bitwise
  * the same products; only the speed differs. */

@@ -1045,6 +1045,19 @@ extern "C" int pf_tuning(void **ctx, int *warps, int *stages, float *ms)
     return PF_SUCCESS;
 }
 
+extern "C" int pf_tuning16(void **ctx, int *warps, int *stages, float *ms)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp || !warps || !stages || !ms) return PF_FAILURE;
+    if (!cp->km16_ok) {
+        set_error("pf_tuning16: the FP16 storkm has not been packed (no FP16 product yet)");
+        return PF_FAILURE;
+    }
+    if (h16_config(cp->h16_cfg, warps, stages)) return PF_FAILURE;
+    for (int i = 0; i < 3; ++i) ms[i] = cp->tune16_ms[i];
+    return PF_SUCCESS;
+}
+
 extern "C" int pf_set_tuning(void **ctx, const int *config)
 {
     Ctx *cp = get_ctx(ctx);

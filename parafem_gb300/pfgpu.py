@@ -61,6 +61,7 @@ _SIGS = {
     "pf_element_stresses": [_VPP, ctypes.c_void_p, _IP, _IP, ctypes.c_void_p],
     "pf_kernel_launches": [_VPP, _LLP],
     "pf_tuning": [_VPP, _IP, _IP, ctypes.c_void_p],
+    "pf_tuning16": [_VPP, _IP, _IP, ctypes.c_void_p],
     "pf_set_tuning": [_VPP, _IP],
     "pf_set_graphs": [_VPP, _IP],
     "pf_ebe_matvec_noalloc": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -423,6 +424,14 @@ class Solver:
         _check(lib().pf_tuning(self._ref, ctypes.byref(w), ctypes.byref(st), ms.ctypes.data), "pf_tuning")
         return {"warps": w.value, "stages": st.value,
                 "ms": {"14x2": float(ms[0]), "12x2": float(ms[1]), "8x3": float(ms[2])}}
+
+    def tuning16(self):
+        """The autotuned (warps, stages) of the packed FP16 kernel and the timed configurations."""
+        w, st = ctypes.c_int(0), ctypes.c_int(0)
+        ms = np.zeros(3, np.float32)
+        _check(lib().pf_tuning16(self._ref, ctypes.byref(w), ctypes.byref(st), ms.ctypes.data), "pf_tuning16")
+        return {"warps": w.value, "stages": st.value,
+                "ms": {"20x2": float(ms[0]), "24x2": float(ms[1]), "16x3": float(ms[2])}}
 
     def set_graphs(self, on: bool) -> None:
         """Replay PCG iterations from a CUDA graph (default) or launch each kernel directly."""
