@@ -59,8 +59,9 @@ def parse_args():
                                                     "0 = all requests at t=0")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serving: device-memory budget of the batch")
     ap.add_argument("--chunk", type=int, default=10, help="serving: PCG iterations per launch/sync cycle")
-    ap.add_argument("--serving-prec", type=int, default=32, choices=[32, 64],
-                    help="serving: 32 = FP32 products with FP64 residual replacement, 64 = FP64")
+    ap.add_argument("--serving-prec", type=int, default=32, choices=[16, 32, 64],
+                    help="serving: 32 = FP32 products with FP64 residual replacement, 16 = FP16 storkm "
+                         "products with the same replacement, 64 = FP64")
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--limit", type=int, default=50000, help="multirhs60: PCG iteration limit of the block solves")
     ap.add_argument("--tuning", type=int, default=-1, choices=[-1, 0, 1, 2],
@@ -523,8 +524,9 @@ def run_serving(args, rank, world, local, dist):
     line = {"metric": METRIC, "value": best["dof_iter_per_s"], "unit": UNIT, "n_gpus": world,
             "steps": n_req, "warmup": 0, "ms_per_step": best["makespan_s"] * 1e3 / n_req,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": ("f32 storkm products + f64 residual replacement / f64 vectors" if args.serving_prec == 32
-                      else "f64 storkm / f64 vectors"), "data": "synthetic",
+            "dtype": {32: "f32 storkm products + f64 residual replacement / f64 vectors",
+                      16: "f16 storkm products + f64 residual replacement / f64 vectors",
+                      64: "f64 storkm / f64 vectors"}[args.serving_prec], "data": "synthetic",
             "config": {"workload": f"serving stream: {n_req} Poisson-arrival requests, hex20 cubes with edges "
                                    f"uniform in 4..40, E log-uniform [10,1000], v uniform [0.2,0.35], fixed "
                                    f"base, top pressure uniform [0.5,2.0], tol 1e-8, budget {args.budget_gb} GB, "

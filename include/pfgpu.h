@@ -247,7 +247,8 @@ int pf_multi_free(void **ctx);
 /* A batch on one device with a fixed device-memory budget (bytes) for its
  * arenas and at most max_meshes solves resident at once.  prec 64: FP64
  * element products; prec 32: FP32 products with FP64 residual replacement
- * per mesh (the PF_MODE_MIXED scheme). */
+ * per mesh (the PF_MODE_MIXED scheme); prec 16: FP16 storkm in the products
+ * (the PF_MODE_MIXED16 scheme). */
 int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes, const int *prec,
                     void **batch);
 int pf_batch_destroy(void **batch);

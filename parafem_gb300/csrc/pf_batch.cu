@@ -19,11 +19,12 @@
 // and node arenas); a request that does not fit yet gets PF_BUSY.
 //
 // The solve is p121's Jacobi-PCG (p121.f90:86-104) stopped at
-// ||r||_2/||f||_2 <= tol, with one of two element products chosen at
-// creation: FP64 storkm, or the packed-symmetric FP32 storkm (products by
-// the bulk-copy kernel of the single-mesh path, through a map from active
-// element positions to arena elements) with FP64 residual replacement per
-// mesh (the PF_MODE_MIXED scheme: a mesh whose recursive residual has
+// ||r||_2/||f||_2 <= tol, with one of three element products chosen at
+// creation: FP64 storkm, or the packed-symmetric FP32 (prec 32) or FP16
+// (prec 16) storkm (products by the bulk-copy kernels of the single-mesh
+// path, through a map from active element positions to arena elements) with
+// FP64 residual replacement per mesh (the PF_MODE_MIXED / PF_MODE_MIXED16
+// scheme: a mesh whose recursive residual has
 // dropped 10x pauses, the host computes its FP64 true residual at the next
 // sync and either retires it or replaces its residual and resumes it).
 // Each retired solve reports the FP64 true residual ||f - K x||_2/||f||_2.
@@ -467,12 +468,13 @@ struct Batch {
     int prec = 64;                   // 64: FP64 products; 32: FP32 products + FP64 residual replacement
     cudaStream_t stream = nullptr;
     int *kerr = nullptr;             // bulk-copy wait timeouts of the element kernel
-    int *emap = nullptr;             // [cap_el] arena element of each active element (prec 32)
+    int *emap = nullptr;             // [cap_el] arena element of each active element (prec 32 and 16)
     long long cap_el = 0, cap_nodes = 0;
     int max_meshes = 0, capb_s = 0, capb_v = 0;
     // arenas
     double *km64 = nullptr, *coord = nullptr, *ediag = nullptr, *ut = nullptr, *mat_e = nullptr, *mat_v = nullptr;
     float *km32p = nullptr;          // packed-symmetric FP32 storkm (prec 32): 1832 floats per element
+    uint32_t *km16p = nullptr;       // packed-symmetric FP16 storkm (prec 16): 916 words per element
     int *conn = nullptr, *list = nullptr;
     int2 *nptr = nullptr;
     uint8_t *fm = nullptr;
@@ -544,7 +546,7 @@ Batch *get_batch(void **h)
 
 void free_batch(Batch &B)
 {
-    void *ptrs[] = {B.km32p, B.kerr, B.emap, B.km64, B.coord, B.ediag, B.ut, B.mat_e, B.mat_v, B.conn, B.list, B.nptr, B.fm, B.f, B.x, B.r,
+    void *ptrs[] = {B.km32p, B.km16p, B.kerr, B.emap, B.km64, B.coord, B.ediag, B.ut, B.mat_e, B.mat_v, B.conn, B.list, B.nptr, B.fm, B.f, B.x, B.r,
                     B.d, B.p, B.u, B.dinv, B.rres, B.part_s, B.part_u, B.part_i, B.scr, B.gp, B.st, B.d_segs,
                     B.d_blk_s, B.d_blk_v};
     for (void *q : ptrs)
@@ -596,7 +598,7 @@ int rebuild_tables(Batch &B)
         BCK(cudaMemcpy(B.d_segs, segs.data(), segs.size() * sizeof(BSeg), cudaMemcpyHostToDevice));
         BCK(cudaMemcpy(B.d_blk_s, bs.data(), bs.size() * sizeof(int), cudaMemcpyHostToDevice));
         BCK(cudaMemcpy(B.d_blk_v, bv.data(), bv.size() * sizeof(int), cudaMemcpyHostToDevice));
-        if (B.prec == 32) {
+        if (B.prec != 64) {
             long long g = (cum + 255) / 256;
             if (g > (long long)B.nsm * 8) g = (long long)B.nsm * 8;
             k_bt_emap<<<(int)g, 256, 0, B.stream>>>(B.nseg, B.d_segs, cum, B.emap);
@@ -643,7 +645,7 @@ int check_or_retire(Batch &B, int id)
     BCK(cudaStreamSynchronize(B.stream));
     const PcgState &T = B.hst[q.sid];
     const double relt = T.ff > 0 ? std::sqrt(rr) / std::sqrt(T.ff) : 0.0;
-    if (B.prec == 32 && relt > q.tol && T.iters < q.limit && !T.err) {
+    if (B.prec != 64 && relt > q.tol && T.iters < q.limit && !T.err) {
         const double thr = 0.1 * relt > q.tol ? 0.1 * relt : 0.5 * q.tol;
         k_bt_replace1<<<q.nbv, 256, 0, B.stream>>>(S, B.rres, B.dinv, B.r, B.d, B.part_i, B.capb_v);
         if (launched(B, "k_bt_replace1")) return 1;
@@ -681,7 +683,15 @@ int batch_iterations(Batch &B, int n)
     if (ge > (long long)B.nsm * 8) ge = (long long)B.nsm * 8;
     if (ge < 1) ge = 1;
     for (int i = 0; i < n; ++i) {
-        if (B.prec == 32) {
+        if (B.prec == 16) {
+            if (launch_elem_sym16_mapped(B.stream, B.nsm, (int)B.total_el, B.km16p, B.conn, B.p, (float *)B.ut,
+                                         B.kerr, B.emap))
+                return 1;
+            B.launches++;
+            k_bt_scatter<float><<<B.nblk_s, 256, 0, B.stream>>>(B.d_blk_s, B.d_segs, B.nptr, B.list,
+                                                                (const float *)B.ut, B.fm, B.p, B.u, B.part_s,
+                                                                B.st);
+        } else if (B.prec == 32) {
             if (launch_elem_sym32_mapped(B.stream, B.nsm, (int)B.total_el, B.km32p, B.conn, B.p, (float *)B.ut,
                                          B.kerr, B.emap))
                 return 1;
@@ -763,8 +773,8 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
                                const int *prec, void **batch)
 {
     if (!device || !budget_bytes || !max_meshes || !prec || !batch || *max_meshes < 1 ||
-        *budget_bytes < (1LL << 20) || (*prec != 64 && *prec != 32)) {
-        set_error("pf_batch_create: invalid arguments (prec must be 64 or 32)");
+        *budget_bytes < (1LL << 20) || (*prec != 64 && *prec != 32 && *prec != 16)) {
+        set_error("pf_batch_create: invalid arguments (prec must be 64, 32 or 16)");
         return PF_FAILURE;
     }
     *batch = nullptr;
@@ -779,11 +789,12 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
     cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, B->device);
     if (B->nsm < 1) B->nsm = 1;
     B->max_meshes = *max_meshes;
-    // bytes per element slot: storkm 28800 (+ packed FP32 7328 and the element
-    // map 4 for prec 32), coord 480, conn 80, element diag 480, results 480,
-    // node list 80, material 16; nodes: 7 per element slot at
-    // 8 (ptr) + 1 (mask) + 8 vectors x 24 bytes
-    const long long per_el = 28800 + (B->prec == 32 ? 7328 + 4 : 0) + 480 + 80 + 480 + 480 + 80 + 16 +
+    // bytes per element slot: storkm 28800 (+ packed FP32 7328 or FP16 3664
+    // and the element map 4 for prec 32 / 16), coord 480, conn 80, element
+    // diag 480, results 480, node list 80, material 16; nodes: 7 per element
+    // slot at 8 (ptr) + 1 (mask) + 8 vectors x 24 bytes
+    const long long per_el = 28800 + (B->prec == 32 ? 7328 + 4 : B->prec == 16 ? 3664 + 4 : 0) + 480 + 80 + 480 +
+                             480 + 80 + 16 +
                              7 * (8 + 1 + 8 * 24);
     B->cap_el = *budget_bytes / per_el;
     if (B->cap_el > 0x7fffffffLL / 60) B->cap_el = 0x7fffffffLL / 60;
@@ -796,10 +807,9 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
         if (ok && cudaMalloc(ptr, bytes ? bytes : 1) != cudaSuccess) ok = false;
     };
     al((void **)&B->km64, E * 3600 * 8);
-    if (B->prec == 32) {
-        al((void **)&B->km32p, E * 1832 * 4);
-        al((void **)&B->emap, E * 4);
-    }
+    if (B->prec == 16) al((void **)&B->km16p, E * 916 * 4);
+    if (B->prec == 32) al((void **)&B->km32p, E * 1832 * 4);
+    if (B->prec != 64) al((void **)&B->emap, E * 4);
     al((void **)&B->kerr, 4);
     al((void **)&B->coord, E * 60 * 8);
     al((void **)&B->ediag, E * 60 * 8);
@@ -832,7 +842,7 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
     cudaMemset(B->st, 0, (size_t)B->max_meshes * sizeof(PcgState));
     cudaMemset(B->kerr, 0, sizeof(int));
     memset(B->hst, 0, (size_t)B->max_meshes * sizeof(PcgState));
-    if (B->prec == 32 && sym32_prepare()) {
+    if ((B->prec == 32 && sym32_prepare()) || (B->prec == 16 && sym16_prepare())) {
         free_batch(*B);
         delete B;
         return PF_FAILURE;
@@ -996,7 +1006,7 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
     // state: tolerance, limit, stopping test
     PcgState T;
     memset(&T, 0, sizeof T);
-    T.tol = B.prec == 32 ? (0.1 > *tol ? 0.1 : *tol) : *tol;   // mixed: first replacement threshold
+    T.tol = B.prec != 64 ? (0.1 > *tol ? 0.1 : *tol) : *tol;   // mixed: first replacement threshold
     T.limit = *limit;
     T.stop_mode = STOP_RELRES;
     T.stop = 1;   // inactive until the init kernel runs
@@ -1030,6 +1040,11 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
     B.launches++;
     if (B.km32p) {
         if (launch_pack_sym32_raw(B.stream, B.nsm, nels, B.km64 + (size_t)el0 * 3600, B.km32p + (size_t)el0 * 1832))
+            return PF_FAILURE;
+        B.launches++;
+    }
+    if (B.km16p) {
+        if (launch_pack_sym16_raw(B.stream, B.nsm, nels, B.km64 + (size_t)el0 * 3600, B.km16p + (size_t)el0 * 916))
             return PF_FAILURE;
         B.launches++;
     }

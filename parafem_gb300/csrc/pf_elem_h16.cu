@@ -73,7 +73,7 @@ template <int kWarps, int kStages, int kAhead>
 __global__ void __launch_bounds__(kWarps * 32, 1)
 k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ conn,
              const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
-             int *__restrict__ err)
+             int *__restrict__ err, const int *__restrict__ emap)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -96,7 +96,9 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
     const int first = e0 + w;
     if (first >= e1) return;
     const int nmine = (e1 - first + kWarps - 1) / kWarps;
-    auto elem = [&](int k) { return first + k * kWarps; };
+    // the k-th element of this warp; emap (serving batches) maps the
+    // position among the active elements to the arena element
+    auto elem = [&](int k) { const int g = first + k * kWarps; return emap ? __ldg(emap + g) : g; };
 
     if (lane == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
@@ -243,7 +245,7 @@ static int launch_h16_cfg(Ctx &c, const double *p, const PcgState *st, int bit)
     }
     const int grid = c.nels < c.nsm * W ? (c.nels + W - 1) / W : c.nsm;
     k_elem_sym16<W, S, A><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km16p, c.conn, p, (float *)c.utemp, st,
-                                                            c.kerr);
+                                                            c.kerr, nullptr);
     c.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -325,6 +327,47 @@ int ensure_km16(Ctx &c)
 int launch_elem_sym16(Ctx &c, const double *p, const PcgState *st)
 {
     return launch_h16_index(c, c.h16_cfg, p, st);
+}
+
+// The serving engine's entry points: the (20, 2, 2) configuration over n
+// active elements mapped to arena elements by emap.  sym16_prepare sets the
+// shared-memory attribute; call it once per device before any stream capture.
+int sym16_prepare()
+{
+    constexpr size_t smem = h16_smem_bytes<20, 2>();
+    const cudaError_t e = cudaFuncSetAttribute(k_elem_sym16<20, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)smem);
+    if (e != cudaSuccess) {
+        set_error("k_elem_sym16: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+int launch_elem_sym16_mapped(cudaStream_t stream, int nsm, int n, const uint32_t *kh, const int *conn,
+                             const double *p, float *ut, int *err, const int *emap)
+{
+    if (n <= 0) return 0;
+    constexpr int W = 20;
+    const int grid = n < nsm * W ? (n + W - 1) / W : nsm;
+    k_elem_sym16<W, 2, 2><<<grid, W * 32, h16_smem_bytes<W, 2>(), stream>>>(n, kh, conn, p, ut, nullptr, err, emap);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("k_elem_sym16: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+int launch_pack_sym16_raw(cudaStream_t stream, int nsm, int nels, const double *km, uint32_t *kh)
+{
+    k_pack_sym16<<<nsm * 8, 256, 0, stream>>>(nels, km, kh);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("k_pack_sym16: launch failed: %s", cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
 }
 
 int h16_config(int idx, int *warps, int *stages)

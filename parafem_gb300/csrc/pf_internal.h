@@ -152,6 +152,10 @@ enum { PREC_FP64 = 64, PREC_FP32_SYM = 32, PREC_FP32_FULL = 31, PREC_FP16_SYM = 
 int ensure_km16(Ctx &c);   // packs (and autotunes) the FP16 storkm if storkm changed; outside stream capture
 int launch_elem_sym16(Ctx &c, const double *p, const PcgState *st);
 int h16_config(int idx, int *warps, int *stages);
+int sym16_prepare();   // shared-memory attribute of the mapped FP16 launch (once per device, outside capture)
+int launch_elem_sym16_mapped(cudaStream_t stream, int nsm, int n, const uint32_t *kh, const int *conn,
+                             const double *p, float *ut, int *err, const int *emap);
+int launch_pack_sym16_raw(cudaStream_t stream, int nsm, int nels, const double *km, uint32_t *kh);
 int launch_pack_sym32(Ctx &c);
 void multi_release(Ctx &c);   // frees the context's block-solve buffers (pf_multi.cu)
 int launch_elem_sym32(Ctx &c, const double *p, const PcgState *st);

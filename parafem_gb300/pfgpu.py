@@ -450,7 +450,8 @@ class Batch:
     admitted by a device-memory budget, retired when converged."""
 
     def __init__(self, budget_bytes: int, max_meshes: int = 256, device: int = 0, prec: int = 64):
-        """prec 64: FP64 element products; 32: FP32 products with FP64 residual replacement."""
+        """prec 64: FP64 element products; 32: FP32 products with FP64 residual replacement;
+        16: FP16 storkm in the products, with the same replacement."""
         self._h = ctypes.c_void_p(None)
         _check(lib().pf_batch_create(_i(device), ctypes.byref(ctypes.c_longlong(int(budget_bytes))),
                                      _i(max_meshes), _i(prec), ctypes.byref(self._h)), "pf_batch_create")

@@ -91,15 +91,16 @@ def test_admission_is_bounded_by_the_budget():
         assert admit(b, prob, e, v) is not None
 
 
-def test_mixed_batch_same_alone_and_in_the_mix_and_accurate():
+@pytest.mark.parametrize("prec", [32, 16])
+def test_mixed_batch_same_alone_and_in_the_mix_and_accurate(prec):
     reqs = [request(sp) for sp in SPECS[:3]]
     cap = max(p["neq"] for p, _, _ in reqs)
     alone = []
     for prob, e, v in reqs:
-        with P.Batch(2 << 30, 8, prec=32) as b:
+        with P.Batch(2 << 30, 8, prec=prec) as b:
             sid = admit(b, prob, e, v)
             alone.append(b.run_all(cap)[sid])
-    with P.Batch(2 << 30, 8, prec=32) as b:
+    with P.Batch(2 << 30, 8, prec=prec) as b:
         ids = [admit(b, *r) for r in reqs]
         res = b.run_all(cap, chunk=5)
     for k, sid in enumerate(ids):
@@ -116,7 +117,7 @@ def test_mixed_batch_same_alone_and_in_the_mix_and_accurate():
         assert np.linalg.norm(x - x_ref) <= 1e-7 * np.linalg.norm(x_ref)
 
 
-@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("prec", [64, 32, 16])
 def test_graph_replay_matches_direct_launches(prec):
     reqs = [request(sp) for sp in SPECS]
     cap = max(p["neq"] for p, _, _ in reqs)
