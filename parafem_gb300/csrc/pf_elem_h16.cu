@@ -32,7 +32,7 @@ using namespace tc;
 namespace {
 constexpr int kH16Words = 916;
 constexpr int kH16Bytes = kH16Words * 4;   // 3664
-constexpr int kPSlot = 120;                // floats of p per warp (p_e twice)
+constexpr int kPSlot = 120;                // floats of p per warp: 60 pairs (p[i], p[i+30 mod 60])
 constexpr unsigned kFull = 0xffffffffu;
 }  // namespace
 
@@ -68,8 +68,11 @@ __global__ void k_pack_sym16(int nels, const double *__restrict__ km, uint32_t *
 
 // u_e = P K_e P p_e for every element, K_e from the FP16 diagonals.
 // kWarps warps per CTA, kStages shared-memory stages per warp, p gathered
-// kAhead (1 or 2) elements ahead of the one being multiplied.
-template <int kWarps, int kStages, int kAhead>
+// kAhead (1 or 2) elements ahead of the one being multiplied.  kMapped
+// kernels (serving batches) read element numbers through emap; the solver's
+// kernels carry no remapping (a runtime test cost the 20-warp configuration
+// 14 % of its time).
+template <int kWarps, int kStages, int kAhead, bool kMapped>
 __global__ void __launch_bounds__(kWarps * 32, 1)
 k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ conn,
              const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
@@ -79,7 +82,7 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     uint32_t *stage = reinterpret_cast<uint32_t *>(smem) + (size_t)w * kStages * kH16Words;
-    float *pp = reinterpret_cast<float *>(smem + (size_t)kWarps * kStages * kH16Bytes) + w * kPSlot;
+    float2 *pp = reinterpret_cast<float2 *>(smem + (size_t)kWarps * kStages * kH16Bytes + (size_t)w * kPSlot * 4);
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + (size_t)kWarps * kStages * kH16Bytes +
                                                  kWarps * kPSlot * 4) + w * kStages;
     static_assert((kWarps * kStages * kH16Bytes + kWarps * kPSlot * 4) % 8 == 0, "mbarrier alignment");
@@ -98,7 +101,11 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
     const int nmine = (e1 - first + kWarps - 1) / kWarps;
     // the k-th element of this warp; emap (serving batches) maps the
     // position among the active elements to the arena element
-    auto elem = [&](int k) { const int g = first + k * kWarps; return emap ? __ldg(emap + g) : g; };
+    auto elem = [&](int k) {
+        const int g = first + k * kWarps;
+        if constexpr (kMapped) return __ldg(emap + g);
+        else return g;
+    };
 
     if (lane == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
@@ -149,12 +156,10 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
             split_f64(pa, ha, la);
             split_f64(pb, hb, lb);
             const float t = 0.05f * sum_mod3(ha + hb, lane);
-            if (active) {
+            if (active) {   // pair i = (p[i], p[i+30 mod 60]): one 8-byte load per step of the walk
                 const float qa = (ha - t) + la, qb = (hb - t) + lb;
-                pp[lane] = qa;
-                pp[lane + 60] = qa;
-                pp[lane + 30] = qb;
-                pp[lane + 90] = qb;
+                pp[lane] = make_float2(qa, qb);
+                pp[lane + 30] = make_float2(qb, qa);
             }
         }
         const bool ok = __all_sync(kFull, mbar_wait(&bar[s], parity));
@@ -166,13 +171,15 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
         const uint32_t *Wd = stage + s * kH16Words;
         float acc_a = 0.f, acc_b = 0.f;
         if (active) {
-            const float *pl = pp + lane;
+            const float2 *pl = pp + lane;
+            const float2 p00 = pl[0];   // (p[l], p[l+30])
             const float2 w0 = __half22float2(*reinterpret_cast<const __half2 *>(Wd + lane));
-            float f0 = w0.x * pl[0], f1 = w0.y * pl[30], g0 = 0.f, g1 = 0.f;
+            float f0 = w0.x * p00.x, f1 = w0.y * p00.y, g0 = 0.f, g1 = 0.f;
 #pragma unroll
             for (int d = 1; d < 30; ++d) {
                 const int t = 30 - d;
-                const float p0 = pl[d], p1 = pl[30 + d];
+                const float2 pd = pl[d];   // (p[l+d], p[l+d+30 mod 60])
+                const float p0 = pd.x, p1 = pd.y;
                 const float2 wf = __half22float2(*reinterpret_cast<const __half2 *>(Wd + 30 * d + lane));
                 f0 = fmaf(wf.x, p0, f0);                                      // K(l, l+d)
                 f1 = fmaf(wf.y, p1, f1);                                      // K(l+30, l+30+d)
@@ -183,8 +190,8 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
                 g0 = fmaf(wrap ? wb.x : wb.y, p1, g0);                        // K(l, l+d+30)
             }
             const float d30 = __half2float(reinterpret_cast<const __half *>(Wd + 900)[lane]);   // K(l, l+30)
-            f0 = fmaf(d30, pl[30], f0);
-            f1 = fmaf(d30, pl[0], f1);
+            f0 = fmaf(d30, p00.y, f0);
+            f1 = fmaf(d30, p00.x, f1);
             const float sc = __uint_as_float(Wd[915]);
             acc_a = (f0 + g0) * sc;
             acc_b = (f1 + g1) * sc;
@@ -236,7 +243,8 @@ static int launch_h16_cfg(Ctx &c, const double *p, const PcgState *st, int bit)
     static_assert(smem <= 227 * 1024, "shared memory per CTA");
     cudaError_t e;
     if (!(c.h16_attr & (1u << bit))) {   // once per context and configuration, before any stream capture
-        e = cudaFuncSetAttribute(k_elem_sym16<W, S, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_elem_sym16<W, S, A, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
         if (e != cudaSuccess) {
             set_error("k_elem_sym16: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
             return 1;
@@ -244,8 +252,8 @@ static int launch_h16_cfg(Ctx &c, const double *p, const PcgState *st, int bit)
         c.h16_attr |= 1u << bit;
     }
     const int grid = c.nels < c.nsm * W ? (c.nels + W - 1) / W : c.nsm;
-    k_elem_sym16<W, S, A><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km16p, c.conn, p, (float *)c.utemp, st,
-                                                            c.kerr, nullptr);
+    k_elem_sym16<W, S, A, false><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km16p, c.conn, p, (float *)c.utemp,
+                                                                   st, c.kerr, nullptr);
     c.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -335,8 +343,8 @@ int launch_elem_sym16(Ctx &c, const double *p, const PcgState *st)
 int sym16_prepare()
 {
     constexpr size_t smem = h16_smem_bytes<20, 2>();
-    const cudaError_t e = cudaFuncSetAttribute(k_elem_sym16<20, 2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem);
+    const cudaError_t e = cudaFuncSetAttribute(k_elem_sym16<20, 2, 2, true>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {
         set_error("k_elem_sym16: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
         return 1;
@@ -350,7 +358,8 @@ int launch_elem_sym16_mapped(cudaStream_t stream, int nsm, int n, const uint32_t
     if (n <= 0) return 0;
     constexpr int W = 20;
     const int grid = n < nsm * W ? (n + W - 1) / W : nsm;
-    k_elem_sym16<W, 2, 2><<<grid, W * 32, h16_smem_bytes<W, 2>(), stream>>>(n, kh, conn, p, ut, nullptr, err, emap);
+    k_elem_sym16<W, 2, 2, true><<<grid, W * 32, h16_smem_bytes<W, 2>(), stream>>>(n, kh, conn, p, ut, nullptr, err,
+                                                                                   emap);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("k_elem_sym16: launch failed: %s", cudaGetErrorString(e));

@@ -66,8 +66,10 @@ __global__ void k_pack_sym32(int nels, const double *__restrict__ km, float *__r
 
 // u_e = P K_e P p_e for every element, K_e from the packed FP32 diagonals.
 // kWarps warps per CTA, kStages shared-memory stages per warp (tuned at
-// run time among the instantiations below).
-template <int kWarps, int kStages>
+// run time among the instantiations below).  kMapped kernels (serving
+// batches) read element numbers through emap; the solver's carry no
+// remapping.
+template <int kWarps, int kStages, bool kMapped>
 __global__ void __launch_bounds__(kWarps * 32, 1)
 k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ conn,
              const double *__restrict__ p, float *__restrict__ ut, const PcgState *__restrict__ st,
@@ -98,7 +100,11 @@ k_elem_sym32(int nels, const float *__restrict__ kp, const int *__restrict__ con
     const int nmine = (e1 - first + kWarps - 1) / kWarps;   // elements of this warp
     // the k-th element of this warp; emap (serving batches) maps the
     // position among the active elements to the arena element
-    auto elem = [&](int k) { const int g = first + k * kWarps; return emap ? __ldg(emap + g) : g; };
+    auto elem = [&](int k) {
+        const int g = first + k * kWarps;
+        if constexpr (kMapped) return __ldg(emap + g);
+        else return g;
+    };
 
     if (lane == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(&bar[s], 1);
@@ -239,7 +245,8 @@ static int launch_sym_cfg(Ctx &c, const double *p, const PcgState *st)
     // stream capture (the autotuner launches every configuration first)
     const unsigned long long bit = 1ull << (W * 4 + S);   // W <= 15, S <= 3
     if (!(c.sym_attr & bit)) {
-        e = cudaFuncSetAttribute(k_elem_sym32<W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_elem_sym32<W, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
         if (e != cudaSuccess) {
             set_error("k_elem_sym32: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
             return 1;
@@ -247,8 +254,8 @@ static int launch_sym_cfg(Ctx &c, const double *p, const PcgState *st)
         c.sym_attr |= bit;
     }
     const int grid = c.nels < c.nsm * W ? (c.nels + W - 1) / W : c.nsm;
-    k_elem_sym32<W, S><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km32p, c.conn, p, (float *)c.utemp, st, c.kerr,
-                                                         nullptr);
+    k_elem_sym32<W, S, false><<<grid, W * 32, smem, c.stream>>>(c.nels, c.km32p, c.conn, p, (float *)c.utemp, st,
+                                                                c.kerr, nullptr);
     c.launches++;
     e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -277,8 +284,8 @@ static int launch_sym_index(Ctx &c, int idx, const double *p, const PcgState *st
 int sym32_prepare()
 {
     constexpr size_t smem = sym_smem_bytes<14, 2>();
-    const cudaError_t e = cudaFuncSetAttribute(k_elem_sym32<14, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)smem);
+    const cudaError_t e = cudaFuncSetAttribute(k_elem_sym32<14, 2, true>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {
         set_error("k_elem_sym32: cannot reserve %zu bytes of shared memory: %s", smem, cudaGetErrorString(e));
         return 1;
@@ -292,7 +299,8 @@ int launch_elem_sym32_mapped(cudaStream_t stream, int nsm, int n, const float *k
     if (n <= 0) return 0;
     constexpr int W = 14;
     const int grid = n < nsm * W ? (n + W - 1) / W : nsm;
-    k_elem_sym32<W, 2><<<grid, W * 32, sym_smem_bytes<W, 2>(), stream>>>(n, kp, conn, p, ut, nullptr, err, emap);
+    k_elem_sym32<W, 2, true><<<grid, W * 32, sym_smem_bytes<W, 2>(), stream>>>(n, kp, conn, p, ut, nullptr, err,
+                                                                                emap);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("k_elem_sym32: launch failed: %s", cudaGetErrorString(e));
