@@ -166,7 +166,7 @@ int pf_tuning(void **ctx, int *warps, int *stages, float *ms);
 
 /* The same for the packed FP16 element kernel (PF_MODE_MIXED16, pf_ebe_matvec
  * prec 16), tuned when the FP16 storkm is packed on its first use:
- * configurations (20,2), (24,2), (16,3).  Fails before that first use. */
+ * configurations (20,2), (24,2), (28,2).  Fails before that first use. */
 int pf_tuning16(void **ctx, int *warps, int *stages, float *ms);
 
 /* Force configuration *config (0: 14x2, 1: 12x2, 2: 8x3) of that kernel, or

@@ -263,18 +263,19 @@ static int launch_h16_cfg(Ctx &c, const double *p, const PcgState *st, int bit)
     return 0;
 }
 
-// the tuned configurations: (warps per CTA, stages per warp)
-// (half the bytes per stage of the FP32 kernel, so more warps fit and hide
-// the latency of the p gather; the 20-warp configuration also gathers two
-// elements ahead, the 24-warp one has no registers left for that)
-static const int kH16Cfg[][2] = {{20, 2}, {24, 2}, {16, 3}};
+// the tuned configurations: (warps per CTA, stages per warp); half the
+// bytes per stage of the FP32 kernel, so more warps fit and hide the latency
+// of the p gather.  The 20- and 24-warp configurations gather p two
+// elements ahead (90 and 78 registers), the 28-warp one, at 70 registers,
+// one element ahead.
+static const int kH16Cfg[][2] = {{20, 2}, {24, 2}, {28, 2}};
 constexpr int kNumH16Cfg = 3;
 
 static int launch_h16_index(Ctx &c, int idx, const double *p, const PcgState *st)
 {
     switch (idx) {
-    case 1: return launch_h16_cfg<24, 2, 1>(c, p, st, 1);
-    case 2: return launch_h16_cfg<16, 3, 2>(c, p, st, 2);
+    case 1: return launch_h16_cfg<24, 2, 2>(c, p, st, 1);
+    case 2: return launch_h16_cfg<28, 2, 1>(c, p, st, 2);
     default: return launch_h16_cfg<20, 2, 2>(c, p, st, 0);
     }
 }

@@ -431,7 +431,7 @@ class Solver:
         ms = np.zeros(3, np.float32)
         _check(lib().pf_tuning16(self._ref, ctypes.byref(w), ctypes.byref(st), ms.ctypes.data), "pf_tuning16")
         return {"warps": w.value, "stages": st.value,
-                "ms": {"20x2": float(ms[0]), "24x2": float(ms[1]), "16x3": float(ms[2])}}
+                "ms": {"20x2": float(ms[0]), "24x2": float(ms[1]), "28x2": float(ms[2])}}
 
     def set_graphs(self, on: bool) -> None:
         """Replay PCG iterations from a CUDA graph (default) or launch each kernel directly."""
