@@ -107,3 +107,21 @@ def test_random_material_deterministic_and_in_range():
 def test_errors_are_reported_not_printed(tmp_path):
     with pytest.raises(P.PfError, match="cannot read"):
         P.p12meshgen(str(tmp_path / "missing"))
+
+
+@pytest.mark.parametrize("run", ["p121_run", "p122_run", "p123_run"])
+def test_whole_jobs_report_a_missing_deck(tmp_path, run):
+    """The deck is read before any GPU work, so this runs without a GPU."""
+    with pytest.raises(P.PfError, match=r"cannot read .*missing\.dat"):
+        getattr(P, run)(str(tmp_path / "missing"))
+
+
+@pytest.mark.parametrize("ext,what", [("bnd", "restraints"), ("lds", "loads")])
+def test_truncated_deck_is_reported(tmp_path, demo_job, ext, what):
+    job = str(tmp_path / "cut")
+    for e in ("dat", "d", "bnd", "lds"):
+        with open(f"{demo_job}.{e}") as src, open(f"{job}.{e}", "w") as dst:
+            lines = src.readlines()
+            dst.writelines(lines[: len(lines) // 2] if e == ext else lines)
+    with pytest.raises(P.PfError, match=rf"cannot read \d+ {what} from .*cut\.{ext}"):
+        P.p121_run(job)
