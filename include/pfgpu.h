@@ -179,6 +179,28 @@ int pf_set_tuning(void **ctx, const int *config);
  * every kernel directly.  Both give bitwise the same iterates. */
 int pf_set_graphs(void **ctx, const int *on);
 
+/* The PCG iteration's scatter, update passes and finish (p121.f90:90-104
+ * with DOT_PRODUCT_P, maths.f90:168-215, and checon_par, maths.f90:999-1069)
+ * run as one persistent cooperative kernel with grid-wide barriers when
+ * *on != 0; FP64 solves (PF_MODE_P121, PF_MODE_FP64_RES) on per-element
+ * storkm then run whole iterations, element products included, up to 32
+ * per launch.  *on == 0, the default, launches the separate scatter, update
+ * and finish kernels, replayed from CUDA graphs, which measure faster on
+ * GB300.  Both give bitwise the same iterates.  Applies to 20-node
+ * contexts; 8-node contexts always use the separate kernels. */
+int pf_set_persistent(void **ctx, const int *on);
+
+/* Self-check of the error path of the bulk-copy element kernels (no
+ * reference counterpart).  Every mbarrier wait in those kernels is bounded;
+ * one that runs out records an error word that the next synchronising call
+ * reports as PF_FAILURE.  This runs one such wait, limited to *polls polls,
+ * on a barrier that no copy completes (no copy is ever in flight), and
+ * reports it the same way: it returns PF_FAILURE with the message "element
+ * kernel: a shared-memory bulk-copy wait timed out (code 2)" and clears the
+ * word, so the context's next call runs normally.  It returns PF_SUCCESS
+ * only if the wait completed, which would mean the check itself is broken. */
+int pf_check_wait_timeout(void **ctx, const int *polls);
+
 /* ---- p123: 3-D Laplace with 8-node bricks (src/programs/5th_ed/p123/p123.f90) ----
  * A context set up with pf_setup_scalar8 holds one freedom per node:
  * g_num(8,nels), g_g(8,nels) (0 = restrained), g_coord(8,3,nels).  pf_solve

@@ -51,6 +51,101 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+CPU_LIB_PATH = os.path.join(BUILD_DIR, "libcpu121.so")
+_cpu_lib = None
+
+
+def build_cpu(force: bool = False) -> str:
+    """Compile the timed CPU baseline (``p121_cpu.c`` with the routines of
+    ``p121_oracle.c`` it calls) into ``oracle/_build/libcpu121.so``: -O3,
+    OpenMP, floating-point contraction allowed.  The parity oracle keeps its
+    own -O2 -ffp-contract=off build."""
+    srcs = [os.path.join(HERE, "p121_cpu.c"), os.path.join(HERE, "p121_oracle.c")]
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(CPU_LIB_PATH)
+            and os.path.getmtime(CPU_LIB_PATH) >= max(os.path.getmtime(s) for s in srcs)):
+        return CPU_LIB_PATH
+    tmp = CPU_LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["gcc", "-O3", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=fast",
+                           "-o", tmp] + srcs + ["-lm"])
+    os.replace(tmp, CPU_LIB_PATH)
+    return CPU_LIB_PATH
+
+
+def cpu_lib():
+    global _cpu_lib
+    with _lock:
+        if _cpu_lib is None:
+            L = ctypes.CDLL(build_cpu())
+            L.cpu121_create.argtypes = [_I, _I, _I, _I, _D, _D]
+            L.cpu121_create.restype = ctypes.c_void_p
+            L.cpu121_destroy.argtypes = [ctypes.c_void_p]
+            L.cpu121_neq.argtypes = [ctypes.c_void_p]
+            L.cpu121_neq.restype = _I
+            L.cpu121_threads.argtypes = [ctypes.c_void_p]
+            L.cpu121_threads.restype = _I
+            L.cpu121_metric.argtypes = [ctypes.c_void_p]
+            L.cpu121_metric.restype = _D
+            L.cpu121_get_storkm.argtypes = [ctypes.c_void_p, _I, _I, _PD]
+            L.cpu121_get_problem.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            L.cpu121_init.argtypes = [ctypes.c_void_p]
+            L.cpu121_iterate.argtypes = [ctypes.c_void_p, _I, _D, _I]
+            L.cpu121_iterate.restype = _I
+            L.cpu121_get_x.argtypes = [ctypes.c_void_p, _PD]
+            _cpu_lib = L
+    return _cpu_lib
+
+
+class CpuP121:
+    """The timed CPU baseline of p121's solve on the fixed-base, top-pressure
+    cube (``p121_cpu.c``): every loop of the PCG iteration on all host threads."""
+
+    def __init__(self, nxe, nye, nze, nip=27, e=100.0, v=0.3):
+        self.L = cpu_lib()
+        self.h = self.L.cpu121_create(nxe, nye, nze, nip, e, v)
+        if not self.h:
+            raise MemoryError(f"CPU baseline: cannot allocate the {nxe}x{nye}x{nze} cube")
+        self.nels = nxe * nye * nze
+        self.neq = self.L.cpu121_neq(self.h)
+        self.threads = self.L.cpu121_threads(self.h)
+
+    def problem(self):
+        g_g = np.zeros((self.nels, 60), np.int32)
+        r = np.zeros(self.neq)
+        self.L.cpu121_get_problem(self.h, g_g.ctypes.data, r.ctypes.data)
+        return g_g, r
+
+    def storkm(self, e0, count):
+        out = np.zeros((count, 60, 60))
+        self.L.cpu121_get_storkm(self.h, e0, count, out)
+        return out
+
+    def init(self):
+        self.L.cpu121_init(self.h)
+
+    def iterate(self, k, tol=0.0, stop_mode=0):
+        return self.L.cpu121_iterate(self.h, k, tol, stop_mode)
+
+    def x(self):
+        out = np.zeros(self.neq)
+        self.L.cpu121_get_x(self.h, out)
+        return out
+
+    def metric(self):
+        return self.L.cpu121_metric(self.h)
+
+    def close(self):
+        if self.h:
+            self.L.cpu121_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def lib():
     global _lib
     with _lock:

@@ -104,6 +104,7 @@ static void free_mesh(Ctx &c)
     c.nels = c.nn = c.neq = c.nslots = 0;
     c.nmat = 0;
     c.have_km = false;
+    for (int &g : c.pk_grid) g = 0;
 }
 
 static int sync(Ctx &c)
@@ -129,7 +130,10 @@ static int check_kernel_error(Ctx &c)
     if (err) {
         cudaMemsetAsync(c.kerr, 0, sizeof(int), c.stream);
         cudaStreamSynchronize(c.stream);
-        set_error("element kernel: a shared-memory bulk-copy wait timed out (code %d)", err);
+        if (err == 3)
+            set_error("persistent PCG kernel: a grid-wide barrier wait timed out (code 3)");
+        else
+            set_error("element kernel: a shared-memory bulk-copy wait timed out (code %d)", err);
         return 1;
     }
     return 0;
@@ -186,6 +190,23 @@ static int run_pcg(Ctx &c, int prec, double *xsol, int limit)
 {
     int launched = 0;
     int chunk = 4;
+    if (persist_fused64(c, prec)) {
+        // whole FP64 iterations in persistent launches, one launch per chunk
+        for (;;) {
+            const int todo = chunk < limit - launched ? chunk : limit - launched;
+            if (todo > 0) TRY(launch_pcg_fused64(c, xsol, todo));
+            launched += todo;
+            TRY(pull_state(c));
+            if (c.hst->stop || launched >= limit) break;
+            if (chunk < 32) chunk *= 2;
+        }
+        if (check_kernel_error(c)) return 1;
+        if (c.hst->err) {
+            set_error("PCG breakdown after %d iterations (non-finite r.d or |x|)", c.hst->iters);
+            return 1;
+        }
+        return 0;
+    }
     for (;;) {
         int todo = chunk < limit - launched ? chunk : limit - launched;
         if (c.use_graphs && todo >= kGraphIters) {
@@ -329,6 +350,8 @@ extern "C" int pf_ctx_create(const int *device, void **ctx)
         cudaMalloc((void **)&c->st, sizeof(PcgState)) != cudaSuccess ||
         cudaMalloc((void **)&c->kerr, sizeof(int)) != cudaSuccess ||
         cudaMemset(c->kerr, 0, sizeof(int)) != cudaSuccess ||
+        cudaMalloc((void **)&c->gbar, sizeof(unsigned long long) * kPersistSlots * kBarWords) != cudaSuccess ||
+        cudaMemset(c->gbar, 0, sizeof(unsigned long long) * kPersistSlots * kBarWords) != cudaSuccess ||
         cudaMallocHost((void **)&c->hst, sizeof(PcgState)) != cudaSuccess) {
         set_error("pf_ctx_create: cannot create stream/state");
         if (c->stream) cudaStreamDestroy(c->stream);
@@ -350,6 +373,7 @@ extern "C" int pf_ctx_destroy(void **ctx)
     free_mesh(*c);   // also drops the iteration graph
     if (c->st) cudaFree(c->st);
     if (c->kerr) cudaFree(c->kerr);
+    if (c->gbar) cudaFree(c->gbar);
     if (c->hst) cudaFreeHost(c->hst);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -960,13 +984,19 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
     std::vector<cudaEvent_t> ev(3 * (size_t)n + 1);
     for (auto &e : ev) CK(cudaEventCreate(&e));
     CK(cudaEventRecord(ev[0], c.stream));
+    const bool tail = c.persistent && c.kind == KIND_SOLID20;
     for (int i = 0; i < n; ++i) {
         TRY(launch_elem(c, *prec, c.p));
         CK(cudaEventRecord(ev[3 * i + 1], c.stream));
-        TRY(launch_scatter(c, *prec, 0, c.p, c.u));
-        CK(cudaEventRecord(ev[3 * i + 2], c.stream));
-        TRY(launch_update1(c, c.c));
-        TRY(launch_update2(c));
+        if (tail) {   // scatter, updates and finish in one persistent launch
+            TRY(launch_pcg_tail(c, *prec, c.c));
+            CK(cudaEventRecord(ev[3 * i + 2], c.stream));
+        } else {
+            TRY(launch_scatter(c, *prec, 0, c.p, c.u));
+            CK(cudaEventRecord(ev[3 * i + 2], c.stream));
+            TRY(launch_update1(c, c.c));
+            TRY(launch_update2(c));
+        }
         CK(cudaEventRecord(ev[3 * i + 3], c.stream));
     }
     CK(cudaStreamSynchronize(c.stream));
@@ -1076,6 +1106,33 @@ extern "C" int pf_set_tuning(void **ctx, const int *config)
         return PF_SUCCESS;
     }
     set_sym_config(c, *config);
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_check_wait_timeout(void **ctx, const int *polls)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    if (!polls || *polls < 1) {
+        set_error("pf_check_wait_timeout: *polls must be at least 1");
+        return PF_FAILURE;
+    }
+    TRY(launch_wait_probe(*cp, *polls));
+    if (check_kernel_error(*cp)) return PF_FAILURE;   // the timeout, reported as the kernels report it
+    set_error("pf_check_wait_timeout: the wait completed, so the timeout path did not run");
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_set_persistent(void **ctx, const int *on)
+{
+    Ctx *cp = get_ctx(ctx);
+    if (!cp) return PF_FAILURE;
+    if (!on) {
+        set_error("pf_set_persistent: null argument");
+        return PF_FAILURE;
+    }
+    cp->persistent = *on != 0;
+    drop_graph(*cp);
     return PF_SUCCESS;
 }
 

@@ -66,6 +66,50 @@ static __device__ __forceinline__ bool block_stopped(const PcgState *st)
     return v;
 }
 
+// Grid-wide barrier of a cooperative launch (every block resident at once).
+// The arrival counter only grows: a block adds one and waits until it
+// reaches the next multiple of the block count, which holds while every
+// launch that uses the counter has the same block count and completes its
+// barriers (the host zeroes it before a run).  Thread 0 releases the
+// block's writes before arriving and acquires the others' after the wait.
+// The wait is bounded: a block that gives up writes code 3 to *err, sets
+// the PCG stop flag (so later launches of the run return at once) and
+// returns false; its caller returns, and the blocks still waiting give up
+// in turn.  (A two-level form, 16 group counters on separate lines feeding
+// a top counter, measured no faster on 600-block grids.)
+constexpr long long kGridSpinLimit = 1LL << 22;
+
+static __device__ __forceinline__ bool grid_barrier(unsigned long long *bar, int *err, PcgState *st)
+{
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long nb = gridDim.x;
+        const unsigned long long target = (atomicAdd(bar, 1ULL) / nb + 1) * nb;
+        int ok = 0;
+        for (long long i = 0; i < kGridSpinLimit; ++i) {
+            unsigned long long v;
+            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(bar) : "memory");
+            if (v >= target) {
+                ok = 1;
+                break;
+            }
+            __nanosleep(32);
+        }
+        if (!ok) {
+            atomicExch(err, 3);
+            atomicExch(&st->stop, 1);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    const bool ok = s_ok != 0;
+    __syncthreads();
+    return ok;
+}
+
 // Sums (or maxes) G block partials in a fixed order; same value in every block.
 static __device__ __forceinline__ double reduce_partials(const double *part, int G, bool is_max)
 {

@@ -24,8 +24,11 @@ __host__ __device__ constexpr int packed_off(int i, int k)
 void set_error(const char *fmt, ...);
 
 // Scalars of one PCG run, resident on the device (pinned host mirror).
-// Only the single-block finish kernel of an iteration writes them, so no
-// kernel writes a value that another block of the same kernel reads.
+// Only the single-block finish kernel of an iteration (or block 0 of a
+// persistent kernel, after its last barrier of the iteration) writes them,
+// so no kernel writes a value that another block of the same kernel reads.
+// The one exception is the error path of a grid-wide barrier, which sets
+// `stop` so that the run's later launches return at once.
 struct PcgState {
     double up;         // r.d entering the next iteration
     double ff;         // f.f (relative-residual denominator)
@@ -42,6 +45,8 @@ struct PcgState {
 };
 
 enum { STOP_CHECON = 0, STOP_RELRES = 1 };
+constexpr int kPersistSlots = 8;   // persistent-kernel instantiations, one barrier counter and grid each
+constexpr int kBarWords = 16;      // u64 words per counter (one 128-byte line each)
 enum { KIND_SOLID20 = 0, KIND_SCALAR8 = 1 };   // 20-node elasticity (p121), 8-node scalar (p123)
 
 struct Ctx {
@@ -65,7 +70,7 @@ struct Ctx {
     double *km64 = nullptr;     // [nels*3600] storkm(60,60,e)
     float *km32 = nullptr;      // [nels*3600] full FP32 copy
     float *km32p = nullptr;     // [nels*1832] packed symmetric storkm (packed_off), FP32
-    int *kerr = nullptr;        // device error word of the bulk-copy kernels (2 = wait timed out)
+    int *kerr = nullptr;        // device error word: 2 = a bulk-copy wait timed out, 3 = a grid barrier did
     bool have_km = false;
 
     double *ediag = nullptr;    // [nels*60] element diagonals
@@ -103,6 +108,11 @@ struct Ctx {
     int sym_warps = 14, sym_stages = 2;
     unsigned long long sym_attr = 0;   // configurations whose shared-memory attribute is set
     float tune_ms[4] = {0, 0, 0, 0};
+
+    // persistent PCG kernels (cooperative launches with grid-wide barriers)
+    bool persistent = false;    // true: persistent cooperative kernels for the iteration (pf_set_persistent)
+    unsigned long long *gbar = nullptr;   // [kPersistSlots] grid-barrier arrival counters, zeroed per run
+    int pk_grid[kPersistSlots] = {};      // blocks of each persistent instantiation (0 = not sized)
 
     int G = 0;                  // blocks of the vector kernels
     int Gs = 0;                 // blocks of the node scatter
@@ -142,6 +152,15 @@ int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, doub
 int launch_update1(Ctx &c, double *xsol);
 int launch_update2(Ctx &c);   // update2 + the one-block finish kernel
 int launch_pcg_iteration(Ctx &c, int prec, double *xsol);
+// Persistent forms: the scatter + updates + finish of one iteration in one
+// cooperative launch (after the element products), and whole FP64
+// iterations (element products included), up to niters per launch.
+int launch_pcg_tail(Ctx &c, int prec, double *xsol);
+int launch_pcg_fused64(Ctx &c, double *xsol, int niters);
+bool persist_fused64(const Ctx &c, int prec);
+// One bounded mbarrier wait that nothing completes (the error path of the
+// bulk-copy kernels, without a fault): records code 2 in c.kerr.
+int launch_wait_probe(Ctx &c, long long polls);
 int launch_axpy(Ctx &c, double *y, const double *xv);          // y += x
 int launch_replace(Ctx &c, double tol);   // r = rres, d = diag*r, up = r.d; p kept
 int launch_sum_partials(Ctx &c, int nvals, double *out_dev);   // out[0] = sum of part_s

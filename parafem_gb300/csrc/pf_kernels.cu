@@ -232,53 +232,60 @@ template <typename KT> struct Vec2;
 template <> struct Vec2<double> { typedef double2 T; };
 template <> struct Vec2<float> { typedef float2 T; };
 
+// One element's product by one warp (the body of k_elem, shared with the
+// persistent FP64 iteration kernel).
+template <typename KT, bool GATHER>
+__device__ __forceinline__ void elem_warp(int e, int lane, const KT *__restrict__ km, const int *__restrict__ conn,
+                                          const double *__restrict__ p, KT *__restrict__ ut)
+{
+    typedef typename Vec2<KT>::T V2;
+    const int j1 = lane + 32;
+    KT p0, p1;
+    if (GATHER) {
+        const int nd = (lane < 20) ? conn[(size_t)e * 20 + lane] : 0;
+        const int n0 = __shfl_sync(FULLMASK, nd, lane / 3);
+        const int n1 = __shfl_sync(FULLMASK, nd, j1 < 60 ? j1 / 3 : 0);
+        p0 = (KT)p[(size_t)3 * n0 + lane % 3];
+        p1 = (j1 < 60) ? (KT)p[(size_t)3 * n1 + j1 % 3] : (KT)0;
+    } else {
+        p0 = (KT)p[(size_t)e * 60 + lane];
+        p1 = (j1 < 60) ? (KT)p[(size_t)e * 60 + j1] : (KT)0;
+    }
+    const KT *ke = km + (size_t)e * 3600 + 2 * lane;
+    KT a0 = 0, a1 = 0;
+#pragma unroll 12
+    for (int j = 0; j < 60; ++j) {
+        const KT pj = __shfl_sync(FULLMASK, j < 32 ? p0 : p1, j & 31);
+        if (lane < 30) {
+            const V2 k2 = __ldg(reinterpret_cast<const V2 *>(ke + 60 * j));
+            a0 = fma(k2.x, pj, a0);
+            a1 = fma(k2.y, pj, a1);
+        }
+    }
+    if (lane < 30) {
+        if constexpr (sizeof(KT) == 4) {   // FP32 results, node-padded: row i at (i/3)*4 + i%3
+            const int i0 = 2 * lane, i1 = 2 * lane + 1;
+            ut[(size_t)e * 80 + (i0 / 3) * 4 + i0 % 3] = a0;
+            ut[(size_t)e * 80 + (i1 / 3) * 4 + i1 % 3] = a1;
+        } else {
+            V2 o;
+            o.x = a0;
+            o.y = a1;
+            reinterpret_cast<V2 *>(ut + (size_t)e * 60)[lane] = o;
+        }
+    }
+}
+
 template <typename KT, bool GATHER>
 __global__ void __launch_bounds__(256)
 k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
        const double *__restrict__ p, KT *__restrict__ ut, const PcgState *__restrict__ st)
 {
     if (st && st->stop) return;
-    typedef typename Vec2<KT>::T V2;
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int j1 = lane + 32;
-    for (int e = warp; e < nels; e += nwarps) {
-        KT p0, p1;
-        if (GATHER) {
-            const int nd = (lane < 20) ? conn[(size_t)e * 20 + lane] : 0;
-            const int n0 = __shfl_sync(FULLMASK, nd, lane / 3);
-            const int n1 = __shfl_sync(FULLMASK, nd, j1 < 60 ? j1 / 3 : 0);
-            p0 = (KT)p[(size_t)3 * n0 + lane % 3];
-            p1 = (j1 < 60) ? (KT)p[(size_t)3 * n1 + j1 % 3] : (KT)0;
-        } else {
-            p0 = (KT)p[(size_t)e * 60 + lane];
-            p1 = (j1 < 60) ? (KT)p[(size_t)e * 60 + j1] : (KT)0;
-        }
-        const KT *ke = km + (size_t)e * 3600 + 2 * lane;
-        KT a0 = 0, a1 = 0;
-#pragma unroll 12
-        for (int j = 0; j < 60; ++j) {
-            const KT pj = __shfl_sync(FULLMASK, j < 32 ? p0 : p1, j & 31);
-            if (lane < 30) {
-                const V2 k2 = __ldg(reinterpret_cast<const V2 *>(ke + 60 * j));
-                a0 = fma(k2.x, pj, a0);
-                a1 = fma(k2.y, pj, a1);
-            }
-        }
-        if (lane < 30) {
-            if constexpr (sizeof(KT) == 4) {   // FP32 results, node-padded: row i at (i/3)*4 + i%3
-                const int i0 = 2 * lane, i1 = 2 * lane + 1;
-                ut[(size_t)e * 80 + (i0 / 3) * 4 + i0 % 3] = a0;
-                ut[(size_t)e * 80 + (i1 / 3) * 4 + i1 % 3] = a1;
-            } else {
-                V2 o;
-                o.x = a0;
-                o.y = a1;
-                reinterpret_cast<V2 *>(ut + (size_t)e * 60)[lane] = o;
-            }
-        }
-    }
+    for (int e = warp; e < nels; e += nwarps) elem_warp<KT, GATHER>(e, lane, km, conn, p, ut);
 }
 
 // Node-centric scatter (SCATTER, gather_scatter.f90:694-854, one rank):
@@ -293,45 +300,52 @@ k_elem(int nels, const KT *__restrict__ km, const int *__restrict__ conn,
 //   MODE 0: out = u (restrained 0), partial p.u       (pf = p)
 //   MODE 1: out = f - u (restrained 0), partial out.out (pf = f)
 //   MODE 2: out += u at free dofs, no partials          (pf unused)
-template <typename UT, int MODE>
-__global__ void __launch_bounds__(256)
-k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
-          const UT *__restrict__ ut, const uint8_t *__restrict__ fm, const double *__restrict__ pf,
-          double *__restrict__ out, double *__restrict__ part, const PcgState *__restrict__ st)
+// One (virtual) block vb of nvb of the scatter: the body of k_scatter,
+// shared with the persistent iteration kernels, which run the same blocks
+// so that every partial sum is formed in the same order.  NC: the element
+// results may be read through the non-coherent path (they were written by an
+// earlier launch).  PF contributions are fetched at a time; the sums are
+// formed in ascending order whatever PF is.
+template <typename UT, int MODE, bool NC, int PF = 8>
+__device__ __forceinline__ void scatter_block(int vb, int nvb, int nn, const int *__restrict__ ptr,
+                                              const int *__restrict__ list, const UT *__restrict__ ut,
+                                              const uint8_t *__restrict__ fm, const double *__restrict__ pf,
+                                              double *__restrict__ out, double *__restrict__ part)
 {
-    if (block_stopped(st)) return;
     double loc = 0.0;
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nn; n += gridDim.x * blockDim.x) {
+    for (int n = vb * blockDim.x + threadIdx.x; n < nn; n += nvb * blockDim.x) {
         UT a0 = 0, a1 = 0, a2 = 0;
         const int k1 = ptr[n + 1];
-        for (int k = ptr[n]; k < k1; k += 8) {
-            int ci[8];
+        for (int k = ptr[n]; k < k1; k += PF) {
+            int ci[PF];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) ci[i] = (k + i < k1) ? __ldg(list + k + i) : -1;
+            for (int i = 0; i < PF; ++i) ci[i] = (k + i < k1) ? __ldg(list + k + i) : -1;
             if constexpr (sizeof(UT) == 4) {
-                float4 v[8];
+                float4 v[PF];
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
-                    if (ci[i] >= 0) v[i] = __ldg(reinterpret_cast<const float4 *>(ut) + ci[i]);
+                for (int i = 0; i < PF; ++i)
+                    if (ci[i] >= 0)
+                        v[i] = NC ? __ldg(reinterpret_cast<const float4 *>(ut) + ci[i])
+                                  : __ldcg(reinterpret_cast<const float4 *>(ut) + ci[i]);
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
+                for (int i = 0; i < PF; ++i)
                     if (ci[i] >= 0) {
                         a0 += v[i].x;
                         a1 += v[i].y;
                         a2 += v[i].z;
                     }
             } else {
-                double v[8][3];
+                double v[PF][3];
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
+                for (int i = 0; i < PF; ++i)
                     if (ci[i] >= 0) {
                         const double *q = ut + (size_t)ci[i] * 3;
-                        v[i][0] = q[0];
-                        v[i][1] = q[1];
-                        v[i][2] = q[2];
+                        v[i][0] = NC ? q[0] : __ldcg(q);
+                        v[i][1] = NC ? q[1] : __ldcg(q + 1);
+                        v[i][2] = NC ? q[2] : __ldcg(q + 2);
                     }
 #pragma unroll
-                for (int i = 0; i < 8; ++i)
+                for (int i = 0; i < PF; ++i)
                     if (ci[i] >= 0) {
                         a0 += v[i][0];
                         a1 += v[i][1];
@@ -361,7 +375,17 @@ k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
     if (MODE == 2) return;   // no partial sums (the kernel has no block barrier after this point)
     double v[1] = {loc};
     block_reduce<1>(v, 0u);
-    if (threadIdx.x == 0) part[blockIdx.x] = v[0];
+    if (threadIdx.x == 0) part[vb] = v[0];
+}
+
+template <typename UT, int MODE>
+__global__ void __launch_bounds__(256)
+k_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list,
+          const UT *__restrict__ ut, const uint8_t *__restrict__ fm, const double *__restrict__ pf,
+          double *__restrict__ out, double *__restrict__ part, const PcgState *__restrict__ st)
+{
+    if (block_stopped(st)) return;
+    scatter_block<UT, MODE, true>(blockIdx.x, gridDim.x, nn, ptr, list, ut, fm, pf, out, part);
 }
 
 // ---------------------------------------------------------------------------
@@ -427,17 +451,13 @@ __global__ void k_pcg_init2(PcgState *st, const double *__restrict__ part, int G
 // st->up only.  The max terms cost four FP64 operations per dof, a slow pipe
 // on GB300, so the residual-stopped runs skip them.
 template <bool CHECON>
-__global__ void __launch_bounds__(256)
-k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict__ ps, int Gs,
-              double *__restrict__ pu_out, int G, double *__restrict__ x, double *__restrict__ r,
-              double *__restrict__ d, const double *__restrict__ p, const double *__restrict__ u,
-              const double *__restrict__ dinv)
+__device__ __forceinline__ void update1_block(int vb, int nvb, int ns, double alpha, double *__restrict__ pu_out,
+                                              int G, double *__restrict__ x, double *__restrict__ r,
+                                              double *__restrict__ d, const double *__restrict__ p,
+                                              const double *__restrict__ u, const double *__restrict__ dinv)
 {
-    if (block_stopped(st)) return;
-    const double pu = reduce_partials(ps, Gs, false);
-    const double alpha = st->up / pu;
     double rd = 0.0, rr = 0.0, mx = 0.0, md = 0.0;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+    for (int s = vb * blockDim.x + threadIdx.x; s < ns; s += nvb * blockDim.x) {
         const double xo = x[s];
         const double xn = fma(p[s], alpha, xo);
         x[s] = xn;
@@ -455,23 +475,32 @@ k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict_
     double v[4] = {rd, rr, mx, md};
     block_reduce<4>(v, 0xCu);
     if (threadIdx.x == 0) {
-        pu_out[0 * G + blockIdx.x] = v[0];
-        pu_out[1 * G + blockIdx.x] = v[1];
-        pu_out[2 * G + blockIdx.x] = v[2];
-        pu_out[3 * G + blockIdx.x] = v[3];
+        pu_out[0 * G + vb] = v[0];
+        pu_out[1 * G + vb] = v[1];
+        pu_out[2 * G + vb] = v[2];
+        pu_out[3 * G + vb] = v[3];
     }
+}
+
+template <bool CHECON>
+__global__ void __launch_bounds__(256)
+k_pcg_update1(int ns, const PcgState *__restrict__ st, const double *__restrict__ ps, int Gs,
+              double *__restrict__ pu_out, int G, double *__restrict__ x, double *__restrict__ r,
+              double *__restrict__ d, const double *__restrict__ p, const double *__restrict__ u,
+              const double *__restrict__ dinv)
+{
+    if (block_stopped(st)) return;
+    const double pu = reduce_partials(ps, Gs, false);
+    const double alpha = st->up / pu;
+    update1_block<CHECON>(blockIdx.x, gridDim.x, ns, alpha, pu_out, G, x, r, d, p, u, dinv);
 }
 
 // update2: beta = (r.d)/up; p = d + p*beta (and its FP32 high and low
 // parts into ps, shared-km contexts).  Reads st->up only.
-__global__ void __launch_bounds__(256)
-k_pcg_update2(int ns, const PcgState *__restrict__ st, const double *__restrict__ part, int G,
-              const double *__restrict__ d, double *__restrict__ p, float2 *__restrict__ ps)
+__device__ __forceinline__ void update2_block(int vb, int nvb, int ns, double beta, const double *__restrict__ d,
+                                              double *__restrict__ p, float2 *__restrict__ ps)
 {
-    if (block_stopped(st)) return;
-    const double rd = reduce_partials(part, G, false);
-    const double beta = rd / st->up;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+    for (int s = vb * blockDim.x + threadIdx.x; s < ns; s += nvb * blockDim.x) {
         const double pn = fma(p[s], beta, d[s]);
         p[s] = pn;
         if (ps) {
@@ -480,6 +509,16 @@ k_pcg_update2(int ns, const PcgState *__restrict__ st, const double *__restrict_
             ps[s] = make_float2(h, l);
         }
     }
+}
+
+__global__ void __launch_bounds__(256)
+k_pcg_update2(int ns, const PcgState *__restrict__ st, const double *__restrict__ part, int G,
+              const double *__restrict__ d, double *__restrict__ p, float2 *__restrict__ ps)
+{
+    if (block_stopped(st)) return;
+    const double rd = reduce_partials(part, G, false);
+    const double beta = rd / st->up;
+    update2_block(blockIdx.x, gridDim.x, ns, beta, d, p, ps);
 }
 
 // finish (one block): the iteration's bookkeeping -- up for the next
@@ -506,6 +545,89 @@ k_pcg_finish(PcgState *__restrict__ st, const double *__restrict__ part, int G)
         st->converged = conv ? 1 : 0;
         if (!isfinite(rd) || !isfinite(mx)) st->err = 1;
         if (conv || k >= st->limit || st->err) st->stop = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent PCG iterations (p121.f90:90-104 with DOT_PRODUCT_P,
+// maths.f90:168-215, and checon_par, maths.f90:1052-1062).  One cooperative
+// launch runs the scatter, both update passes and the finish of an
+// iteration -- and, in the FP64 form (ELEM64), the element products too and
+// up to `niters` whole iterations -- with grid-wide barriers where the
+// separate kernels have launch boundaries.  The launch has at most as many
+// blocks as are resident at once.  Block b runs the virtual blocks b,
+// b + gridDim.x, ... of the Gs-block scatter and of the G-block vector
+// kernels through the same block bodies, and every block forms the
+// reductions of the finish itself in the same fixed order, so the iterates
+// and the stopping decisions are bitwise those of the separate kernels.
+// Block 0 writes the state; the other blocks only read it at the start,
+// before the first barrier.
+struct PersistArgs {
+    int nels, nn, ns, G, Gs, niters;
+    const double *km64;   // FP64 storkm (ELEM64)
+    const int *conn;
+    void *ut;             // element results
+    const int *node_ptr, *node_list;
+    const uint8_t *fm;
+    double *x, *r, *d, *p, *u;
+    const double *dinv;
+    double *part_s, *part_u;
+    float2 *psplit;       // shared-km contexts: FP32 high/low parts of p
+    PcgState *st;
+    unsigned long long *bar;
+    int *kerr;
+};
+
+template <typename UT, bool ELEM64, bool CHECON, int MINB, int PF>
+__global__ void __launch_bounds__(256, MINB) k_pcg_persistent(PersistArgs a)
+{
+    if (block_stopped(a.st)) return;
+    volatile PcgState *vs = a.st;
+    double up = vs->up;
+    int iters = vs->iters;
+    const int limit = vs->limit;
+    const double tol = vs->tol, ff = vs->ff;
+    const int lane = threadIdx.x & 31;
+    for (int it = 0; it < a.niters; ++it) {
+        if (ELEM64) {
+            const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+            const int nw = (gridDim.x * blockDim.x) >> 5;
+            for (int e = warp; e < a.nels; e += nw)
+                elem_warp<double, true>(e, lane, a.km64, a.conn, a.p, (double *)a.ut);
+            if (!grid_barrier(a.bar, a.kerr, a.st)) return;
+        }
+        for (int vb = blockIdx.x; vb < a.Gs; vb += gridDim.x)
+            scatter_block<UT, 0, !ELEM64, PF>(vb, a.Gs, a.nn, a.node_ptr, a.node_list, (const UT *)a.ut, a.fm, a.p,
+                                          a.u, a.part_s);
+        if (!grid_barrier(a.bar, a.kerr, a.st)) return;
+        const double alpha = up / reduce_partials(a.part_s, a.Gs, false);
+        for (int vb = blockIdx.x; vb < a.G; vb += gridDim.x)
+            update1_block<CHECON>(vb, a.G, a.ns, alpha, a.part_u, a.G, a.x, a.r, a.d, a.p, a.u, a.dinv);
+        if (!grid_barrier(a.bar, a.kerr, a.st)) return;
+        const double rd = reduce_partials(a.part_u, a.G, false);
+        const double beta = rd / up;
+        for (int vb = blockIdx.x; vb < a.G; vb += gridDim.x) update2_block(vb, a.G, a.ns, beta, a.d, a.p, a.psplit);
+        // the finish of k_pcg_finish, formed by every block
+        const double rr = reduce_partials(a.part_u + a.G, a.G, false);
+        const double mx = CHECON ? reduce_partials(a.part_u + 2 * a.G, a.G, true) : 1.0;
+        const double md = CHECON ? reduce_partials(a.part_u + 3 * a.G, a.G, true) : 0.0;
+        ++iters;
+        const double metric = CHECON ? md / mx : sqrt(rr) / sqrt(ff);
+        const bool conv = metric <= tol;
+        const bool bad = !isfinite(rd) || !isfinite(mx);
+        const bool stop = conv || iters >= limit || bad;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            vs->up = rd;
+            vs->iters = iters;
+            vs->rr = rr;
+            vs->metric = metric;
+            vs->converged = conv ? 1 : 0;
+            if (bad) vs->err = 1;
+            if (stop) vs->stop = 1;
+        }
+        up = rd;
+        if (stop) return;
+        if (it + 1 < a.niters && !grid_barrier(a.bar, a.kerr, a.st)) return;
     }
 }
 
@@ -644,6 +766,21 @@ __global__ void k_matvec_rows(int n_mat, int n_row, int n_col, const double *__r
         double s = 0.0;
         for (int j = 0; j < n_col; ++j) s = fma(x[j], a[(size_t)j * n_row], s);
         rhs[g] = s;
+    }
+}
+
+// Exercises the bounded mbarrier wait of the bulk-copy kernels on a barrier
+// that nothing completes: one thread arms it for 16 bytes of transactions
+// and issues no copy, so no copy is in flight when the wait gives up.  The
+// kernel then records code 2 in the error word, as those kernels do.
+__global__ void k_wait_probe(long long polls, int *err)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar, 1);
+        tc::mbar_fence_init();
+        tc::mbar_expect_tx(&bar, 16);
+        if (!tc::mbar_wait_n(&bar, 0, polls)) atomicExch(err, 2);
     }
 }
 
@@ -825,6 +962,10 @@ int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
 int launch_pcg_init(Ctx &c, const double *rhs, double *xsol, int stop_mode, double tol, int limit, bool keep_x)
 {
     c.stop_mode = stop_mode;
+    if (cudaMemsetAsync(c.gbar, 0, sizeof(unsigned long long) * kPersistSlots * kBarWords, c.stream) != cudaSuccess) {
+        set_error("k_pcg_init: cannot reset the grid-barrier counters");
+        return 1;
+    }
     k_pcg_init<<<c.G, 256, 0, c.stream>>>(c.nslots, rhs, c.dinv, xsol, c.r, c.d, c.p, c.part_u, c.G, keep_x ? 1 : 0,
                                           c.shared ? c.psplit : nullptr);
     if (check_launch(c, "k_pcg_init")) return 1;
@@ -851,12 +992,91 @@ int launch_update2(Ctx &c)
     return check_launch(c, "k_pcg_finish");
 }
 
+// Blocks of the cooperative launch of one persistent-kernel instantiation:
+// at most the resident capacity, and no more than the virtual blocks (and,
+// with the element phase, the element warps) give work.
+template <typename UT, bool ELEM64, bool CHECON, int MINB, int PF>
+static int persist_grid(const Ctx &c)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_persistent<UT, ELEM64, CHECON, MINB, PF>, 256,
+                                                      0) != cudaSuccess ||
+        per_sm < 1)
+        return 0;
+    long long want = c.G > c.Gs ? c.G : c.Gs;
+    if (ELEM64) {
+        const long long ew = ((long long)c.nels + 7) / 8;
+        if (ew > want) want = ew;
+    }
+    const long long cap = (long long)per_sm * c.nsm;
+    return (int)(want < cap ? want : cap);
+}
+
+template <typename UT, bool ELEM64, bool CHECON>
+static int launch_persist_t(Ctx &c, double *xsol, int niters)
+{
+    constexpr int MINB = 4, PF = sizeof(UT) == 8 ? 4 : 8;
+    const int idx = (ELEM64 ? 4 : 0) + (sizeof(UT) == 4 ? 2 : 0) + (CHECON ? 1 : 0);
+    if (c.pk_grid[idx] == 0) c.pk_grid[idx] = persist_grid<UT, ELEM64, CHECON, MINB, PF>(c);
+    const int grid = c.pk_grid[idx];
+    if (grid < 1) {
+        set_error("persistent PCG kernel: no resident block fits");
+        return 1;
+    }
+    PersistArgs a;
+    a.nels = c.nels; a.nn = c.nn; a.ns = c.nslots; a.G = c.G; a.Gs = c.Gs; a.niters = niters;
+    a.km64 = c.km64; a.conn = c.conn; a.ut = c.utemp; a.node_ptr = c.node_ptr; a.node_list = c.node_list;
+    a.fm = c.freemask; a.x = xsol; a.r = c.r; a.d = c.d; a.p = c.p; a.u = c.u; a.dinv = c.dinv;
+    a.part_s = c.part_s; a.part_u = c.part_u; a.psplit = c.shared ? c.psplit : nullptr; a.st = c.st;
+    a.bar = c.gbar + (size_t)idx * kBarWords; a.kerr = c.kerr;
+    void *args[] = {&a};
+    const cudaError_t e = cudaLaunchCooperativeKernel(
+        (const void *)k_pcg_persistent<UT, ELEM64, CHECON, MINB, PF>, dim3(grid), dim3(256), args, 0, c.stream);
+    c.launches++;
+    if (e != cudaSuccess) {
+        set_error("k_pcg_persistent: cooperative launch of %d blocks failed: %s", grid, cudaGetErrorString(e));
+        return 1;
+    }
+    return 0;
+}
+
+bool persist_fused64(const Ctx &c, int prec)
+{
+    return c.persistent && prec == PREC_FP64 && !c.shared && c.kind == KIND_SOLID20;
+}
+
+int launch_pcg_tail(Ctx &c, int prec, double *xsol)
+{
+    const bool ck = c.stop_mode == STOP_CHECON;
+    if (prec == PREC_FP64)
+        return ck ? launch_persist_t<double, false, true>(c, xsol, 1) : launch_persist_t<double, false, false>(c, xsol, 1);
+    return ck ? launch_persist_t<float, false, true>(c, xsol, 1) : launch_persist_t<float, false, false>(c, xsol, 1);
+}
+
+int launch_pcg_fused64(Ctx &c, double *xsol, int niters)
+{
+    return c.stop_mode == STOP_CHECON ? launch_persist_t<double, true, true>(c, xsol, niters)
+                                      : launch_persist_t<double, true, false>(c, xsol, niters);
+}
+
 int launch_pcg_iteration(Ctx &c, int prec, double *xsol)
 {
+    if (c.persistent && c.kind == KIND_SOLID20) {
+        if (persist_fused64(c, prec)) return launch_pcg_fused64(c, xsol, 1);
+        if (launch_elem(c, prec, c.p)) return 1;
+        return launch_pcg_tail(c, prec, xsol);
+    }
+
     if (launch_elem(c, prec, c.p)) return 1;
     if (launch_scatter(c, prec, 0, c.p, c.u)) return 1;
     if (launch_update1(c, xsol)) return 1;
     return launch_update2(c);
+}
+
+int launch_wait_probe(Ctx &c, long long polls)
+{
+    k_wait_probe<<<1, 32, 0, c.stream>>>(polls, c.kerr);
+    return check_launch(c, "k_wait_probe");
 }
 
 int launch_axpy(Ctx &c, double *y, const double *xv)

@@ -44,13 +44,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait for the phase with the given parity: false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+// Bounded wait for the phase with the given parity: false when `limit`
+// polls ran out.
+__device__ __forceinline__ bool mbar_wait_n(uint64_t *bar, uint32_t parity, long long limit)
 {
-    for (long long i = 0; i < kSpinLimit; ++i)
+    for (long long i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) { return mbar_wait_n(bar, parity, kSpinLimit); }
 
 // ---------------------------------------------------------------------------
 // bulk copies global -> shared (16-byte aligned addresses, size a multiple of 16)

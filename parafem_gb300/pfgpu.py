@@ -64,6 +64,8 @@ _SIGS = {
     "pf_tuning16": [_VPP, _IP, _IP, ctypes.c_void_p],
     "pf_set_tuning": [_VPP, _IP],
     "pf_set_graphs": [_VPP, _IP],
+    "pf_set_persistent": [_VPP, _IP],
+    "pf_check_wait_timeout": [_VPP, _IP],
     "pf_ebe_matvec_noalloc": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p],
     "pf_solve_multi": [_VPP, _IP, ctypes.c_void_p, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p,
@@ -436,6 +438,19 @@ class Solver:
     def set_graphs(self, on: bool) -> None:
         """Replay PCG iterations from a CUDA graph (default) or launch each kernel directly."""
         _check(lib().pf_set_graphs(self._ref, ctypes.byref(ctypes.c_int(1 if on else 0))), "pf_set_graphs")
+
+    def set_persistent(self, on: bool) -> None:
+        """Run the PCG iteration's scatter, updates and finish (and whole FP64
+        iterations) as persistent cooperative kernels, or as the separate
+        kernels (the default)."""
+        _check(lib().pf_set_persistent(self._ref, ctypes.byref(ctypes.c_int(1 if on else 0))), "pf_set_persistent")
+
+    def check_wait_timeout(self, polls: int) -> tuple[int, str]:
+        """Runs one bounded bulk-copy wait that nothing completes; returns the
+        status code and the recorded error message (PF_FAILURE and the
+        timeout message when the error path works)."""
+        rc = lib().pf_check_wait_timeout(self._ref, ctypes.byref(ctypes.c_int(polls)))
+        return rc, last_error()
 
     def set_tuning(self, config: int) -> None:
         """Force configuration 0 (14x2), 1 (12x2) or 2 (8x3); -1 re-runs the autotuner."""
