@@ -1,9 +1,9 @@
 #!/usr/bin/env python
 """EBE-PCG benchmark of the p121 solve on GB300.
 
-Workload: the 100x100x100 20-node hexahedron cube (nip=27, E=100, v=0.3, every
-dof of the base face fixed, uniform top pressure with total load -1), ~12.2M
-equations, synthetic (generated in memory; no dataset).
+Headline workload: the 100x100x100 20-node hexahedron cube (nip=27, E=100,
+v=0.3, every dof of the base face fixed, uniform top pressure with total
+load -1), ~12.2M equations, synthetic (generated in memory; no dataset).
 
   step   = one PCG iteration over the whole mesh (element products, node
            scatter, fused updates and reductions) of the mixed-precision
@@ -12,10 +12,19 @@ equations, synthetic (generated in memory; no dataset).
   e2e    = one full mixed-precision solve to ||f-Ku||/||f|| <= 1e-8 through
            pf_solve with host buffers (load vector in, displacements out),
            DOF.iter/s over its wall time;
-  time_to_1e8 = wall time of that solve and of the plain FP64 solve.
+  time_to_1e8 = wall time of that solve and of the plain FP64 solve, and
+           the displacement error of both against FP64 solved to 1e-12.
 
---impl reference times the CPU restatement of p121's PCG (oracle/, OpenMP on
-all host cores) on a bounded slab of the same cube.
+The default run also measures the other configurations of the benchmark in
+the same line ("configs"): the 80^3 heterogeneous cube (mixed vs FP64 at
+1e-8, errors against FP64 at 1e-12), the 60^3 cube with 16 load cases
+(block solve on the tensor cores vs 16 sequential FP64 solves) and the
+serving stream (continuous batching, p50/p99 latency and solves/s); the
+10^3 CPU-runnable case is in the CPU baseline leg, against the CPU build.
+
+--impl reference times the CPU build of p121's PCG (oracle/p121_cpu.c,
+OpenMP on all host cores, every loop of the iteration parallel) on the same
+100^3 cube.
 """
 from __future__ import annotations
 
@@ -40,12 +49,17 @@ UNIT = "DOF·iter/s"
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=100, help="elements per cube edge")
     ap.add_argument("--no-solves", action="store_true", help="skip the time-to-1e-8 solves")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="cube100: skip the other configurations (heterogeneous 80^3, 16 load cases at 60^3, "
+                         "serving stream)")
+    ap.add_argument("--serving-requests", type=int, default=500,
+                    help="cube100: requests of the serving stream measured in the default line")
     ap.add_argument("--workload", default="cube100",
                     choices=["cube100", "hetero80", "serving", "multirhs60", "cube10", "shared100", "p123book",
                              "p122book"],
@@ -192,21 +206,50 @@ def elem_bytes(nels, nslots, storkm_bytes, result_bytes):
     return nels * (storkm_bytes + 20 * 4 + 60 * result_bytes) + nslots * 8
 
 
-def cpu_port_leg(n, k_steps, warm):
-    """The oracle (C restatement of p121's PCG, OpenMP) on an n x n x 8 slab."""
+def cpu_build_leg(n, k_steps, warm):
+    """The CPU build of p121's PCG (oracle/p121_cpu.c: OpenMP over every loop
+    of the iteration, -O3 with contraction) on the n^3 cube: storkm formed on
+    the host, then `warm` untimed and `k_steps` timed PCG iterations."""
     from oracle import oracle as O
-    nz = 8
-    prob = oracle_cube(n, n, nz)
-    km = O.form_storkm(prob["gc"], 27, 100.0, 0.3)
-    dg = O.diag(prob["g_g"], km, prob["neq"])
-    O.pcg(prob["g_g"], km, dg, prob["r"], 0.0, max(warm, 1), 0)
     t0 = time.perf_counter()
-    O.pcg(prob["g_g"], km, dg, prob["r"], 0.0, k_steps, 0)
-    dt = time.perf_counter() - t0
-    return {"value": prob["neq"] * k_steps / dt, "unit": UNIT, "cores": O.lib().orc_num_threads(),
-            "kind": "port", "seconds": dt,
-            "sample": f"{n}x{n}x{nz} slab of the same cube (neq {prob['neq']}), nip 27, FP64, "
-                      f"{k_steps} p121 PCG iterations of the C restatement"}
+    c = O.CpuP121(n, n, n, 27, 100.0, 0.3)
+    t_setup = time.perf_counter() - t0
+    try:
+        c.init()
+        c.iterate(max(warm, 1))
+        t1 = time.perf_counter()
+        c.iterate(k_steps)
+        dt = time.perf_counter() - t1
+        return {"value": c.neq * k_steps / dt, "unit": UNIT, "cores": c.threads, "kind": "port", "seconds": dt,
+                "setup_s": t_setup,
+                "sample": f"{n}x{n}x{n} cube (neq {c.neq}, storkm {n ** 3 * 28800 / 1e9:.1f} GB FP64), nip 27, "
+                          f"{k_steps} p121 PCG iterations of the CPU build (oracle/p121_cpu.c: GATHER, element "
+                          f"products, node-centric SCATTER, dot products, updates and checon_par on "
+                          f"{c.threads} OpenMP threads, gcc -O3 -ffp-contract=fast)"}
+    finally:
+        c.close()
+
+
+def cpu_config1(gpu_x, gpu_iters, gpu_wall):
+    """Config 1 (10^3, checon_par tol 1e-6, limit 5000) on the CPU build:
+    its iterations, time and solution against the GPU drop-in's."""
+    from oracle import oracle as O
+    c = O.CpuP121(10, 10, 10, 27, 100.0, 0.3)
+    try:
+        c.init()
+        t0 = time.perf_counter()
+        it = c.iterate(5000, 1e-6, 0)
+        dt = time.perf_counter() - t0
+        x = c.x()
+    finally:
+        c.close()
+    return {"workload": "p121 10^3 hex20 cube (the CPU-runnable case), nip 27, E 100, v 0.3, fixed base, top "
+                        "pressure (total -1), checon_par tol 1e-6, limit 5000",
+            "neq": int(x.size), "gpu_p121_drop_in": {"iters": gpu_iters, "solve_wall_s": gpu_wall},
+            "cpu_build": {"iters": it, "solve_wall_s": dt},
+            "iters_equal": gpu_iters == it,
+            "rel_err_2": float(np.linalg.norm(gpu_x - x) / np.linalg.norm(x)),
+            "rel_err_inf": float(np.abs(gpu_x - x).max() / np.abs(x).max()), "tolerance": 1e-6}
 
 
 def oracle_cube(nxe, nye, nze):
@@ -244,7 +287,7 @@ def run_reference(args, rank):
     if rank != 0:
         return 0
     n = args.size
-    leg = cpu_port_leg(n, args.steps, args.warmup)
+    leg = cpu_build_leg(n, args.steps, args.warmup)
     line = {
         "metric": METRIC, "value": leg["value"], "unit": UNIT, "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -253,8 +296,10 @@ def run_reference(args, rank):
         "config": config_of(args),
         "cpu_baseline": {k: leg[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": leg["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "ParaFEM's Fortran/MPI p121 cannot be built here (no Fortran compiler or MPI); "
-                "the timed reference is the C restatement of its PCG in oracle/",
+        "setup_s": leg["setup_s"],
+        "note": "ParaFEM's Fortran/MPI p121 cannot be built here (no Fortran compiler or MPI); the timed "
+                "reference is the CPU build of its PCG in oracle/p121_cpu.c, every loop of the iteration on "
+                "all host threads, as MPI p121 spreads them over ranks",
     }
     print(json.dumps(line))
     return 0
@@ -384,57 +429,98 @@ def run_gb300(args, rank, world, local, dist):
         "time_to_1e8": solves, "roofline": roof, "gpu_launches": int(launches),
         "clocks": clocks, "extra": extra,
     }
+    s.close()
+    if not args.no_configs and world == 1:
+        line["configs"] = other_configs(args, local)
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = {k: v for k, v in cpu_port_leg(n, 20, 2).items() if k != "seconds"}
+            leg = cpu_build_leg(n, 10, 2)
+            line["cpu_baseline"] = {k: v for k, v in leg.items() if k not in ("seconds",)}
+            x1, it1, t1 = gpu_config1(local)
+            line["cpu_baseline"]["config1_vs_gpu_drop_in"] = cpu_config1(x1, it1, t1)
         except Exception as exc:  # the baseline is reported, never the target
             line["cpu_baseline"] = {"error": str(exc)}
-    s.close()
     if rank == 0:
         print(json.dumps(line))
     return 0
 
 
-def run_hetero(args, rank, world, local, dist):
-    """80^3 cube with per-element E log-uniform in [1, 1000] and v uniform in
-    [0.2, 0.35] (Philox4x32-10, key = seed, counter = element index): mixed
-    vs FP64 iterations and time to relres 1e-8, displacement error of both
-    against the FP64 solve converged to relres 1e-12."""
+def other_configs(args, local):
+    """The benchmark's other configurations, measured in the default run:
+    heterogeneous 80^3 (mixed and FP64 to 1e-8, errors against FP64 at
+    1e-12), 16 load cases at 60^3 (tensor-core block solve against 16
+    sequential FP64 solves) and the serving stream (a Poisson stream at 20
+    requests/s and the same requests all at once)."""
+    out = {}
+    t0 = time.perf_counter()
+    out["hetero80"] = hetero_solves(80, args.seed, local, ("mixed", "fp64"))
+    out["hetero80"]["bench_wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    out["multirhs60"] = multirhs_solves(60, 16, args.seed, local, args.limit, (16,), True)
+    out["multirhs60"]["bench_wall_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nreq = args.serving_requests
+    res = serving_stream(nreq, [20.0, 0.0], args.budget_gb, args.chunk, args.serving_prec, args.seed, local)
+    out["serving"] = {"workload": serving_workload(nreq, args.budget_gb, args.seed),
+                      "prec": args.serving_prec, "at_20_per_s": res[0], "all_at_once": res[1],
+                      "bench_wall_s": time.perf_counter() - t0}
+    return out
+
+
+def hetero_solves(n, seed, local, modes=("mixed", "fp64")):
+    """n^3 cube with per-element E log-uniform in [1, 1000] and v uniform in
+    [0.2, 0.35] (Philox4x32-10, key = seed, counter = element index): the
+    given solves to relres 1e-8, and the displacement error of each against
+    the FP64 solve converged to relres 1e-12."""
     import parafem_gb300 as P
-    n = args.size if args.size != 100 else 80
     prob = P.cube_problem(n, n, n)
     nels = n ** 3
-    e, v = P.random_material(nels, args.seed, 1.0, 1000.0, 0.2, 0.35)
+    e, v = P.random_material(nels, seed, 1.0, 1000.0, 0.2, 0.35)
     s = P.Solver(local)
-    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
-    s.set_material(e, v)
-    s.form_storkm(27)
-    neq, r = prob["neq"], prob["r"]
-    out = {}
-    xr, itr, relr = s.solve(r, 1e-12, 50000, P.MODE_FP64_RES)
-    out["oracle_fp64_1e-12"] = {"iters": itr, "relres": relr, "device_s": s.stats()["solve_ms"] / 1e3}
-    nr = np.linalg.norm(xr)
-    s.ebe_matvec(np.zeros(neq), 16)   # packs the FP16 storkm once, outside the timed solves
-    for name, mode in (("mixed", P.MODE_MIXED), ("mixed16", P.MODE_MIXED16), ("fp64", P.MODE_FP64_RES),
-                       ("mixed_restart", P.MODE_MIXED_RESTART)):
-        t0 = time.perf_counter()
-        x, it, rel = s.solve(r, 1e-8, 50000, mode)
-        wall = time.perf_counter() - t0
-        st = s.stats()
-        out[name] = {"iters": it, "relres": rel, "wall_s": wall, "device_s": st["solve_ms"] / 1e3,
-                     "corrections": st["outer"], "rel_err_2": float(np.linalg.norm(x - xr) / nr),
-                     "rel_err_inf": float(np.abs(x - xr).max() / np.abs(xr).max())}
-    s.close()
-    value = neq * out["mixed"]["iters"] / out["mixed"]["device_s"]
+    try:
+        s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+        s.set_material(e, v)
+        s.form_storkm(27)
+        neq, r = prob["neq"], prob["r"]
+        out = {"workload": f"heterogeneous {n}^3 hex20 cube, E log-uniform [1,1000], v uniform [0.2,0.35], "
+                           f"Philox4x32-10 seed {seed}, nip 27, fixed base, top pressure, tol 1e-8",
+               "nels": nels, "neq": neq}
+        xr, itr, relr = s.solve(r, 1e-12, 50000, P.MODE_FP64_RES)
+        out["oracle_fp64_1e-12"] = {"iters": itr, "relres": relr, "device_s": s.stats()["solve_ms"] / 1e3}
+        nr = np.linalg.norm(xr)
+        if "mixed16" in modes:
+            s.ebe_matvec(np.zeros(neq), 16)   # packs the FP16 storkm once, outside the timed solves
+        names = {"mixed": P.MODE_MIXED, "mixed16": P.MODE_MIXED16, "fp64": P.MODE_FP64_RES,
+                 "mixed_restart": P.MODE_MIXED_RESTART}
+        for name in modes:
+            t0 = time.perf_counter()
+            x, it, rel = s.solve(r, 1e-8, 50000, names[name])
+            wall = time.perf_counter() - t0
+            st = s.stats()
+            out[name] = {"iters": it, "relres": rel, "wall_s": wall, "device_s": st["solve_ms"] / 1e3,
+                         "corrections": st["outer"], "rel_err_2": float(np.linalg.norm(x - xr) / nr),
+                         "rel_err_inf": float(np.abs(x - xr).max() / np.abs(xr).max())}
+        if "mixed" in out and "fp64" in out:
+            out["mixed_over_fp64_time"] = out["mixed"]["wall_s"] / out["fp64"]["wall_s"]
+            out["mixed_dof_iter_per_s"] = neq * out["mixed"]["iters"] / out["mixed"]["device_s"]
+        if "mixed16" in out and "fp64" in out:
+            out["mixed16_over_fp64_time"] = out["mixed16"]["wall_s"] / out["fp64"]["wall_s"]
+        return out
+    finally:
+        s.close()
+
+
+def run_hetero(args, rank, world, local, dist):
+    """The heterogeneous cube (80^3 by default) with every solve mode."""
+    n = args.size if args.size != 100 else 80
+    out = hetero_solves(n, args.seed, local, ("mixed", "mixed16", "fp64", "mixed_restart"))
+    value = out["mixed_dof_iter_per_s"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
             "ms_per_step": out["mixed"]["device_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (packed-symmetric storkm) / f64 vectors and reductions",
             "data": "synthetic",
-            "config": {"workload": f"heterogeneous {n}^3 hex20 cube, E log-uniform [1,1000], v uniform "
-                                   f"[0.2,0.35], Philox4x32-10 seed {args.seed}, nip 27, fixed base, top "
-                                   f"pressure, tol 1e-8", "nels": nels, "neq": neq},
-            "solves": out, "mixed_over_fp64_time": out["mixed"]["wall_s"] / out["fp64"]["wall_s"],
-            "mixed16_over_fp64_time": out["mixed16"]["wall_s"] / out["fp64"]["wall_s"]}
+            "config": {"workload": out["workload"], "nels": out["nels"], "neq": out["neq"]},
+            "solves": out}
     if rank == 0:
         print(json.dumps(line))
     return 0
@@ -452,17 +538,19 @@ def serving_requests(n, seed):
     return dims, e, v, pres
 
 
-def run_serving(args, rank, world, local, dist):
+def serving_stream(n_req, rates, budget_gb, chunk, prec, seed, local):
+    """Continuous batching of a Poisson request stream (requests from
+    serving_requests): one result per arrival rate (0 = every request at
+    t = 0) with p50/p99 latency, solves/s and DOF.iter/s."""
     import collections
     import parafem_gb300 as P
-    n_req = args.requests
-    dims, es, vs, pres = serving_requests(n_req, args.seed)
+    dims, es, vs, pres = serving_requests(n_req, seed)
     results = []
-    for rate in [float(t) for t in args.rates.split(",")]:
-        rng = np.random.default_rng(args.seed + 1)
+    for rate in rates:
+        rng = np.random.default_rng(seed + 1)
         gaps = rng.exponential(1.0 / rate, n_req) if rate > 0 else np.zeros(n_req)
         arrivals = np.cumsum(gaps) - (gaps[0] if rate > 0 else 0.0)
-        b = P.Batch(int(args.budget_gb * (1 << 30)), 512, local, prec=args.serving_prec)
+        b = P.Batch(int(budget_gb * (1 << 30)), 512, local, prec=prec)
         cache = {}
 
         def build(i):
@@ -497,7 +585,7 @@ def run_serving(args, rank, world, local, dist):
                 del cache[i]
                 active += 1
             if active:
-                b.launch(args.chunk)
+                b.launch(chunk)
                 if queue:
                     build(queue[0])          # host prepares the next request while the GPU iterates
                 active, nd = b.sync()
@@ -520,6 +608,19 @@ def run_serving(args, rank, world, local, dist):
                         "p99_ms": float(np.percentile(L, 99)), "mean_ms": float(L.mean()),
                         "dof_iter_per_s": dof_it / makespan, "max_relres": float(max(relres.values())),
                         "mean_iters": float(np.mean(list(iters.values()))), "gpu_launches": launches})
+    return results
+
+
+def serving_workload(n_req, budget_gb, seed):
+    return (f"serving stream: {n_req} Poisson-arrival requests, hex20 cubes with edges uniform in 4..40, E "
+            f"log-uniform [10,1000], v uniform [0.2,0.35], fixed base, top pressure uniform [0.5,2.0], tol 1e-8, "
+            f"budget {budget_gb} GB, seed {seed}")
+
+
+def run_serving(args, rank, world, local, dist):
+    n_req = args.requests
+    results = serving_stream(n_req, [float(t) for t in args.rates.split(",")], args.budget_gb, args.chunk,
+                             args.serving_prec, args.seed, local)
     best = max(results, key=lambda r: r["dof_iter_per_s"])
     line = {"metric": METRIC, "value": best["dof_iter_per_s"], "unit": UNIT, "n_gpus": world,
             "steps": n_req, "warmup": 0, "ms_per_step": best["makespan_s"] * 1e3 / n_req,
@@ -527,63 +628,73 @@ def run_serving(args, rank, world, local, dist):
             "dtype": {32: "f32 storkm products + f64 residual replacement / f64 vectors",
                       16: "f16 storkm products + f64 residual replacement / f64 vectors",
                       64: "f64 storkm / f64 vectors"}[args.serving_prec], "data": "synthetic",
-            "config": {"workload": f"serving stream: {n_req} Poisson-arrival requests, hex20 cubes with edges "
-                                   f"uniform in 4..40, E log-uniform [10,1000], v uniform [0.2,0.35], fixed "
-                                   f"base, top pressure uniform [0.5,2.0], tol 1e-8, budget {args.budget_gb} GB, "
-                                   f"seed {args.seed}", "parallelism": "continuous batching"},
+            "config": {"workload": serving_workload(n_req, args.budget_gb, args.seed),
+                       "parallelism": "continuous batching"},
             "serving": results}
     if rank == 0:
         print(json.dumps(line))
     return 0
 
 
-def run_multirhs(args, rank, world, local, dist):
-    """60^3 cube, E=100, v=0.3, 16 load cases of i.i.d. N(0,1) vertical forces
-    on the top-face nodes (seeded): the block solve with tensor-core products
-    against 16 sequential FP64 solves, all to relres 1e-8."""
+def multirhs_solves(n, k, seed, local, limit, precs=(16, 32), sequential=True):
+    """n^3 cube, E=100, v=0.3, k load cases of i.i.d. N(0,1) vertical forces
+    on the top-face nodes (seeded): block solves (16 = tensor-core products,
+    32 = FP32 CUDA-core products) against k sequential FP64 solves, all to
+    relres 1e-8."""
     import parafem_gb300 as P
-    n = args.size if args.size != 100 else 60
     prob = P.cube_problem(n, n, n)
     s = P.Solver(local)
-    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
-    s.set_material(100.0, 0.3)
-    s.form_storkm(27)
-    neq = prob["neq"]
-    R = P.random_top_loads(prob["g_g"], n, n, neq, 16, args.seed)
-    out = {}
-    for prec, name in ((16, "block_tensor_cores"), (32, "block_fp32_cuda_cores")):
-        t0 = time.perf_counter()
-        X, it, rel = s.solve_multi(R, 1e-8, args.limit, prec)
-        st = s.stats_raw()
-        n_it = max(st[6], 1)
-        out[name] = {"wall_s": time.perf_counter() - t0, "device_s": st[2] / 1e3,
-                     "max_iters": int(it.max()), "mean_iters": float(it.mean()), "max_relres": float(rel.max()),
-                     "corrections": int(st[1]), "launched_iters": int(st[6]),
-                     "elem_ms_per_iter": st[3] / n_it, "scatter_ms_per_iter": st[4] / n_it,
-                     "iter_ms": st[5] / n_it}
-        if prec == 16:
-            Xtc = X
-    if not args.no_solves:
-        t0 = time.perf_counter()
-        errs, its = [], []
-        for j in range(16):
-            x64, it64, rel64 = s.solve(R[:, j], 1e-8, 50000, P.MODE_FP64_RES)
-            errs.append(float(np.linalg.norm(Xtc[:, j] - x64) / np.linalg.norm(x64)))
-            its.append(it64)
-        out["sequential_fp64"] = {"wall_s": time.perf_counter() - t0, "mean_iters": float(np.mean(its)),
-                                  "max_iters": int(max(its))}
-        out["block_vs_fp64_rel_err_2_max"] = max(errs)
-        out["speedup_block_tc_vs_sequential_fp64"] = (out["sequential_fp64"]["wall_s"] /
-                                                      out["block_tensor_cores"]["wall_s"])
-    s.close()
-    value = neq * 16 * out["block_tensor_cores"]["mean_iters"] / out["block_tensor_cores"]["device_s"]
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
-            "ms_per_step": out["block_tensor_cores"]["device_s"] * 1e3, "higher_is_better": True,
+    try:
+        s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+        s.set_material(100.0, 0.3)
+        s.form_storkm(27)
+        neq = prob["neq"]
+        R = P.random_top_loads(prob["g_g"], n, n, neq, k, seed)
+        out = {"workload": f"multi-RHS {n}^3 hex20 cube, E 100, v 0.3, {k} load cases N(0,1) on top-face nodes "
+                           f"(seed {seed}), nip 27, tol 1e-8", "neq": neq, "cases": k}
+        Xtc = None
+        for prec in precs:
+            name = {16: "block_tensor_cores", 32: "block_fp32_cuda_cores"}[prec]
+            t0 = time.perf_counter()
+            X, it, rel = s.solve_multi(R, 1e-8, limit, prec)
+            st = s.stats_raw()
+            n_it = max(st[6], 1)
+            out[name] = {"wall_s": time.perf_counter() - t0, "device_s": st[2] / 1e3,
+                         "max_iters": int(it.max()), "mean_iters": float(it.mean()),
+                         "max_relres": float(rel.max()), "corrections": int(st[1]), "launched_iters": int(st[6]),
+                         "elem_ms_per_iter": st[3] / n_it, "scatter_ms_per_iter": st[4] / n_it,
+                         "iter_ms": st[5] / n_it,
+                         "dof_iter_per_s": neq * k * float(it.mean()) / (st[2] / 1e3)}
+            if prec == precs[0]:
+                Xtc = X
+        if sequential:
+            t0 = time.perf_counter()
+            errs, its = [], []
+            for j in range(k):
+                x64, it64, rel64 = s.solve(R[:, j], 1e-8, 50000, P.MODE_FP64_RES)
+                errs.append(float(np.linalg.norm(Xtc[:, j] - x64) / np.linalg.norm(x64)))
+                its.append(it64)
+            out["sequential_fp64"] = {"wall_s": time.perf_counter() - t0, "mean_iters": float(np.mean(its)),
+                                      "max_iters": int(max(its))}
+            first = {16: "block_tensor_cores", 32: "block_fp32_cuda_cores"}[precs[0]]
+            out["block_vs_fp64_rel_err_2_max"] = max(errs)
+            out["speedup_block_vs_sequential_fp64"] = out["sequential_fp64"]["wall_s"] / out[first]["wall_s"]
+        return out
+    finally:
+        s.close()
+
+
+def run_multirhs(args, rank, world, local, dist):
+    """The 16-load-case cube (60^3 by default)."""
+    n = args.size if args.size != 100 else 60
+    out = multirhs_solves(n, 16, args.seed, local, args.limit, (16, 32), not args.no_solves)
+    tc = out["block_tensor_cores"]
+    line = {"metric": METRIC, "value": tc["dof_iter_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": tc["device_s"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "bf16x3 tensor-core products, f32 accumulation / f64 vectors and reductions",
             "data": "synthetic",
-            "config": {"workload": f"multi-RHS {n}^3 hex20 cube, E 100, v 0.3, 16 load cases N(0,1) on top-face "
-                                   f"nodes (seed {args.seed}), nip 27, tol 1e-8", "neq": neq, "cases": 16},
+            "config": {"workload": out["workload"], "neq": out["neq"], "cases": 16},
             "multirhs": out}
     if rank == 0:
         print(json.dumps(line))
@@ -740,42 +851,31 @@ def run_p122(args, rank, world, local, dist):
     return 0
 
 
+def gpu_config1(local):
+    """Config 1 on the GPU drop-in (PF_MODE_P121): 10^3, checon_par tol 1e-6."""
+    import parafem_gb300 as P
+    prob = P.cube_problem(10, 10, 10)
+    with P.Solver(local) as s:
+        s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
+        s.set_material(100.0, 0.3)
+        s.form_storkm(27)
+        s.solve(prob["r"], 1e-6, 5000, P.MODE_P121)          # warm-up
+        t1 = time.perf_counter()
+        x, it, _ = s.solve(prob["r"], 1e-6, 5000, P.MODE_P121)
+        return x, it, time.perf_counter() - t1
+
+
 def run_cube10(args, rank, world, local, dist):
     """The reference's CPU-runnable case: 10^3 cube, nip 27, E 100, v 0.3,
     fixed base, top pressure (total -1), checon_par tol 1e-6, limit 5000.
-    GPU drop-in (PF_MODE_P121) vs the C restatement of p121 on all host
-    cores, same inputs; parity of iterations and displacements."""
-    import parafem_gb300 as P
-    from oracle import oracle as O
-    prob = P.cube_problem(10, 10, 10)
-    s = P.Solver(local)
-    s.setup(prob["g_num"], prob["g_g"], prob["g_coord"], prob["nn"], prob["neq"])
-    s.set_material(100.0, 0.3)
-    t0 = time.perf_counter()
-    s.form_storkm(27)
-    t_form = time.perf_counter() - t0
-    s.solve(prob["r"], 1e-6, 5000, P.MODE_P121)          # warm-up
-    t1 = time.perf_counter()
-    x, it, rel = s.solve(prob["r"], 1e-6, 5000, P.MODE_P121)
-    t_gpu = time.perf_counter() - t1
-    s.close()
-    t2 = time.perf_counter()
-    km = O.form_storkm(prob["g_coord"], 27, 100.0, 0.3)
-    dg = O.diag(prob["g_g"], km, prob["neq"])
-    t3 = time.perf_counter()
-    it_ref, x_ref, _ = O.pcg(prob["g_g"], km, dg, prob["r"], 1e-6, 5000, 0)
-    t_cpu = time.perf_counter() - t3
-    neq = prob["neq"]
+    GPU drop-in (PF_MODE_P121) vs the CPU build of p121, same inputs."""
+    x, it, t_gpu = gpu_config1(local)
+    cfg = cpu_config1(x, it, t_gpu)
+    neq = cfg["neq"]
     line = {"metric": METRIC, "value": neq * it / t_gpu, "unit": UNIT, "n_gpus": world, "steps": it,
             "warmup": 1, "ms_per_step": 1e3 * t_gpu / it, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "p121 10^3 hex20 cube (the CPU-runnable case), nip 27, E 100, v 0.3, fixed "
-                                   "base, top pressure (total -1), checon_par tol 1e-6, limit 5000", "neq": neq},
-            "gpu": {"iters": it, "solve_wall_s": t_gpu, "storkm_formation_s": t_form},
-            "cpu_restatement": {"iters": it_ref, "solve_wall_s": t_cpu, "storkm_and_diag_s": t3 - t2,
-                                "cores": O.lib().orc_num_threads(), "dof_iter_per_s": neq * it_ref / t_cpu},
-            "parity": {"iters_equal": it == it_ref,
-                       "rel_err_2": float(np.linalg.norm(x - x_ref) / np.linalg.norm(x_ref))}}
+            "config": {"workload": cfg["workload"], "neq": neq}, "cube10": cfg}
     if rank == 0:
         print(json.dumps(line))
     return 0
