@@ -243,17 +243,25 @@ int pf_kernel_launches(void **ctx, long long *count);
  * (one load case per run); the shared-matrix products follow the idea of
  * xx9's batched MATMUL (src/programs/dev/xx9/mathsgpu.f90:479).          */
 
-/* k = 16 independent solves K x_j = r_j that share every element-matrix
- * read: r and xnew are (neq, k) column-major; iters and relres hold k
- * values (relres: FP64 true residual).  prec 16: block products on the
- * tensor cores (tcgen05, three-term BF16 splits, FP32 accumulation);
- * 32: the same products on CUDA cores in FP32.  FP64 vectors, dots and
- * alpha/beta; FP64 residual replacement as PF_MODE_MIXED. */
+/* k independent solves K x_j = r_j that share every element-matrix read
+ * (k a multiple of 8, 8..128): r and xnew are (neq, k) column-major; iters
+ * and relres hold k values (relres: FP64 true residual).  prec 16: block
+ * products on the tensor cores (tcgen05, K_e and P_e each split into two
+ * FP16 terms scaled by powers of two, FP32 accumulation; the cases taken
+ * in passes of up to 64, the pass width autotuned on the mesh); 32: the
+ * same products on CUDA cores in FP32.  FP64 vectors, dots and alpha/beta;
+ * FP64 residual replacement as PF_MODE_MIXED. */
 int pf_solve_multi(void **ctx, const int *k, const double *r, const double *tol, const int *limit,
                    const int *prec, double *xnew, int *iters, double *relres);
-/* Block product U = K P for k = 16 cases (equation order, (neq,k)
- * column-major); prec 16 (tensor cores), 32 (FP32 CUDA cores), 64 (FP64). */
+/* Block product U = K P for k cases (k a multiple of 8, 8..128; equation
+ * order, (neq,k) column-major); prec 16 (tensor cores), 32 (FP32 CUDA
+ * cores), 64 (FP64). */
 int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, const double *p, double *u);
+/* The tensor-core block product's autotuner: *kb = the pass width (cases
+ * per pass) chosen for the context's current k; cand[4] the widths timed
+ * (0 = unused) and ms[4] one full product with each (0 when only one width
+ * was possible). */
+int pf_multi_tuning(void **ctx, int *kb, int *cand, float *ms);
 /* Releases the context's block-solve buffers (allocated by the first
  * pf_solve_multi or pf_ebe_matvec_multi; also released with the mesh and by
  * pf_ctx_destroy). */

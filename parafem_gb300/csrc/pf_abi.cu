@@ -97,6 +97,7 @@ static void free_mesh(Ctx &c)
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
     dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.psplit); dfree(c.km16p);
     c.km16_ok = false;
+    c.mr_ok = false;
     c.shared = false;
     c.kind = KIND_SOLID20;
     dfree(c.ediag); dfree(c.diag); dfree(c.dinv); dfree(c.f); dfree(c.x); dfree(c.c); dfree(c.r);
@@ -621,6 +622,7 @@ static int ensure_storkm(Ctx &c)
     if (!c.km32 && dalloc(&c.km32, ne * 3600, "FP32 storkm")) return 1;
     if (!c.km32p && dalloc(&c.km32p, ne * 1832, "packed FP32 storkm")) return 1;
     c.km16_ok = false;   // repacked on the next FP16 use
+    c.mr_ok = false;     // and the tensor-core block records on the next block product
     c.shared = false;
     drop_graph(c);
     return 0;

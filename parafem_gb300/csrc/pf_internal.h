@@ -104,6 +104,7 @@ struct Ctx {
     unsigned h16_attr = 0;      // FP16 configurations whose shared-memory attribute is set
     float tune16_ms[3] = {0, 0, 0};
     MultiBufs *multi = nullptr; // block-solve vectors, allocated on the first block solve or product
+    bool mr_ok = false;         // multi->rec holds the tensor-core element records of the current storkm
     int sym_cfg = 0;            // autotuned configuration of the packed-symmetric kernel
     int sym_warps = 14, sym_stages = 2;
     unsigned long long sym_attr = 0;   // configurations whose shared-memory attribute is set

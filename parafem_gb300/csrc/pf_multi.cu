@@ -3,20 +3,24 @@
 // k independent Jacobi-PCG solves (p121.f90:86-104) share every element
 // matrix read: one iteration computes U = K P for a 60 x k block per element.
 // Vectors are interleaved per slot, v[slot*k + j], so the gather of an
-// element's block and the node scatter touch k consecutive values.
+// element's block and the node scatter touch k consecutive values.  k is
+// any multiple of 8 up to kMaxK.
 //
 // Element products:
-//   k_mr_elem_tc   tensor cores (tcgen05.mma, kind::f16, BF16 operands, FP32
-//                  accumulation in TMEM), operands from the packed-symmetric
-//                  FP32 storkm by bulk copy.  K_e and P_e are each split into
-//                  three BF16 terms (x = h1 + h2 + h3, about 24 significant
-//                  bits) and the six products of order <= 2^-16 are summed:
-//                  the block product reaches FP32 accuracy.  A two-term split
-//                  (about 16 bits) leaves too large a perturbation of K for
-//                  the inner PCG to converge on these meshes.
-//   k_mr_elem_cc   the same product on CUDA cores in FP32 (check and fallback
-//                  kernel for the tensor-core one, selectable by prec).
-//   k_mr_elem_64   FP64 (DFMA) block product for the true residual f - K x.
+//   k_mr_elem_h16  tensor cores (tcgen05.mma, kind::f16, FP16 operands, FP32
+//                  accumulation in TMEM).  K_e is split once, when storkm is
+//                  formed or set, into two FP16 terms (hi + lo, about 22
+//                  significant bits, scaled per element by a power of two)
+//                  stored in the tensor cores' shared-memory tile layout;
+//                  P_e less a translation of each case is split the same way
+//                  per element and case.  The three products of order
+//                  <= 2^-11 (hi.hi, hi.lo, lo.hi) are summed: the block
+//                  product reaches FP32-class accuracy.  Cases are taken in
+//                  passes of 64, 32, 16 or 8 (the MMA's N is twice that),
+//                  the widest pass chosen by timing on the mesh.
+//   k_mr_elem_cc   the same product on CUDA cores in FP32 (check kernel for
+//                  the tensor-core one, selectable by prec) and in FP64
+//                  (DFMA) for the true residual f - K x.
 // The inner PCG runs on the FP32-class product with FP64 vectors, dots and
 // alpha/beta; the recursive residuals are replaced by the FP64 true residual
 // whenever an active load case has dropped 10x (as PF_MODE_MIXED does).
@@ -25,6 +29,8 @@
 #include "pfgpu.h"
 
 #include <cstring>
+#include <cuda.h>   // CUtensorMap (the encoder is reached through the runtime's driver entry point)
+#include <cuda_fp16.h>
 #include <vector>
 
 namespace pf {
@@ -33,139 +39,273 @@ using namespace tc;
 
 namespace {
 
-constexpr int KR = 16;               // load cases per block (the kernels are written for 16)
+constexpr int kMaxK = 128;           // load cases of one block solve
+constexpr int kMaxKB = 64;           // cases of one tensor-core pass (the MMA's N)
 constexpr unsigned kFullMask = 0xffffffffu;
 
-// Tile geometry (BF16, K-major, no swizzle; 8-row x 16-byte core matrices,
-// LBO = 128 B between core matrices adjacent in K, SBO = 1024 B between
-// 8-row groups).  A term holds 96 rows: for direction d, rows 32d + i
-// (i < 20) are K_e's rows 3i + d, row 32d + 20 is the sum of those rows, rows
-// 32d + 21..31 stay zero.  The MMA reads M = 128 rows, so rows 96..127 of a
-// term are the next 4 KB of shared memory: they only feed accumulator rows
-// 96..127, which nobody reads.
-constexpr int kRowsA = 96;
-constexpr int kTermA = kRowsA * 64 * 2;      // 12288
-constexpr int kBufA = 3 * kTermA + 4096;     // 3 terms + the 4 KB read as rows 96..127 of the last
-constexpr int kTermB = 16 * 64 * 2;          // 2048: 16 load cases x 64 K
-constexpr int kBufB = 3 * kTermB;
-constexpr int kStK = 7328;                   // packed-symmetric FP32 K_e (1830 + 2 pad floats)
-constexpr int kStP = 20 * 3 * KR * 8;        // P of the 20 nodes: 20 x 384 B
-constexpr int kStC = 3 * 64 * 4;             // direction sums of K_e's rows (3 x 64 FP32)
-constexpr int kStage = kStK + kStP + kStC;   // 15776 B, a multiple of 16
-constexpr int kNst = 4;                      // operand stages (bulk copies in flight)
-constexpr int kNTile = 3;                    // BF16 tile sets (A + B)
-constexpr int kNAcc = 4;                     // TMEM accumulators (16 columns each)
-constexpr int kBuildWarps = 16;              // warps 0-15 split K_e and P_e
-constexpr int kGroups = 2;                   // builder groups: warps 8g..8g+7 build the elements t = g mod 2
-constexpr int kGroupWarps = kBuildWarps / kGroups;
-constexpr int kBWarps = 4;                   // warps 8g..8g+3 also split P_e (one B task per thread)
-constexpr int kEpiWarp0 = 16;                // warps 16-18 read TMEM lanes 32d..32d+31 back (direction d)
-constexpr int kNEpi = 3;
-constexpr int kProdWarp = 19;                // warp 19 issues the bulk copies
-constexpr int kMmaWarp = 20;                 // warp 20, lane 0 issues the MMAs
-constexpr int kTcThreads = 21 * 32;
-static_assert(kGroupWarps * 32 * 2 >= 63 * 8, "two A tasks (row, 8 K-values) per builder thread");
-static_assert(kBWarps * 32 == KR * 8, "one B task (load case, 8 dofs) per thread of a group's first four warps");
-constexpr int kOffB = kNTile * kBufA;
-constexpr int kOffSt = kOffB + kNTile * kBufB;
-constexpr int kOffAux = kOffSt + kNst * kStage;
-constexpr int kOffSum = kOffAux + 256;       // [group][2][8][KR][3] partial direction sums of P_e
-constexpr int kTcSmem = kOffSum + kGroups * 2 * 8 * KR * 3 * 4;
-constexpr uint32_t kIdesc = idesc_bf16(128, 16);
-static_assert(kOffSt % 16 == 0 && kStage % 16 == 0 && kOffAux % 8 == 0, "bulk-copy alignment");
-static_assert(kTcSmem <= 227 * 1024, "shared memory per CTA");
-static_assert(kEpiWarp0 % 4 == 0, "epilogue warp kEpiWarp0 + d must reach TMEM lanes 32d..32d+31");
+// ---- the stored element record of the tensor-core product -----------------
+// A tile (M = 64 rows, K = 64 columns, FP16, K-major, no swizzle): 8 x 8 core
+// matrices of 8 rows x 16 bytes, core matrix (I, J) at 1024 I + 128 J
+// (SBO = 1024 B between row groups, LBO = 128 B between column groups).
+// Rows and columns are ordered by direction: row (column) 20 d + i is dof
+// 3 i + d of the element, i < 20; rows 60 + d hold the direction sums of the
+// stored rows (sum over i of row 3 i + d, for the mean translation of the
+// result); row 63 and columns 60..63 are zero.  K_e is symmetric, so of
+// each term the record keeps the core matrices (I, J) with I <= J, and all
+// of block row 7 (which carries the sum rows): 43 core matrices, the
+// blocks of a block row contiguous, in block-row order.  Then the second
+// term, then 1 / s_e (FP32) and 12 zero bytes: 11,024 bytes per element.
+constexpr int kTileA = 8192;                  // one term of the A tile
+constexpr int kRecTerm = 43 * 128;            // 5504
+constexpr int kRecBytes = 2 * kRecTerm + 16;  // 11024
+
+// stored index of core matrix (I, J) of a term (I <= J, or I == 7)
+__host__ __device__ constexpr int rec_block(int I, int J) { return I < 7 ? 8 * I - I * (I - 1) / 2 + (J - I) : 35 + J; }
+
+// dof of the element for direction-ordered row or column r < 60
+__host__ __device__ constexpr int dir_dof(int r) { return 3 * (r % 20) + r / 20; }
+
+// ---- pipeline of the tensor-core kernel ------------------------------------
+constexpr int kNTile = 4;            // tile sets (A and B operands, output scales)
+constexpr int kNAcc = 4;             // TMEM accumulators (128 columns each)
+constexpr int kAccCols = 128;
+constexpr int kEpiGroups = 2;        // warps 0-7: two epilogue groups of four warps on alternate elements;
+constexpr int kEpiWarps = 4;         //   warp w reads TMEM lanes 32 (w % 4) .. +15 = rows 16 (w % 4) .. +15
+constexpr int kBldWarp0 = 8;         // warps 8-15: two builder groups of four warps on alternate elements
+constexpr int kBldGroups = 2;
+constexpr int kBldWarps = 4;
+constexpr int kProdWarp = 16;        // warp 16 issues the copies
+constexpr int kMmaWarp = 17;         // warp 17, lane 0 issues the MMAs
+constexpr int kH16Threads = 18 * 32;
+constexpr int kPlaceMoves = 6;       // record rows (16 B) a builder thread places per element: 2 x 43 x 8 / 128
+constexpr int kNodeGroups = 16;      // most node groups of a builder's per-case maxima (128 / kb, kb >= 8)
+constexpr int kRecStage = 11136;     // the record's place in a stage (11,024 bytes, rounded up to 128)
+
+// shared-memory plan for kb cases per pass and nst operand stages
+struct Plan {
+    int kb, nst;
+    int stage;     // bytes of one stage: the element record, then P of the 20 nodes
+    int tile;      // bytes of one tile set: A (2 terms), B (2 terms), the per-case output scales
+    int off_tile, off_aux, smem;
+};
+
+__host__ __device__ inline Plan make_plan(int kb, int nst)
+{
+    Plan p;
+    p.kb = kb;
+    p.nst = nst;
+    p.stage = kRecStage + 480 * kb;
+    p.tile = 2 * kTileA + 256 * kb + 256;
+    p.off_tile = nst * p.stage;
+    p.off_aux = p.off_tile + kNTile * p.tile;
+    // aux: mbarriers (64 words), tmem slot + flags (64 B), per builder
+    // group the translations (3 x 64 floats), scales (64) and per-case
+    // partial maxima (16 x 64), per epilogue group two sets of sum rows
+    // (2 x 3 x 64)
+    p.smem = p.off_aux + 64 * 8 + 64 + kBldGroups * (4 + kNodeGroups) * kMaxKB * 4 +
+             kEpiGroups * 6 * kMaxKB * 4;
+    return p;
+}
 
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
+__device__ __forceinline__ void named_sync(int id, int n)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory");
+}
+
+// (a, b) = hi + lo in FP16, both rounded to nearest even: the words of the
+// two terms, (a_hi, b_hi) and (a_lo, b_lo), a in the low half-word.
+__device__ __forceinline__ void split2_f16(float a, float b, uint32_t &w_hi, uint32_t &w_lo)
+{
+    const __half ha = __float2half_rn(a), hb = __float2half_rn(b);
+    const float ra = a - __half2float(ha), rb = b - __half2float(hb);
+    w_hi = (uint32_t)__half_as_ushort(ha) | ((uint32_t)__half_as_ushort(hb) << 16);
+    w_lo = cvt_f16x2(ra, rb);
+}
+
 }  // namespace
 
-// Block element products on the tensor cores: ut[e][i][j] = sum_c K_e(i,c) P(slot(c), j).
-//
-// The product is P K_e P P_e, P removing each load case's mean translation
-// over the element's 20 nodes (an identity in exact arithmetic, since K_e
-// annihilates rigid translations; in FP32-class arithmetic it keeps the
-// rounding away from the smooth part of P, as the single-case kernels do).
-//
-// One persistent CTA of 21 warps per SM walks the elements e = blockIdx.x +
-// t * gridDim.x with warp-specialised roles linked by mbarriers:
-//   warp 19      bulk copies (cp.async.bulk) of the packed symmetric storkm of
-//                K_e (7,328 B), of the 16-case P blocks of the element's
-//                20 nodes (384 B each, contiguous in the interleaved vector)
-//                and of the direction sums of K_e's rows (768 B) into a ring
-//                of kNst stages;
-//   warps 0-15   split K_e (rows by direction, with the row sums) and P_e
-//                less its mean translations into three BF16 terms each and
-//                write them into a ring of kNTile tile sets.  Two groups of
-//                eight warps take alternate elements; a thread has two
-//                8-value row segments of K_e (shared-memory offsets computed
-//                once), and a group's warps 0-3 also one 8-dof segment of
-//                P_e each, exchanging partial sums through shared memory;
-//   warp 20      one thread issues the six products of order <= 2^-16
-//                (24 MMAs, M=128, N=16, K=16) into a ring of kNAcc TMEM
-//                accumulators and commits them to mbarriers that free the
-//                tile set and fill the accumulator;
-//   warps 16-18  read the accumulators back (TMEM lanes 32d..32d+20,
-//                direction d), subtract the mean of the direction's rows and
-//                store the 60 x 16 results.
-// Every wait is bounded.  A wait that runs out sets a shared failure flag
-// that every role checks before its next wait, writes 3 to the device error
-// word, and the CTA waits (bounded) for the copies and MMAs it has in flight
-// before it frees its TMEM and returns.
-__global__ void __launch_bounds__(kTcThreads, 1)
-k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ ksum, const int *__restrict__ conn,
-             const double *__restrict__ P, float *__restrict__ ut, int *__restrict__ err,
-             const int *__restrict__ skip)
+// ---------------------------------------------------------------------------
+// Set-up: the element records of the tensor-core product from FP64 storkm.
+// One 128-thread block per element (grid-stride): s_e = 2^(14 - E) with
+// max |K_e| (and max |direction sum|) < 2^E, the two FP16 terms of every
+// scaled entry, the direction sums of the stored (rounded) rows formed in
+// FP64 from hi + lo and split in turn, then the 43 core matrices of each
+// term.
+__global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restrict__ km, unsigned char *__restrict__ rec)
 {
+    __shared__ uint32_t t2[64 * 64];   // (hi, lo) half pairs of the 64 x 64 tile, row-major
+    __shared__ double red[4];
+    const int tid = threadIdx.x;
+    for (int e = blockIdx.x; e < nels; e += gridDim.x) {
+        const double *ke = km + (size_t)e * 3600;
+        double mx = 0.0;
+        for (int q = tid; q < 3600; q += 128) mx = fmax(mx, fabs(ke[q]));
+        for (int q = tid; q < 3 * 60; q += 128) {   // the direction sums must fit FP16 too
+            const int d = q / 60, c = q % 60;
+            double sum = 0.0;
+            for (int i = 0; i < 20; ++i) sum += ke[60 * dir_dof(c) + 3 * i + d];
+            mx = fmax(mx, fabs(sum));
+        }
+        mx = warp_max(mx);
+        if ((tid & 31) == 0) red[tid >> 5] = mx;
+        __syncthreads();
+        mx = fmax(fmax(red[0], red[1]), fmax(red[2], red[3]));
+        int ex = 0;
+        frexp(mx, &ex);                              // mx < 2^ex
+        const double sc = mx > 0.0 ? ldexp(1.0, 14 - ex) : 1.0;
+        for (int q = tid; q < 64 * 64; q += 128) {
+            const int r = q / 64, c = q % 64;
+            float x = 0.f;
+            if (r < 60 && c < 60) x = (float)(ke[60 * dir_dof(c) + dir_dof(r)] * sc);
+            uint32_t wh, wl;
+            split2_f16(x, 0.f, wh, wl);
+            t2[q] = (wh & 0xffffu) | (wl << 16);
+        }
+        __syncthreads();
+        // rows 60..62: sums over i of the stored rows 20 d + i
+        for (int q = tid; q < 3 * 60; q += 128) {
+            const int d = q / 60, c = q % 60;
+            double s = 0.0;
+            for (int i = 0; i < 20; ++i) {
+                const uint32_t w = t2[(20 * d + i) * 64 + c];
+                s += (double)__half2float(__ushort_as_half((unsigned short)(w & 0xffffu))) +
+                     (double)__half2float(__ushort_as_half((unsigned short)(w >> 16)));
+            }
+            uint32_t wh, wl;
+            split2_f16((float)s, 0.f, wh, wl);
+            t2[(60 + d) * 64 + c] = (wh & 0xffffu) | (wl << 16);
+        }
+        __syncthreads();
+        // 2 terms x 43 core matrices x 8 rows of 16 bytes
+        unsigned char *out = rec + (size_t)e * kRecBytes;
+        for (int q = tid; q < 2 * 43 * 8; q += 128) {
+            const int term = q / (43 * 8), rem = q % (43 * 8), blk = rem / 8, rr = rem % 8;
+            int I, J;
+            if (blk >= 35) {
+                I = 7;
+                J = blk - 35;
+            } else {
+                I = 0;
+                while (I < 6 && rec_block(I + 1, I + 1) <= blk) ++I;
+                J = I + (blk - rec_block(I, I));
+            }
+            const int row = 8 * I + rr;
+            uint32_t w[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) {
+                const uint32_t a = t2[row * 64 + 8 * J + 2 * g], b = t2[row * 64 + 8 * J + 2 * g + 1];
+                w[g] = term == 0 ? ((a & 0xffffu) | (b << 16)) : ((a >> 16) | (b & 0xffff0000u));
+            }
+            *reinterpret_cast<uint4 *>(out + term * kRecTerm + blk * 128 + rr * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+        if (tid == 0) {
+            float *tail = reinterpret_cast<float *>(out + 2 * kRecTerm);
+            tail[0] = (float)(1.0 / sc);
+            tail[1] = tail[2] = tail[3] = 0.f;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block element products on the tensor cores, cases c0 .. c0+KB-1 of k:
+// ut[e][i][c0 + j] = (P K_e (P_e - t_j))(i, j), t_j a translation of case j
+// and P removing each case's mean translation from the result over the
+// element's 20 nodes (identities in exact arithmetic, since K_e annihilates
+// rigid translations; with rounded operands they keep the rounding away
+// from the smooth part of P and the product symmetric, as the single-case
+// kernels do).
+//
+// One persistent CTA of 18 warps per SM walks the elements e = blockIdx.x +
+// t * gridDim.x with warp-specialised roles linked by mbarriers:
+//   warp 16     fills a ring of nst stages: the element record by one bulk
+//               copy (cp.async.bulk), and the P rows of the element's 20
+//               nodes (FP32 high and low parts, kept beside P by the update
+//               kernels) by TMA gathers of four rows each (one row per node
+//               when a pass covers all k cases, else one per node and
+//               direction), counted on the same mbarrier;
+//   warps 8-15  two groups of four warps on alternate elements: place the
+//               record's core matrices in a tile set's A tile, fill its
+//               lower core matrices (I > J, I < 7) as transposes of the
+//               stored ones (ldmatrix.trans + stmatrix), free the stage
+//               once P is read, and build the B tile: per case j a
+//               translation t_j (node 0's value) and a power-of-two scale
+//               s_j, then (P_e - t_j) s_j split into two FP16 terms, the
+//               high term's KB rows followed by the low term's;
+//   warp 17     one thread issues the products into a ring of kNAcc TMEM
+//               accumulators: A_hi x [B_hi | B_lo] (N = 2 KB) and A_lo x B_hi
+//               into the first KB columns, four K-steps each, and commits
+//               them to the accumulator's mbarrier;
+//   warps 0-7   two groups of four warps on alternate elements read the
+//               accumulator rows back (warp w: rows 16 (w % 4) .. +15 in TMEM
+//               lanes 32 (w % 4) .. +15), add its two halves, subtract a
+//               twentieth of the direction's sum row, undo the scales and
+//               store.
+// Every wait is bounded; where a group of warps meets at a named barrier,
+// one thread waits and the group follows its verdict.  A wait that runs out
+// sets a shared failure flag that every role checks before its next wait,
+// writes 3 to the device error word, and the CTA waits (bounded) for the
+// copies and MMAs it has in flight before it frees its TMEM and returns.
+// tmap: P as 2-D FP64-sized elements, rows of one node (3 KB elements, box
+// 3 KB x 1) when whole != 0, else rows of one slot (k elements, box KB x 1,
+// gathered from column c0).
+template <int KB>
+__global__ void __launch_bounds__(kH16Threads, 1)
+k_mr_elem_h16(int nels, int k, int c0, int nst, const unsigned char *__restrict__ rec,
+              const int *__restrict__ conn, const __grid_constant__ CUtensorMap tmap, int whole,
+              float *__restrict__ ut, int *__restrict__ err, const int *__restrict__ skip)
+{
+    constexpr int kb = KB;
     if (skip && *skip) return;   // a residual replacement is pending: nothing to compute
     extern __shared__ __align__(1024) unsigned char sm[];
-    unsigned char *A = sm;
-    unsigned char *B = sm + kOffB;
-    unsigned char *stg = sm + kOffSt;
-    uint64_t *st_full = reinterpret_cast<uint64_t *>(sm + kOffAux);
-    uint64_t *st_empty = st_full + kNst;
-    uint64_t *tl_full = st_empty + kNst;
-    uint64_t *tl_empty = tl_full + kNTile;
-    uint64_t *ac_full = tl_empty + kNTile;
-    uint64_t *ac_empty = ac_full + kNAcc;
-    uint64_t *sum_bar = ac_empty + kNAcc;   // [group]: its four B warps' partial sums of an element are written
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sum_bar + kGroups);
-    float *psum = reinterpret_cast<float *>(sm + kOffSum);   // [group][k & 1][chunk][case][direction]
+    const Plan pl = make_plan(kb, nst);
+    unsigned char *stg = sm;
+    unsigned char *tiles = sm + pl.off_tile;
+    uint64_t *st_full = reinterpret_cast<uint64_t *>(sm + pl.off_aux);
+    uint64_t *st_empty = st_full + 8;
+    uint64_t *tl_full = st_empty + 8;
+    uint64_t *tl_empty = tl_full + 8;
+    uint64_t *ac_full = tl_empty + 8;
+    uint64_t *ac_empty = ac_full + 8;
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + pl.off_aux + 64 * 8);
     volatile int *s_fail = reinterpret_cast<volatile int *>(tslot + 1);
-    int *s_count = reinterpret_cast<int *>(tslot + 2);   // [0] copies issued, [1] MMA groups committed
+    int *s_count = reinterpret_cast<int *>(tslot + 2);          // [0] elements copied, [1] elements committed
+    volatile int *g_ok = reinterpret_cast<volatile int *>(tslot + 4);   // [role group][element parity]: waits passed
+    float *b_aux = reinterpret_cast<float *>(sm + pl.off_aux + 64 * 8 + 64);   // per builder group, below
+    float *e_aux = b_aux + kBldGroups * (4 + kNodeGroups) * kMaxKB;            // [epi group][parity][d][j]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nmine = blockIdx.x < nels ? (nels - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto elem = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
 
-    for (int i = tid; i < kOffSt / 16; i += kTcThreads) reinterpret_cast<uint4 *>(sm)[i] = make_uint4(0, 0, 0, 0);
-    if (warp == 0) tmem_alloc(tslot, 64);
+    if (warp == 0) tmem_alloc(tslot, kNAcc * kAccCols);
     if (tid == 0) {
-        for (int i = 0; i < kNst; ++i) {
-            mbar_init(&st_full[i], 1);
-            mbar_init(&st_empty[i], kGroupWarps);
+        for (int i = 0; i < nst; ++i) {
+            mbar_init(&st_full[i], 1);            // the producer's arrival (with the bytes it expects)
+            mbar_init(&st_empty[i], kBldWarps);   // the four warps of the group that read the stage
         }
         for (int i = 0; i < kNTile; ++i) {
-            mbar_init(&tl_full[i], kGroupWarps);
-            mbar_init(&tl_empty[i], 1);
+            mbar_init(&tl_full[i], kBldWarps);    // the four warps of the group that builds the tile
+            mbar_init(&tl_empty[i], kEpiWarps);   // the four epilogue warps that read its scales
         }
         for (int i = 0; i < kNAcc; ++i) {
             mbar_init(&ac_full[i], 1);
-            mbar_init(&ac_empty[i], kNEpi);
+            mbar_init(&ac_empty[i], kEpiWarps);
         }
-        for (int g = 0; g < kGroups; ++g) mbar_init(&sum_bar[g], kBWarps);
         mbar_fence_init();
         *s_fail = 0;
         s_count[0] = s_count[1] = 0;
+        for (int i = 0; i < 8; ++i) g_ok[i] = 0;
     }
     fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    // bounded wait that also gives up at once when another role has failed
     auto wait = [&](uint64_t *bar, uint32_t parity) {
         if (*s_fail) return false;
         if (mbar_wait(bar, parity)) return true;
@@ -174,124 +314,180 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
     };
 
     if (warp == kProdWarp) {
-        // the connectivity (lane a: node a of the element) is loaded kCD
-        // elements ahead, so its latency is not paid once per element
-        constexpr int kCD = 8;
+        constexpr int kCD = 8;   // connectivity loaded kCD elements ahead
         int ndr[kCD];
 #pragma unroll
         for (int j = 0; j < kCD; ++j) ndr[j] = (lane < 20 && j < nmine) ? conn[(size_t)elem(j) * 20 + lane] : 0;
-        int issued = 0;   // elements whose copies are in flight or done
+        // gathers per element and their rows: whole, lane g < 5 takes nodes
+        // 4g..4g+3; else lane g < 15 takes the node-direction rows r = 4g..4g+3
+        // (node r / 3, direction r % 3)
+        const int ngat = whole ? 5 : 15;
+        const int rowbytes = whole ? 24 * kb : 8 * kb;
+        const uint32_t pbytes = 480 * kb;
+        int issued = 0;
         bool stop = false;
         for (int t0 = 0; t0 < nmine && !stop; t0 += kCD) {
 #pragma unroll
             for (int j = 0; j < kCD; ++j) {
                 const int t = t0 + j;
                 if (t >= nmine) break;
-                const int s = t % kNst;
-                if (t >= kNst && !wait(&st_empty[s], (uint32_t)((t / kNst - 1) & 1))) {
+                const int s = t % nst;
+                int ok = 1;
+                if (t >= nst && lane == 0) ok = wait(&st_empty[s], (uint32_t)((t / nst - 1) & 1)) ? 1 : 0;
+                if (!__shfl_sync(kFullMask, ok, 0)) {
                     stop = true;
                     break;
                 }
-                unsigned char *dst = stg + s * kStage;
-                if (lane == 0) mbar_expect_tx(&st_full[s], kStage);
+                unsigned char *dst = stg + (size_t)s * pl.stage;
+                int rows[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 4 * (lane < ngat ? lane : 0) + i;
+                    const int node = __shfl_sync(kFullMask, ndr[j], whole ? r : r / 3);
+                    rows[i] = whole ? node : 3 * node + r % 3;
+                }
+                if (lane == 0) mbar_expect_tx(&st_full[s], kRecBytes + pbytes);
                 __syncwarp();
-                if (lane == 0) bulk_g2s(dst, kp + (size_t)elem(t) * 1832, kStK, &st_full[s]);
-                if (lane < 20) bulk_g2s(dst + kStK + lane * 384, P + (size_t)3 * ndr[j] * KR, 384, &st_full[s]);
-                if (lane == 20) bulk_g2s(dst + kStK + kStP, ksum + (size_t)elem(t) * 192, kStC, &st_full[s]);
+                if (lane == 0) bulk_g2s(dst, rec + (size_t)elem(t) * kRecBytes, kRecBytes, &st_full[s]);
+                if (lane < ngat)
+                    tma_gather4(dst + kRecStage + lane * 4 * rowbytes, &tmap, whole ? 0 : c0, rows[0], rows[1],
+                                rows[2], rows[3], &st_full[s]);
                 ndr[j] = (lane < 20 && t + kCD < nmine) ? conn[(size_t)elem(t + kCD) * 20 + lane] : 0;
                 issued = t + 1;
             }
         }
         if (lane == 0) s_count[0] = issued;
-    } else if (warp < kBuildWarps) {
-        // Two groups of eight warps build alternate elements, so two
-        // elements are in the build stage at once.  A thread of a group has
-        // two A tasks (of 504): A row 32d + i, K-values 8q..8q+7.  i < 20:
-        // K(3i + d, k) at packed_off; i = 20: the sum of direction d's rows,
-        // after the P blocks in the stage; K-values past 59 read the zero
-        // pad at 1830.
-        const int grp = warp / kGroupWarps, gw = warp % kGroupWarps, gtid = tid % (kGroupWarps * 32);
-        int off[2][8];
-        uint32_t a_off[2];
-        bool a_task[2];
+    } else if (warp >= kBldWarp0 && warp < kBldWarp0 + kBldGroups * kBldWarps) {
+        // group grp builds the elements t = grp, grp + 2, ...; its 128 threads
+        // synchronise on named barrier 1 + grp
+        const int grp = (warp - kBldWarp0) / kBldWarps, bw = (warp - kBldWarp0) % kBldWarps;
+        const int bt = tid - (kBldWarp0 + grp * kBldWarps) * 32;   // thread of the group (0..127)
+        float *tt = b_aux + grp * (4 + kNodeGroups) * kMaxKB;      // [d][j] translation of case j
+        float *sc = tt + 3 * kMaxKB;                                // [j] scale s_j
+        float *pm = sc + kMaxKB;                                    // [node group][j] partial maxima
+        constexpr int ngr = 128 / kb;                               // node groups
+        const int mj = bt % kb, mg = bt / kb;                       // this thread's case and node group
+        const int bar_id = 1 + grp;
+        // the same for every element: this thread's record rows (16 B) and
+        // their places in the A tile, and this lane's transposed core-matrix rows
+        int pl_src[kPlaceMoves], pl_dst[kPlaceMoves];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int task = gtid + h * kGroupWarps * 32;
-            a_task[h] = task < 63 * 8;
-            const int r63 = task % 63, q = task / 63;
-            const int d = r63 / 21, i = r63 % 21;
-#pragma unroll
-            for (int g = 0; g < 8; ++g) {
-                const int k = 8 * q + g;
-                off[h][g] = (!a_task[h] || k >= 60) ? 1830
-                            : i < 20                ? packed_off(3 * i + d, k)
-                                                    : (kStK + kStP) / 4 + 64 * d + k;
+        for (int u = 0; u < kPlaceMoves; ++u) {
+            const int x = bt + 128 * u;
+            pl_src[u] = -1;
+            pl_dst[u] = 0;
+            if (x < 2 * 43 * 8) {
+                const int term = x / (43 * 8), rem = x % (43 * 8), blk = rem / 8, rr = rem % 8;
+                int I = 0, J;
+                if (blk >= 35) {
+                    I = 7;
+                    J = blk - 35;
+                } else {
+                    while (I < 6 && rec_block(I + 1, I + 1) <= blk) ++I;
+                    J = I + (blk - rec_block(I, I));
+                }
+                pl_src[u] = term * kRecTerm + blk * 128 + rr * 16;
+                pl_dst[u] = term * kTileA + I * 1024 + J * 128 + rr * 16;
             }
-            a_off[h] = a_task[h] ? kmajor_off(32 * d + i, 8 * q) : 0u;
         }
-        // B task (the group's warps 0-3): load case j, dofs 8qb..8qb+7 (dof c
-        // has direction (rb + c - 8qb) % 3)
-        const int j = gtid & (KR - 1), qb = gtid >> 4;
-        const int rb = (2 * qb) % 3;
-        const bool b_task = gw < kBWarps;
-        uint64_t *my_sum = &sum_bar[grp];
-        for (int t = grp; t < nmine; t += kGroups) {
-            const int s = t % kNst, b = t % kNTile, kk = t / kGroups;
-            if (!wait(&st_full[s], (uint32_t)((t / kNst) & 1))) break;
-            if (t >= kNTile && !wait(&tl_empty[b], (uint32_t)((t / kNTile - 1) & 1))) break;
-            const float *U = reinterpret_cast<const float *>(stg + s * kStage);
-            const double *Pe = reinterpret_cast<const double *>(stg + s * kStage + kStK);
-            unsigned char *Ab = A + b * kBufA, *Bb = B + b * kBufB;
-            float *ps = psum + (grp * 2 + (kk & 1)) * (8 * KR * 3);
-            float hi[8], lo[8];
-            if (b_task) {
-                // P_e(c, j) at c*16 + j: FP32 high and low parts, and this
-                // segment's sums by direction for the case's mean translation
+        int tr_src[3], tr_dst[3];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) {
-                    const int c = 8 * qb + g;
-                    split_f64(c < 60 ? Pe[c * KR + j] : 0.0, hi[g], lo[g]);
+        for (int u = 0; u < 3; ++u) {
+            const int g = bw + kBldWarps * u;   // groups of four matrices: 11 over the four warps
+            int m = 4 * g + (lane >> 3);
+            if (m > 41) m = 41;
+            const int term = m / 21, r = m % 21;
+            int I = 1;
+            while (I < 6 && (I + 1) * I / 2 <= r) ++I;   // blocks before row I: I (I - 1) / 2
+            const int J = r - I * (I - 1) / 2;
+            tr_src[u] = g < 11 ? term * kRecTerm + rec_block(J, I) * 128 + (lane & 7) * 16 : -1;
+            tr_dst[u] = term * kTileA + I * 1024 + J * 128 + (lane & 7) * 16;
+        }
+        for (int t = grp; t < nmine; t += kBldGroups) {
+            const int s = t % nst, b = t % kNTile, kk = t / kBldGroups;
+            // one thread waits for the stage and the tile; the group follows its verdict
+            if (bt == 0)
+                g_ok[2 * grp + (kk & 1)] = wait(&st_full[s], (uint32_t)((t / nst) & 1)) &&
+                                           (t < kNTile || wait(&tl_empty[b], (uint32_t)((t / kNTile - 1) & 1)));
+            named_sync(bar_id, kBldWarps * 32);
+            if (!g_ok[2 * grp + (kk & 1)]) break;
+            const unsigned char *R = stg + (size_t)s * pl.stage;                        // the record
+            const float2 *Pe = reinterpret_cast<const float2 *>(R + kRecStage);        // [node][d][j]: hi, lo
+            const float inv_se = *reinterpret_cast<const float *>(R + 2 * kRecTerm);
+            unsigned char *A = tiles + (size_t)b * pl.tile;
+            unsigned char *B = A + 2 * kTileA;
+            float *oscale = reinterpret_cast<float *>(B + 256 * kb);   // per case: 1 / (s_e s_j)
+            // the record's 2 x 43 core matrices to their places in the A tile
+#pragma unroll
+            for (int u = 0; u < kPlaceMoves; ++u)
+                if (pl_src[u] >= 0)
+                    *reinterpret_cast<uint4 *>(A + pl_dst[u]) = *reinterpret_cast<const uint4 *>(R + pl_src[u]);
+            // lower core matrices: 42 = 2 terms x 21 blocks (I, J), 1 <= I <= 6, J < I, transposed
+            // from the record's (J, I), four per ldmatrix/stmatrix pair (the last group repeats its
+            // final matrix)
+#pragma unroll
+            for (int u = 0; u < 3; ++u)
+                if (tr_src[u] >= 0) {   // uniform over the warp
+                    uint32_t v[4];
+                    ldsm_x4_trans(smem_u32(R + tr_src[u]), v);
+                    stsm_x4(smem_u32(A + tr_dst[u]), v);
                 }
-                const float u0 = hi[0] + hi[3] + hi[6], u1 = hi[1] + hi[4] + hi[7], u2 = hi[2] + hi[5];
-                ps[(qb * KR + j) * 3 + 0] = rb == 0 ? u0 : rb == 1 ? u2 : u1;
-                ps[(qb * KR + j) * 3 + 1] = rb == 0 ? u1 : rb == 1 ? u0 : u2;
-                ps[(qb * KR + j) * 3 + 2] = rb == 0 ? u2 : rb == 1 ? u1 : u0;
-                __syncwarp();
-                if (lane == 0) mbar_arrive(my_sum);
+            // per case j: the translation t_j (node 0's value: any translation
+            // serves) and the largest |p - t_j| over this thread's nodes
+            if (mg < ngr) {
+                float t3[3], mx = 0.f;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) t3[d] = Pe[d * kb + mj].x;
+                for (int a = mg; a < 20; a += ngr)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        const float2 v = Pe[(a * 3 + d) * kb + mj];
+                        mx = fmaxf(mx, fabsf((v.x - t3[d]) + v.y));
+                    }
+                pm[mg * kMaxKB + mj] = mx;
+                if (mg == 0)
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) tt[d * kMaxKB + mj] = t3[d];
             }
+            named_sync(bar_id, kBldWarps * 32);
+            // s_j = 2^(14 - E) with max |p - t_j| < 2^E
+            if (bt < kb) {
+                float mx = 0.f;
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                if (a_task[h]) {
-                    float xv[8];
-#pragma unroll
-                    for (int g = 0; g < 8; ++g) xv[g] = U[off[h][g]];
-                    split3_store8(xv, Ab + a_off[h], kTermA);
-                }
+                for (int g = 0; g < ngr; ++g) mx = fmaxf(mx, pm[g * kMaxKB + bt]);
+                int ex = 0;
+                frexpf(mx, &ex);
+                const float sj = mx > 0.f ? ldexpf(1.f, 14 - ex) : 1.f;
+                sc[bt] = sj;
+                oscale[bt] = inv_se / sj;
             }
-            if (b_task) {
-                // the four B warps' partial sums are in (bounded wait; the
-                // double buffer is safe because no warp of the group passes
-                // the wait for its next element before every one of them has
-                // arrived for it)
-                if (!wait(my_sum, (uint32_t)(kk & 1))) break;
-                float tdir[3];
-#pragma unroll
-                for (int dd = 0; dd < 3; ++dd) {
-                    float acc = 0.f;
-#pragma unroll
-                    for (int c8 = 0; c8 < 8; ++c8) acc += ps[(c8 * KR + j) * 3 + dd];
-                    tdir[dd] = 0.05f * acc;
-                }
-                const float t0 = tdir[0], t1 = tdir[1], t2 = tdir[2];
-                const float tr[3] = {rb == 0 ? t0 : rb == 1 ? t1 : t2, rb == 0 ? t1 : rb == 1 ? t2 : t0,
-                                     rb == 0 ? t2 : rb == 1 ? t0 : t1};
+            named_sync(bar_id, kBldWarps * 32);
+            // B tile: row j (case), K-columns 8q..8q+7 (direction-ordered dofs);
+            // the low term's rows follow the high term's (rows kb + j)
+            for (int x = bt; x < 8 * kb; x += 128) {
+                const int j = x % kb, q = x / kb;
+                const float sj = sc[j];
                 float xv[8];
 #pragma unroll
-                for (int g = 0; g < 8; ++g) xv[g] = (8 * qb + g < 60) ? (hi[g] - tr[g % 3]) + lo[g] : 0.f;
-                split3_store8(xv, Bb + kmajor_off(j, 8 * qb), kTermB);
+                for (int g = 0; g < 8; ++g) {
+                    const int col = 8 * q + g;
+                    if (col < 60) {
+                        const int d = col / 20, i = col % 20;
+                        const float2 v = Pe[(i * 3 + d) * kb + j];
+                        xv[g] = ((v.x - tt[d * kMaxKB + j]) + v.y) * sj;
+                    } else {
+                        xv[g] = 0.f;
+                    }
+                }
+                uint32_t wh[4], wl[4];
+#pragma unroll
+                for (int g = 0; g < 4; ++g) split2_f16(xv[2 * g], xv[2 * g + 1], wh[g], wl[g]);
+                const uint32_t off = kmajor_off(j, 8 * q);
+                *reinterpret_cast<uint4 *>(B + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+                *reinterpret_cast<uint4 *>(B + 128 * kb + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
             }
-            fence_proxy_async();   // this thread's tile writes -> the tensor cores
-            __syncwarp();
+            fence_proxy_async();   // this thread's tile writes -> the tensor cores; its stage reads before refills
+            named_sync(bar_id, kBldWarps * 32);   // the translations, maxima and scales are reused for the next element
             if (lane == 0) {
                 mbar_arrive(&st_empty[s]);
                 mbar_arrive(&tl_full[b]);
@@ -300,53 +496,97 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
     } else if (warp == kMmaWarp) {
         int t = 0;
         if (lane == 0) {
+            // kind::f16 with both operands FP16 (the format is in the instruction descriptor)
+            const uint32_t idesc2 = idesc_f16(64, 2u * kb), idesc1 = idesc_f16(64, (uint32_t)kb);
             for (; t < nmine; ++t) {
                 const int b = t % kNTile, a = t % kNAcc;
                 if (!wait(&tl_full[b], (uint32_t)((t / kNTile) & 1))) break;
                 if (t >= kNAcc && !wait(&ac_empty[a], (uint32_t)((t / kNAcc - 1) & 1))) break;
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(A + b * kBufA), b0 = smem_u32(B + b * kBufB);
-                // the six products of order <= 2^-16: (1,1) (1,2) (2,1) (1,3) (2,2) (3,1)
-                const int ta[6] = {0, 0, 1, 0, 1, 2};
-                const int tb[6] = {0, 1, 0, 2, 1, 0};
-                uint32_t acc = 0;
+                const uint32_t a0 = smem_u32(tiles + (size_t)b * pl.tile);
+                const uint32_t b0 = a0 + 2 * kTileA;
+                const uint32_t d0 = tmem + (uint32_t)(kAccCols * a);
+                // A_hi x [B_hi | B_lo]: the products of order 1 and 2^-11 side by side
 #pragma unroll
-                for (int tt = 0; tt < 6; ++tt)
+                for (int ks = 0; ks < 4; ++ks)   // K = 64 in steps of 16 (two core matrices)
+                    mma_bf16(d0, umma_desc(a0 + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024), idesc2,
+                             ks > 0 ? 1u : 0u);
+                // A_lo x B_hi into the first kb columns
 #pragma unroll
-                    for (int ks = 0; ks < 4; ++ks) {   // K = 64 in steps of 16 (two core matrices)
-                        mma_bf16(tmem + (uint32_t)(16 * a), umma_desc(a0 + ta[tt] * kTermA + ks * 256, 128, 1024),
-                                 umma_desc(b0 + tb[tt] * kTermB + ks * 256, 128, 1024), kIdesc, acc);
-                        acc = 1;
-                    }
-                mma_commit(&tl_empty[b]);
+                for (int ks = 0; ks < 4; ++ks)
+                    mma_bf16(d0, umma_desc(a0 + kTileA + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024),
+                             idesc1, 1u);
                 mma_commit(&ac_full[a]);
             }
             s_count[1] = t;
         }
         __syncwarp();
-    } else if (warp >= kEpiWarp0 && warp < kEpiWarp0 + kNEpi) {
-        // direction dn: TMEM lane i < 20 holds row 3i + dn for the 16 cases,
-        // lane 20 the sum of those rows; subtracting a twentieth of it
-        // removes each case's mean translation from the result
-        const int dn = warp - kEpiWarp0;
-        for (int t = 0; t < nmine; ++t) {
-            const int a = t % kNAcc;
-            if (!wait(&ac_full[a], (uint32_t)((t / kNAcc) & 1))) break;
+    } else if (warp < kEpiGroups * kEpiWarps) {
+        // group eg takes the elements t = eg, eg + 2, ...; lanes 0..15 of its
+        // warp q = warp % 4 hold rows 16q..16q+15 (direction-ordered); lanes
+        // 16..31 read TMEM lanes the M = 64 product leaves unused and store
+        // nothing
+        const int eg = warp / kEpiWarps, q = warp % kEpiWarps, et = tid - eg * kEpiWarps * 32;
+        const int row = lane < 16 ? 16 * q + lane : 64;
+        const int dn = row < 60 ? row / 20 : 0;
+        const int bar_id = 6 + eg;
+        for (int t = eg; t < nmine; t += kEpiGroups) {
+            const int a = t % kNAcc, b = t % kNTile, kk = t / kEpiGroups;
+            if (et == 0) g_ok[4 + 2 * eg + (kk & 1)] = wait(&ac_full[a], (uint32_t)((t / kNAcc) & 1));
+            named_sync(bar_id, kEpiWarps * 32);
+            if (!g_ok[4 + 2 * eg + (kk & 1)]) break;
             tc_fence_after();
-            float v[16];
-            tmem_ld_32x32b_x16(tmem + ((uint32_t)(32 * dn) << 16) + (uint32_t)(16 * a), v);
+            // 32 columns per load, each load with its wait in one asm statement
+            // (the registers are defined only once the wait has returned); the
+            // accumulator's columns j and kb + j add up to case j
+            const uint32_t ta = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(kAccCols * a);
+            float v[kb];
+            if constexpr (kb <= 16) {
+                float w[32];
+                tmem_ld_32x32b_x32(ta, w);
+#pragma unroll
+                for (int j = 0; j < kb; ++j) v[j] = w[j] + w[kb + j];
+            } else {
+#pragma unroll
+                for (int c = 0; c < kb / 32; ++c) {
+                    float w[32];
+                    tmem_ld_32x32b_x32(ta + 32 * c, w);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[32 * c + i] = w[i];
+                }
+#pragma unroll
+                for (int c = 0; c < kb / 32; ++c) {
+                    float w[32];
+                    tmem_ld_32x32b_x32(ta + kb + 32 * c, w);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[32 * c + i] += w[i];
+                }
+            }
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ac_empty[a]);
+            // the sum rows 60..62 sit in lanes 12..14 of the group's warp 3
+            float *es = e_aux + (eg * 2 + (kk & 1)) * 3 * kMaxKB;
+            if (q == 3 && lane >= 12 && lane < 15) {
 #pragma unroll
-            for (int x = 0; x < 16; ++x) v[x] -= 0.05f * __shfl_sync(kFullMask, v[x], 20);
-            if (lane < 20) {
-                float4 *o = reinterpret_cast<float4 *>(ut + ((size_t)elem(t) * 60 + 3 * lane + dn) * KR);
-                o[0] = make_float4(v[0], v[1], v[2], v[3]);
-                o[1] = make_float4(v[4], v[5], v[6], v[7]);
-                o[2] = make_float4(v[8], v[9], v[10], v[11]);
-                o[3] = make_float4(v[12], v[13], v[14], v[15]);
+                for (int j = 0; j < kb; ++j) es[(lane - 12) * kMaxKB + j] = v[j];
             }
+            named_sync(bar_id, kEpiWarps * 32);
+            const float *osc = reinterpret_cast<const float *>(tiles + (size_t)b * pl.tile + 2 * kTileA + 256 * kb);
+            if (row < 60) {
+                float *o = ut + ((size_t)elem(t) * 60 + dir_dof(row)) * k + c0;
+#pragma unroll
+                for (int j4 = 0; j4 < kb; j4 += 4) {
+                    float4 w;
+                    w.x = (v[j4] - 0.05f * es[dn * kMaxKB + j4]) * osc[j4];
+                    w.y = (v[j4 + 1] - 0.05f * es[dn * kMaxKB + j4 + 1]) * osc[j4 + 1];
+                    w.z = (v[j4 + 2] - 0.05f * es[dn * kMaxKB + j4 + 2]) * osc[j4 + 2];
+                    w.w = (v[j4 + 3] - 0.05f * es[dn * kMaxKB + j4 + 3]) * osc[j4 + 3];
+                    *reinterpret_cast<float4 *>(o + j4) = w;
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tl_empty[b]);   // the tile's output scales are read
         }
     }
     __syncthreads();
@@ -355,87 +595,120 @@ k_mr_elem_tc(int nels, const float *__restrict__ kp, const float *__restrict__ k
             atomicExch(err, 3);
             // copies issued: elements 0 .. s_count[0]-1; MMA groups committed: 0 .. s_count[1]-1.
             // Wait (bounded) for the last phase of every stage and accumulator still owed.
-            for (int t = s_count[0] - kNst; t < s_count[0]; ++t)
-                if (t >= 0) mbar_wait(&st_full[t % kNst], (uint32_t)((t / kNst) & 1));
+            for (int t = s_count[0] - nst; t < s_count[0]; ++t)
+                if (t >= 0) mbar_wait(&st_full[t % nst], (uint32_t)((t / nst) & 1));
             for (int t = s_count[1] - kNAcc; t < s_count[1]; ++t)
                 if (t >= 0) mbar_wait(&ac_full[t % kNAcc], (uint32_t)((t / kNAcc) & 1));
         }
         __syncthreads();
     }
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, 64);
+    if (warp == 0) tmem_dealloc(tmem, kNAcc * kAccCols);
 }
 
 // Block element products on CUDA cores (FP32 or FP64): one warp per element,
-// lanes own rows 2l, 2l+1; P_e staged in shared memory per warp.
+// lanes own rows 2l, 2l+1; the cases in chunks of 8, each chunk's P_e staged
+// in shared memory per warp.
 template <typename KT, typename OT>
 __global__ void __launch_bounds__(256)
-k_mr_elem_cc(int nels, const KT *__restrict__ km, const int *__restrict__ conn, const double *__restrict__ P,
+k_mr_elem_cc(int nels, int k, const KT *__restrict__ km, const int *__restrict__ conn, const double *__restrict__ P,
              OT *__restrict__ ut, const int *__restrict__ skip)
 {
-    constexpr int WPB = 32 / (int)sizeof(KT);   // warps per block: 8 (FP32) or 4 (FP64), 30 KB of P blocks
-    __shared__ KT ps[WPB][60 * KR];
+    constexpr int CB = 8;
+    __shared__ KT ps[8][60 * CB];
     if (skip && *skip) return;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int e = warp; e < nels; e += nwarps) {
-        for (int idx = lane; idx < 60 * KR; idx += 32) {
-            const int c = idx / KR, j = idx - KR * c;
-            const int nd = conn[(size_t)e * 20 + c / 3];
-            ps[w][idx] = (KT)P[((size_t)3 * nd + c % 3) * KR + j];
-        }
-        __syncwarp();
-        if (lane < 30) {
-            KT a0[KR], a1[KR];
+        for (int cc = 0; cc < k; cc += CB) {
+            for (int idx = lane; idx < 60 * CB; idx += 32) {
+                const int c = idx / CB, j = idx - CB * c;
+                const int nd = conn[(size_t)e * 20 + c / 3];
+                ps[w][idx] = (KT)P[((size_t)3 * nd + c % 3) * k + cc + j];
+            }
+            __syncwarp();
+            if (lane < 30) {
+                KT a0[CB], a1[CB];
 #pragma unroll
-            for (int j = 0; j < KR; ++j) a0[j] = a1[j] = (KT)0;
-            const KT *ke = km + (size_t)e * 3600 + 2 * lane;
-            for (int c = 0; c < 60; ++c) {
-                const KT k0 = ke[60 * c], k1 = ke[60 * c + 1];
+                for (int j = 0; j < CB; ++j) a0[j] = a1[j] = (KT)0;
+                const KT *ke = km + (size_t)e * 3600 + 2 * lane;
+                for (int c = 0; c < 60; ++c) {
+                    const KT k0 = ke[60 * c], k1 = ke[60 * c + 1];
 #pragma unroll
-                for (int j = 0; j < KR; ++j) {
-                    const KT pj = ps[w][c * KR + j];
-                    a0[j] = fma(k0, pj, a0[j]);
-                    a1[j] = fma(k1, pj, a1[j]);
+                    for (int j = 0; j < CB; ++j) {
+                        const KT pj = ps[w][c * CB + j];
+                        a0[j] = fma(k0, pj, a0[j]);
+                        a1[j] = fma(k1, pj, a1[j]);
+                    }
+                }
+                OT *o0 = ut + ((size_t)e * 60 + 2 * lane) * k + cc;
+#pragma unroll
+                for (int j = 0; j < CB; ++j) {
+                    o0[j] = (OT)a0[j];
+                    o0[k + j] = (OT)a1[j];
                 }
             }
-            OT *o0 = ut + ((size_t)e * 60 + 2 * lane) * KR;
-#pragma unroll
-            for (int j = 0; j < KR; ++j) {
-                o0[j] = (OT)a0[j];
-                o0[KR + j] = (OT)a1[j];
-            }
+            __syncwarp();
         }
-        __syncwarp();
     }
+}
+
+// Threads of the block kernels over (slot or node, case): a multiple of k,
+// so that a thread's case j = threadIdx.x % k stays fixed in the
+// grid-stride loop.
+__host__ __device__ inline int case_threads(int k) { return k * (256 / k); }
+
+// Sums NV per-thread values over the threads of each case in thread order
+// (kinds bit = max) and writes part[v * stride + blockIdx.x * k + j].
+template <int NV>
+__device__ __forceinline__ void case_block_reduce(double (&v)[NV], unsigned kinds, double *out, size_t stride, int k)
+{
+    __shared__ double sh[NV][256];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) sh[q][threadIdx.x] = v[q];
+    __syncthreads();
+    if ((int)threadIdx.x < k) {
+        const int ng = blockDim.x / k;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = 0.0;
+            for (int g = 0; g < ng; ++g) {
+                const double x = sh[q][g * k + threadIdx.x];
+                s = ((kinds >> q) & 1) ? fmax(s, x) : s + x;
+            }
+            out[q * stride + (size_t)blockIdx.x * k + threadIdx.x] = s;
+        }
+    }
+    __syncthreads();
 }
 
 // Node scatter for k load cases: thread (node, j), ascending element order.
 // MODE 0: U = sum, partial p.u per case; MODE 1: RRES = F - sum, partial rr.
 template <typename UT, int MODE>
 __global__ void __launch_bounds__(256)
-k_mr_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list, const UT *__restrict__ ut,
+k_mr_scatter(int nn, int k, const int *__restrict__ ptr, const int *__restrict__ list, const UT *__restrict__ ut,
              const uint8_t *__restrict__ fm, const double *__restrict__ pf, double *__restrict__ out,
              double *__restrict__ part, const int *__restrict__ skip)
 {
     if (skip && *skip) return;   // uniform: the flag does not change during the kernel
-    const int j = threadIdx.x & (KR - 1);
+    const int j = threadIdx.x % k;
     double loc = 0.0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nn * KR; t += gridDim.x * blockDim.x) {
-        const int n = t / KR;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < (size_t)nn * k;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const int n = (int)(t / k);
         UT a0 = 0, a1 = 0, a2 = 0;   // FP32 products are summed in FP32, FP64 ones in FP64
-        for (int k = ptr[n]; k < ptr[n + 1]; ++k) {
-            const size_t base = (size_t)list[k] * 3 * KR + j;   // list holds e*20+a
+        for (int q = ptr[n]; q < ptr[n + 1]; ++q) {
+            const size_t base = (size_t)list[q] * 3 * k + j;   // list holds e*20+a
             a0 += ut[base];
-            a1 += ut[base + KR];
-            a2 += ut[base + 2 * KR];
+            a1 += ut[base + k];
+            a2 += ut[base + 2 * k];
         }
         const int m = fm[n];
         const double a[3] = {(double)a0, (double)a1, (double)a2};
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const size_t s = ((size_t)3 * n + d) * KR + j;
+            const size_t s = ((size_t)3 * n + d) * k + j;
             const bool fr = (m >> d) & 1;
             if (MODE == 0) {
                 const double uv = fr ? a[d] : 0.0;
@@ -448,113 +721,86 @@ k_mr_scatter(int nn, const int *__restrict__ ptr, const int *__restrict__ list, 
             }
         }
     }
-    // per-case block reduction: lanes l and l+16 share a case
-    loc += __shfl_xor_sync(kFullMask, loc, 16);
-    __shared__ double sh[8][KR];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane < KR) sh[w][lane] = loc;
-    __syncthreads();
-    if (threadIdx.x < KR) {
-        double s = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i][threadIdx.x];
-        part[(size_t)blockIdx.x * KR + threadIdx.x] = s;
-    }
+    double v[1] = {loc};
+    case_block_reduce<1>(v, 0u, part, 0, k);
 }
 
 // per-case state
 struct MState {
-    double up[KR], ff[KR], rr[KR], thr[KR];
-    double alpha[KR], beta[KR];   // this iteration's step lengths (0 for inactive cases)
-    int active[KR];      // 1 until the case's true residual reaches tol
-    int flag[KR];        // recursive residual reached thr (replacement wanted)
-    int iters[KR];
+    double up[kMaxK], ff[kMaxK], rr[kMaxK], thr[kMaxK];
+    double alpha[kMaxK], beta[kMaxK];   // this iteration's step lengths (0 for inactive cases)
+    int active[kMaxK];   // 1 until the case's true residual reaches tol
+    int flag[kMaxK];     // recursive residual reached thr (replacement wanted)
+    int iters[kMaxK];
     int any_flag;        // stop iterating: some active case wants a replacement
     int pending;         // set by this iteration's k_mr_beta, moved to any_flag by k_mr_finish
     int err;
 };
 
-// per-case sums of block partials (fixed order, same value in every block)
-__device__ __forceinline__ double case_sum(const double *part, int G, int j)
+// per-case sums of block partials (fixed order)
+__device__ __forceinline__ double case_sum(const double *part, int G, int j, int k)
 {
     double s = 0.0;
-    for (int b = 0; b < G; ++b) s += part[(size_t)b * KR + j];
+    for (int b = 0; b < G; ++b) s += part[(size_t)b * k + j];
     return s;
 }
 
-// The same sums by one 256-thread block: thread (g, j) adds partials
-// g, g+16, ... of case j, then thread j adds the 16 group sums in order.
-// Fixed order, so the result is the same in every run.
-__device__ __forceinline__ double case_sum_block(const double *part, int G, double (*sh)[KR])
+// The same sums by one 256-thread block: thread (g, j) adds partials g, g+ng,
+// ... of case j (ng = 256 / k groups), then thread j adds the ng group sums
+// in order.  Fixed order, so the result is the same in every run.  Valid in
+// threads 0..k-1.
+__device__ __forceinline__ double case_sum_block(const double *part, int G, double *sh, int k)
 {
-    const int j = threadIdx.x & (KR - 1), g = threadIdx.x >> 4;
+    const int ng = 256 / k;
+    const int j = threadIdx.x % k, g = threadIdx.x / k;
     double s = 0.0;
-    for (int b = g; b < G; b += 16) s += part[(size_t)b * KR + j];
-    sh[g][j] = s;
+    if (g < ng)
+        for (int b = g; b < G; b += ng) s += part[(size_t)b * k + j];
+    sh[threadIdx.x] = s;
     __syncthreads();
     double t = 0.0;
-    if (threadIdx.x < KR)
-        for (int i = 0; i < 16; ++i) t += sh[i][threadIdx.x];
+    if ((int)threadIdx.x < k)
+        for (int i = 0; i < ng; ++i) t += sh[i * k + threadIdx.x];
     __syncthreads();
-    return t;   // valid in threads 0..15
-}
-
-template <int NV>
-__device__ __forceinline__ void case_block_reduce(double (&v)[NV], unsigned kinds, double *out, size_t stride)
-{
-    // lanes l and l+16 hold the same case
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        const double o = __shfl_xor_sync(kFullMask, v[k], 16);
-        v[k] = ((kinds >> k) & 1) ? fmax(v[k], o) : v[k] + o;
-    }
-    __shared__ double sh[NV][8][KR];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane < KR)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) sh[k][w][lane] = v[k];
-    __syncthreads();
-    if (threadIdx.x < KR)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double s = 0.0;
-            for (int i = 0; i < (int)(blockDim.x >> 5); ++i)
-                s = ((kinds >> k) & 1) ? fmax(s, sh[k][i][threadIdx.x]) : s + sh[k][i][threadIdx.x];
-            out[k * stride + (size_t)blockIdx.x * KR + threadIdx.x] = s;
-        }
+    return t;
 }
 
 __global__ void __launch_bounds__(256)
-k_mr_init(int ns, const double *__restrict__ F, const double *__restrict__ dinv, double *__restrict__ X,
-          double *__restrict__ R, double *__restrict__ D, double *__restrict__ P, double *__restrict__ part, int G)
+k_mr_init(int ns, int k, const double *__restrict__ F, const double *__restrict__ dinv, double *__restrict__ X,
+          double *__restrict__ R, double *__restrict__ D, double *__restrict__ P, float2 *__restrict__ Ps,
+          double *__restrict__ part, int G)
 {
     double rd = 0.0, rr = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
          t += (size_t)gridDim.x * blockDim.x) {
-        const double rv = F[t], dv = dinv[t / KR] * rv;
+        const double rv = F[t], dv = dinv[t / k] * rv;
         X[t] = 0.0;
         R[t] = rv;
         D[t] = dv;
         P[t] = dv;
+        float h, l;
+        split_f64(dv, h, l);
+        Ps[t] = make_float2(h, l);
         rd = fma(rv, dv, rd);
         rr = fma(rv, rv, rr);
     }
     double v[2] = {rd, rr};
-    case_block_reduce<2>(v, 0u, part, (size_t)G * KR);
+    case_block_reduce<2>(v, 0u, part, (size_t)G * k, k);
 }
 
-__global__ void k_mr_init2(MState *st, const double *__restrict__ part, int G, double tol)
+__global__ void k_mr_init2(MState *st, const double *__restrict__ part, int G, int k, double tol)
 {
-    const int j = threadIdx.x;
-    if (j >= KR) return;
-    const double rd = case_sum(part, G, j), rr = case_sum(part + (size_t)G * KR, G, j);
-    st->up[j] = rd;
-    st->ff[j] = rr;
-    st->rr[j] = rr;
-    st->thr[j] = 0.1 > tol ? 0.1 : tol;
-    st->active[j] = rr > 0.0 ? 1 : 0;
-    st->flag[j] = 0;
-    st->iters[j] = 0;
-    if (j == 0) {
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+        const double rd = case_sum(part, G, j, k), rr = case_sum(part + (size_t)G * k, G, j, k);
+        st->up[j] = rd;
+        st->ff[j] = rr;
+        st->rr[j] = rr;
+        st->thr[j] = 0.1 > tol ? 0.1 : tol;
+        st->active[j] = rr > 0.0 ? 1 : 0;
+        st->flag[j] = 0;
+        st->iters[j] = 0;
+    }
+    if (threadIdx.x == 0) {
         st->any_flag = 0;
         st->pending = 0;
         st->err = 0;
@@ -562,51 +808,51 @@ __global__ void k_mr_init2(MState *st, const double *__restrict__ part, int G, d
 }
 
 // alpha = up / (p.u) per case, from the scatter's partials (one block)
-__global__ void __launch_bounds__(256) k_mr_alpha(MState *st, const double *__restrict__ ps, int Gs)
+__global__ void __launch_bounds__(256) k_mr_alpha(MState *st, const double *__restrict__ ps, int Gs, int k)
 {
-    __shared__ double sh[16][KR];
+    __shared__ double sh[256];
     if (st->any_flag) return;
-    const double pu = case_sum_block(ps, Gs, sh);
+    const double pu = case_sum_block(ps, Gs, sh, k);
     const int j = threadIdx.x;
-    if (j < KR) st->alpha[j] = st->active[j] ? st->up[j] / pu : 0.0;
+    if (j < k) st->alpha[j] = st->active[j] ? st->up[j] / pu : 0.0;
 }
 
 __global__ void __launch_bounds__(256)
-k_mr_update1(int ns, const MState *__restrict__ st, double *__restrict__ pu_out, int G, double *__restrict__ X,
+k_mr_update1(int ns, int k, const MState *__restrict__ st, double *__restrict__ pu_out, int G, double *__restrict__ X,
              double *__restrict__ R, double *__restrict__ D, const double *__restrict__ P,
              const double *__restrict__ U, const double *__restrict__ dinv)
 {
     if (st->any_flag) return;
-    const int j = threadIdx.x & (KR - 1);
+    const int j = threadIdx.x % k;
     const double alpha = st->alpha[j];
     double rd = 0.0, rr = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
          t += (size_t)gridDim.x * blockDim.x) {
         X[t] = fma(P[t], alpha, X[t]);
         const double rn = fma(-U[t], alpha, R[t]);
         R[t] = rn;
-        const double dn = dinv[t / KR] * rn;
+        const double dn = dinv[t / k] * rn;
         D[t] = dn;
         rd = fma(rn, dn, rd);
         rr = fma(rn, rn, rr);
     }
     double v[2] = {rd, rr};
-    case_block_reduce<2>(v, 0u, pu_out, (size_t)G * KR);
+    case_block_reduce<2>(v, 0u, pu_out, (size_t)G * k, k);
 }
 
 // r.d and r.r per case; beta = (r.d)_new / up; the new up, rr and iteration
 // count; the stopping test (one block).  The flag raised here reaches
 // any_flag only in k_mr_finish, after this iteration's k_mr_update2.
-__global__ void __launch_bounds__(256) k_mr_beta(MState *st, const double *__restrict__ part, int G, int limit)
+__global__ void __launch_bounds__(256) k_mr_beta(MState *st, const double *__restrict__ part, int G, int k, int limit)
 {
-    __shared__ double sh[16][KR];
+    __shared__ double sh[256];
     __shared__ int s_any;
     if (st->any_flag) return;
     if (threadIdx.x == 0) s_any = 0;
-    const double rd = case_sum_block(part, G, sh);
-    const double rr = case_sum_block(part + (size_t)G * KR, G, sh);
+    const double rd = case_sum_block(part, G, sh, k);
+    const double rr = case_sum_block(part + (size_t)G * k, G, sh, k);
     const int j = threadIdx.x;
-    if (j < KR) {
+    if (j < k) {
         if (st->active[j]) {
             st->beta[j] = rd / st->up[j];
             st->up[j] = rd;
@@ -624,16 +870,34 @@ __global__ void __launch_bounds__(256) k_mr_beta(MState *st, const double *__res
     if (threadIdx.x == 0 && s_any) st->pending = 1;
 }
 
+// p = d + beta p for the active cases, with p's FP32 high and low parts
+// (the tensor-core product's input) beside it
 __global__ void __launch_bounds__(256)
-k_mr_update2(int ns, const MState *__restrict__ st, const double *__restrict__ D, double *__restrict__ P)
+k_mr_update2(int ns, int k, const MState *__restrict__ st, const double *__restrict__ D, double *__restrict__ P,
+             float2 *__restrict__ Ps)
 {
     if (st->any_flag) return;
-    const int j = threadIdx.x & (KR - 1);
+    const int j = threadIdx.x % k;
     const double beta = st->beta[j];
-    const bool act = st->active[j] != 0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
-         t += (size_t)gridDim.x * blockDim.x)
-        if (act) P[t] = fma(P[t], beta, D[t]);
+    if (!st->active[j]) return;   // this thread's case is fixed
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const double pn = fma(P[t], beta, D[t]);
+        P[t] = pn;
+        float h, l;
+        split_f64(pn, h, l);
+        Ps[t] = make_float2(h, l);
+    }
+}
+
+// Ps = FP32 high and low parts of P (block products outside a solve)
+__global__ void k_mr_psplit(size_t n, const double *__restrict__ P, float2 *__restrict__ Ps)
+{
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        float h, l;
+        split_f64(P[t], h, l);
+        Ps[t] = make_float2(h, l);
+    }
 }
 
 __global__ void k_mr_finish(MState *st)
@@ -646,107 +910,112 @@ __global__ void k_mr_finish(MState *st)
 
 // residual replacement: R = RRES for active cases, D = dinv*R, partials r.d, r.r
 __global__ void __launch_bounds__(256)
-k_mr_replace(int ns, const MState *__restrict__ st, const double *__restrict__ RRES,
+k_mr_replace(int ns, int k, const MState *__restrict__ st, const double *__restrict__ RRES,
              const double *__restrict__ dinv, double *__restrict__ R, double *__restrict__ D,
              double *__restrict__ part, int G)
 {
-    const int j = threadIdx.x & (KR - 1);
+    const int j = threadIdx.x % k;
+    const bool act = st->active[j] != 0;
     double rd = 0.0, rr = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
          t += (size_t)gridDim.x * blockDim.x) {
-        if (!st->active[j]) continue;
-        const double rv = RRES[t], dv = dinv[t / KR] * rv;
+        if (!act) continue;
+        const double rv = RRES[t], dv = dinv[t / k] * rv;
         R[t] = rv;
         D[t] = dv;
         rd = fma(rv, dv, rd);
         rr = fma(rv, rv, rr);
     }
     double v[2] = {rd, rr};
-    case_block_reduce<2>(v, 0u, part, (size_t)G * KR);
+    case_block_reduce<2>(v, 0u, part, (size_t)G * k, k);
 }
 
-__global__ void k_mr_replace2(MState *st, const double *__restrict__ part, int G)
+__global__ void k_mr_replace2(MState *st, const double *__restrict__ part, int G, int k)
 {
-    const int j = threadIdx.x;
-    if (j < KR && st->active[j]) {
-        st->up[j] = case_sum(part, G, j);
-        st->rr[j] = case_sum(part + (size_t)G * KR, G, j);
-        st->flag[j] = 0;
-    }
-    if (j == 0) {
+    for (int j = threadIdx.x; j < k; j += blockDim.x)
+        if (st->active[j]) {
+            st->up[j] = case_sum(part, G, j, k);
+            st->rr[j] = case_sum(part + (size_t)G * k, G, j, k);
+            st->flag[j] = 0;
+        }
+    if (threadIdx.x == 0) {
         st->any_flag = 0;
         st->pending = 0;
     }
 }
 
-// ksum[e][d][k] = sum over the 20 nodes a of K_e(3a + d, k) from the packed
-// FP32 storkm (summed in FP64), 0 for k = 60..63: the direction sums of
-// K_e's rows that the tensor-core block product adds to its A operand.
-__global__ void k_mr_rowsums(int nels, const float *__restrict__ kp, float *__restrict__ ksum)
+__global__ void k_mr_sums(const double *__restrict__ part, int G, int k, double *__restrict__ out)
 {
-    const size_t total = (size_t)nels * 192;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (size_t)gridDim.x * blockDim.x) {
-        const size_t e = idx / 192;
-        const int r = (int)(idx - e * 192), d = r / 64, k = r % 64;
-        float v = 0.f;
-        if (k < 60) {
-            const float *ke = kp + e * 1832;
-            double sum = 0.0;
-            for (int a = 0; a < 20; ++a) sum += (double)ke[packed_off(3 * a + d, k)];
-            v = (float)sum;
-        }
-        ksum[idx] = v;
-    }
+    for (int j = threadIdx.x; j < k; j += blockDim.x) out[j] = case_sum(part, G, j, k);
 }
 
-__global__ void k_mr_sums(const double *__restrict__ part, int G, double *__restrict__ out)
-{
-    if (threadIdx.x < KR) out[threadIdx.x] = case_sum(part, G, threadIdx.x);
-}
-
-__global__ void k_mr_eq_to_slot(int ns, const int *__restrict__ slot_eq, int neq, const double *__restrict__ Req,
+__global__ void k_mr_eq_to_slot(int ns, int k, const int *__restrict__ slot_eq, int neq, const double *__restrict__ Req,
                                 double *__restrict__ F)
 {
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * KR;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
          t += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = t / KR, j = t % KR;
+        const size_t s = t / k, j = t % k;
         const int q = slot_eq[s];
         F[t] = q > 0 ? Req[j * (size_t)neq + q - 1] : 0.0;
     }
 }
 
-__global__ void k_mr_slot_to_eq(int neq, const int *__restrict__ eq_slot, const double *__restrict__ X,
+__global__ void k_mr_slot_to_eq(int neq, int k, const int *__restrict__ eq_slot, const double *__restrict__ X,
                                 double *__restrict__ Xeq)
 {
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)neq * KR;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)neq * k;
          t += (size_t)gridDim.x * blockDim.x) {
         const size_t j = t / neq, q = t % neq;
-        Xeq[t] = X[(size_t)eq_slot[q] * KR + j];
+        Xeq[t] = X[(size_t)eq_slot[q] * k + j];
     }
 }
 
 // ---------------------------------------------------------------------------
 // Block-solve buffers of one context (Ctx::multi), allocated on the first
-// block solve or product and kept while the mesh is unchanged.
+// block solve or product and kept while the mesh and k are unchanged.
 struct MultiBufs {
-    int ns = 0;
+    int ns = 0, ne = 0, k = 0;
     double *F = nullptr, *X = nullptr, *R = nullptr, *D = nullptr, *P = nullptr, *U = nullptr, *RR = nullptr,
            *eq = nullptr;
-    int ne = 0;
     float *ut32 = nullptr;
-    float *ksum = nullptr;   // [nels][3][64] direction sums of K_e's rows (tensor-core products)
+    float2 *Ps = nullptr;           // [ns*k] FP32 high and low parts of P (the tensor-core product's input)
+    unsigned char *rec = nullptr;   // [nels][kRecBytes] tensor-core element records
     double *ut64 = nullptr, *part = nullptr, *sums = nullptr;
     MState *st = nullptr;
     MState *hst = nullptr;
+    // TMA maps of Ps for the tensor-core product's gathers: rows of one node
+    // (box 3k x 1, passes over all k cases) and rows of one slot (box kb x 1
+    // for kb = 8, 16, 32, 64); bit 0 / bit 1 + i set once encoded for Ps
+    CUtensorMap tm_node;
+    CUtensorMap tm_slot[4];
+    unsigned tm_have = 0;
+    // autotuned tensor-core pass width (cases per pass) for this k, and the
+    // timings of the candidates (ms per full product)
+    int kb = 0;
+    int cand[4] = {0, 0, 0, 0};
+    float cand_ms[4] = {0, 0, 0, 0};
 };
 namespace {
-void mb_free(MultiBufs &m)
+void mb_free_vectors(MultiBufs &m)
 {
-    void *p[] = {m.F, m.X, m.R, m.D, m.P, m.U, m.RR, m.eq, m.ut32, m.ksum, m.ut64, m.part, m.sums, m.st};
+    void *p[] = {m.F, m.X, m.R, m.D, m.P, m.U, m.RR, m.eq, m.ut32, m.Ps, m.ut64, m.part, m.sums, m.st};
     for (void *q : p)
         if (q) cudaFree(q);
     if (m.hst) cudaFreeHost(m.hst);
+    m.F = m.X = m.R = m.D = m.P = m.U = m.RR = m.eq = m.ut64 = m.part = m.sums = nullptr;
+    m.ut32 = nullptr;
+    m.Ps = nullptr;
+    m.st = nullptr;
+    m.hst = nullptr;
+    m.ns = 0;
+    m.k = 0;
+    m.kb = 0;
+    m.tm_have = 0;
+}
+void mb_free(MultiBufs &m)
+{
+    mb_free_vectors(m);
+    if (m.rec) cudaFree(m.rec);
     m = MultiBufs();
 }
 }  // namespace
@@ -757,6 +1026,7 @@ void multi_release(Ctx &c)
     mb_free(*c.multi);
     delete c.multi;
     c.multi = nullptr;
+    c.mr_ok = false;
 }
 
 }  // namespace pf
@@ -783,77 +1053,235 @@ static int mr_launched(Ctx &c, const char *name)
     return 0;
 }
 
-// U = K P for the block (prec 16: tensor cores, 32: CUDA-core FP32, 64: FP64
-// into ut64).  skip: device flag that turns the launch into a no-op.
+// stages that fit the shared memory for kb cases per pass (at most 4)
+static int mr_stages(int kb)
+{
+    for (int nst = 4; nst >= 2; --nst)
+        if (make_plan(kb, nst).smem <= 227 * 1024) return nst;
+    return 0;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the
+// library does not link the driver library itself)
+static EncodeTiledFn encode_tiled()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// A 2-D map of Ps (8-byte elements, rows of `cols` elements, `rows` rows),
+// box `box` x 1: one gathered row per box.
+static int mr_encode(CUtensorMap *tm, const float2 *Ps, int cols, size_t rows, int box)
+{
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) {
+        set_error("pf_solve_multi: cuTensorMapEncodeTiled is not available from the driver");
+        return 1;
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)cols * 8};
+    const cuuint32_t boxd[2] = {(cuuint32_t)box, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, (void *)Ps, dims, strides, boxd, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("pf_solve_multi: cuTensorMapEncodeTiled failed (%d) for %d x %zu, box %d", (int)r, cols, rows, box);
+        return 1;
+    }
+    return 0;
+}
+
+template <int KB>
+static int mr_tc_pass_t(Ctx &c, int c0, const int *skip)
+{
+    MultiBufs &m = *c.multi;
+    const int whole = KB == m.k ? 1 : 0;
+    constexpr int slot = KB == 64 ? 3 : KB == 32 ? 2 : KB == 16 ? 1 : 0;
+    CUtensorMap *tm = whole ? &m.tm_node : &m.tm_slot[slot];
+    const unsigned bit = whole ? 1u : 2u << slot;
+    if (!(m.tm_have & bit)) {
+        if (whole ? mr_encode(tm, m.Ps, 3 * m.k, (size_t)c.nn, 3 * KB)
+                  : mr_encode(tm, m.Ps, m.k, (size_t)c.nslots, KB))
+            return 1;
+        m.tm_have |= bit;
+    }
+    const int nst = mr_stages(KB);
+    const Plan pl = make_plan(KB, nst);
+    static thread_local int attr_dev = -1;
+    if (attr_dev != c.device) {
+        MCK(cudaFuncSetAttribute(k_mr_elem_h16<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr_dev = c.device;
+    }
+    const int grid = c.nels < c.nsm ? c.nels : c.nsm;
+    k_mr_elem_h16<KB><<<grid, kH16Threads, pl.smem, c.stream>>>(c.nels, m.k, c0, nst, m.rec, c.conn, *tm, whole,
+                                                               m.ut32, c.kerr, skip);
+    return mr_launched(c, "k_mr_elem_h16");
+}
+
+// the tensor-core product of cases c0 .. c0+kb-1, kb in {8, 16, 32, 64}
+// (input: the split P, m.Ps)
+static int mr_tc_pass(Ctx &c, int kb, int c0, const int *skip)
+{
+    switch (kb) {
+    case 64: return mr_tc_pass_t<64>(c, c0, skip);
+    case 32: return mr_tc_pass_t<32>(c, c0, skip);
+    case 16: return mr_tc_pass_t<16>(c, c0, skip);
+    default: return mr_tc_pass_t<8>(c, c0, skip);
+    }
+}
+
+// all k cases in passes of at most w cases: the widest of 64, 32, 16, 8 that
+// fits the cases left (every k that is a multiple of 8 decomposes)
+static int mr_tc_product(Ctx &c, int w, const int *skip)
+{
+    const int k = c.multi->k;
+    for (int c0 = 0; c0 < k;) {
+        int kb = 64;
+        while (kb > w || kb > k - c0) kb >>= 1;
+        if (mr_tc_pass(c, kb, c0, skip)) return 1;
+        c0 += kb;
+    }
+    return 0;
+}
+
+// U = K P for the block (prec 16: tensor cores, on P's split copy m.Ps, which
+// must hold P; 32: CUDA-core FP32, 64: FP64 into ut64).  skip: device flag
+// that turns the launch into a no-op.
 static int mr_elem(Ctx &c, int prec, const double *P, const int *skip)
 {
     MultiBufs &m = *c.multi;
-    if (prec == 16) {
-        const int smem = kTcSmem;
-        MCK(cudaFuncSetAttribute(k_mr_elem_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        const int grid = c.nels < c.nsm ? c.nels : c.nsm;
-        k_mr_elem_tc<<<grid, kTcThreads, smem, c.stream>>>(c.nels, c.km32p, m.ksum, c.conn, P, m.ut32, c.kerr, skip);
-        return mr_launched(c, "k_mr_elem_tc");
-    }
+    if (prec == 16) return mr_tc_product(c, m.kb, skip);
+    const int grid = (c.nels + 7) / 8 < c.nsm * 8 ? (c.nels + 7) / 8 : c.nsm * 8;
     if (prec == 32) {
-        const int grid = (c.nels + 7) / 8 < c.nsm * 8 ? (c.nels + 7) / 8 : c.nsm * 8;
-        k_mr_elem_cc<float, float><<<grid, 256, 0, c.stream>>>(c.nels, c.km32, c.conn, P, m.ut32, skip);
+        k_mr_elem_cc<float, float><<<grid, 256, 0, c.stream>>>(c.nels, m.k, c.km32, c.conn, P, m.ut32, skip);
         return mr_launched(c, "k_mr_elem_cc<float>");
     }
-    const int grid = (c.nels + 3) / 4 < c.nsm * 16 ? (c.nels + 3) / 4 : c.nsm * 16;
-    k_mr_elem_cc<double, double><<<grid, 128, 0, c.stream>>>(c.nels, c.km64, c.conn, P, m.ut64, skip);
+    k_mr_elem_cc<double, double><<<grid, 256, 0, c.stream>>>(c.nels, m.k, c.km64, c.conn, P, m.ut64, skip);
     return mr_launched(c, "k_mr_elem_cc<double>");
 }
 
 static int mr_scatter(Ctx &c, int prec, int mode, const double *pf, double *out, const int *skip)
 {
     MultiBufs &m = *c.multi;
-    const int G = c.Gs;
+    const int G = c.Gs, T = case_threads(m.k);
     if (prec == 64) {
-        if (mode == 0) k_mr_scatter<double, 0><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut64, c.freemask, pf, out, m.part, skip);
-        else k_mr_scatter<double, 1><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut64, c.freemask, pf, out, m.part, skip);
+        if (mode == 0)
+            k_mr_scatter<double, 0><<<G, T, 0, c.stream>>>(c.nn, m.k, c.node_ptr, c.node_list, m.ut64, c.freemask, pf,
+                                                          out, m.part, skip);
+        else
+            k_mr_scatter<double, 1><<<G, T, 0, c.stream>>>(c.nn, m.k, c.node_ptr, c.node_list, m.ut64, c.freemask, pf,
+                                                          out, m.part, skip);
     } else {
-        if (mode == 0) k_mr_scatter<float, 0><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut32, c.freemask, pf, out, m.part, skip);
-        else k_mr_scatter<float, 1><<<G, 256, 0, c.stream>>>(c.nn, c.node_ptr, c.node_list, m.ut32, c.freemask, pf, out, m.part, skip);
+        if (mode == 0)
+            k_mr_scatter<float, 0><<<G, T, 0, c.stream>>>(c.nn, m.k, c.node_ptr, c.node_list, m.ut32, c.freemask, pf,
+                                                         out, m.part, skip);
+        else
+            k_mr_scatter<float, 1><<<G, T, 0, c.stream>>>(c.nn, m.k, c.node_ptr, c.node_list, m.ut32, c.freemask, pf,
+                                                         out, m.part, skip);
     }
     return mr_launched(c, "k_mr_scatter");
 }
 
-static int mr_alloc(Ctx &c)
+static int mr_alloc(Ctx &c, int k)
 {
     if (!c.multi) c.multi = new MultiBufs();
     MultiBufs &m = *c.multi;
-    if (m.ns == c.nslots && m.ne == c.nels && m.F) return 0;
-    mb_free(m);
-    const size_t n = (size_t)c.nslots * KR;
-    const size_t parts = (size_t)(c.Gs > c.G ? c.Gs : c.G) * KR * 4 + 64;
+    if (m.ne != c.nels) {
+        mb_free(m);
+        c.mr_ok = false;
+    }
+    if (!m.rec && cudaMalloc((void **)&m.rec, (size_t)c.nels * kRecBytes) != cudaSuccess) {
+        set_error("pf_solve_multi: cannot allocate the tensor-core element records (%zu bytes)",
+                  (size_t)c.nels * kRecBytes);
+        return 1;
+    }
+    m.ne = c.nels;
+    if (m.ns == c.nslots && m.k == k && m.F) return 0;
+    mb_free_vectors(m);
+    const size_t n = (size_t)c.nslots * k;
+    const size_t parts = (size_t)(c.Gs > c.G ? c.Gs : c.G) * k * 4 + 64;
     double **v[] = {&m.F, &m.X, &m.R, &m.D, &m.P, &m.U, &m.RR};
     for (double **q : v)
         if (cudaMalloc((void **)q, n * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&m.eq, (size_t)(c.neq > 0 ? c.neq : 1) * KR * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&m.ut32, (size_t)c.nels * 60 * KR * 4) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&m.ksum, (size_t)c.nels * 192 * 4) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&m.ut64, (size_t)c.nels * 60 * KR * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.eq, (size_t)(c.neq > 0 ? c.neq : 1) * k * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.ut32, (size_t)c.nels * 60 * k * 4) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.Ps, n * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.ut64, (size_t)c.nels * 60 * k * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&m.part, parts * 8) != cudaSuccess) goto fail;
-    if (cudaMalloc((void **)&m.sums, 64 * 8) != cudaSuccess) goto fail;
+    if (cudaMalloc((void **)&m.sums, kMaxK * 8) != cudaSuccess) goto fail;
     if (cudaMalloc((void **)&m.st, sizeof(MState)) != cudaSuccess) goto fail;
     if (cudaMallocHost((void **)&m.hst, sizeof(MState)) != cudaSuccess) goto fail;
     m.ns = c.nslots;
-    m.ne = c.nels;
+    m.k = k;
     return 0;
 fail:
-    mb_free(m);
-    set_error("pf_solve_multi: cannot allocate the block vectors (%zu slots x %d cases)", (size_t)c.nslots, KR);
+    mb_free_vectors(m);
+    set_error("pf_solve_multi: cannot allocate the block vectors (%zu slots x %d cases)", (size_t)c.nslots, k);
     return 1;
 }
 
-// direction sums of the packed storkm's rows for the tensor-core block
-// product (once per solve or product call: storkm may have changed)
-static int mr_rowsums(Ctx &c)
+// The element records of the tensor-core product (when storkm changed), and
+// the widest pass for this k: each candidate (the three widest of 64, 32,
+// 16, 8 that do not exceed k) times one full product (after one untimed),
+// the fastest is kept.  The candidates differ only in how many cases one
+// pass carries; each case's operands, scales and products are formed the
+// same way.
+static int mr_prepare_tc(Ctx &c)
 {
-    const int grid = c.nsm * 8;
-    k_mr_rowsums<<<grid, 256, 0, c.stream>>>(c.nels, c.km32p, c.multi->ksum);
-    return mr_launched(c, "k_mr_rowsums");
+    MultiBufs &m = *c.multi;
+    if (!c.mr_ok) {
+        k_mr_pack<<<c.nsm * 16, 128, 0, c.stream>>>(c.nels, c.km64, m.rec);
+        if (mr_launched(c, "k_mr_pack")) return 1;
+        c.mr_ok = true;
+        m.kb = 0;
+    }
+    if (m.kb) return 0;
+    const int k = m.k;
+    int n = 0;
+    for (int w : {64, 32, 16, 8})
+        if (w <= k && n < 3) m.cand[n++] = w;
+    for (int i = n; i < 4; ++i) m.cand[i] = 0, m.cand_ms[i] = 0.f;
+    if (n == 1) {
+        m.kb = m.cand[0];
+        m.cand_ms[0] = 0.f;
+        return 0;
+    }
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+        set_error("multi-RHS autotune: cannot create events");
+        return 1;
+    }
+    float best = 1e30f;
+    for (int i = 0; i < n; ++i) {
+        if (mr_tc_product(c, m.cand[i], nullptr)) return 1;
+        cudaEventRecord(a, c.stream);
+        if (mr_tc_product(c, m.cand[i], nullptr)) return 1;
+        cudaEventRecord(b, c.stream);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        m.cand_ms[i] = ms;
+        if (ms < best) {
+            best = ms;
+            m.kb = m.cand[i];
+        }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return 0;
 }
 
 // FP64 true residuals of all cases; returns per-case ||f - K x||^2 in rr_out
@@ -862,26 +1290,45 @@ static int mr_true_residual(Ctx &c, double *rr_out)
     MultiBufs &m = *c.multi;
     if (mr_elem(c, 64, m.X, nullptr)) return 1;
     if (mr_scatter(c, 64, 1, m.F, m.RR, nullptr)) return 1;
-    k_mr_sums<<<1, 32, 0, c.stream>>>(m.part, c.Gs, m.sums);
+    k_mr_sums<<<1, 128, 0, c.stream>>>(m.part, c.Gs, m.k, m.sums);
     if (mr_launched(c, "k_mr_sums")) return 1;
-    MCK(cudaMemcpyAsync(rr_out, m.sums, KR * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MCK(cudaMemcpyAsync(rr_out, m.sums, m.k * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     MCK(cudaStreamSynchronize(c.stream));
     return 0;
 }
 
-extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const double *tol, const int *limit,
+static int mr_check_k(const char *who, int k)
+{
+    if (k < 8 || k > kMaxK || k % 8) {
+        set_error("%s: k must be a multiple of 8 in 8..%d (got %d)", who, kMaxK, k);
+        return 1;
+    }
+    return 0;
+}
+
+static int mr_kernel_error(Ctx &c, const char *who)
+{
+    int kerr = 0;
+    MCK(cudaMemcpy(&kerr, c.kerr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (kerr) {
+        cudaMemset(c.kerr, 0, sizeof(int));
+        set_error("%s: tensor-core product wait timed out", who);
+        return 1;
+    }
+    return 0;
+}
+
+extern "C" int pf_solve_multi(void **ctx, const int *k_p, const double *r, const double *tol, const int *limit,
                               const int *prec, double *xnew, int *iters, double *relres)
 {
-    if (!ctx || !*ctx || !k || !r || !tol || !limit || !prec || !xnew || !iters || !relres) {
+    if (!ctx || !*ctx || !k_p || !r || !tol || !limit || !prec || !xnew || !iters || !relres) {
         set_error("pf_solve_multi: null argument");
         return PF_FAILURE;
     }
     Ctx &c = *(Ctx *)*ctx;
     MCK(cudaSetDevice(c.device));
-    if (*k != KR) {
-        set_error("pf_solve_multi: k must be %d", KR);
-        return PF_FAILURE;
-    }
+    if (mr_check_k("pf_solve_multi", *k_p)) return PF_FAILURE;
+    const int k = *k_p;
     if (c.shared || c.kind != KIND_SOLID20) {
         set_error("pf_solve_multi: needs per-element 20-node storkm");
         return PF_FAILURE;
@@ -890,25 +1337,30 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
         set_error("pf_solve_multi: needs storkm, limit >= 1 and prec 16 (tensor cores) or 32 (CUDA cores)");
         return PF_FAILURE;
     }
-    if (mr_alloc(c)) return PF_FAILURE;
-    if (*prec == 16 && mr_rowsums(c)) return PF_FAILURE;
+    if (mr_alloc(c, k)) return PF_FAILURE;
     MultiBufs &m = *c.multi;
-    const int G = c.G, Gs = c.Gs;
+    const int G = c.G, Gs = c.Gs, T = case_threads(k);
     // load cases: r(neq, k) column-major
-    MCK(cudaMemcpyAsync(m.eq, r, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
-    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, c.slot_eq, c.neq, m.eq, m.F);
+    MCK(cudaMemcpyAsync(m.eq, r, (size_t)c.neq * k * 8, cudaMemcpyHostToDevice, c.stream));
+    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, k, c.slot_eq, c.neq, m.eq, m.F);
     if (mr_launched(c, "k_mr_eq_to_slot")) return PF_FAILURE;
+    if (*prec == 16) {
+        // the autotuner times products of the initial search directions
+        k_mr_init<<<G, T, 0, c.stream>>>(c.nslots, k, m.F, c.dinv, m.X, m.R, m.D, m.P, m.Ps, m.part, G);
+        if (mr_launched(c, "k_mr_init")) return PF_FAILURE;
+        if (mr_prepare_tc(c)) return PF_FAILURE;
+    }
     cudaEvent_t e0, e1;
     MCK(cudaEventCreate(&e0));
     MCK(cudaEventCreate(&e1));
     MCK(cudaEventRecord(e0, c.stream));
-    k_mr_init<<<G, 256, 0, c.stream>>>(c.nslots, m.F, c.dinv, m.X, m.R, m.D, m.P, m.part, G);
+    k_mr_init<<<G, T, 0, c.stream>>>(c.nslots, k, m.F, c.dinv, m.X, m.R, m.D, m.P, m.Ps, m.part, G);
     if (mr_launched(c, "k_mr_init")) return PF_FAILURE;
-    k_mr_init2<<<1, 32, 0, c.stream>>>(m.st, m.part, G, *tol);
+    k_mr_init2<<<1, 128, 0, c.stream>>>(m.st, m.part, G, k, *tol);
     if (mr_launched(c, "k_mr_init2")) return PF_FAILURE;
-    double *pu = m.part + (size_t)Gs * KR;   // update partials after the scatter partials
+    double *pu = m.part + (size_t)Gs * k;   // update partials after the scatter partials
     int total = 0, chunk = 4, corrections = 0;
-    double rel[KR] = {0};
+    std::vector<double> rel(k, 0.0), rr(k, 0.0);
     // per-kernel timing of the iterations: events around the element product
     // and the scatter of every launched iteration (pool reused per chunk)
     constexpr int kMaxChunk = 32;
@@ -923,13 +1375,13 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
             MCK(cudaEventRecord(tev[3 * i + 1], c.stream));
             if (mr_scatter(c, *prec, 0, m.P, m.U, skip)) return PF_FAILURE;
             MCK(cudaEventRecord(tev[3 * i + 2], c.stream));
-            k_mr_alpha<<<1, 256, 0, c.stream>>>(m.st, m.part, Gs);
+            k_mr_alpha<<<1, 256, 0, c.stream>>>(m.st, m.part, Gs, k);
             if (mr_launched(c, "k_mr_alpha")) return PF_FAILURE;
-            k_mr_update1<<<G, 256, 0, c.stream>>>(c.nslots, m.st, pu, G, m.X, m.R, m.D, m.P, m.U, c.dinv);
+            k_mr_update1<<<G, T, 0, c.stream>>>(c.nslots, k, m.st, pu, G, m.X, m.R, m.D, m.P, m.U, c.dinv);
             if (mr_launched(c, "k_mr_update1")) return PF_FAILURE;
-            k_mr_beta<<<1, 256, 0, c.stream>>>(m.st, pu, G, *limit);
+            k_mr_beta<<<1, 256, 0, c.stream>>>(m.st, pu, G, k, *limit);
             if (mr_launched(c, "k_mr_beta")) return PF_FAILURE;
-            k_mr_update2<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.D, m.P);
+            k_mr_update2<<<G, T, 0, c.stream>>>(c.nslots, k, m.st, m.D, m.P, m.Ps);
             if (mr_launched(c, "k_mr_update2")) return PF_FAILURE;
             k_mr_finish<<<1, 32, 0, c.stream>>>(m.st);
             if (mr_launched(c, "k_mr_finish")) return PF_FAILURE;
@@ -947,23 +1399,16 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
             ms_iter += d;
         }
         if (chunk < kMaxChunk) chunk *= 2;
-        int kerr = 0;
-        MCK(cudaMemcpy(&kerr, c.kerr, sizeof(int), cudaMemcpyDeviceToHost));
-        if (kerr) {
-            cudaMemset(c.kerr, 0, sizeof(int));
-            set_error("pf_solve_multi: tensor-core product wait timed out");
-            return PF_FAILURE;
-        }
+        if (mr_kernel_error(c, "pf_solve_multi")) return PF_FAILURE;
         if (m.hst->err) {
             set_error("pf_solve_multi: PCG breakdown (non-finite r.d)");
             return PF_FAILURE;
         }
         if (!m.hst->any_flag) continue;
         // some active case reached its threshold (or the limit): FP64 true residuals
-        double rr[KR];
-        if (mr_true_residual(c, rr)) return PF_FAILURE;
+        if (mr_true_residual(c, rr.data())) return PF_FAILURE;
         int n_active = 0;
-        for (int j = 0; j < KR; ++j) {
+        for (int j = 0; j < k; ++j) {
             rel[j] = m.hst->ff[j] > 0 ? std::sqrt(rr[j]) / std::sqrt(m.hst->ff[j]) : 0.0;
             if (m.hst->active[j]) {
                 if (rel[j] <= *tol || m.hst->iters[j] >= *limit) m.hst->active[j] = 0;
@@ -976,29 +1421,29 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
         if (n_active == 0) break;
         // push the new thresholds and active flags, then replace the residuals
         MCK(cudaMemcpyAsync(m.st, m.hst, sizeof(MState), cudaMemcpyHostToDevice, c.stream));
-        k_mr_replace<<<G, 256, 0, c.stream>>>(c.nslots, m.st, m.RR, c.dinv, m.R, m.D, m.part, G);
+        k_mr_replace<<<G, T, 0, c.stream>>>(c.nslots, k, m.st, m.RR, c.dinv, m.R, m.D, m.part, G);
         if (mr_launched(c, "k_mr_replace")) return PF_FAILURE;
-        k_mr_replace2<<<1, 32, 0, c.stream>>>(m.st, m.part, G);
+        k_mr_replace2<<<1, 128, 0, c.stream>>>(m.st, m.part, G, k);
         if (mr_launched(c, "k_mr_replace2")) return PF_FAILURE;
         ++corrections;
         chunk = 4;
     }
     for (auto &ev : tev) cudaEventDestroy(ev);
     MCK(cudaEventRecord(e1, c.stream));
-    k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, c.eq_slot, m.X, m.eq);
+    k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, k, c.eq_slot, m.X, m.eq);
     if (mr_launched(c, "k_mr_slot_to_eq")) return PF_FAILURE;
-    MCK(cudaMemcpyAsync(xnew, m.eq, (size_t)c.neq * KR * 8, cudaMemcpyDeviceToHost, c.stream));
+    MCK(cudaMemcpyAsync(xnew, m.eq, (size_t)c.neq * k * 8, cudaMemcpyDeviceToHost, c.stream));
     MCK(cudaStreamSynchronize(c.stream));
     float ms = 0.f;
     MCK(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    for (int j = 0; j < KR; ++j) {
+    for (int j = 0; j < k; ++j) {
         iters[j] = m.hst->iters[j];
         relres[j] = rel[j];
     }
     c.stats[0] = 0;
-    for (int j = 0; j < KR; ++j) c.stats[0] = iters[j] > c.stats[0] ? iters[j] : c.stats[0];
+    for (int j = 0; j < k; ++j) c.stats[0] = iters[j] > c.stats[0] ? iters[j] : c.stats[0];
     c.stats[1] = corrections;
     c.stats[2] = ms;
     c.stats[3] = ms_elem;   // summed element-product time of the launched iterations
@@ -1008,38 +1453,57 @@ extern "C" int pf_solve_multi(void **ctx, const int *k, const double *r, const d
     return PF_SUCCESS;
 }
 
-// Block product U = K P for k = 16 cases in equation order (tests): prec 16,
-// 32 or 64.
-extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, const double *p, double *u)
+// Block product U = K P for k cases in equation order (tests): prec 16, 32
+// or 64.
+extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k_p, const int *prec, const double *p, double *u)
 {
-    if (!ctx || !*ctx || !k || !prec || !p || !u) {
+    if (!ctx || !*ctx || !k_p || !prec || !p || !u) {
         set_error("pf_ebe_matvec_multi: null argument");
         return PF_FAILURE;
     }
     Ctx &c = *(Ctx *)*ctx;
     MCK(cudaSetDevice(c.device));
-    if (*k != KR || !c.have_km || c.shared || c.kind != KIND_SOLID20 || (*prec != 16 && *prec != 32 && *prec != 64)) {
-        set_error("pf_ebe_matvec_multi: k must be %d, prec 16/32/64, per-element storkm formed", KR);
+    if (mr_check_k("pf_ebe_matvec_multi", *k_p)) return PF_FAILURE;
+    const int k = *k_p;
+    if (!c.have_km || c.shared || c.kind != KIND_SOLID20 || (*prec != 16 && *prec != 32 && *prec != 64)) {
+        set_error("pf_ebe_matvec_multi: prec 16/32/64 and per-element storkm formed");
         return PF_FAILURE;
     }
-    if (mr_alloc(c)) return PF_FAILURE;
-    if (*prec == 16 && mr_rowsums(c)) return PF_FAILURE;
+    if (mr_alloc(c, k)) return PF_FAILURE;
     MultiBufs &m = *c.multi;
-    MCK(cudaMemcpyAsync(m.eq, p, (size_t)c.neq * KR * 8, cudaMemcpyHostToDevice, c.stream));
-    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, c.slot_eq, c.neq, m.eq, m.P);
+    MCK(cudaMemcpyAsync(m.eq, p, (size_t)c.neq * k * 8, cudaMemcpyHostToDevice, c.stream));
+    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, k, c.slot_eq, c.neq, m.eq, m.P);
     if (mr_launched(c, "k_mr_eq_to_slot")) return PF_FAILURE;
+    if (*prec == 16) {
+        k_mr_psplit<<<c.nsm * 8, 256, 0, c.stream>>>((size_t)c.nslots * k, m.P, m.Ps);
+        if (mr_launched(c, "k_mr_psplit")) return PF_FAILURE;
+        if (mr_prepare_tc(c)) return PF_FAILURE;
+    }
     if (mr_elem(c, *prec, m.P, nullptr)) return PF_FAILURE;
     if (mr_scatter(c, *prec, 0, m.P, m.U, nullptr)) return PF_FAILURE;
-    k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, c.eq_slot, m.U, m.eq);
+    k_mr_slot_to_eq<<<c.nsm * 8, 256, 0, c.stream>>>(c.neq, k, c.eq_slot, m.U, m.eq);
     if (mr_launched(c, "k_mr_slot_to_eq")) return PF_FAILURE;
-    MCK(cudaMemcpyAsync(u, m.eq, (size_t)c.neq * KR * 8, cudaMemcpyDeviceToHost, c.stream));
+    MCK(cudaMemcpyAsync(u, m.eq, (size_t)c.neq * k * 8, cudaMemcpyDeviceToHost, c.stream));
     MCK(cudaStreamSynchronize(c.stream));
-    int kerr = 0;
-    MCK(cudaMemcpy(&kerr, c.kerr, sizeof(int), cudaMemcpyDeviceToHost));
-    if (kerr) {
-        cudaMemset(c.kerr, 0, sizeof(int));
-        set_error("pf_ebe_matvec_multi: tensor-core product wait timed out");
+    if (mr_kernel_error(c, "pf_ebe_matvec_multi")) return PF_FAILURE;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_multi_tuning(void **ctx, int *kb, int *cand, float *ms)
+{
+    if (!ctx || !*ctx || !kb || !cand || !ms) {
+        set_error("pf_multi_tuning: null argument");
         return PF_FAILURE;
+    }
+    Ctx &c = *(Ctx *)*ctx;
+    if (!c.multi || !c.multi->kb) {
+        set_error("pf_multi_tuning: no tensor-core block product has run on this context");
+        return PF_FAILURE;
+    }
+    *kb = c.multi->kb;
+    for (int i = 0; i < 4; ++i) {
+        cand[i] = c.multi->cand[i];
+        ms[i] = c.multi->cand_ms[i];
     }
     return PF_SUCCESS;
 }

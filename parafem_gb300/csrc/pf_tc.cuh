@@ -66,6 +66,37 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
+// 16-byte copy global -> shared that bypasses L1 (cp.async, both addresses
+// 16-byte aligned); completion is tracked per thread, see cp_async_arrive
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+// The mbarrier receives one arrival when every cp.async this thread issued
+// so far has completed.  The barrier's pending count is raised by one first,
+// so the arrival leaves the count the phase expects unchanged: issue it
+// before the phase's last ordinary arrival.
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar)
+{
+    asm volatile("cp.async.mbarrier.arrive.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// TMA gather: four rows (y0..y3) of a 2-D tensor, each the tensor map's box
+// (one row high) starting at column x, to consecutive places in shared
+// memory (dst 128-byte aligned; x * element size a multiple of 16 bytes);
+// completion counted in bytes on the mbarrier.  tmap is the generic address
+// of a CUtensorMap kernel parameter.
+__device__ __forceinline__ void tma_gather4(void *dst, const void *tmap, int x, int y0, int y1, int y2, int y3,
+                                            uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y0), "r"(y1), "r"(y2), "r"(y3), "r"(smem_u32(bar))
+        : "memory");
+}
+
 // orders this thread's generic-proxy shared-memory accesses with the async proxy
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
@@ -88,6 +119,13 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint
 constexpr uint32_t idesc_bf16(uint32_t m, uint32_t n)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((m >> 4) << 24);
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = F16 (format code 0),
+// both K-major.  n may be a run-time value (a multiple of 8).
+__host__ __device__ constexpr uint32_t idesc_f16(uint32_t m, uint32_t n)
+{
+    return (1u << 4) | ((n >> 3) << 17) | ((m >> 4) << 24);
 }
 
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
@@ -125,6 +163,34 @@ __device__ __forceinline__ void tmem_dealloc(uint32_t base, uint32_t ncols)
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Four 8x8 16-bit matrices between shared memory and registers: ldmatrix
+// with .trans hands each thread its fragment of the transposed matrices,
+// stmatrix writes fragments back as rows.  Thread i gives the address of row
+// i % 8 of matrix i / 8 (16 bytes, 16-byte aligned).
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t addr, uint32_t (&r)[4])
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr)
+                 : "memory");
+}
+
+__device__ __forceinline__ void stsm_x4(uint32_t addr, const uint32_t (&r)[4])
+{
+    asm volatile("stmatrix.sync.aligned.m8n8.x4.shared.b16 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(r[0]), "r"(r[1]),
+                 "r"(r[2]), "r"(r[3])
+                 : "memory");
+}
+
+// Two floats rounded to nearest-even FP16 in one instruction: lo in bits
+// 0..15, hi in bits 16..31.
+__device__ __forceinline__ uint32_t cvt_f16x2(float lo, float hi)
+{
+    uint32_t r;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
 
 // 16 consecutive FP32 columns of this warp's 32 TMEM lanes (lane = row)
 __device__ __forceinline__ void tmem_ld_32x32b_x16(uint32_t taddr, float (&v)[16])

@@ -72,6 +72,7 @@ _SIGS = {
                        ctypes.c_void_p],
     "pf_ebe_matvec_multi": [_VPP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_multi_free": [_VPP],
+    "pf_multi_tuning": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_batch_create": [_IP, _LLP, _IP, _IP, _VPP],
     "pf_batch_destroy": [_VPP],
     "pf_batch_capacity": [_VPP, _LLP, _LLP],
@@ -381,23 +382,36 @@ class Solver:
         _check(lib().pf_multi_free(self._ref), "pf_multi_free")
 
     def solve_multi(self, R, tol, limit, prec=16):
-        """k = 16 load cases together: R (neq, 16) -> X (neq, 16), iters (16,), relres (16,)."""
+        """k load cases together (k = R.shape[1], a multiple of 8): R (neq, k)
+        -> X (neq, k), iters (k,), relres (k,)."""
         Rf = np.asfortranarray(R, dtype=np.float64)
-        if Rf.shape != (self.neq, 16):
-            raise ValueError("R must be (neq, 16)")
-        X = np.zeros((self.neq, 16), order="F")
-        it = np.zeros(16, np.int32)
-        rel = np.zeros(16)
-        _check(lib().pf_solve_multi(self._ref, _i(16), Rf.ctypes.data, _d(tol), _i(limit), _i(prec),
+        if Rf.ndim != 2 or Rf.shape[0] != self.neq:
+            raise ValueError("R must be (neq, k)")
+        k = Rf.shape[1]
+        X = np.zeros((self.neq, k), order="F")
+        it = np.zeros(k, np.int32)
+        rel = np.zeros(k)
+        _check(lib().pf_solve_multi(self._ref, _i(k), Rf.ctypes.data, _d(tol), _i(limit), _i(prec),
                                     X.ctypes.data, it.ctypes.data, rel.ctypes.data), "pf_solve_multi")
         return X, it, rel
 
     def ebe_matvec_multi(self, Pm, prec=16):
         Pf = np.asfortranarray(Pm, dtype=np.float64)
-        U = np.zeros((self.neq, 16), order="F")
-        _check(lib().pf_ebe_matvec_multi(self._ref, _i(16), _i(prec), Pf.ctypes.data, U.ctypes.data),
+        k = Pf.shape[1]
+        U = np.zeros((self.neq, k), order="F")
+        _check(lib().pf_ebe_matvec_multi(self._ref, _i(k), _i(prec), Pf.ctypes.data, U.ctypes.data),
                "pf_ebe_matvec_multi")
         return U
+
+    def multi_tuning(self):
+        """The tensor-core block product's pass width for the current k and
+        the candidates' timings (ms per full product)."""
+        kb = ctypes.c_int(0)
+        cand = np.zeros(4, np.int32)
+        ms = np.zeros(4, np.float32)
+        _check(lib().pf_multi_tuning(self._ref, ctypes.byref(kb), cand.ctypes.data, ms.ctypes.data),
+               "pf_multi_tuning")
+        return {"kb": kb.value, "ms": {int(c): float(m) for c, m in zip(cand, ms) if c}}
 
     def centroid_stress(self, x, iel: int = 1):
         x, px = _arr(x, np.float64)
