@@ -11,8 +11,13 @@
 //
 // The array holds PF_NOALLOC_MAX_NELS elements and PF_NOALLOC_MAX_NEQ
 // equations (about 14.3 MiB).  Every GPU that loads libpfgpu.so keeps it
-// until the process exits.  All calls share it: calls that overlap on the GPU
-// (from two host threads, or on two streams) race on it and must not be made.
+// until the process exits; with CUDA's lazy module loading the device memory
+// is taken when the first call on a device looks the array up, so a caller
+// makes that first call (a set-up-only call with *nels = 0 does just that)
+// before it reserves the rest of device memory.  All calls share the array:
+// calls that overlap on the GPU (from two host threads, or on two streams)
+// race on it and must not be made.  A call runs on the legacy default stream
+// and waits for the whole device before it returns.
 #include "pfgpu.h"
 
 #include <cuda_runtime.h>
@@ -131,8 +136,11 @@ __global__ void k_na_fill(int nels, int neq, const int *__restrict__ g_g, Noallo
 
 // Per equation: sort the bucket by (element, local dof) and sum in that
 // order -- the order of the serial SCATTER (gather_scatter.f90:694-854).
+// Writes nothing when k_na_elem found a g_g entry out of range, so the
+// caller's u survives a failed call.
 __global__ void k_na_gather(int neq, NoallocScratch *S, double *__restrict__ u)
 {
+    if (S->err) return;   // written by k_na_elem, earlier on the same stream
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < neq; q += gridDim.x * blockDim.x) {
         const int b = S->ptr[q], e = S->ptr[q + 1];
         int *L = S->list;
@@ -179,24 +187,31 @@ int scratch_for_current_device(NoallocScratch **out)
     return 0;
 }
 
-bool is_device_pointer(const void *p)
+// Device memory of device dev (the scratch belongs to the current device),
+// or managed memory.
+bool is_device_pointer(const void *p, int dev)
 {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    return (a.type == cudaMemoryTypeDevice && a.device == dev) || a.type == cudaMemoryTypeManaged;
 }
 
 }  // namespace
 
 // u(neq) = K p over the elements of g_g, all buffers on the current device.
-// The first call on each device looks up the scratch array's address; make
-// that first call before capturing any stream.
+// The first call on each device looks up the scratch array's address (and so
+// loads it); make that first call during set-up and before capturing any
+// stream.  *nels = *neq = 0 does only that set-up.
 extern "C" int pf_ebe_matvec_noalloc(const int *nels_p, const int *neq_p, const double *d_storkm,
                                      const int *d_g_g, const double *d_p, double *d_u)
 {
+    if (nels_p && neq_p && *nels_p == 0 && *neq_p == 0) {   // set-up only
+        NoallocScratch *S = nullptr;
+        return scratch_for_current_device(&S) ? PF_FAILURE : PF_SUCCESS;
+    }
     if (!nels_p || !neq_p || !d_storkm || !d_g_g || !d_p || !d_u) {
         set_error("pf_ebe_matvec_noalloc: null argument");
         return PF_FAILURE;
@@ -208,9 +223,14 @@ extern "C" int pf_ebe_matvec_noalloc(const int *nels_p, const int *neq_p, const 
                   nels, neq, PF_NOALLOC_MAX_NELS, PF_NOALLOC_MAX_NEQ);
         return PF_FAILURE;
     }
-    if (!is_device_pointer(d_storkm) || !is_device_pointer(d_g_g) || !is_device_pointer(d_p) ||
-        !is_device_pointer(d_u)) {
-        set_error("pf_ebe_matvec_noalloc: storkm, g_g, p and u must be device pointers");
+    int cur = 0;
+    if (cudaGetDevice(&cur) != cudaSuccess) {
+        set_error("pf_ebe_matvec_noalloc: no current device");
+        return PF_FAILURE;
+    }
+    if (!is_device_pointer(d_storkm, cur) || !is_device_pointer(d_g_g, cur) || !is_device_pointer(d_p, cur) ||
+        !is_device_pointer(d_u, cur)) {
+        set_error("pf_ebe_matvec_noalloc: storkm, g_g, p and u must be memory of the current device %d", cur);
         return PF_FAILURE;
     }
     NoallocScratch *S = nullptr;
@@ -239,7 +259,7 @@ extern "C" int pf_ebe_matvec_noalloc(const int *nels_p, const int *neq_p, const 
         return PF_FAILURE;
     }
     if (err) {
-        set_error("pf_ebe_matvec_noalloc: g_g holds an equation number outside 0..%d", neq);
+        set_error("pf_ebe_matvec_noalloc: g_g holds an equation number outside 0..%d (u left unchanged)", neq);
         return PF_FAILURE;
     }
     return PF_SUCCESS;

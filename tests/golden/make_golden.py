@@ -136,6 +136,8 @@ def main122(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
-    main123(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
-    main122(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/parafem")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <root of the ParaFEM tree (the directory holding examples/)>")
+    main(sys.argv[1])
+    main123(sys.argv[1])
+    main122(sys.argv[1])

@@ -73,3 +73,37 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     dummy = ctypes.c_void_p(1)
     rc = L.pf_ebe_matvec_noalloc(_i(16385), _i(1000), dummy, dummy, dummy, dummy)
     assert rc == 1 and "scratch limits" in P.last_error()
+
+
+def test_noalloc_takes_no_device_memory_per_call_and_keeps_u_on_failure():
+    """After the set-up call, calls change the device's free memory by
+    nothing; a g_g entry out of range fails the call and leaves u as it was."""
+    torch = pytest.importorskip("torch")
+    L = P.lib()
+    torch.cuda.mem_get_info(0)   # the runtime context exists before the measurements
+    assert L.pf_ebe_matvec_noalloc(_i(0), _i(0), None, None, None, None) == 0, P.last_error()
+    prob = P.cube_problem(3, 3, 3)
+    nels, neq = prob["g_num"].shape[0], prob["neq"]
+    rng = np.random.default_rng(12)
+    km = rng.standard_normal((nels, 60, 60))
+    g_g = prob["g_g"].astype(np.int32)
+    bufs = [DeviceBuffer(km), DeviceBuffer(g_g), DeviceBuffer(rng.standard_normal(neq)),
+            DeviceBuffer(np.full(neq, 7.0))]
+    d_km, d_gg, d_p, d_u = bufs
+    try:
+        free0, _ = torch.cuda.mem_get_info(0)
+        for _ in range(2):
+            assert L.pf_ebe_matvec_noalloc(_i(nels), _i(neq), d_km.ptr, d_gg.ptr, d_p.ptr, d_u.ptr) == 0
+        free1, _ = torch.cuda.mem_get_info(0)
+        assert free1 == free0
+        good = d_u.read()
+        bad = g_g.copy()
+        bad[0, 0] = neq + 5
+        d_bad = DeviceBuffer(bad)
+        bufs.append(d_bad)
+        rc = L.pf_ebe_matvec_noalloc(_i(nels), _i(neq), d_km.ptr, d_bad.ptr, d_p.ptr, d_u.ptr)
+        assert rc == 1 and "outside 0.." in P.last_error()
+        assert np.array_equal(d_u.read(), good)
+    finally:
+        for b in bufs:
+            b.free()
