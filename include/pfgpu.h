@@ -262,6 +262,10 @@ int pf_ebe_matvec_multi(void **ctx, const int *k, const int *prec, const double 
  * (0 = unused) and ms[4] one full product with each (0 when only one width
  * was possible). */
 int pf_multi_tuning(void **ctx, int *kb, int *cand, float *ms);
+/* Device time (CUDA events, ms per product, averaged over *reps after one
+ * warm-up) of the tensor-core block product U = K P for the k columns of p
+ * ((neq, k) column-major), with P resident on the device. */
+int pf_multi_product_ms(void **ctx, const int *k, const double *p, const int *reps, double *ms);
 /* Releases the context's block-solve buffers (allocated by the first
  * pf_solve_multi or pf_ebe_matvec_multi; also released with the mesh and by
  * pf_ctx_destroy). */
@@ -312,8 +316,14 @@ int pf_batch_launches(void **batch, long long *count);
  * scratch is a fixed array inside libpfgpu.so (about 14.3 MiB, held on every
  * device that loads the library until exit) that limits nels <= 16384 and
  * neq <= 262144; larger sizes are rejected.  The first call on a device looks
- * the array up and should come before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race and must not be made. */
+ * the array up, which (under CUDA's lazy module loading) is also when its
+ * device memory is taken: make that first call during set-up, before the
+ * caller reserves the rest of device memory and before any stream capture; a
+ * call with *nels = *neq = 0 does only this set-up.  Each call runs on the
+ * legacy default stream and waits for the whole device before it returns.
+ * If g_g holds an equation number outside 0..neq the call fails and leaves u
+ * unchanged.  All calls share the array: calls that overlap on the GPU race
+ * and must not be made. */
 int pf_ebe_matvec_noalloc(const int *nels, const int *neq, const double *storkm,
                           const int *g_g, const double *p, double *u);
 

@@ -13,9 +13,9 @@
 //                  significant bits, scaled per element by a power of two)
 //                  stored in the tensor cores' shared-memory tile layout;
 //                  P_e less a translation of each case is split the same way
-//                  per element and case.  The three products of order
-//                  <= 2^-11 (hi.hi, hi.lo, lo.hi) are summed: the block
-//                  product reaches FP32-class accuracy.  Cases are taken in
+//                  per element and case.  The four products of the two
+//                  splits are summed: the block product reaches FP32-class
+//                  accuracy.  Cases are taken in
 //                  passes of 64, 32, 16 or 8 (the MMA's N is twice that),
 //                  the widest pass chosen by timing on the mesh.
 //   k_mr_elem_cc   the same product on CUDA cores in FP32 (check kernel for
@@ -44,66 +44,68 @@ constexpr int kMaxKB = 64;           // cases of one tensor-core pass (the MMA's
 constexpr unsigned kFullMask = 0xffffffffu;
 
 // ---- the stored element record of the tensor-core product -----------------
-// A tile (M = 64 rows, K = 64 columns, FP16, K-major, no swizzle): 8 x 8 core
-// matrices of 8 rows x 16 bytes, core matrix (I, J) at 1024 I + 128 J
+// A tile (M = 128 rows, K = 64 columns, FP16, K-major, no swizzle): 16 x 8
+// core matrices of 8 rows x 16 bytes, core matrix (I, J) at 1024 I + 128 J
 // (SBO = 1024 B between row groups, LBO = 128 B between column groups).
-// Rows and columns are ordered by direction: row (column) 20 d + i is dof
-// 3 i + d of the element, i < 20; rows 60 + d hold the direction sums of the
-// stored rows (sum over i of row 3 i + d, for the mean translation of the
-// result); row 63 and columns 60..63 are zero.  K_e is symmetric, so of
-// each term the record keeps the core matrices (I, J) with I <= J, and all
-// of block row 7 (which carries the sum rows): 43 core matrices, the
-// blocks of a block row contiguous, in block-row order.  Then the second
-// term, then 1 / s_e (FP32) and 12 zero bytes: 11,024 bytes per element.
-constexpr int kTileA = 8192;                  // one term of the A tile
-constexpr int kRecTerm = 43 * 128;            // 5504
-constexpr int kRecBytes = 2 * kRecTerm + 16;  // 11024
-
-// stored index of core matrix (I, J) of a term (I <= J, or I == 7)
-__host__ __device__ constexpr int rec_block(int I, int J) { return I < 7 ? 8 * I - I * (I - 1) / 2 + (J - I) : 35 + J; }
+// Rows 0..63 hold the high FP16 term of K_e, rows 64..127 the low term.
+// Within a term, rows and columns are ordered by direction: row (column)
+// 20 d + i is dof 3 i + d of the element, i < 20; rows 60 + d hold the
+// direction sums of the stored rows (sum over i of row 3 i + d, for the mean
+// translation of the result); row 63 and columns 60..63 are zero.  The tile
+// is stored as it sits in shared memory, followed by 1 / s_e (FP32) and 12
+// zero bytes: 16,400 bytes per element, one bulk copy.
+constexpr int kTileA = 8192;                  // one term of the A tile (64 rows)
+constexpr int kRecBytes = 2 * kTileA + 16;    // 16400
+constexpr int kRecStage = 2 * kTileA + 128;   // bytes of one record stage (16,512)
 
 // dof of the element for direction-ordered row or column r < 60
 __host__ __device__ constexpr int dir_dof(int r) { return 3 * (r % 20) + r / 20; }
 
 // ---- pipeline of the tensor-core kernel ------------------------------------
-constexpr int kNTile = 4;            // tile sets (A and B operands, output scales)
 constexpr int kNAcc = 4;             // TMEM accumulators (128 columns each)
 constexpr int kAccCols = 128;
 constexpr int kEpiGroups = 2;        // warps 0-7: two epilogue groups of four warps on alternate elements;
-constexpr int kEpiWarps = 4;         //   warp w reads TMEM lanes 32 (w % 4) .. +15 = rows 16 (w % 4) .. +15
-constexpr int kBldWarp0 = 8;         // warps 8-15: two builder groups of four warps on alternate elements
-constexpr int kBldGroups = 2;
-constexpr int kBldWarps = 4;
-constexpr int kProdWarp = 16;        // warp 16 issues the copies
-constexpr int kMmaWarp = 17;         // warp 17, lane 0 issues the MMAs
-constexpr int kH16Threads = 18 * 32;
-constexpr int kPlaceMoves = 6;       // record rows (16 B) a builder thread places per element: 2 x 43 x 8 / 128
-constexpr int kNodeGroups = 16;      // most node groups of a builder's per-case maxima (128 / kb, kb >= 8)
-constexpr int kRecStage = 11136;     // the record's place in a stage (11,024 bytes, rounded up to 128)
+constexpr int kEpiWarps = 4;         //   warp w reads TMEM lanes 32 (w % 4) .. +31 = rows 32 (w % 4) .. +31
+constexpr int kBldWarp0 = 8;         // warps 8 .. 8 + np - 1 build the B tiles, warp 8 + w the elements
+constexpr int kBldWarps = 8;         //   t = w (mod np), from P stage w into tile set w (np <= 8)
+constexpr int kProdWarp = 16;        // warp 16 copies the element records, warps 17-18 gather P
+constexpr int kGatherWarps = 2;      //   on alternate elements (np even: one warp fills each P stage)
+constexpr int kMaxRec = 12;          // record stages
+constexpr int kMmaWarp = 19;         // warp 19, lane 0 issues the MMAs
+constexpr int kH16Threads = 20 * 32;
+static_assert(kBldWarp0 + kBldWarps == kProdWarp, "warp roles overlap");
 
-// shared-memory plan for kb cases per pass and nst operand stages
+// shared-memory plan for kb cases per pass and nr record stages
 struct Plan {
-    int kb, nst;
-    int stage;     // bytes of one stage: the element record, then P of the 20 nodes
-    int tile;      // bytes of one tile set: A (2 terms), B (2 terms), the per-case output scales
-    int off_tile, off_aux, smem;
+    int kb, nr;
+    int np;        // P stages = tile sets = builder warps
+    int pst;       // bytes of one P stage: P of the 20 nodes, then 1/s_e (16 B)
+    int tile;      // bytes of one tile set: B (2 terms), the per-case output scales
+    int off_p, off_tile, off_aux, smem;
 };
 
-__host__ __device__ inline Plan make_plan(int kb, int nst)
+__host__ __device__ constexpr int plan_np(int kb) { return kb <= 8 ? 8 : kb == 16 ? 6 : kb == 32 ? 4 : 2; }
+static_assert(plan_np(8) % kGatherWarps == 0 && plan_np(16) % kGatherWarps == 0 &&
+                  plan_np(32) % kGatherWarps == 0 && plan_np(64) % kGatherWarps == 0,
+              "each P stage must have one gather warp");
+
+__host__ __device__ inline Plan make_plan(int kb, int nr)
 {
     Plan p;
     p.kb = kb;
-    p.nst = nst;
-    p.stage = kRecStage + 480 * kb;
-    p.tile = 2 * kTileA + 256 * kb + 256;
-    p.off_tile = nst * p.stage;
-    p.off_aux = p.off_tile + kNTile * p.tile;
-    // aux: mbarriers (64 words), tmem slot + flags (64 B), per builder
-    // group the translations (3 x 64 floats), scales (64) and per-case
-    // partial maxima (16 x 64), per epilogue group two sets of sum rows
-    // (2 x 3 x 64)
-    p.smem = p.off_aux + 64 * 8 + 64 + kBldGroups * (4 + kNodeGroups) * kMaxKB * 4 +
-             kEpiGroups * 6 * kMaxKB * 4;
+    p.nr = nr;
+    p.np = plan_np(kb);
+    p.pst = 480 * kb + 128;
+    p.tile = 256 * kb + 256;
+    p.off_p = nr * kRecStage;
+    p.off_tile = p.off_p + p.np * p.pst;
+    p.off_aux = p.off_tile + p.np * p.tile;
+    // aux: mbarriers (64 words), tmem slot, flags and counters (128 B), per
+    // epilogue group two sets of sum rows (2 x 3 x 64 floats)
+    p.smem = p.off_aux + 64 * 8 + 128 + kEpiGroups * 6 * kMaxKB * 4;
+    // at least half the SM's shared memory, so that one CTA holds an SM (its
+    // TMEM allocation takes all 512 columns)
+    if (p.smem < 116 * 1024) p.smem = 116 * 1024;
     return p;
 }
 
@@ -134,8 +136,7 @@ __device__ __forceinline__ void split2_f16(float a, float b, uint32_t &w_hi, uin
 // One 128-thread block per element (grid-stride): s_e = 2^(14 - E) with
 // max |K_e| (and max |direction sum|) < 2^E, the two FP16 terms of every
 // scaled entry, the direction sums of the stored (rounded) rows formed in
-// FP64 from hi + lo and split in turn, then the 43 core matrices of each
-// term.
+// FP64 from hi + lo and split in turn, then the two terms' tiles.
 __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restrict__ km, unsigned char *__restrict__ rec)
 {
     __shared__ uint32_t t2[64 * 64];   // (hi, lo) half pairs of the 64 x 64 tile, row-major
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restr
         for (int q = tid; q < 3 * 60; q += 128) {   // the direction sums must fit FP16 too
             const int d = q / 60, c = q % 60;
             double sum = 0.0;
-            for (int i = 0; i < 20; ++i) sum += ke[60 * dir_dof(c) + 3 * i + d];
+            for (int i = 0; i < 20; ++i) sum += ke[60 * c + 3 * i + d];
             mx = fmax(mx, fabs(sum));
         }
         mx = warp_max(mx);
@@ -161,7 +162,7 @@ __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restr
         for (int q = tid; q < 64 * 64; q += 128) {
             const int r = q / 64, c = q % 64;
             float x = 0.f;
-            if (r < 60 && c < 60) x = (float)(ke[60 * dir_dof(c) + dir_dof(r)] * sc);
+            if (r < 60 && c < 60) x = (float)(ke[60 * c + dir_dof(r)] * sc);
             uint32_t wh, wl;
             split2_f16(x, 0.f, wh, wl);
             t2[q] = (wh & 0xffffu) | (wl << 16);
@@ -181,19 +182,10 @@ __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restr
             t2[(60 + d) * 64 + c] = (wh & 0xffffu) | (wl << 16);
         }
         __syncthreads();
-        // 2 terms x 43 core matrices x 8 rows of 16 bytes
+        // the A tile: 2 terms x 8 x 8 core matrices x 8 rows of 16 bytes
         unsigned char *out = rec + (size_t)e * kRecBytes;
-        for (int q = tid; q < 2 * 43 * 8; q += 128) {
-            const int term = q / (43 * 8), rem = q % (43 * 8), blk = rem / 8, rr = rem % 8;
-            int I, J;
-            if (blk >= 35) {
-                I = 7;
-                J = blk - 35;
-            } else {
-                I = 0;
-                while (I < 6 && rec_block(I + 1, I + 1) <= blk) ++I;
-                J = I + (blk - rec_block(I, I));
-            }
+        for (int q = tid; q < 2 * 64 * 8; q += 128) {
+            const int term = q / 512, rem = q % 512, I = rem / 64, J = (rem / 8) % 8, rr = rem % 8;
             const int row = 8 * I + rr;
             uint32_t w[4];
 #pragma unroll
@@ -201,10 +193,11 @@ __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restr
                 const uint32_t a = t2[row * 64 + 8 * J + 2 * g], b = t2[row * 64 + 8 * J + 2 * g + 1];
                 w[g] = term == 0 ? ((a & 0xffffu) | (b << 16)) : ((a >> 16) | (b & 0xffff0000u));
             }
-            *reinterpret_cast<uint4 *>(out + term * kRecTerm + blk * 128 + rr * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+            *reinterpret_cast<uint4 *>(out + term * kTileA + I * 1024 + J * 128 + rr * 16) =
+                make_uint4(w[0], w[1], w[2], w[3]);
         }
         if (tid == 0) {
-            float *tail = reinterpret_cast<float *>(out + 2 * kRecTerm);
+            float *tail = reinterpret_cast<float *>(out + 2 * kTileA);
             tail[0] = (float)(1.0 / sc);
             tail[1] = tail[2] = tail[3] = 0.f;
         }
@@ -221,76 +214,95 @@ __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restr
 // from the smooth part of P and the product symmetric, as the single-case
 // kernels do).
 //
-// One persistent CTA of 18 warps per SM walks the elements e = blockIdx.x +
-// t * gridDim.x with warp-specialised roles linked by mbarriers:
-//   warp 16     fills a ring of nst stages: the element record by one bulk
-//               copy (cp.async.bulk), and the P rows of the element's 20
+// One persistent CTA of 20 warps per SM walks the elements e = blockIdx.x +
+// t * gridDim.x with warp-specialised roles linked by mbarriers.  The
+// element records, the stream that HBM bounds, have a ring of their own
+// (nr stages) that only the copy warp and the MMA hold, so that most of it
+// is in flight at any time; P and the B tiles have a second ring (np
+// stages, one per builder warp):
+//   warp 16     one thread copies the element record (the A tile of both
+//               terms and 1/s_e) by one bulk copy (cp.async.bulk) into the
+//               record ring;
+//   warps 17-18 on alternate elements gather the P rows of the element's 20
 //               nodes (FP32 high and low parts, kept beside P by the update
 //               kernels) by TMA gathers of four rows each (one row per node
 //               when a pass covers all k cases, else one per node and
-//               direction), counted on the same mbarrier;
-//   warps 8-15  two groups of four warps on alternate elements: place the
-//               record's core matrices in a tile set's A tile, fill its
-//               lower core matrices (I > J, I < 7) as transposes of the
-//               stored ones (ldmatrix.trans + stmatrix), free the stage
-//               once P is read, and build the B tile: per case j a
-//               translation t_j (node 0's value) and a power-of-two scale
-//               s_j, then (P_e - t_j) s_j split into two FP16 terms, the
-//               high term's KB rows followed by the low term's;
-//   warp 17     one thread issues the products into a ring of kNAcc TMEM
-//               accumulators: A_hi x [B_hi | B_lo] (N = 2 KB) and A_lo x B_hi
-//               into the first KB columns, four K-steps each, and commits
-//               them to the accumulator's mbarrier;
+//               direction), and 1/s_e from the record's tail, into the P
+//               ring;
+//   warps 8-15  warp 8 + w (w < np) builds the B tiles of the elements
+//               t = w (mod np) from P stage w into tile set w: per case j a
+//               translation t_j (node 0's value) and a power-of-two scale s_j
+//               (the case's largest |p - t_j| met in warp shuffles), then
+//               (P_e - t_j) s_j split into two FP16 terms, the high term's KB
+//               rows followed by the low term's;
+//   warp 19     one thread issues [A_hi; A_lo] x [B_hi | B_lo] (M = 128,
+//               N = 2 KB, four K-steps, A from the record stage, B from the
+//               tile) into a ring of kNAcc TMEM accumulators and commits them
+//               to mbarriers that free the record stage and fill the
+//               accumulator;
 //   warps 0-7   two groups of four warps on alternate elements read the
-//               accumulator rows back (warp w: rows 16 (w % 4) .. +15 in TMEM
-//               lanes 32 (w % 4) .. +15), add its two halves, subtract a
-//               twentieth of the direction's sum row, undo the scales and
-//               store.
+//               accumulator back (warp w: TMEM lanes 32 (w % 4) .. +31, which
+//               hold row 32 (w % 4) + lane of D), add each row's two column
+//               halves, pass the low-term rows 64..127 through the tile's B
+//               region (the MMA is done with it) to the high-term rows,
+//               subtract a twentieth of the direction's sum row, undo the
+//               scales, store, and free the tile.
+// Each ring is filled by one warp in element order and every barrier is
+// waited on by one thread that passes its phases in turn, so no parity wait
+// can run two phases ahead.
 // Every wait is bounded; where a group of warps meets at a named barrier,
 // one thread waits and the group follows its verdict.  A wait that runs out
 // sets a shared failure flag that every role checks before its next wait,
 // writes 3 to the device error word, and the CTA waits (bounded) for the
 // copies and MMAs it has in flight before it frees its TMEM and returns.
+//
 // tmap: P as 2-D FP64-sized elements, rows of one node (3 KB elements, box
 // 3 KB x 1) when whole != 0, else rows of one slot (k elements, box KB x 1,
 // gathered from column c0).
 template <int KB>
 __global__ void __launch_bounds__(kH16Threads, 1)
-k_mr_elem_h16(int nels, int k, int c0, int nst, const unsigned char *__restrict__ rec,
+k_mr_elem_h16(int nels, int k, int c0, int nr, const unsigned char *__restrict__ rec,
               const int *__restrict__ conn, const __grid_constant__ CUtensorMap tmap, int whole,
               float *__restrict__ ut, int *__restrict__ err, const int *__restrict__ skip)
 {
     constexpr int kb = KB;
     if (skip && *skip) return;   // a residual replacement is pending: nothing to compute
     extern __shared__ __align__(1024) unsigned char sm[];
-    const Plan pl = make_plan(kb, nst);
-    unsigned char *stg = sm;
-    unsigned char *tiles = sm + pl.off_tile;
-    uint64_t *st_full = reinterpret_cast<uint64_t *>(sm + pl.off_aux);
-    uint64_t *st_empty = st_full + 8;
-    uint64_t *tl_full = st_empty + 8;
+    const Plan pl = make_plan(kb, nr);
+    const int np = pl.np;
+    unsigned char *rstg = sm;                  // record stages
+    unsigned char *pstg = sm + pl.off_p;       // P stages
+    unsigned char *tiles = sm + pl.off_tile;   // B tile sets
+    uint64_t *rc_full = reinterpret_cast<uint64_t *>(sm + pl.off_aux);
+    uint64_t *rc_empty = rc_full + kMaxRec;
+    uint64_t *pp_full = rc_empty + kMaxRec;
+    uint64_t *pp_empty = pp_full + 8;
+    uint64_t *tl_full = pp_empty + 8;
     uint64_t *tl_empty = tl_full + 8;
     uint64_t *ac_full = tl_empty + 8;
-    uint64_t *ac_empty = ac_full + 8;
+    uint64_t *ac_empty = ac_full + kNAcc;      // 64 words in all
     uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + pl.off_aux + 64 * 8);
     volatile int *s_fail = reinterpret_cast<volatile int *>(tslot + 1);
-    int *s_count = reinterpret_cast<int *>(tslot + 2);          // [0] elements copied, [1] elements committed
-    volatile int *g_ok = reinterpret_cast<volatile int *>(tslot + 4);   // [role group][element parity]: waits passed
-    float *b_aux = reinterpret_cast<float *>(sm + pl.off_aux + 64 * 8 + 64);   // per builder group, below
-    float *e_aux = b_aux + kBldGroups * (4 + kNodeGroups) * kMaxKB;            // [epi group][parity][d][j]
+    int *s_count = reinterpret_cast<int *>(tslot + 2);          // [1] MMA groups committed
+    volatile int *g_ok = reinterpret_cast<volatile int *>(tslot + 4);     // [epi group][element parity]: waits passed
+    volatile int *r_last = reinterpret_cast<volatile int *>(tslot + 8);   // [record stage]: last element copied in
+    volatile int *p_last = reinterpret_cast<volatile int *>(tslot + 20);  // [P stage]: last element gathered in
+    float *e_aux = reinterpret_cast<float *>(sm + pl.off_aux + 64 * 8 + 128);   // [epi group][parity][d][j]
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nmine = blockIdx.x < nels ? (nels - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     auto elem = [&](int t) { return (int)blockIdx.x + t * (int)gridDim.x; };
 
     if (warp == 0) tmem_alloc(tslot, kNAcc * kAccCols);
     if (tid == 0) {
-        for (int i = 0; i < nst; ++i) {
-            mbar_init(&st_full[i], 1);            // the producer's arrival (with the bytes it expects)
-            mbar_init(&st_empty[i], kBldWarps);   // the four warps of the group that read the stage
+        for (int i = 0; i < nr; ++i) {
+            mbar_init(&rc_full[i], 1);            // the record warp's arrival (with the bytes it expects)
+            mbar_init(&rc_empty[i], 1);           // the MMA's commit (A read)
         }
-        for (int i = 0; i < kNTile; ++i) {
-            mbar_init(&tl_full[i], kBldWarps);    // the four warps of the group that builds the tile
-            mbar_init(&tl_empty[i], kEpiWarps);   // the four epilogue warps that read its scales
+        for (int i = 0; i < np; ++i) {
+            mbar_init(&pp_full[i], 1);            // the gather warp's arrival (with the bytes it expects)
+            mbar_init(&pp_empty[i], 1);           // the builder warp, done reading P
+            mbar_init(&tl_full[i], 1);            // the builder warp, done writing B
+            mbar_init(&tl_empty[i], kEpiWarps);   // the four epilogue warps that used the tile last
         }
         for (int i = 0; i < kNAcc; ++i) {
             mbar_init(&ac_full[i], 1);
@@ -299,7 +311,9 @@ k_mr_elem_h16(int nels, int k, int c0, int nst, const unsigned char *__restrict_
         mbar_fence_init();
         *s_fail = 0;
         s_count[0] = s_count[1] = 0;
-        for (int i = 0; i < 8; ++i) g_ok[i] = 0;
+        for (int i = 0; i < 4; ++i) g_ok[i] = 0;
+        for (int i = 0; i < kMaxRec; ++i) r_last[i] = -1;
+        for (int i = 0; i < 8; ++i) p_last[i] = -1;
     }
     fence_proxy_async();
     tc_fence_before();
@@ -314,227 +328,205 @@ k_mr_elem_h16(int nels, int k, int c0, int nst, const unsigned char *__restrict_
     };
 
     if (warp == kProdWarp) {
-        constexpr int kCD = 8;   // connectivity loaded kCD elements ahead
-        int ndr[kCD];
-#pragma unroll
-        for (int j = 0; j < kCD; ++j) ndr[j] = (lane < 20 && j < nmine) ? conn[(size_t)elem(j) * 20 + lane] : 0;
-        // gathers per element and their rows: whole, lane g < 5 takes nodes
-        // 4g..4g+3; else lane g < 15 takes the node-direction rows r = 4g..4g+3
-        // (node r / 3, direction r % 3)
+        // the element records (A tile, 1/s_e), one bulk copy each, into the
+        // ring of nr record stages
+        if (lane == 0) {
+            for (int t = 0; t < nmine; ++t) {
+                const int r = t % nr;
+                if (t >= nr && !wait(&rc_empty[r], (uint32_t)((t / nr - 1) & 1))) break;
+                mbar_expect_tx(&rc_full[r], kRecBytes);
+                bulk_g2s(rstg + (size_t)r * kRecStage, rec + (size_t)elem(t) * kRecBytes, kRecBytes, &rc_full[r]);
+                r_last[r] = t;   // for the drain after a failure
+            }
+        }
+        __syncwarp();
+    } else if (warp > kProdWarp && warp <= kProdWarp + kGatherWarps) {
+        // gather warp gw takes the elements t = gw (mod 2): the P rows of the
+        // element's 20 nodes (FP32 high and low parts) by TMA gathers of four
+        // rows, and 1/s_e from the record's tail, into P stage t % np.  Whole:
+        // lane g < 5 takes nodes 4g..4g+3; else lane g < 15 takes the
+        // node-direction rows r = 4g..4g+3 (node r / 3, direction r % 3).  Each
+        // lane loads its own rows' nodes, kCD elements ahead.
+        const int gw = warp - kProdWarp - 1;
         const int ngat = whole ? 5 : 15;
         const int rowbytes = whole ? 24 * kb : 8 * kb;
         const uint32_t pbytes = 480 * kb;
-        int issued = 0;
+        auto rows_of = [&](int t) {
+            int4 v = make_int4(0, 0, 0, 0);
+            if (t < nmine && lane < ngat) {
+                const int *ce = conn + (size_t)elem(t) * 20;
+                if (whole) {
+                    v = *reinterpret_cast<const int4 *>(ce + 4 * lane);
+                } else {
+                    const int r = 4 * lane;
+                    v = make_int4(3 * ce[r / 3] + r % 3, 3 * ce[(r + 1) / 3] + (r + 1) % 3,
+                                  3 * ce[(r + 2) / 3] + (r + 2) % 3, 3 * ce[(r + 3) / 3] + (r + 3) % 3);
+                }
+            }
+            return v;
+        };
+        constexpr int kCD = 4;
+        int4 nd[kCD];
+#pragma unroll
+        for (int j = 0; j < kCD; ++j) nd[j] = rows_of(gw + kGatherWarps * j);
         bool stop = false;
-        for (int t0 = 0; t0 < nmine && !stop; t0 += kCD) {
+        for (int t0 = gw; t0 < nmine && !stop; t0 += kGatherWarps * kCD) {
 #pragma unroll
             for (int j = 0; j < kCD; ++j) {
-                const int t = t0 + j;
+                const int t = t0 + kGatherWarps * j;
                 if (t >= nmine) break;
-                const int s = t % nst;
+                const int w = t % np;
                 int ok = 1;
-                if (t >= nst && lane == 0) ok = wait(&st_empty[s], (uint32_t)((t / nst - 1) & 1)) ? 1 : 0;
+                if (t >= np && lane == 0 && !mbar_test(&pp_empty[w], (uint32_t)((t / np - 1) & 1)))
+                    ok = wait(&pp_empty[w], (uint32_t)((t / np - 1) & 1)) ? 1 : 0;
                 if (!__shfl_sync(kFullMask, ok, 0)) {
                     stop = true;
                     break;
                 }
-                unsigned char *dst = stg + (size_t)s * pl.stage;
-                int rows[4];
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int r = 4 * (lane < ngat ? lane : 0) + i;
-                    const int node = __shfl_sync(kFullMask, ndr[j], whole ? r : r / 3);
-                    rows[i] = whole ? node : 3 * node + r % 3;
-                }
-                if (lane == 0) mbar_expect_tx(&st_full[s], kRecBytes + pbytes);
+                if (lane == 0) mbar_expect_tx(&pp_full[w], pbytes + 16);
                 __syncwarp();
-                if (lane == 0) bulk_g2s(dst, rec + (size_t)elem(t) * kRecBytes, kRecBytes, &st_full[s]);
+                unsigned char *dst = pstg + (size_t)w * pl.pst;
                 if (lane < ngat)
-                    tma_gather4(dst + kRecStage + lane * 4 * rowbytes, &tmap, whole ? 0 : c0, rows[0], rows[1],
-                                rows[2], rows[3], &st_full[s]);
-                ndr[j] = (lane < 20 && t + kCD < nmine) ? conn[(size_t)elem(t + kCD) * 20 + lane] : 0;
-                issued = t + 1;
+                    tma_gather4(dst + lane * 4 * rowbytes, &tmap, whole ? 0 : c0, nd[j].x, nd[j].y, nd[j].z, nd[j].w,
+                                &pp_full[w]);
+                if (lane == 31) bulk_g2s(dst + pbytes, rec + (size_t)elem(t) * kRecBytes + 2 * kTileA, 16, &pp_full[w]);
+                nd[j] = rows_of(t + kGatherWarps * kCD);
+                if (lane == 0) p_last[w] = t;   // for the drain after a failure
             }
         }
-        if (lane == 0) s_count[0] = issued;
-    } else if (warp >= kBldWarp0 && warp < kBldWarp0 + kBldGroups * kBldWarps) {
-        // group grp builds the elements t = grp, grp + 2, ...; its 128 threads
-        // synchronise on named barrier 1 + grp
-        const int grp = (warp - kBldWarp0) / kBldWarps, bw = (warp - kBldWarp0) % kBldWarps;
-        const int bt = tid - (kBldWarp0 + grp * kBldWarps) * 32;   // thread of the group (0..127)
-        float *tt = b_aux + grp * (4 + kNodeGroups) * kMaxKB;      // [d][j] translation of case j
-        float *sc = tt + 3 * kMaxKB;                                // [j] scale s_j
-        float *pm = sc + kMaxKB;                                    // [node group][j] partial maxima
-        constexpr int ngr = 128 / kb;                               // node groups
-        const int mj = bt % kb, mg = bt / kb;                       // this thread's case and node group
-        const int bar_id = 1 + grp;
-        // the same for every element: this thread's record rows (16 B) and
-        // their places in the A tile, and this lane's transposed core-matrix rows
-        int pl_src[kPlaceMoves], pl_dst[kPlaceMoves];
-#pragma unroll
-        for (int u = 0; u < kPlaceMoves; ++u) {
-            const int x = bt + 128 * u;
-            pl_src[u] = -1;
-            pl_dst[u] = 0;
-            if (x < 2 * 43 * 8) {
-                const int term = x / (43 * 8), rem = x % (43 * 8), blk = rem / 8, rr = rem % 8;
-                int I = 0, J;
-                if (blk >= 35) {
-                    I = 7;
-                    J = blk - 35;
-                } else {
-                    while (I < 6 && rec_block(I + 1, I + 1) <= blk) ++I;
-                    J = I + (blk - rec_block(I, I));
-                }
-                pl_src[u] = term * kRecTerm + blk * 128 + rr * 16;
-                pl_dst[u] = term * kTileA + I * 1024 + J * 128 + rr * 16;
-            }
-        }
-        int tr_src[3], tr_dst[3];
-#pragma unroll
-        for (int u = 0; u < 3; ++u) {
-            const int g = bw + kBldWarps * u;   // groups of four matrices: 11 over the four warps
-            int m = 4 * g + (lane >> 3);
-            if (m > 41) m = 41;
-            const int term = m / 21, r = m % 21;
-            int I = 1;
-            while (I < 6 && (I + 1) * I / 2 <= r) ++I;   // blocks before row I: I (I - 1) / 2
-            const int J = r - I * (I - 1) / 2;
-            tr_src[u] = g < 11 ? term * kRecTerm + rec_block(J, I) * 128 + (lane & 7) * 16 : -1;
-            tr_dst[u] = term * kTileA + I * 1024 + J * 128 + (lane & 7) * 16;
-        }
-        for (int t = grp; t < nmine; t += kBldGroups) {
-            const int s = t % nst, b = t % kNTile, kk = t / kBldGroups;
-            // one thread waits for the stage and the tile; the group follows its verdict
-            if (bt == 0)
-                g_ok[2 * grp + (kk & 1)] = wait(&st_full[s], (uint32_t)((t / nst) & 1)) &&
-                                           (t < kNTile || wait(&tl_empty[b], (uint32_t)((t / kNTile - 1) & 1)));
-            named_sync(bar_id, kBldWarps * 32);
-            if (!g_ok[2 * grp + (kk & 1)]) break;
-            const unsigned char *R = stg + (size_t)s * pl.stage;                        // the record
-            const float2 *Pe = reinterpret_cast<const float2 *>(R + kRecStage);        // [node][d][j]: hi, lo
-            const float inv_se = *reinterpret_cast<const float *>(R + 2 * kRecTerm);
-            unsigned char *A = tiles + (size_t)b * pl.tile;
-            unsigned char *B = A + 2 * kTileA;
+    } else if (warp >= kBldWarp0 && warp < kBldWarp0 + np) {
+        // Warp w builds the B tiles of the elements t = w (mod np), so that
+        // it alone waits on P stage w and tile set w and passes each of their
+        // mbarrier phases in turn (a parity wait must never run two phases
+        // ahead).  Lane l takes case j = l % kb (kb <= 32;
+        // case 32 c + l of slice c for kb = 64) and the K-column chunks of
+        // eight q = l / kb + L m, so that the lanes of one case meet in
+        // shuffles for the case's largest |p - t_j|.  The K columns are the
+        // element's dofs in their natural order (c = 3 i + d), so column c of
+        // B row j is P row c of the stage: every load is a fixed offset from
+        // the lane's base.
+        constexpr int L = kb >= 32 ? 1 : 32 / kb;   // lanes per case
+        constexpr int NQ = 8 / L;                   // chunks per lane
+        constexpr int NS = kb > 32 ? kb / 32 : 1;   // case slices
+        constexpr bool kRegs = NQ <= 4;             // up to 16 cases: the values stay in registers
+        const int w = warp - kBldWarp0;
+        const int q0 = NS > 1 ? 0 : lane / kb;
+        const bool tail = q0 == L - 1;              // this lane's last chunk holds columns 56..63 (60..63 zero)
+        const int dbase = (2 * q0) % 3;             // direction of column 8 q0
+        for (int t = w; t < nmine; t += np) {
+            const uint32_t ph = (uint32_t)((t / np) & 1);
+            int ok = 1;
+            if (lane == 0 && !(mbar_test(&pp_full[w], ph) & (t < np || mbar_test(&tl_empty[w], ph ^ 1u))))
+                ok = wait(&pp_full[w], ph) && (t < np || wait(&tl_empty[w], ph ^ 1u));
+            if (!__shfl_sync(kFullMask, ok, 0)) break;
+            const unsigned char *S = pstg + (size_t)w * pl.pst;
+            const float2 *Pe = reinterpret_cast<const float2 *>(S);   // [dof][j]: hi, lo
+            const float inv_se = *reinterpret_cast<const float *>(S + 480 * kb);
+            unsigned char *B = tiles + (size_t)w * pl.tile;
             float *oscale = reinterpret_cast<float *>(B + 256 * kb);   // per case: 1 / (s_e s_j)
-            // the record's 2 x 43 core matrices to their places in the A tile
 #pragma unroll
-            for (int u = 0; u < kPlaceMoves; ++u)
-                if (pl_src[u] >= 0)
-                    *reinterpret_cast<uint4 *>(A + pl_dst[u]) = *reinterpret_cast<const uint4 *>(R + pl_src[u]);
-            // lower core matrices: 42 = 2 terms x 21 blocks (I, J), 1 <= I <= 6, J < I, transposed
-            // from the record's (J, I), four per ldmatrix/stmatrix pair (the last group repeats its
-            // final matrix)
+            for (int cs = 0; cs < NS; ++cs) {
+                const int j = NS > 1 ? 32 * cs + lane : lane % kb;
+                // the translation t_j: node 0's value (any translation serves);
+                // u[r] is the one of column 8 q0 + r (mod 3)
+                float t3[3];
 #pragma unroll
-            for (int u = 0; u < 3; ++u)
-                if (tr_src[u] >= 0) {   // uniform over the warp
-                    uint32_t v[4];
-                    ldsm_x4_trans(smem_u32(R + tr_src[u]), v);
-                    stsm_x4(smem_u32(A + tr_dst[u]), v);
-                }
-            // per case j: the translation t_j (node 0's value: any translation
-            // serves) and the largest |p - t_j| over this thread's nodes
-            if (mg < ngr) {
-                float t3[3], mx = 0.f;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) t3[d] = Pe[d * kb + mj].x;
-                for (int a = mg; a < 20; a += ngr)
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        const float2 v = Pe[(a * 3 + d) * kb + mj];
-                        mx = fmaxf(mx, fabsf((v.x - t3[d]) + v.y));
-                    }
-                pm[mg * kMaxKB + mj] = mx;
-                if (mg == 0)
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) tt[d * kMaxKB + mj] = t3[d];
-            }
-            named_sync(bar_id, kBldWarps * 32);
-            // s_j = 2^(14 - E) with max |p - t_j| < 2^E
-            if (bt < kb) {
+                for (int d = 0; d < 3; ++d) t3[d] = Pe[d * kb + j].x;
+                const float u[3] = {dbase == 0 ? t3[0] : dbase == 1 ? t3[1] : t3[2],
+                                    dbase == 0 ? t3[1] : dbase == 1 ? t3[2] : t3[0],
+                                    dbase == 0 ? t3[2] : dbase == 1 ? t3[0] : t3[1]};
+                const float2 *Pj = Pe + (size_t)(8 * q0) * kb + j;
+                // p - t_j at column 8 (q0 + L m) + g (zero past 60)
+                auto val = [&](int m, int g) {
+                    if (m == NQ - 1 && g >= 4 && tail) return 0.f;
+                    const float2 v = Pj[(8 * L * m + g) * kb];
+                    return (v.x - u[(8 * L * m + g) % 3]) + v.y;
+                };
+                float xv[kRegs ? NQ : 1][8];
                 float mx = 0.f;
 #pragma unroll
-                for (int g = 0; g < ngr; ++g) mx = fmaxf(mx, pm[g * kMaxKB + bt]);
+                for (int m = 0; m < NQ; ++m)
+#pragma unroll
+                    for (int g = 0; g < 8; ++g) {
+                        const float x = val(m, g);
+                        if constexpr (kRegs) xv[m][g] = x;
+                        mx = fmaxf(mx, fabsf(x));
+                    }
+#pragma unroll
+                for (int o = kb; o < 32; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(kFullMask, mx, o));
+                // s_j = 2^(14 - E) with max |p - t_j| < 2^E
                 int ex = 0;
                 frexpf(mx, &ex);
                 const float sj = mx > 0.f ? ldexpf(1.f, 14 - ex) : 1.f;
-                sc[bt] = sj;
-                oscale[bt] = inv_se / sj;
-            }
-            named_sync(bar_id, kBldWarps * 32);
-            // B tile: row j (case), K-columns 8q..8q+7 (direction-ordered dofs);
-            // the low term's rows follow the high term's (rows kb + j)
-            for (int x = bt; x < 8 * kb; x += 128) {
-                const int j = x % kb, q = x / kb;
-                const float sj = sc[j];
-                float xv[8];
+                if (q0 == 0) oscale[j] = inv_se / sj;
+                // B tile: row j (case), K-columns 8 q .. 8 q + 7; the low
+                // term's rows follow the high term's (rows kb + j)
 #pragma unroll
-                for (int g = 0; g < 8; ++g) {
-                    const int col = 8 * q + g;
-                    if (col < 60) {
-                        const int d = col / 20, i = col % 20;
-                        const float2 v = Pe[(i * 3 + d) * kb + j];
-                        xv[g] = ((v.x - tt[d * kMaxKB + j]) + v.y) * sj;
-                    } else {
-                        xv[g] = 0.f;
-                    }
+                for (int m = 0; m < NQ; ++m) {
+                    const int q = q0 + L * m;
+                    float x8[8];
+#pragma unroll
+                    for (int g = 0; g < 8; ++g) x8[g] = (kRegs ? xv[kRegs ? m : 0][g] : val(m, g)) * sj;
+                    uint32_t wh[4], wl[4];
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) split2_f16(x8[2 * g], x8[2 * g + 1], wh[g], wl[g]);
+                    const uint32_t off = kmajor_off(j, 8 * q);
+                    *reinterpret_cast<uint4 *>(B + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
+                    *reinterpret_cast<uint4 *>(B + 128 * kb + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
                 }
-                uint32_t wh[4], wl[4];
-#pragma unroll
-                for (int g = 0; g < 4; ++g) split2_f16(xv[2 * g], xv[2 * g + 1], wh[g], wl[g]);
-                const uint32_t off = kmajor_off(j, 8 * q);
-                *reinterpret_cast<uint4 *>(B + off) = make_uint4(wh[0], wh[1], wh[2], wh[3]);
-                *reinterpret_cast<uint4 *>(B + 128 * kb + off) = make_uint4(wl[0], wl[1], wl[2], wl[3]);
             }
-            fence_proxy_async();   // this thread's tile writes -> the tensor cores; its stage reads before refills
-            named_sync(bar_id, kBldWarps * 32);   // the translations, maxima and scales are reused for the next element
+            fence_proxy_async();   // this lane's tile writes -> the tensor cores
+            __syncwarp();
             if (lane == 0) {
-                mbar_arrive(&st_empty[s]);
-                mbar_arrive(&tl_full[b]);
+                mbar_arrive(&pp_empty[w]);   // P read: the stage may be refilled
+                mbar_arrive(&tl_full[w]);
             }
         }
     } else if (warp == kMmaWarp) {
         int t = 0;
         if (lane == 0) {
             // kind::f16 with both operands FP16 (the format is in the instruction descriptor)
-            const uint32_t idesc2 = idesc_f16(64, 2u * kb), idesc1 = idesc_f16(64, (uint32_t)kb);
+            const uint32_t idesc = idesc_f16(128, 2u * kb);
             for (; t < nmine; ++t) {
-                const int b = t % kNTile, a = t % kNAcc;
-                if (!wait(&tl_full[b], (uint32_t)((t / kNTile) & 1))) break;
-                if (t >= kNAcc && !wait(&ac_empty[a], (uint32_t)((t / kNAcc - 1) & 1))) break;
+                const int r = t % nr, b = t % np, a = t % kNAcc;
+                const uint32_t pr = (uint32_t)((t / nr) & 1), pb = (uint32_t)((t / np) & 1),
+                               pa = (uint32_t)((t / kNAcc - 1) & 1);
+                // the three barriers tested at once; the bounded waits only when one is not ready
+                const bool ready = mbar_test(&rc_full[r], pr) & mbar_test(&tl_full[b], pb) &
+                                   (t < kNAcc || mbar_test(&ac_empty[a], pa));
+                if (!ready) {
+                    if (!wait(&rc_full[r], pr)) break;
+                    if (!wait(&tl_full[b], pb)) break;
+                    if (t >= kNAcc && !wait(&ac_empty[a], pa)) break;
+                }
                 tc_fence_after();
-                const uint32_t a0 = smem_u32(tiles + (size_t)b * pl.tile);
-                const uint32_t b0 = a0 + 2 * kTileA;
+                const uint32_t a0 = smem_u32(rstg + (size_t)r * kRecStage);
+                const uint32_t b0 = smem_u32(tiles + (size_t)b * pl.tile);
                 const uint32_t d0 = tmem + (uint32_t)(kAccCols * a);
-                // A_hi x [B_hi | B_lo]: the products of order 1 and 2^-11 side by side
+                // [A_hi; A_lo] x [B_hi | B_lo]: the four products of the two splits
 #pragma unroll
                 for (int ks = 0; ks < 4; ++ks)   // K = 64 in steps of 16 (two core matrices)
-                    mma_bf16(d0, umma_desc(a0 + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024), idesc2,
+                    mma_bf16(d0, umma_desc(a0 + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024), idesc,
                              ks > 0 ? 1u : 0u);
-                // A_lo x B_hi into the first kb columns
-#pragma unroll
-                for (int ks = 0; ks < 4; ++ks)
-                    mma_bf16(d0, umma_desc(a0 + kTileA + ks * 256, 128, 1024), umma_desc(b0 + ks * 256, 128, 1024),
-                             idesc1, 1u);
+                mma_commit(&rc_empty[r]);
                 mma_commit(&ac_full[a]);
             }
             s_count[1] = t;
         }
         __syncwarp();
     } else if (warp < kEpiGroups * kEpiWarps) {
-        // group eg takes the elements t = eg, eg + 2, ...; lanes 0..15 of its
-        // warp q = warp % 4 hold rows 16q..16q+15 (direction-ordered); lanes
-        // 16..31 read TMEM lanes the M = 64 product leaves unused and store
-        // nothing
+        // group eg takes the elements t = eg, eg + 2, ...; lane l of its warp
+        // q = warp % 4 holds row 32q + l of D: rows 0..63 are the high term's
+        // products of the direction-ordered rows, rows 64..127 the low term's
         const int eg = warp / kEpiWarps, q = warp % kEpiWarps, et = tid - eg * kEpiWarps * 32;
-        const int row = lane < 16 ? 16 * q + lane : 64;
+        const int row = 32 * (q & 1) + lane;        // the element row this lane adds into
         const int dn = row < 60 ? row / 20 : 0;
         const int bar_id = 6 + eg;
         for (int t = eg; t < nmine; t += kEpiGroups) {
-            const int a = t % kNAcc, b = t % kNTile, kk = t / kEpiGroups;
-            if (et == 0) g_ok[4 + 2 * eg + (kk & 1)] = wait(&ac_full[a], (uint32_t)((t / kNAcc) & 1));
+            const int a = t % kNAcc, b = t % np, kk = t / kEpiGroups;
+            if (et == 0) g_ok[2 * eg + (kk & 1)] = wait(&ac_full[a], (uint32_t)((t / kNAcc) & 1));
             named_sync(bar_id, kEpiWarps * 32);
-            if (!g_ok[4 + 2 * eg + (kk & 1)]) break;
+            if (!g_ok[2 * eg + (kk & 1)]) break;
             tc_fence_after();
             // 32 columns per load, each load with its wait in one asm statement
             // (the registers are defined only once the wait has returned); the
@@ -565,15 +557,27 @@ k_mr_elem_h16(int nels, int k, int c0, int nst, const unsigned char *__restrict_
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ac_empty[a]);
-            // the sum rows 60..62 sit in lanes 12..14 of the group's warp 3
-            float *es = e_aux + (eg * 2 + (kk & 1)) * 3 * kMaxKB;
-            if (q == 3 && lane >= 12 && lane < 15) {
+            // the low-term rows pass through the tile's B region (64 rows x kb floats)
+            unsigned char *T = tiles + (size_t)b * pl.tile;
+            float *xl = reinterpret_cast<float *>(T);
+            if (q >= 2) {
 #pragma unroll
-                for (int j = 0; j < kb; ++j) es[(lane - 12) * kMaxKB + j] = v[j];
+                for (int j = 0; j < kb; ++j) xl[row * kb + j] = v[j];
             }
             named_sync(bar_id, kEpiWarps * 32);
-            const float *osc = reinterpret_cast<const float *>(tiles + (size_t)b * pl.tile + 2 * kTileA + 256 * kb);
-            if (row < 60) {
+            float *es = e_aux + (eg * 2 + (kk & 1)) * 3 * kMaxKB;
+            if (q < 2) {
+#pragma unroll
+                for (int j = 0; j < kb; ++j) v[j] += xl[row * kb + j];
+                // the sum rows 60..62: lanes 28..30 of warp 1
+                if (q == 1 && lane >= 28 && lane < 31) {
+#pragma unroll
+                    for (int j = 0; j < kb; ++j) es[(lane - 28) * kMaxKB + j] = v[j];
+                }
+            }
+            named_sync(bar_id, kEpiWarps * 32);
+            const float *osc = reinterpret_cast<const float *>(T + 256 * kb);
+            if (q < 2 && row < 60) {
                 float *o = ut + ((size_t)elem(t) * 60 + dir_dof(row)) * k + c0;
 #pragma unroll
                 for (int j4 = 0; j4 < kb; j4 += 4) {
@@ -586,19 +590,27 @@ k_mr_elem_h16(int nels, int k, int c0, int nst, const unsigned char *__restrict_
                 }
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&tl_empty[b]);   // the tile's output scales are read
+            if (lane == 0) mbar_arrive(&tl_empty[b]);   // the tile is free for the next B operand
         }
     }
     __syncthreads();
     if (*s_fail) {
         if (tid == 0) {
             atomicExch(err, 3);
-            // copies issued: elements 0 .. s_count[0]-1; MMA groups committed: 0 .. s_count[1]-1.
-            // Wait (bounded) for the last phase of every stage and accumulator still owed.
-            for (int t = s_count[0] - nst; t < s_count[0]; ++t)
-                if (t >= 0) mbar_wait(&st_full[t % nst], (uint32_t)((t / nst) & 1));
-            for (int t = s_count[1] - kNAcc; t < s_count[1]; ++t)
-                if (t >= 0) mbar_wait(&ac_full[t % kNAcc], (uint32_t)((t / kNAcc) & 1));
+            // Wait (bounded) for the copies and MMAs still in flight: the last
+            // copy into each stage (a stage is refilled only after its
+            // previous copy was consumed) and the last MMA commit (it
+            // completes after every MMA issued before it).
+            for (int i = 0; i < nr; ++i) {
+                const int t = r_last[i];
+                if (t >= 0) mbar_wait(&rc_full[i], (uint32_t)((t / nr) & 1));
+            }
+            for (int i = 0; i < np; ++i) {
+                const int t = p_last[i];
+                if (t >= 0) mbar_wait(&pp_full[i], (uint32_t)((t / np) & 1));
+            }
+            const int tm = s_count[1] - 1;
+            if (tm >= 0) mbar_wait(&ac_full[tm % kNAcc], (uint32_t)((tm / kNAcc) & 1));
         }
         __syncthreads();
     }
@@ -1053,11 +1065,12 @@ static int mr_launched(Ctx &c, const char *name)
     return 0;
 }
 
-// stages that fit the shared memory for kb cases per pass (at most 4)
+// record stages that fit the shared memory beside the P stages and tile sets
+// for kb cases per pass (at most kMaxRec)
 static int mr_stages(int kb)
 {
-    for (int nst = 4; nst >= 2; --nst)
-        if (make_plan(kb, nst).smem <= 227 * 1024) return nst;
+    for (int nr = kMaxRec; nr >= 2; --nr)
+        if (make_plan(kb, nr).smem <= 227 * 1024) return nr;
     return 0;
 }
 
@@ -1118,15 +1131,15 @@ static int mr_tc_pass_t(Ctx &c, int c0, const int *skip)
             return 1;
         m.tm_have |= bit;
     }
-    const int nst = mr_stages(KB);
-    const Plan pl = make_plan(KB, nst);
+    const int nr = mr_stages(KB);
+    const Plan pl = make_plan(KB, nr);
     static thread_local int attr_dev = -1;
     if (attr_dev != c.device) {
         MCK(cudaFuncSetAttribute(k_mr_elem_h16<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
         attr_dev = c.device;
     }
     const int grid = c.nels < c.nsm ? c.nels : c.nsm;
-    k_mr_elem_h16<KB><<<grid, kH16Threads, pl.smem, c.stream>>>(c.nels, m.k, c0, nst, m.rec, c.conn, *tm, whole,
+    k_mr_elem_h16<KB><<<grid, kH16Threads, pl.smem, c.stream>>>(c.nels, m.k, c0, nr, m.rec, c.conn, *tm, whole,
                                                                m.ut32, c.kerr, skip);
     return mr_launched(c, "k_mr_elem_h16");
 }
@@ -1486,6 +1499,46 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k_p, const int *prec, 
     MCK(cudaMemcpyAsync(u, m.eq, (size_t)c.neq * k * 8, cudaMemcpyDeviceToHost, c.stream));
     MCK(cudaStreamSynchronize(c.stream));
     if (mr_kernel_error(c, "pf_ebe_matvec_multi")) return PF_FAILURE;
+    return PF_SUCCESS;
+}
+
+extern "C" int pf_multi_product_ms(void **ctx, const int *k_p, const double *p, const int *reps, double *ms)
+{
+    if (!ctx || !*ctx || !k_p || !p || !reps || !ms || *reps < 1) {
+        set_error("pf_multi_product_ms: null argument or reps < 1");
+        return PF_FAILURE;
+    }
+    Ctx &c = *(Ctx *)*ctx;
+    MCK(cudaSetDevice(c.device));
+    if (mr_check_k("pf_multi_product_ms", *k_p)) return PF_FAILURE;
+    const int k = *k_p;
+    if (!c.have_km || c.shared || c.kind != KIND_SOLID20) {
+        set_error("pf_multi_product_ms: needs per-element 20-node storkm");
+        return PF_FAILURE;
+    }
+    if (mr_alloc(c, k)) return PF_FAILURE;
+    MultiBufs &m = *c.multi;
+    MCK(cudaMemcpyAsync(m.eq, p, (size_t)c.neq * k * 8, cudaMemcpyHostToDevice, c.stream));
+    k_mr_eq_to_slot<<<c.nsm * 8, 256, 0, c.stream>>>(c.nslots, k, c.slot_eq, c.neq, m.eq, m.P);
+    if (mr_launched(c, "k_mr_eq_to_slot")) return PF_FAILURE;
+    k_mr_psplit<<<c.nsm * 8, 256, 0, c.stream>>>((size_t)c.nslots * k, m.P, m.Ps);
+    if (mr_launched(c, "k_mr_psplit")) return PF_FAILURE;
+    if (mr_prepare_tc(c)) return PF_FAILURE;
+    if (mr_tc_product(c, m.kb, nullptr)) return PF_FAILURE;   // warm-up
+    cudaEvent_t a, b;
+    MCK(cudaEventCreate(&a));
+    MCK(cudaEventCreate(&b));
+    MCK(cudaEventRecord(a, c.stream));
+    for (int r = 0; r < *reps; ++r)
+        if (mr_tc_product(c, m.kb, nullptr)) return PF_FAILURE;
+    MCK(cudaEventRecord(b, c.stream));
+    MCK(cudaEventSynchronize(b));
+    float t = 0.f;
+    MCK(cudaEventElapsedTime(&t, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (mr_kernel_error(c, "pf_multi_product_ms")) return PF_FAILURE;
+    *ms = t / *reps;
     return PF_SUCCESS;
 }
 

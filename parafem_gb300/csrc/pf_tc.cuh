@@ -4,7 +4,9 @@
 // three-term split used to reach FP32 accuracy on BF16 tensor cores.
 //
 // Every wait here is bounded: mbar_wait returns false after kSpinLimit polls
-// and the caller records an error and drains what it has in flight.
+// (each poll suspends the thread for at most kSuspendNs nanoseconds, so a
+// wait gives up after about four seconds) and the caller records an error
+// and drains what it has in flight.
 #pragma once
 #include <cstdint>
 
@@ -12,6 +14,7 @@ namespace pf {
 namespace tc {
 
 constexpr long long kSpinLimit = 1LL << 22;   // try_wait polls before giving up
+constexpr uint32_t kSuspendNs = 1000;          // longest suspension of one poll
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -36,7 +39,22 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(kSuspendNs)
+        : "memory");
+    return ok != 0;
+}
+
+// Non-blocking test of the phase with the given parity: independent tests
+// of several barriers overlap their shared-memory round trips.
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
         : "r"(smem_u32(bar)), "r"(parity)

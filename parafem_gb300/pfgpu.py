@@ -73,6 +73,7 @@ _SIGS = {
     "pf_ebe_matvec_multi": [_VPP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_multi_free": [_VPP],
     "pf_multi_tuning": [_VPP, _IP, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_multi_product_ms": [_VPP, _IP, ctypes.c_void_p, _IP, ctypes.c_void_p],
     "pf_batch_create": [_IP, _LLP, _IP, _IP, _VPP],
     "pf_batch_destroy": [_VPP],
     "pf_batch_capacity": [_VPP, _LLP, _LLP],
@@ -402,6 +403,15 @@ class Solver:
         _check(lib().pf_ebe_matvec_multi(self._ref, _i(k), _i(prec), Pf.ctypes.data, U.ctypes.data),
                "pf_ebe_matvec_multi")
         return U
+
+    def multi_product_ms(self, Pm, reps: int = 5) -> float:
+        """Average device time of one tensor-core block product U = K P over
+        the k columns of Pm (resident on the device; CUDA events)."""
+        Pf = np.asfortranarray(Pm, dtype=np.float64)
+        ms = ctypes.c_double(0)
+        _check(lib().pf_multi_product_ms(self._ref, _i(Pf.shape[1]), Pf.ctypes.data, _i(reps), ctypes.byref(ms)),
+               "pf_multi_product_ms")
+        return ms.value
 
     def multi_tuning(self):
         """The tensor-core block product's pass width for the current k and
