@@ -717,7 +717,7 @@ def run_multirhs(args, rank, world, local, dist):
     line = {"metric": METRIC, "value": tc["dof_iter_per_s"], "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
             "ms_per_step": tc["device_s"] * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "bf16x3 tensor-core products, f32 accumulation / f64 vectors and reductions",
+            "dtype": "fp16x2 tensor-core products, f32 accumulation / f64 vectors and reductions",
             "data": "synthetic",
             "config": {"workload": out["workload"], "neq": out["neq"], "cases": 16},
             "multirhs": out}

@@ -84,7 +84,9 @@ struct Plan {
     int off_p, off_tile, off_aux, smem;
 };
 
-__host__ __device__ constexpr int plan_np(int kb) { return kb <= 8 ? 8 : kb == 16 ? 6 : kb == 32 ? 4 : 2; }
+// P stages per pass width: the builders' B tiles cost more than a deeper
+// record ring buys (measured at 8 to 64 cases on GB300)
+__host__ __device__ constexpr int plan_np(int kb) { return kb <= 16 ? 8 : kb == 32 ? 6 : 4; }
 static_assert(plan_np(8) % kGatherWarps == 0 && plan_np(16) % kGatherWarps == 0 &&
                   plan_np(32) % kGatherWarps == 0 && plan_np(64) % kGatherWarps == 0,
               "each P stage must have one gather warp");
