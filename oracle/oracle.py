@@ -193,6 +193,9 @@ def lib():
             L.orc_p122.argtypes = [_I, _I, _PI, _PD, _I, _D, _D, _D, _D, _D, _I, _PD, _I, _I, _D, _D, _PD, _PD,
                                    ctypes.c_void_p]
             L.orc_p122.restype = _I
+            L.orc_p122n.argtypes = [_I, _I, _I, _PI, _PD, _I, _D, _D, _D, _D, _D, _I, _PD, _I, _I, _D, _D,
+                                    ctypes.c_void_p, _I, ctypes.c_void_p, ctypes.c_void_p, _PD, ctypes.c_void_p]
+            L.orc_p122n.restype = _I
             L.orc_invar.argtypes = [_PD, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]
             L.orc_mocouf.argtypes = [_D, _D, _D, _D, _D]
             L.orc_mocouf.restype = _D
@@ -522,4 +525,79 @@ def run_p122(prob, nip, phi, c, psi, e, v, qinc, plasits, cjits, plastol, cjtol,
                        np.ascontiguousarray(prob["g_coord"]), nip, phi, c, psi, e, v, incs, qinc, plasits, cjits,
                        plastol, cjtol, np.ascontiguousarray(prob["ld0"]), out,
                        totd.ctypes.data if keep_totd else None)
+    return out[:n], (totd[:n] if keep_totd else None)
+
+
+def steering_n(g_num, rest):
+    """find_g (src/modules/shared/new_library.f90:3218-3243), which p122 calls
+    after REARRANGE, for bricks of any node count -> g_g (nels, 3 nod),
+    1-based, 0 = restrained.  For freedom k of node l it counts the
+    restrained freedoms of the listed nodes below l and of node l before k:
+    g = 3 l - count - (3 - k), the freedoms numbered in node order.
+    (REARRANGE leaves a restrained flag 0 and makes free ones nonzero, and
+    find_g tests only for 0, so the original flags serve.)"""
+    nels, nod = g_num.shape
+    nn = int(max(g_num.max(), np.asarray(rest)[:, 0].max()))
+    free = np.ones((nn, 3), bool)
+    rest = np.asarray(rest)
+    free[rest[:, 0] - 1] = rest[:, 1:4] != 0
+    eq = np.zeros((nn, 3), np.int64)
+    eq[free] = np.arange(1, int(free.sum()) + 1)
+    return np.ascontiguousarray(eq[g_num - 1].reshape(nels, 3 * nod).astype(np.int32))
+
+
+def fixed_equations(g_num, g_g, node, sense):
+    """find_no: the equation of freedom `sense` (1..3) of each node."""
+    eq = np.zeros(len(node), np.int32)
+    nod = g_num.shape[1]
+    for i, (nd, sn) in enumerate(zip(node, sense)):
+        e, a = np.argwhere(g_num == nd)[0]
+        eq[i] = g_g[e, 3 * a + sn - 1]
+    assert np.all(eq > 0), "a fixed freedom is restrained"
+    return eq
+
+
+def p122_demo_problem(golden_dir):
+    """The p122 demo deck (8-node bricks, 19 fixed freedoms) from its fixtures:
+    dict(g_num, g_coord, g_g, neq, nn, nr, fix_eq, fix_val, mat, qinc, gold,
+    displ)."""
+    import json
+    import os
+    with open(os.path.join(golden_dir, "p122_golden.json")) as f:
+        g = json.load(f)
+    z = np.load(os.path.join(golden_dir, "p122_demo.npz"))
+    tok = g["demo_dat"].replace("'", " ").split()
+    incs = int(tok[15])
+    mat = dict(nip=int(tok[6]), nod=int(tok[7]), phi=float(tok[10]), c=float(tok[11]), psi=float(tok[12]),
+               e=float(tok[13]), v=float(tok[14]), plasits=int(tok[16]), cjits=int(tok[17]),
+               plastol=float(tok[18]), cjtol=float(tok[19]))
+    g_num = np.ascontiguousarray(z["g_num"])
+    g_g = steering_n(g_num, z["rest"])
+    g_coord = np.ascontiguousarray(z["coords"][g_num - 1].transpose(0, 2, 1))
+    fix_eq = fixed_equations(g_num, g_g, z["fix_node"], z["fix_sense"])
+    return dict(g_num=g_num, g_coord=g_coord, g_g=g_g, neq=int(g_g.max()), nn=z["coords"].shape[0],
+                nr=z["rest"].shape[0], coords=z["coords"], rest=z["rest"], matid=z["matid"],
+                fix_node=z["fix_node"], fix_sense=z["fix_sense"], fix_eq=fix_eq,
+                fix_val=np.ascontiguousarray(z["fix_val"], dtype=np.float64), mat=mat,
+                qinc=[float(t) for t in tok[20:20 + incs]], gold=g["demo"], displ=z["displ"], dat=g["demo_dat"])
+
+
+def run_p122n(prob, nip, phi, c, psi, e, v, qinc, plasits, cjits, plastol, cjtol, ld0=None, fix_eq=(),
+              fix_val=(), keep_totd=False):
+    """The p122 solve for bricks of prob["g_num"].shape[1] nodes, with fixed
+    freedoms (1-based equations fix_eq, values fix_val) and optional nodal
+    loads ld0: per increment (totd(1), sigma z, sigma x, sigma y of element 1
+    Gauss point 1, cj iterations, plastic iterations)."""
+    qinc = np.ascontiguousarray(qinc, dtype=np.float64)
+    incs = qinc.size
+    out = np.zeros((incs, 6))
+    totd = np.zeros((incs, prob["neq"])) if keep_totd else None
+    fe = np.ascontiguousarray(fix_eq, dtype=np.int32)
+    fv = np.ascontiguousarray(fix_val, dtype=np.float64)
+    ld = np.ascontiguousarray(ld0, dtype=np.float64) if ld0 is not None else None
+    n = lib().orc_p122n(prob["g_num"].shape[1], prob["g_num"].shape[0], prob["neq"],
+                        np.ascontiguousarray(prob["g_g"]), np.ascontiguousarray(prob["g_coord"]), nip, phi, c, psi,
+                        e, v, incs, qinc, plasits, cjits, plastol, cjtol, ld.ctypes.data if ld is not None else None,
+                        int(fe.size), fe.ctypes.data if fe.size else None, fv.ctypes.data if fv.size else None, out,
+                        totd.ctypes.data if keep_totd else None)
     return out[:n], (totd[:n] if keep_totd else None)

@@ -7,7 +7,11 @@ Reads the reference's own recorded runs (examples/5th_ed/p121, p123) and writes
                         inputs, and sha256 of the demo deck files
   p121_demo_displ.npz   the demo displacement field (p121_demo.ensi.DISPL-000001)
   p123_golden.json      .res figures of the p123 book run and its .mg input
-  p122_golden.json      per-increment .res figures of the p122 book run and its .mg input
+  p122_golden.json      per-increment .res figures of the p122 book and demo runs, the
+                        book's .mg input and the demo's .dat record
+  p122_demo.npz         the p122 demo deck (8-node bricks: connectivity, material
+                        ids, coordinates, restraints, fixed freedoms) and its
+                        ten recorded displacement fields (ensi.DISPL-0000nn)
 The fixtures let the tests run where the reference tree is absent.
 """
 from __future__ import annotations
@@ -125,14 +129,49 @@ def parse_res122(path):
     return out
 
 
+def read_displ(path, nn):
+    """An ensi.DISPL file: 4 header lines, then the x, y and z blocks."""
+    with open(path) as f:
+        lines = f.read().splitlines()[4:]
+    vals = np.array([float(t) for t in lines if t.strip()], dtype=np.float64)
+    return vals.reshape(3, nn).T
+
+
 def main122(root):
     ex = os.path.join(root, "examples", "5th_ed", "p122", "book")
-    gold = {"source": "examples/5th_ed/p122/book of the ParaFEM tree",
+    gold = {"source": "examples/5th_ed/p122/book and demo of the ParaFEM tree",
             "book": parse_res122(os.path.join(ex, "p122.res")),
             "book_mg": open(os.path.join(ex, "p122.mg")).read()}
+    demo = os.path.join(root, "examples", "5th_ed", "p122", "demo", "p122_demo")
+    gold["demo"] = parse_res122(demo + ".res")
+    gold["demo_dat"] = open(demo + ".dat").read()
+    gold["demo_deck_sha256"] = {}
+    for ext in ("dat", "d", "bnd", "fix"):
+        with open(demo + "." + ext, "rb") as f:
+            gold["demo_deck_sha256"][ext] = hashlib.sha256(f.read()).hexdigest()
     with open(os.path.join(HERE, "p122_golden.json"), "w") as f:
         json.dump(gold, f, indent=1, sort_keys=True)
-    print("wrote", os.path.join(HERE, "p122_golden.json"))
+    # the demo deck: .d (nodes; elements "id 3 8 1 n1..n8 matid"), .bnd, .fix
+    tok = gold["demo_dat"].replace("'", " ").split()
+    nels, nn, nr, nod, nfix = int(tok[3]), int(tok[4]), int(tok[5]), int(tok[7]), int(tok[8])
+    incs = int(tok[15])
+    with open(demo + ".d") as f:
+        lines = f.read().splitlines()
+    i = lines.index("*NODES") + 1
+    coords = np.array([[float(t) for t in ln.split()[1:4]] for ln in lines[i:i + nn]])
+    j = lines.index("*ELEMENTS") + 1
+    el = np.array([[int(t) for t in ln.split()] for ln in lines[j:j + nels]], dtype=np.int64)
+    g_num, matid = el[:, 4:4 + nod].astype(np.int32), el[:, 4 + nod].astype(np.int32)
+    rest = np.array([[int(t) for t in ln.split()] for ln in open(demo + ".bnd").read().splitlines()[:nr]],
+                    dtype=np.int32)
+    fx = [ln.split() for ln in open(demo + ".fix").read().splitlines()[:nfix]]
+    fix_node = np.array([int(t[0]) for t in fx], dtype=np.int32)
+    fix_sense = np.array([int(t[1]) for t in fx], dtype=np.int32)
+    fix_val = np.array([float(t[2]) for t in fx])
+    displ = np.stack([read_displ(demo + ".ensi.DISPL-%06d" % k, nn) for k in range(1, incs + 1)])
+    np.savez_compressed(os.path.join(HERE, "p122_demo.npz"), g_num=g_num, matid=matid, coords=coords, rest=rest,
+                        fix_node=fix_node, fix_sense=fix_sense, fix_val=fix_val, displ=displ)
+    print("wrote", os.path.join(HERE, "p122_golden.json"), os.path.join(HERE, "p122_demo.npz"), displ.shape)
 
 
 if __name__ == "__main__":

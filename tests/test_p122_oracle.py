@@ -78,3 +78,52 @@ def test_mohr_coulomb_routines():
     for m in (m1, m2, m3):
         mm = m.reshape(6, 6)
         assert np.array_equal(mm, mm.T)
+
+
+def demo_node_displacements(prob, totd):
+    """Nodal displacements (nn, 3) of an equation vector, 0 at restrained freedoms."""
+    node_eq = np.zeros((prob["nn"], 3), np.int64)
+    for e in range(prob["g_num"].shape[0]):
+        node_eq[prob["g_num"][e] - 1] = prob["g_g"][e].reshape(-1, 3)
+    return np.concatenate([[0.0], totd])[node_eq]
+
+
+def within_printed(x, gold):
+    """x against E12.4 text values: within half a unit in the fourth digit."""
+    ulp = np.where(gold != 0, 10.0 ** (np.floor(np.log10(np.abs(np.where(gold != 0, gold, 1.0)))) - 3), 0.0)
+    return np.abs(x - gold) <= 0.5 * ulp * (1 + 1e-9) + 1e-15
+
+
+def test_oracle_reproduces_p122_demo_run():
+    """The reference's demo run (8-node bricks, 19 fixed freedoms under
+    displacement control, 4 ranks): every increment's .res figures, iteration
+    counts included, and all ten ensi.DISPL fields."""
+    prob = O.p122_demo_problem(GOLDEN_DIR)
+    m, gold = prob["mat"], prob["gold"]
+    assert (prob["nn"], prob["nr"], prob["neq"]) == (gold["nn"], gold["nr"], gold["neq"])
+    out, totd = O.run_p122n(prob, m["nip"], m["phi"], m["c"], m["psi"], m["e"], m["v"], prob["qinc"], m["plasits"],
+                            m["cjits"], m["plastol"], m["cjtol"], fix_eq=prob["fix_eq"], fix_val=prob["fix_val"],
+                            keep_totd=True)
+    assert out.shape[0] == len(gold["increments"]) == 10
+    for k, g in enumerate(gold["increments"]):
+        assert within_printed(out[k, 0], float(g["displacement_text"])), (k, out[k, 0])
+        for j in range(3):
+            assert within_printed(out[k, 1 + j], float(g["stress_text"][j])), (k, j, out[k, 1 + j])
+        assert (out[k, 4], out[k, 5]) == (g["cj_iterations"], g["plastic_iterations"]), k
+        assert np.all(within_printed(demo_node_displacements(prob, totd[k]), prob["displ"][k])), k
+
+
+def test_p122_demo_numbering_is_find_g():
+    """find_g's numbering (freedoms in node order) gives every equation one
+    freedom; 3,636 equations as the reference printed."""
+    prob = O.p122_demo_problem(GOLDEN_DIR)
+    g = prob["g_g"]
+    owners = {}
+    for e in range(g.shape[0]):
+        for a in range(8):
+            for d in range(3):
+                if g[e, 3 * a + d]:
+                    owners.setdefault(int(g[e, 3 * a + d]), set()).add((int(prob["g_num"][e, a]), d))
+    assert sorted(owners) == list(range(1, prob["neq"] + 1))
+    assert all(len(o) == 1 for o in owners.values())
+    assert prob["neq"] == prob["gold"]["neq"] == 3636
