@@ -218,6 +218,17 @@ int pf_get_storkc(void **ctx, const int *first, const int *count, double *storkc
  * (pf_get_diag gives diag(eq) after this call).  pf_form_storkc clears them. */
 int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const double *penalty);
 
+/* ---- 8-node elasticity bricks (p122's demo deck: nod = 8, three freedoms per node) ----
+ * g_num(8,nels), g_g(24,nels) (0 = restrained), g_coord(8,3,nels), the node
+ * order of SHAPE_DER's 8-node brick.  pf_set_material, pf_form_storkm (FP64
+ * storkm(24,24,e) and the Jacobi diagonal), pf_get_storkm, pf_get_diag,
+ * pf_set_fixed, pf_solve (PF_MODE_P121 or PF_MODE_FP64_RES), pf_ebe_matvec
+ * (prec 64) and pf_p122_solve_fixed apply.  Inside a PCG run the product at
+ * a fixed freedom is p * store (pf_set_fixed); the residual f - K x uses the
+ * plain K, as p122 forms r = loads - K x (p122.f90:142-146). */
+int pf_setup_solid8(void **ctx, const int *nels, const int *nn, const int *neq,
+                    const int *g_num, const int *g_g, const double *g_coord);
+
 /* ---- p122: elastic-plastic (Mohr-Coulomb) solid, viscoplastic strain method ----
  * The solve of src/programs/5th_ed/p122/p122.f90:78-225 for 20-node bricks
  * under load control, on a context with storkm formed (pf_form_storkm with
@@ -234,6 +245,21 @@ int pf_p122_solve(void **ctx, const int *nip, const double *phi, const double *c
                   const int *incs, const double *qinc, const int *plasits, const int *cjits,
                   const double *plastol, const double *cjtol, const double *ld0, double *results,
                   double *totd, int *incs_done);
+/* The same solve on a 20-node or an 8-node context (pf_setup_solid8), with
+ * displacement control: nfix fixed freedoms (p122.f90:96-113), equations
+ * fix_eqs(nfix) (1-based) with prescribed values fix_vals(nfix).  Their
+ * diagonal takes the penalty 1e20 and store = the penalised diagonal; on the
+ * first plastic iteration of an increment loads(fix) = store * value *
+ * qinc(iy) and the PCG product there is p * store, after it loads(fix) = 0
+ * and the product is 0 (p122.f90:122-158).  ld0 may be NULL (no loaded
+ * nodes); with both, the first plastic iteration's loads are ld0 * qinc +
+ * bdylds everywhere, as p122 computes them.  Fixed freedoms need an 8-node
+ * context.  The context's diagonal is restored afterwards. */
+int pf_p122_solve_fixed(void **ctx, const int *nip, const double *phi, const double *c, const double *psi,
+                        const int *incs, const double *qinc, const int *plasits, const int *cjits,
+                        const double *plastol, const double *cjtol, const double *ld0, const int *nfix,
+                        const int *fix_eqs, const double *fix_vals, double *results, double *totd,
+                        int *incs_done);
 
 /* Number of kernels this library launched since the context was created. */
 int pf_kernel_launches(void **ctx, long long *count);

@@ -22,7 +22,7 @@ PROGRAMS = [("p121_main.cpp", EXE), ("p123_main.cpp", EXE123), ("p122_main.cpp",
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["pf_kernels.cu", "pf_elem_sym.cu", "pf_elem_h16.cu", "pf_shared.cu", "pf_scalar8.cu",
-                "pf_plastic.cu", "pf_batch.cu", "pf_multi.cu", "pf_abi.cu", "pf_noalloc.cu"]
+                "pf_solid8.cu", "pf_plastic.cu", "pf_batch.cu", "pf_multi.cu", "pf_abi.cu", "pf_noalloc.cu"]
 CXX_SOURCES = ["pf_host.cpp"]
 HEADERS = ["pf_internal.h", "pf_device.cuh", "pf_tc.cuh"]
 

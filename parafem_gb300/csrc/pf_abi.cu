@@ -95,7 +95,8 @@ static void free_mesh(Ctx &c)
     multi_release(c);
     dfree(c.conn); dfree(c.node_ptr); dfree(c.node_list); dfree(c.slot_eq); dfree(c.eq_slot);
     dfree(c.freemask); dfree(c.coord); dfree(c.mat_e); dfree(c.mat_v); dfree(c.km64); dfree(c.km32);
-    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.psplit); dfree(c.km16p);
+    dfree(c.km32p); dfree(c.skm64); dfree(c.skm32); dfree(c.fstore); dfree(c.fscale); dfree(c.psplit);
+    dfree(c.km16p);
     c.km16_ok = false;
     c.mr_ok = false;
     c.shared = false;
@@ -459,7 +460,7 @@ static int setup_mesh(void **ctx, const int *nels_p, const int *nn_p, const int 
         }
 
     c.nels = nels; c.nn = nn; c.neq = neq; c.nslots = ns;
-    c.kind = nod == 8 ? KIND_SCALAR8 : KIND_SOLID20;
+    c.kind = nod == 8 ? (nodof == 1 ? KIND_SCALAR8 : KIND_SOLID8) : KIND_SOLID20;
     long long g = ((long long)ns + 255) / 256;
     if (g > (long long)c.nsm * 8) g = (long long)c.nsm * 8;
     c.G = (int)(g < 1 ? 1 : g);
@@ -471,7 +472,8 @@ static int setup_mesh(void **ctx, const int *nels_p, const int *nn_p, const int 
         dalloc(&c.node_list, ne * nod, "node table") || dalloc(&c.slot_eq, ns, "slot map") ||
         dalloc(&c.eq_slot, neq, "equation map") || dalloc(&c.freemask, nn, "restraint mask") ||
         dalloc(&c.coord, ne * nod * 3, "coordinates") || dalloc(&c.ediag, ne * ntot, "element diagonals") ||
-        (nodof == 1 && dalloc(&c.fstore, ns, "fixed freedoms")) ||
+        (nod == 8 && dalloc(&c.fstore, ns, "fixed freedoms")) ||
+        (c.kind == KIND_SOLID8 && dalloc(&c.fscale, 1, "fixed-freedom factor")) ||
         dalloc(&c.diag, ns, "diag") || dalloc(&c.dinv, ns, "diag") || dalloc(&c.f, ns, "f") ||
         dalloc(&c.x, ns, "x") || dalloc(&c.c, ns, "c") || dalloc(&c.r, ns, "r") || dalloc(&c.d, ns, "d") ||
         dalloc(&c.p, ns, "p") || dalloc(&c.u, ns, "u") || dalloc(&c.rres, ns, "rres") ||
@@ -493,6 +495,10 @@ static int setup_mesh(void **ctx, const int *nels_p, const int *nn_p, const int 
     CK(cudaMemcpyAsync(c.freemask, fm.data(), nn, cudaMemcpyHostToDevice, c.stream));
     CK(cudaMemcpyAsync(c.coord, g_coord, ne * nod * 3 * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     if (c.fstore) CK(cudaMemsetAsync(c.fstore, 0, ns * sizeof(double), c.stream));
+    if (c.fscale) {
+        static const double one = 1.0;
+        CK(cudaMemcpyAsync(c.fscale, &one, sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    }
     CK(cudaMemsetAsync(c.x, 0, ns * sizeof(double), c.stream));
     CK(cudaMemsetAsync(c.f, 0, ns * sizeof(double), c.stream));
     CK(cudaStreamSynchronize(c.stream));
@@ -509,6 +515,12 @@ extern "C" int pf_setup_scalar8(void **ctx, const int *nels, const int *nn, cons
                                 const int *g_g, const double *g_coord)
 {
     return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 8, 1);
+}
+
+extern "C" int pf_setup_solid8(void **ctx, const int *nels, const int *nn, const int *neq, const int *g_num,
+                               const int *g_g, const double *g_coord)
+{
+    return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 8, 3);
 }
 
 extern "C" int pf_form_storkc(void **ctx, const int *nip, const double *kx, const double *ky, const double *kz)
@@ -554,8 +566,8 @@ extern "C" int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const d
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (c.kind != KIND_SCALAR8 || !c.have_km) {
-        set_error("pf_set_fixed: needs a scalar 8-node context with storkc formed");
+    if ((c.kind != KIND_SCALAR8 && c.kind != KIND_SOLID8) || !c.have_km) {
+        set_error("pf_set_fixed: needs an 8-node context with its element matrices formed");
         return PF_FAILURE;
     }
     if (!nfix || *nfix < 0 || (*nfix > 0 && !eqs) || !penalty) {
@@ -618,6 +630,11 @@ extern "C" int pf_set_material(void **ctx, const int *n, const double *e, const 
 static int ensure_storkm(Ctx &c)
 {
     const size_t ne = (size_t)c.nels;
+    if (c.kind == KIND_SOLID8) {   // FP64 storkm(24,24,e) only
+        if (!c.km64 && dalloc(&c.km64, ne * 576, "FP64 storkm")) return 1;
+        drop_graph(c);
+        return 0;
+    }
     if (!c.km64 && dalloc(&c.km64, ne * 3600, "FP64 storkm")) return 1;
     if (!c.km32 && dalloc(&c.km32, ne * 3600, "FP32 storkm")) return 1;
     if (!c.km32p && dalloc(&c.km32p, ne * 1832, "packed FP32 storkm")) return 1;
@@ -633,8 +650,8 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (c.kind != KIND_SOLID20) {
-        set_error("pf_form_storkm: needs a 20-node context (pf_setup)");
+    if (c.kind != KIND_SOLID20 && c.kind != KIND_SOLID8) {
+        set_error("pf_form_storkm: needs an elasticity context (pf_setup or pf_setup_solid8)");
         return PF_FAILURE;
     }
     if (!nip || !flags || (*nip != 8 && *nip != 27)) {
@@ -647,6 +664,14 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
     }
     const bool exact = (*flags & PF_FORM_EXACT_WEIGHTS) != 0;
     TRY(ensure_storkm(c));
+    if (c.kind == KIND_SOLID8) {   // FP64 storkm, the diagonal; fixed freedoms cleared
+        TRY(launch_form_storkm(c, *nip, exact, false));
+        TRY(launch_assemble_diag(c));
+        CK(cudaMemsetAsync(c.fstore, 0, (size_t)c.nslots * sizeof(double), c.stream));
+        TRY(sync(c));
+        c.have_km = true;
+        return PF_SUCCESS;
+    }
     TRY(launch_form_storkm(c, *nip, exact, true));
     TRY(launch_pack_sym32(c));
     TRY(launch_assemble_diag(c));
@@ -764,8 +789,8 @@ extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, dou
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
-    if (c.kind != KIND_SOLID20) {
-        set_error("pf_get_storkm: needs a 20-node context (pf_setup)");
+    if (c.kind != KIND_SOLID20 && c.kind != KIND_SOLID8) {
+        set_error("pf_get_storkm: needs an elasticity context (pf_setup or pf_setup_solid8)");
         return PF_FAILURE;
     }
     if (c.shared) {
@@ -776,7 +801,8 @@ extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, dou
         set_error("pf_get_storkm: invalid range or no storkm");
         return PF_FAILURE;
     }
-    CK(cudaMemcpyAsync(storkm, c.km64 + (size_t)*first * 3600, (size_t)*count * 3600 * sizeof(double),
+    const size_t ke = c.kind == KIND_SOLID8 ? 576 : 3600;
+    CK(cudaMemcpyAsync(storkm, c.km64 + (size_t)*first * ke, (size_t)*count * ke * sizeof(double),
                        cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
@@ -800,8 +826,8 @@ extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, doubl
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
     if (!prec || !p || !u || !c.have_km || (*prec != 64 && *prec != 32 && *prec != 31 && *prec != 16) ||
-        (c.kind == KIND_SCALAR8 && *prec != 64) || (c.shared && *prec == 16)) {
-        set_error("pf_ebe_matvec: invalid arguments or no storkm (8-node scalar contexts: prec 64; "
+        (c.kind != KIND_SOLID20 && *prec != 64) || (c.shared && *prec == 16)) {
+        set_error("pf_ebe_matvec: invalid arguments or no storkm (8-node contexts: prec 64; "
                   "prec 16 needs per-element storkm)");
         return PF_FAILURE;
     }
@@ -896,9 +922,9 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
         set_error("pf_solve: invalid arguments or no storkm");
         return PF_FAILURE;
     }
-    if (c.kind == KIND_SCALAR8 &&
+    if (c.kind != KIND_SOLID20 &&
         (*mode == PF_MODE_MIXED || *mode == PF_MODE_MIXED_RESTART || *mode == PF_MODE_MIXED16)) {
-        set_error("pf_solve: the mixed modes need 20-node elements; 8-node scalar contexts solve in FP64");
+        set_error("pf_solve: the mixed modes need 20-node elements; 8-node contexts solve in FP64");
         return PF_FAILURE;
     }
     if (*mode == PF_MODE_MIXED16 && c.shared) {
@@ -968,9 +994,9 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
     if (!prec || !steps || *steps < 1 || !c.have_km ||
-        (*prec != 32 && *prec != 31 && *prec != 64 && *prec != 16) || (c.kind == KIND_SCALAR8 && *prec != 64) ||
+        (*prec != 32 && *prec != 31 && *prec != 64 && *prec != 16) || (c.kind != KIND_SOLID20 && *prec != 64) ||
         (c.shared && *prec == 16)) {
-        set_error("pf_bench_iterations: invalid arguments or no storkm (8-node scalar contexts: prec 64; "
+        set_error("pf_bench_iterations: invalid arguments or no storkm (8-node contexts: prec 64; "
                   "prec 16 needs per-element storkm)");
         return PF_FAILURE;
     }

@@ -149,6 +149,19 @@ static __device__ __forceinline__ void shape_der20(int l, double xi, double eta,
     }
 }
 
+// SHAPE_DER for one node l of the 8-node brick (new_library.f90:769-793):
+// node signs (xi, eta, zeta) in Smith-Griffiths order, l = 0..7.
+static __device__ __forceinline__ void shape_der8(int l, double xi, double eta, double zeta, double *d)
+{
+    const double sx = (l == 2 || l == 3 || l == 6 || l == 7) ? 1.0 : -1.0;
+    const double se = l >= 4 ? 1.0 : -1.0;
+    const double sz = (l == 1 || l == 2 || l == 5 || l == 6) ? 1.0 : -1.0;
+    const double a = 1.0 + xi * sx, b = 1.0 + eta * se, c = 1.0 + zeta * sz;
+    d[0] = 0.125 * sx * b * c;
+    d[1] = 0.125 * se * a * c;
+    d[2] = 0.125 * sz * a * b;
+}
+
 // DEEMAT nst=6 (new_library.f90:1671-1689): the three distinct entries.
 static __device__ __forceinline__ void deemat3(double e, double v, double &d11, double &d12, double &d44)
 {

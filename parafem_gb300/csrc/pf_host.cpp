@@ -234,7 +234,7 @@ struct Deck {
     int meshgen = 0, partitioner = 0, nels = 0, nn = 0, nr = 0, nip = 0, nod = 0, loaded = 0, limit = 0;
     double e = 0, v = 0, tol = 0;
     std::vector<double> coords;   // (3, nn)
-    std::vector<int> g_num;       // (20, nels)
+    std::vector<int> g_num;       // (nod, nels)
     std::vector<int> rest;        // (4, nr) row-major per node
     std::vector<int> lnode;
     std::vector<double> lval;     // (3, loaded)
@@ -270,9 +270,9 @@ int read_deck(const std::string &job, Deck &D)
     return read_mesh_files(job, D);
 }
 
-// job.d (nodes, 20-node elements), job.bnd and job.lds of a deck whose
-// .dat record is already in D (READ_G_NUM_PP, READ_G_COORD_PP, READ_REST,
-// READ_LOADS of src/modules/mpi/input.f90)
+// job.d (nodes, elements of D.nod = 20 or 8 nodes), job.bnd and job.lds of a
+// deck whose .dat record is already in D (READ_G_NUM_PP, READ_G_COORD_PP,
+// READ_REST, READ_LOADS of src/modules/mpi/input.f90)
 int read_mesh_files(const std::string &job, Deck &D)
 {
     std::ifstream f(job + ".d");
@@ -294,22 +294,26 @@ int read_mesh_files(const std::string &job, Deck &D)
         D.coords[3 * (size_t)i + 2] = to_d(c);
     }
     std::getline(f, line);   // *ELEMENTS
-    D.g_num.assign((size_t)20 * D.nels, 0);
+    const int nod = D.nod;
+    if (nod != 20 && nod != 8) { set_error("%s: %d-node elements are not supported", job.c_str(), nod); return 1; }
+    D.g_num.assign((size_t)nod * D.nels, 0);
     for (int e = 0; e < D.nels; ++e) {
         if (!std::getline(f, line)) { set_error("%s.d: short element list", job.c_str()); return 1; }
         std::istringstream ss(line);
         long long k;
         ss >> k >> k >> k >> k;
-        for (int a = 0; a < 20; ++a) ss >> D.g_num[20 * (size_t)e + a];
+        for (int a = 0; a < nod; ++a) ss >> D.g_num[nod * (size_t)e + a];
         if (!ss) { set_error("%s.d: bad element line %d", job.c_str(), e + 1); return 1; }
     }
-    if (D.meshgen == 2) {   // ABAQUS2SG (new_library.f90:3569-3597)
-        static const int from[20] = {4, 12, 1, 9, 2, 10, 3, 11, 20, 17, 18, 19, 8, 16, 5, 13, 6, 14, 7, 15};
+    if (D.meshgen == 2) {   // ABAQUS2SG (new_library.f90:3569-3627): node i takes file node from[i]
+        static const int from20[20] = {4, 12, 1, 9, 2, 10, 3, 11, 20, 17, 18, 19, 8, 16, 5, 13, 6, 14, 7, 15};
+        static const int from8[8] = {1, 5, 6, 2, 4, 8, 7, 3};
+        const int *from = nod == 20 ? from20 : from8;
         int tmp[20];
         for (int e = 0; e < D.nels; ++e) {
-            int *g = &D.g_num[20 * (size_t)e];
-            std::copy(g, g + 20, tmp);
-            for (int a = 0; a < 20; ++a) g[a] = tmp[from[a] - 1];
+            int *g = &D.g_num[nod * (size_t)e];
+            std::copy(g, g + nod, tmp);
+            for (int a = 0; a < nod; ++a) g[a] = tmp[from[a] - 1];
         }
     }
     std::vector<std::string> tb;
@@ -1192,8 +1196,10 @@ static int p12meshgen_p122(const std::string &job, const std::vector<std::string
 }
 
 // The p122 job (p122.f90:1-233) with the solve on the GPU: reads job.dat
-// (READ_P122, input.f90, and the qinc values that follow), .d, .bnd, .lds;
-// writes job.res and job.ensi.DISPL-0000nn for every increment.
+// (READ_P122, input.f90, and the qinc values that follow), .d (20-node or
+// 8-node hexahedra), .bnd, .lds (loaded nodes) and .fix (fixed freedoms:
+// node, sense, value; READ_FIXED, input.f90:2483-2564); writes job.res and
+// job.ensi.DISPL-0000nn for every increment.
 extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
 {
     if (!job_c || !device) { set_error("pf_p122_run: null argument"); return PF_FAILURE; }
@@ -1224,9 +1230,11 @@ extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
     D.v = to_d(t[14]);
     const int incs = atoi(t[15].c_str()), plasits = atoi(t[16].c_str()), cjits = atoi(t[17].c_str());
     const double plastol = to_d(t[18]), cjtol = to_d(t[19]);
-    if (D.element != "hexahedron" || D.nod != 20 || fixed != 0 || incs < 1 || t.size() < (size_t)20 + incs) {
-        set_error("%s.dat: p122 decks of 20-node hexahedra under load control only (nod=%d, fixed freedoms %d)",
-                  job.c_str(), D.nod, fixed);
+    if (D.element != "hexahedron" || (D.nod != 20 && D.nod != 8) || fixed < 0 || (fixed > 0 && D.nod != 8) ||
+        (fixed == 0 && D.loaded <= 0) || incs < 1 || t.size() < (size_t)20 + incs) {
+        set_error("%s.dat: p122 decks of 20-node hexahedra under load control or 8-node hexahedra under load or "
+                  "displacement control (nod=%d, fixed freedoms %d, loaded nodes %d)",
+                  job.c_str(), D.nod, fixed, D.loaded);
         return PF_FAILURE;
     }
     std::vector<double> qinc(incs);
@@ -1234,16 +1242,44 @@ extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
     if (read_mesh_files(job, D)) return PF_FAILURE;
     std::vector<int> fix;
     if (rest_to_fix(D.nn, D.nr, D.rest.data(), fix)) return PF_FAILURE;
-    std::vector<int> g_g((size_t)60 * D.nels);
-    int neq = 0;
-    if (pf_number_equations(&D.nels, &D.nn, D.g_num.data(), fix.data(), g_g.data(), &neq)) return PF_FAILURE;
-    std::vector<double> gcoord((size_t)60 * D.nels);
-    for (size_t e = 0; e < (size_t)D.nels; ++e)
-        for (int a = 0; a < 20; ++a)
-            for (int d = 0; d < 3; ++d)
-                gcoord[60 * e + a + 20 * d] = D.coords[3 * (size_t)(D.g_num[20 * e + a] - 1) + d];
+    // equations in node order over the free freedoms (find_g, new_library.f90:3218-3243)
     std::vector<int> node_eq;
-    number_nodes(D.nn, fix.data(), node_eq);
+    const int neq = number_nodes(D.nn, fix.data(), node_eq);
+    const int nod = D.nod, ne = 3 * nod;
+    std::vector<int> g_g((size_t)ne * D.nels);
+    std::vector<double> gcoord((size_t)ne * D.nels);
+    for (size_t e = 0; e < (size_t)D.nels; ++e)
+        for (int a = 0; a < nod; ++a) {
+            const int nd = D.g_num[nod * e + a];
+            if (nd < 1 || nd > D.nn) {
+                set_error("%s.d: element %zu names node %d outside 1..%d", job.c_str(), e + 1, nd, D.nn);
+                return PF_FAILURE;
+            }
+            for (int d = 0; d < 3; ++d) {
+                g_g[ne * e + 3 * a + d] = node_eq[(size_t)(nd - 1) * 3 + d];
+                gcoord[ne * e + a + nod * d] = D.coords[3 * (size_t)(nd - 1) + d];
+            }
+        }
+    // fixed freedoms: the equation of freedom `sense` of each node (find_no)
+    std::vector<int> fix_eq(fixed > 0 ? fixed : 1);
+    std::vector<double> fix_val(fixed > 0 ? fixed : 1);
+    if (fixed > 0) {
+        std::vector<std::string> tf;
+        if (!read_tokens(job + ".fix", tf) || tf.size() < (size_t)3 * fixed) {
+            set_error("cannot read %d fixed freedoms from %s.fix", fixed, job.c_str());
+            return PF_FAILURE;
+        }
+        for (int i = 0; i < fixed; ++i) {
+            const int nd = atoi(tf[3 * (size_t)i].c_str()), sense = atoi(tf[3 * (size_t)i + 1].c_str());
+            if (nd < 1 || nd > D.nn || sense < 1 || sense > 3 || node_eq[(size_t)(nd - 1) * 3 + sense - 1] == 0) {
+                set_error("%s.fix: line %d: node %d freedom %d is not a free freedom", job.c_str(), i + 1, nd,
+                          sense);
+                return PF_FAILURE;
+            }
+            fix_eq[i] = node_eq[(size_t)(nd - 1) * 3 + sense - 1];
+            fix_val[i] = to_d(tf[3 * (size_t)i + 2]);
+        }
+    }
     std::vector<double> ld0(neq > 0 ? neq : 1, 0.0);
     {   // LOAD + SCATTER_NOADD (loading.f90:36-146): assignment, the last node entry wins
         std::vector<int> node_slot((size_t)D.nn + 1, -1);
@@ -1264,13 +1300,17 @@ extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
     double t_setup = 0.0;
     do {
         if (pf_ctx_create(device, &ctx)) break;
-        if (pf_setup(&ctx, &D.nels, &D.nn, &neq, D.g_num.data(), g_g.data(), gcoord.data())) break;
+        int nq = neq;
+        if (nod == 8 ? pf_setup_solid8(&ctx, &D.nels, &D.nn, &nq, D.g_num.data(), g_g.data(), gcoord.data())
+                     : pf_setup(&ctx, &D.nels, &D.nn, &nq, D.g_num.data(), g_g.data(), gcoord.data()))
+            break;
         if (pf_set_material(&ctx, &one, &D.e, &D.v)) break;
         if (pf_form_storkm(&ctx, &D.nip, &flags)) break;
         t_setup = secs(t0);
         int incs_i = incs;
-        if (pf_p122_solve(&ctx, &D.nip, &phi, &coh, &psi, &incs_i, qinc.data(), &plasits, &cjits, &plastol, &cjtol,
-                          ld0.data(), res.data(), totd.data(), &done))
+        if (pf_p122_solve_fixed(&ctx, &D.nip, &phi, &coh, &psi, &incs_i, qinc.data(), &plasits, &cjits, &plastol,
+                                &cjtol, D.loaded > 0 ? ld0.data() : nullptr, &fixed, fix_eq.data(), fix_val.data(),
+                                res.data(), totd.data(), &done))
             break;
         rc = PF_SUCCESS;
     } while (0);

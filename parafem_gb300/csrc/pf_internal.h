@@ -47,7 +47,8 @@ struct PcgState {
 enum { STOP_CHECON = 0, STOP_RELRES = 1 };
 constexpr int kPersistSlots = 8;   // persistent-kernel instantiations, one barrier counter and grid each
 constexpr int kBarWords = 16;      // u64 words per counter (one 128-byte line each)
-enum { KIND_SOLID20 = 0, KIND_SCALAR8 = 1 };   // 20-node elasticity (p121), 8-node scalar (p123)
+// 20-node elasticity (p121), 8-node scalar (p123), 8-node elasticity (p122's demo)
+enum { KIND_SOLID20 = 0, KIND_SCALAR8 = 1, KIND_SOLID8 = 2 };
 
 struct Ctx {
     int device = 0;
@@ -90,8 +91,9 @@ struct Ctx {
     double *it_xsol = nullptr;
     long long it_launches = 0;  // kernels in one replay
     bool use_graphs = true;
-    int kind = 0;               // KIND_SOLID20 (p121) or KIND_SCALAR8 (p123)
-    double *fstore = nullptr;   // [nn] KIND_SCALAR8: penalty store of fixed freedoms, 0 = free
+    int kind = 0;               // KIND_SOLID20 (p121), KIND_SCALAR8 (p123) or KIND_SOLID8
+    double *fstore = nullptr;   // [nslots] 8-node kinds: penalty store of fixed freedoms, 0 = free
+    double *fscale = nullptr;   // [1] KIND_SOLID8: the PCG product at a fixed freedom is p * store * fscale
     // one element matrix shared by every element (PCG_KM); per-element storkm unused
     bool shared = false;
     double *skm64 = nullptr;    // [3600] column-major
@@ -191,6 +193,9 @@ int launch_elem8(Ctx &c, const double *p, const PcgState *st);
 int launch_scatter1(Ctx &c, int mode, const double *xin, const double *pf, double *out, const PcgState *st);
 int launch_assemble_diag1(Ctx &c);
 int launch_set_fixed(Ctx &c, int nfix, const int *slots_dev, double penalty);
+// pf_solid8.cu: 8-node elasticity bricks (24 freedoms per element), FP64
+int launch_elem24(Ctx &c, const double *p, const PcgState *st);
+int launch_scatter3_fixed(Ctx &c, const double *p, double *out, const PcgState *st);
 int launch_shared_ediag(Ctx &c);
 void set_sym_config(Ctx &c, int idx);           // 0: 14 warps x 2 stages, 1: 12 x 2, 2: 8 x 3
 int launch_matvec_generic(int n_mat, int n_row, int n_col, const double *lhs,

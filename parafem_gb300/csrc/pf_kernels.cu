@@ -86,34 +86,38 @@ __global__ void k_sample(int nip, int exact, double *gp)
 // blocks (a, b) and (b, a) = (a, b)'.  GB300's FP64 rate is about 1/60 of its
 // FP32 rate; this order needs about 64k FP64 operations per element at
 // nip = 27 instead of the 486k of a per-point B'DB.
+// The same for 8-node bricks (NOD = 8: 36 node pairs, 24 x 24 storkm).
 constexpr int kFormThreads = 224;
+template <int NOD>
 __global__ void __launch_bounds__(kFormThreads)
 k_form_storkm(int nels, int nip, const double *__restrict__ gp, const double *__restrict__ coord,
               const double *__restrict__ me, const double *__restrict__ mv, int nmat,
               double *__restrict__ km64, float *__restrict__ km32, double *__restrict__ ediag)
 {
-    __shared__ double s_der[27][60];   // der(3,20) at each point
+    constexpr int NE = 3 * NOD, NP = NOD * (NOD + 1) / 2;
+    __shared__ double s_der[27][NE];   // der(3,NOD) at each point
     __shared__ double s_w[27];
-    __shared__ double s_coord[60];     // coord(20,3)
+    __shared__ double s_coord[NE];     // coord(NOD,3)
     __shared__ double s_jac[27][9];    // jac, then its inverse
     __shared__ double s_wd[27];        // det * w
-    __shared__ double s_g[27][60];     // deriv(3,20) = jac^-1 der
-    __shared__ double s_h[27][60];     // det * w * deriv
+    __shared__ double s_g[27][NE];     // deriv(3,NOD) = jac^-1 der
+    __shared__ double s_h[27][NE];     // det * w * deriv
     __shared__ double s_D[3];
     const int t = threadIdx.x;
-    for (int k = t; k < nip * 20; k += kFormThreads) {
-        const int ig = k / 20, l = k % 20;
-        shape_der20(l, gp[4 * ig], gp[4 * ig + 1], gp[4 * ig + 2], &s_der[ig][3 * l]);
+    for (int k = t; k < nip * NOD; k += kFormThreads) {
+        const int ig = k / NOD, l = k % NOD;
+        if constexpr (NOD == 20) shape_der20(l, gp[4 * ig], gp[4 * ig + 1], gp[4 * ig + 2], &s_der[ig][3 * l]);
+        else shape_der8(l, gp[4 * ig], gp[4 * ig + 1], gp[4 * ig + 2], &s_der[ig][3 * l]);
         if (l == 0) s_w[ig] = gp[4 * ig + 3];
     }
     // this thread's node pair: t = b(b+1)/2 + a, a <= b
     int pa = 0, pb = 0;
-    if (t < 210) {
+    if (t < NP) {
         while ((pb + 1) * (pb + 2) / 2 <= t) ++pb;
         pa = t - pb * (pb + 1) / 2;
     }
     for (int e = blockIdx.x; e < nels; e += gridDim.x) {
-        if (t < 60) s_coord[t] = coord[(size_t)e * 60 + t];
+        if (t < NE) s_coord[t] = coord[(size_t)e * NE + t];
         if (t == 0) {
             const int m = nmat == 1 ? 0 : e;
             deemat3(me[m], mv[m], s_D[0], s_D[1], s_D[2]);
@@ -122,21 +126,21 @@ k_form_storkm(int nels, int nip, const double *__restrict__ gp, const double *__
         for (int k = t; k < nip * 9; k += kFormThreads) {   // jac = MATMUL(der, coord)
             const int ig = k / 9, a = k % 3, b = (k / 3) % 3;
             double s = 0.0;
-            for (int n = 0; n < 20; ++n) s += s_der[ig][a + 3 * n] * s_coord[n + 20 * b];
+            for (int n = 0; n < NOD; ++n) s += s_der[ig][a + 3 * n] * s_coord[n + NOD * b];
             s_jac[ig][a + 3 * b] = s;
         }
         __syncthreads();
         if (t < nip) s_wd[t] = det_invert3(s_jac[t]) * s_w[t];
         __syncthreads();
-        for (int k = t; k < nip * 60; k += kFormThreads) {   // deriv = MATMUL(jac^-1, der)
-            const int ig = k / 60, a = k % 3, l = (k / 3) % 20;
+        for (int k = t; k < nip * NE; k += kFormThreads) {   // deriv = MATMUL(jac^-1, der)
+            const int ig = k / NE, a = k % 3, l = (k / 3) % NOD;
             const double *j = s_jac[ig];
             const double g = j[a] * s_der[ig][3 * l] + j[a + 3] * s_der[ig][1 + 3 * l] + j[a + 6] * s_der[ig][2 + 3 * l];
             s_g[ig][a + 3 * l] = g;
             s_h[ig][a + 3 * l] = s_wd[ig] * g;
         }
         __syncthreads();
-        if (t < 210) {
+        if (t < NP) {
             double M[9];
 #pragma unroll
             for (int k = 0; k < 9; ++k) M[k] = 0.0;
@@ -160,14 +164,14 @@ k_form_storkm(int nels, int nip, const double *__restrict__ gp, const double *__
                         K[i + 3 * j] = D12 * M[i + 3 * j] + D44 * M[j + 3 * i];
                     }
                 }
-            double *ke = km64 ? km64 + (size_t)e * 3600 : nullptr;
-            float *kf = km32 ? km32 + (size_t)e * 3600 : nullptr;
+            double *ke = km64 ? km64 + (size_t)e * NE * NE : nullptr;
+            float *kf = km32 ? km32 + (size_t)e * NE * NE : nullptr;
 #pragma unroll
             for (int j = 0; j < 3; ++j)
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
                     const double v = K[i + 3 * j];
-                    const int ab = (3 * pb + j) * 60 + 3 * pa + i, ba = (3 * pa + i) * 60 + 3 * pb + j;
+                    const int ab = (3 * pb + j) * NE + 3 * pa + i, ba = (3 * pa + i) * NE + 3 * pb + j;
                     if (ke) {
                         ke[ab] = v;
                         if (pa != pb) ke[ba] = v;
@@ -176,7 +180,7 @@ k_form_storkm(int nels, int nip, const double *__restrict__ gp, const double *__
                         kf[ab] = (float)v;
                         if (pa != pb) kf[ba] = (float)v;
                     }
-                    if (pa == pb && i == j) ediag[(size_t)e * 60 + 3 * pa + i] = v;
+                    if (pa == pb && i == j) ediag[(size_t)e * NE + 3 * pa + i] = v;
                 }
         }
         __syncthreads();
@@ -805,8 +809,12 @@ int launch_form_storkm(Ctx &c, int nip, bool exact_weights, bool keep32)
     k_sample<<<1, 1, 0, c.stream>>>(nip, exact_weights ? 1 : 0, gp);
     if (check_launch(c, "k_sample")) return 1;
     const int grid = c.nels < c.nsm * 16 ? c.nels : c.nsm * 16;
-    k_form_storkm<<<grid, kFormThreads, 0, c.stream>>>(c.nels, nip, gp, c.coord, c.mat_e, c.mat_v, c.nmat,
-                                                       c.km64, keep32 ? c.km32 : nullptr, c.ediag);
+    if (c.kind == KIND_SOLID8)
+        k_form_storkm<8><<<grid, kFormThreads, 0, c.stream>>>(c.nels, nip, gp, c.coord, c.mat_e, c.mat_v, c.nmat,
+                                                              c.km64, nullptr, c.ediag);
+    else
+        k_form_storkm<20><<<grid, kFormThreads, 0, c.stream>>>(c.nels, nip, gp, c.coord, c.mat_e, c.mat_v, c.nmat,
+                                                               c.km64, keep32 ? c.km32 : nullptr, c.ediag);
     if (check_launch(c, "k_form_storkm")) return 1;
     cudaFreeAsync(gp, c.stream);
     return 0;
@@ -828,7 +836,7 @@ int launch_form_storkm_raw(cudaStream_t stream, int nsm, int nels, int nip, cons
                            float *km32, double *ediag)
 {
     const int grid = nels < nsm * 16 ? nels : nsm * 16;
-    k_form_storkm<<<grid, kFormThreads, 0, stream>>>(nels, nip, gp, coord, me, mv, nmat, km64, km32, ediag);
+    k_form_storkm<20><<<grid, kFormThreads, 0, stream>>>(nels, nip, gp, coord, me, mv, nmat, km64, km32, ediag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_error("k_form_storkm: launch failed: %s", cudaGetErrorString(e));
@@ -869,6 +877,7 @@ int launch_slot_to_eq(Ctx &c, const double *slot, double *eq)
 int launch_elem(Ctx &c, int prec, const double *p)
 {
     if (c.kind == KIND_SCALAR8) return launch_elem8(c, p, c.st);
+    if (c.kind == KIND_SOLID8) return launch_elem24(c, p, c.st);
     if (c.shared) return launch_elem_shared(c, prec, p, c.st);
     if (prec == PREC_FP32_SYM) return launch_elem_sym32(c, p, c.st);
     if (prec == PREC_FP16_SYM) return launch_elem_sym16(c, p, c.st);
@@ -884,6 +893,7 @@ int launch_elem(Ctx &c, int prec, const double *p)
 int launch_scatter(Ctx &c, int prec, int mode, const double *pf, double *out)
 {
     if (c.kind == KIND_SCALAR8) return launch_scatter1(c, mode, pf, pf, out, mode == 0 ? c.st : nullptr);
+    if (c.kind == KIND_SOLID8 && mode == 0) return launch_scatter3_fixed(c, pf, out, c.st);
     const PcgState *st = mode == 0 ? c.st : nullptr;
     if (prec != PREC_FP64) {
         if (mode == 0)
@@ -909,6 +919,10 @@ int launch_matvec(Ctx &c, int prec, const double *p, double *u)
     if (c.kind == KIND_SCALAR8) {
         if (launch_elem8(c, p, nullptr)) return 1;
         return launch_scatter1(c, 0, p, p, u, nullptr);
+    }
+    if (c.kind == KIND_SOLID8) {
+        if (launch_elem24(c, p, nullptr)) return 1;
+        return launch_scatter3_fixed(c, p, u, nullptr);
     }
     const int grid = grid_for(c, c.nels, 8, 8);
     if (c.shared) {
@@ -948,7 +962,10 @@ int launch_residual(Ctx &c, const double *f, const double *x, double *rres)
         return launch_scatter1(c, 1, x, f, rres, nullptr);
     }
     const int grid = grid_for(c, c.nels, 8, 8);
-    if (c.shared) {
+    if (c.kind == KIND_SOLID8) {
+        // f - K x with the plain K, as p122 forms r = loads - K x (p122.f90:142-146)
+        if (launch_elem24(c, x, nullptr)) return 1;
+    } else if (c.shared) {
         if (launch_elem_shared(c, PREC_FP64, x, nullptr)) return 1;
     } else {
         k_elem<double, true><<<grid, 256, 0, c.stream>>>(c.nels, c.km64, c.conn, x, (double *)c.utemp, nullptr);

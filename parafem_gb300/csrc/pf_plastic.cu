@@ -1,11 +1,12 @@
 // pf_plastic.cu -- p122: 3-D strain of an elastic-plastic (Mohr-Coulomb)
 // solid by the viscoplastic strain method (src/programs/5th_ed/p122/p122.f90),
-// 20-node bricks, load control, on the GPU.
+// 20-node bricks or 8-node bricks, load control, displacement control (fixed
+// freedoms by the penalty method) or both, on the GPU.
 //
 // Every plastic iteration is one warm-started element-by-element PCG solve
 // (the p121 kernels: r = loads - K x, then p121's iteration with checon_par)
 // followed by one pass over the Gauss points:
-//   k_p122_bee       B (6 x 60), det and weight at every Gauss point, once;
+//   k_p122_bee       B (6 x 3 nod), det and weight at every Gauss point, once;
 //   k_p122_plastic   one warp per element: eps = B u_e - evpt, sigma = D eps,
 //                    stress = sigma + tensor; INVAR, MOCOUF; at a yielding
 //                    point MOCOUQ, FORMM, the viscoplastic strain rate, evpt
@@ -24,44 +25,52 @@ namespace {
 
 struct P122 {
     int nip = 0;
-    double *bee = nullptr;     // [nels][nip][6*60] column-major B
+    double *bee = nullptr;     // [nels][nip][6 * 3 nod] column-major B
     double *detw = nullptr;    // [nels][nip][2]: det, weight
     double *evpt = nullptr;    // [nels][nip][6]
     double *tensor = nullptr;  // [nels][nip][6]
     double *ld0 = nullptr, *loads = nullptr, *bdylds = nullptr, *oldis = nullptr, *totd = nullptr;   // slots
     double *red = nullptr;     // [2 * G + 8] checon partials and results
+    int *fslot = nullptr;      // [nfix] slots of the fixed freedoms
+    double *fval = nullptr;    // [nfix] their prescribed values
 };
 
 void p122_free(P122 &q)
 {
-    double *ptrs[] = {q.bee, q.detw, q.evpt, q.tensor, q.ld0, q.loads, q.bdylds, q.oldis, q.totd, q.red};
+    double *ptrs[] = {q.bee, q.detw, q.evpt, q.tensor, q.ld0, q.loads, q.bdylds, q.oldis, q.totd, q.red, q.fval};
     for (double *x : ptrs)
         if (x) cudaFree(x);
+    if (q.fslot) cudaFree(q.fslot);
     q = P122();
 }
 
 }  // namespace
 
-// B, det and weight at Gauss point g of element e (thread per point)
+// B, det and weight at Gauss point g of element e (thread per point), NOD-node bricks
+template <int NOD>
 __global__ void k_p122_bee(int nels, int nip, const double *__restrict__ gp, const double *__restrict__ coord,
                            double *__restrict__ bee, double *__restrict__ detw)
 {
+    constexpr int NE = 3 * NOD;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)nels * nip;
          t += (long long)gridDim.x * blockDim.x) {
         const size_t e = (size_t)(t / nip);
         const int g = (int)(t % nip);
-        const double *co = coord + e * 60;
-        double der[60], jac[9];
-        for (int l = 0; l < 20; ++l) shape_der20(l, gp[4 * g], gp[4 * g + 1], gp[4 * g + 2], &der[3 * l]);
+        const double *co = coord + e * NE;
+        double der[NE], jac[9];
+        for (int l = 0; l < NOD; ++l) {
+            if constexpr (NOD == 20) shape_der20(l, gp[4 * g], gp[4 * g + 1], gp[4 * g + 2], &der[3 * l]);
+            else shape_der8(l, gp[4 * g], gp[4 * g + 1], gp[4 * g + 2], &der[3 * l]);
+        }
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
                 double s = 0.0;
-                for (int k = 0; k < 20; ++k) s += der[a + 3 * k] * co[k + 20 * b];
+                for (int k = 0; k < NOD; ++k) s += der[a + 3 * k] * co[k + NOD * b];
                 jac[a + 3 * b] = s;
             }
         const double det = det_invert3(jac);
-        double *B = bee + (size_t)t * 360;
-        for (int m = 0; m < 20; ++m) {
+        double *B = bee + (size_t)t * 6 * NE;
+        for (int m = 0; m < NOD; ++m) {
             // deriv = jac^-1 der (ascending k), BEEMAT rows ex, ey, ez, gxy, gyz, gzx
             double dd[3];
             for (int a = 0; a < 3; ++a) {
@@ -108,9 +117,11 @@ __device__ void invar6(const double *s, double &sigm, double &dsbar, double &the
 }
 
 // One warp per element: the Gauss-point loop of p122.f90:172-202.  Lane l
-// owns rows l and l+32 of the element vectors; every lane evaluates the
-// point's scalar plasticity (the same values), lane 0 writes evpt / tensor.
-// bload = sum over points (in order) of B' devp det w, into ut[e*60 + k].
+// owns rows l and l+32 of the element vectors (rows below 3 NOD); every lane
+// evaluates the point's scalar plasticity (the same values), lane 0 writes
+// evpt / tensor.  bload = sum over points (in order) of B' devp det w, into
+// ut[e * 3 NOD + k].
+template <int NOD>
 __global__ void __launch_bounds__(256)
 k_p122_plastic(int nels, int nip, const int *__restrict__ conn, const double *__restrict__ loads,
                const double *__restrict__ bee, const double *__restrict__ detw, double *__restrict__ evpt,
@@ -126,20 +137,23 @@ k_p122_plastic(int nels, int nip, const int *__restrict__ conn, const double *__
     const double pi4 = 4.0 * atan(1.0);
     const double phir = phi * pi4 / 180.0, psir = psi * pi4 / 180.0;
     const double snph = sin(phir), csph = cos(phir), snps = sin(psir), sq3 = sqrt(3.0);
+    constexpr int NE = 3 * NOD;
     const int k0 = lane, k1 = lane + 32;
+    const bool h0 = k0 < NE, h1 = k1 < NE;   // the rows this lane holds
     for (int el = warp; el < nels; el += nwarps) {
-        const int n0 = __shfl_sync(FULLMASK, lane < 20 ? conn[(size_t)el * 20 + lane] : 0, k0 / 3);
-        const int n1 = __shfl_sync(FULLMASK, lane < 20 ? conn[(size_t)el * 20 + lane] : 0, k1 < 60 ? k1 / 3 : 0);
-        const double u0 = loads[(size_t)3 * n0 + k0 % 3];
-        const double u1 = k1 < 60 ? loads[(size_t)3 * n1 + k1 % 3] : 0.0;
+        const int cn = lane < NOD ? conn[(size_t)el * NOD + lane] : 0;
+        const int n0 = __shfl_sync(FULLMASK, cn, h0 ? k0 / 3 : 0);
+        const int n1 = __shfl_sync(FULLMASK, cn, h1 ? k1 / 3 : 0);
+        const double u0 = h0 ? loads[(size_t)3 * n0 + k0 % 3] : 0.0;
+        const double u1 = h1 ? loads[(size_t)3 * n1 + k1 % 3] : 0.0;
         double bl0 = 0.0, bl1 = 0.0;
         for (int g = 0; g < nip; ++g) {
             const size_t gi = (size_t)el * nip + g;
-            const double *B = bee + gi * 360;
+            const double *B = bee + gi * 6 * NE;
             double eps[6];
 #pragma unroll
             for (int a = 0; a < 6; ++a) {
-                double t = B[a + 6 * k0] * u0 + (k1 < 60 ? B[a + 6 * k1] * u1 : 0.0);
+                double t = (h0 ? B[a + 6 * k0] * u0 : 0.0) + (h1 ? B[a + 6 * k1] * u1 : 0.0);
                 eps[a] = warp_sum(t);
             }
             double *ev = evpt + gi * 6, *tn = tensor + gi * 6;
@@ -229,8 +243,8 @@ k_p122_plastic(int nels, int nip, const int *__restrict__ conn, const double *__
                 double s0 = 0.0, s1 = 0.0;
 #pragma unroll
                 for (int a = 0; a < 6; ++a) {
-                    s0 += B[a + 6 * k0] * devp[a];
-                    if (k1 < 60) s1 += B[a + 6 * k1] * devp[a];
+                    if (h0) s0 += B[a + 6 * k0] * devp[a];
+                    if (h1) s1 += B[a + 6 * k1] * devp[a];
                 }
                 bl0 = bl0 + s0 * dw * w;
                 bl1 = bl1 + s1 * dw * w;
@@ -238,17 +252,30 @@ k_p122_plastic(int nels, int nip, const int *__restrict__ conn, const double *__
             if (last && lane == 0)
                 for (int a = 0; a < 6; ++a) tn[a] = stress[a];
         }
-        ut[(size_t)el * 60 + k0] = bl0;
-        if (k1 < 60) ut[(size_t)el * 60 + k1] = bl1;
+        if (h0) ut[(size_t)el * NE + k0] = bl0;
+        if (h1) ut[(size_t)el * NE + k1] = bl1;
     }
 }
 
-// loads = ld0 * q + bdylds (slots)
+// The load vector of a plastic iteration (p122.f90:121-140), over slots:
+// with nodal loads, loads = ld0 * q + bdylds; without, loads = bdylds, or 0
+// on the first plastic iteration (first != 0).
 __global__ void k_p122_loads(int ns, const double *__restrict__ ld0, double q, const double *__restrict__ bdylds,
-                             double *__restrict__ loads)
+                             int first, double *__restrict__ loads)
 {
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x)
-        loads[s] = ld0[s] * q + bdylds[s];
+        loads[s] = ld0 ? ld0[s] * q + bdylds[s] : (first ? 0.0 : bdylds[s]);
+}
+
+// fixed freedoms (p122.f90:122-139): on the first plastic iteration
+// loads = store * value * q, after it loads = 0
+__global__ void k_p122_fixed_loads(int nfix, const int *__restrict__ slot, const double *__restrict__ val,
+                                   const double *__restrict__ fstore, double q, int first, double *__restrict__ loads)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nfix; i += gridDim.x * blockDim.x) {
+        const int s = slot[i];
+        loads[s] = first ? fstore[s] * val[i] * q : 0.0;
+    }
 }
 
 // checon_par on (x, oldis): block partials of max|x| and max|x - oldis|; oldis = x
@@ -321,13 +348,14 @@ static int p122_launched(Ctx &c, const char *name)
     return 0;
 }
 
-extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, const double *c_coh, const double *psi,
-                             const int *incs, const double *qinc, const int *plasits, const int *cjits,
-                             const double *plastol, const double *cjtol, const double *ld0, double *results,
-                             double *totd_out, int *incs_done)
+extern "C" int pf_p122_solve_fixed(void **ctx, const int *nip, const double *phi, const double *c_coh,
+                                   const double *psi, const int *incs, const double *qinc, const int *plasits,
+                                   const int *cjits, const double *plastol, const double *cjtol, const double *ld0,
+                                   const int *nfix_p, const int *fix_eqs, const double *fix_vals, double *results,
+                                   double *totd_out, int *incs_done)
 {
     if (!ctx || !*ctx || !nip || !phi || !c_coh || !psi || !incs || !qinc || !plasits || !cjits || !plastol ||
-        !cjtol || !ld0 || !results || !incs_done) {
+        !cjtol || !nfix_p || !results || !incs_done) {
         set_error("pf_p122_solve: null argument");
         return PF_FAILURE;
     }
@@ -336,29 +364,58 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
         set_error("pf_p122_solve: cannot select the device");
         return PF_FAILURE;
     }
-    if (c.kind != KIND_SOLID20 || c.shared || !c.have_km || !c.km64 || c.nmat != 1 || *incs < 1 || *plasits < 1 ||
-        *cjits < 1 || (*nip != 8 && *nip != 27)) {
-        set_error("pf_p122_solve: needs a 20-node context with storkm formed from one material, incs, "
-                  "plasits, cjits >= 1 and nip 8 or 27");
+    const int nfix = *nfix_p;
+    if ((c.kind != KIND_SOLID20 && c.kind != KIND_SOLID8) || c.shared || !c.have_km || !c.km64 || c.nmat != 1 ||
+        *incs < 1 || *plasits < 1 || *cjits < 1 || (*nip != 8 && *nip != 27) || nfix < 0 ||
+        (nfix > 0 && (!fix_eqs || !fix_vals)) || (nfix == 0 && !ld0)) {
+        set_error("pf_p122_solve: needs an elasticity context with storkm formed from one material, incs, "
+                  "plasits, cjits >= 1, nip 8 or 27, and nodal loads or fixed freedoms");
         return PF_FAILURE;
     }
+    if (nfix > 0 && c.kind != KIND_SOLID8) {
+        set_error("pf_p122_solve: fixed freedoms need an 8-node context (pf_setup_solid8)");
+        return PF_FAILURE;
+    }
+    const bool solid8 = c.kind == KIND_SOLID8;
+    const int ne = solid8 ? 24 : 60;
     P122 q;
     q.nip = *nip;
     const size_t ns = c.nslots, ngp = (size_t)c.nels * q.nip;
-    PCK(cudaMalloc(&q.bee, ngp * 360 * sizeof(double)));
+    PCK(cudaMalloc(&q.bee, ngp * 6 * ne * sizeof(double)));
     PCK(cudaMalloc(&q.detw, ngp * 2 * sizeof(double)));
     PCK(cudaMalloc(&q.evpt, ngp * 6 * sizeof(double)));
     PCK(cudaMalloc(&q.tensor, ngp * 6 * sizeof(double)));
-    double **vecs[] = {&q.ld0, &q.loads, &q.bdylds, &q.oldis, &q.totd};
+    double **vecs[] = {&q.loads, &q.bdylds, &q.oldis, &q.totd};
     for (double **v : vecs) PCK(cudaMalloc(v, ns * sizeof(double)));
     PCK(cudaMalloc(&q.red, (2 * (size_t)c.G + 8) * sizeof(double)));
     PCK(cudaMemsetAsync(q.tensor, 0, ngp * 6 * sizeof(double), c.stream));
     PCK(cudaMemsetAsync(q.oldis, 0, ns * sizeof(double), c.stream));
     PCK(cudaMemsetAsync(q.totd, 0, ns * sizeof(double), c.stream));
     PCK(cudaMemsetAsync(c.x, 0, ns * sizeof(double), c.stream));
-    // ld0 to slots
-    PCK(cudaMemcpyAsync(c.eqbuf, ld0, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
-    PTRY(launch_eq_to_slot(c, c.eqbuf, q.ld0));
+    if (ld0) {   // ld0 to slots
+        PCK(cudaMalloc(&q.ld0, ns * sizeof(double)));
+        PCK(cudaMemcpyAsync(c.eqbuf, ld0, (size_t)c.neq * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        PTRY(launch_eq_to_slot(c, c.eqbuf, q.ld0));
+    }
+    if (nfix > 0) {
+        // the penalty on the fixed freedoms' diagonal, store = the penalised
+        // diagonal (p122.f90:108-113)
+        std::vector<int> eq_slot(c.neq), slots(nfix);
+        PCK(cudaMemcpy(eq_slot.data(), c.eq_slot, (size_t)c.neq * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < nfix; ++i) {
+            if (fix_eqs[i] < 1 || fix_eqs[i] > c.neq) {
+                set_error("pf_p122_solve: fixed freedom %d: equation %d outside 1..%d", i + 1, fix_eqs[i], c.neq);
+                p122_free(q);
+                return PF_FAILURE;
+            }
+            slots[i] = eq_slot[fix_eqs[i] - 1];
+        }
+        PCK(cudaMalloc(&q.fslot, nfix * sizeof(int)));
+        PCK(cudaMalloc(&q.fval, nfix * sizeof(double)));
+        PCK(cudaMemcpyAsync(q.fslot, slots.data(), nfix * sizeof(int), cudaMemcpyHostToDevice, c.stream));
+        PCK(cudaMemcpyAsync(q.fval, fix_vals, nfix * sizeof(double), cudaMemcpyHostToDevice, c.stream));
+        PTRY(launch_set_fixed(c, nfix, q.fslot, 1.e20));
+    }
     // B, det, w at every Gauss point
     double *gp = nullptr;
     PCK(cudaMalloc(&gp, sizeof(double) * 4 * 27));
@@ -367,7 +424,10 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
         p122_free(q);
         return PF_FAILURE;
     }
-    k_p122_bee<<<c.nsm * 8, 128, 0, c.stream>>>(c.nels, q.nip, gp, c.coord, q.bee, q.detw);
+    if (solid8)
+        k_p122_bee<8><<<c.nsm * 8, 128, 0, c.stream>>>(c.nels, q.nip, gp, c.coord, q.bee, q.detw);
+    else
+        k_p122_bee<20><<<c.nsm * 8, 128, 0, c.stream>>>(c.nels, q.nip, gp, c.coord, q.bee, q.detw);
     if (p122_launched(c, "k_p122_bee")) {
         cudaFree(gp);
         p122_free(q);
@@ -381,6 +441,7 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
     const double pi = std::acos(-1.0), snph = std::sin(*phi * pi / 180.0);
     const double dt = 4.0 * (1.0 + v) * (1.0 - 2.0 * v) / (e * (1.0 - 2.0 * v + snph * snph));
     const int gv = c.G, ge = c.nels < c.nsm * 64 ? (c.nels + 7) / 8 : c.nsm * 8;
+    static const double kOne = 1.0, kZero = 0.0;
     // slot of equation 1 for the printed displacement
     int slot1 = -1;
     if (c.neq > 0) PCK(cudaMemcpy(&slot1, c.eq_slot, sizeof(int), cudaMemcpyDeviceToHost));
@@ -391,8 +452,17 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
         PCK(cudaMemsetAsync(q.evpt, 0, ngp * 6 * sizeof(double), c.stream));
         for (;;) {
             ++plasiters;
-            k_p122_loads<<<gv, 256, 0, c.stream>>>((int)ns, q.ld0, qinc[iy - 1], q.bdylds, q.loads);
+            const int first = plasiters == 1 ? 1 : 0;
+            k_p122_loads<<<gv, 256, 0, c.stream>>>((int)ns, q.ld0, qinc[iy - 1], q.bdylds, first, q.loads);
             PTRY(p122_launched(c, "k_p122_loads"));
+            if (nfix > 0 && !(first && ld0)) {   // with nodal loads the first iteration's vector replaces them
+                k_p122_fixed_loads<<<1, 256, 0, c.stream>>>(nfix, q.fslot, q.fval, c.fstore, qinc[iy - 1], first,
+                                                            q.loads);
+                PTRY(p122_launched(c, "k_p122_fixed_loads"));
+            }
+            if (solid8)   // the product at a fixed freedom: p * store on the first iteration, 0 after
+                PCK(cudaMemcpyAsync(c.fscale, first ? &kOne : &kZero, sizeof(double), cudaMemcpyHostToDevice,
+                                    c.stream));
             // r = loads - K x (warm start from the previous solution), then PCG with checon_par
             PTRY(launch_residual(c, q.loads, c.x, c.rres));
             PTRY(launch_pcg_init(c, c.rres, c.x, STOP_CHECON, *cjtol, *cjits, true));
@@ -410,9 +480,14 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
             const bool conv = plasiters > 1 && mx[1] / mx[0] <= *plastol;
             const bool last = conv || plasiters == *plasits;
             if (last) PCK(cudaMemsetAsync(q.bdylds, 0, ns * sizeof(double), c.stream));
-            k_p122_plastic<<<ge, 256, 0, c.stream>>>(c.nels, q.nip, c.conn, q.loads, q.bee, q.detw, q.evpt,
-                                                     q.tensor, *phi, *c_coh, *psi, e, v, dt, last ? 1 : 0,
-                                                     (double *)c.utemp);
+            if (solid8)
+                k_p122_plastic<8><<<ge, 256, 0, c.stream>>>(c.nels, q.nip, c.conn, q.loads, q.bee, q.detw, q.evpt,
+                                                            q.tensor, *phi, *c_coh, *psi, e, v, dt, last ? 1 : 0,
+                                                            (double *)c.utemp);
+            else
+                k_p122_plastic<20><<<ge, 256, 0, c.stream>>>(c.nels, q.nip, c.conn, q.loads, q.bee, q.detw, q.evpt,
+                                                             q.tensor, *phi, *c_coh, *psi, e, v, dt, last ? 1 : 0,
+                                                             (double *)c.utemp);
             PTRY(p122_launched(c, "k_p122_plastic"));
             PTRY(launch_scatter_add64(c, q.bdylds));
             if (last) break;
@@ -438,6 +513,26 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
         if (plasiters == *plasits) break;
     }
     *incs_done = iy > *incs ? *incs : iy;
+    if (nfix > 0) {   // the context's diagonal without the penalties, no fixed freedoms
+        PTRY(launch_assemble_diag(c));
+        PCK(cudaMemsetAsync(c.fstore, 0, ns * sizeof(double), c.stream));
+    }
+    if (solid8) PCK(cudaMemcpyAsync(c.fscale, &kOne, sizeof(double), cudaMemcpyHostToDevice, c.stream));
+    PCK(cudaStreamSynchronize(c.stream));
     p122_free(q);
     return PF_SUCCESS;
+}
+
+extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, const double *c_coh, const double *psi,
+                             const int *incs, const double *qinc, const int *plasits, const int *cjits,
+                             const double *plastol, const double *cjtol, const double *ld0, double *results,
+                             double *totd_out, int *incs_done)
+{
+    if (!ld0) {
+        set_error("pf_p122_solve: null argument");
+        return PF_FAILURE;
+    }
+    const int zero = 0;
+    return pf_p122_solve_fixed(ctx, nip, phi, c_coh, psi, incs, qinc, plasits, cjits, plastol, cjtol, ld0, &zero,
+                               nullptr, nullptr, results, totd_out, incs_done);
 }

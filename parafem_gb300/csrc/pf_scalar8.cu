@@ -18,12 +18,6 @@
 
 namespace pf {
 
-// SHAPE_DER, 3-D 8-node brick (new_library.f90:769-793): node signs in
-// Smith-Griffiths order
-__constant__ double c8_xi[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
-__constant__ double c8_eta[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
-__constant__ double c8_zeta[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
-
 // Eight threads per element; thread c owns column c of kcx, kcy, kcz.
 __global__ void __launch_bounds__(128)
 k_form_storkc(int nels, int nip, const double *__restrict__ gp, const double *__restrict__ coord, double kx,
@@ -39,12 +33,7 @@ k_form_storkc(int nels, int nip, const double *__restrict__ gp, const double *__
         for (int g = 0; g < nip; ++g) {
             const double xi = gp[4 * g], eta = gp[4 * g + 1], zeta = gp[4 * g + 2], w = gp[4 * g + 3];
             double der[24];
-            for (int l = 0; l < 8; ++l) {
-                const double a = 1.0 + xi * c8_xi[l], b = 1.0 + eta * c8_eta[l], d = 1.0 + zeta * c8_zeta[l];
-                der[3 * l] = 0.125 * c8_xi[l] * b * d;
-                der[3 * l + 1] = 0.125 * c8_eta[l] * a * d;
-                der[3 * l + 2] = 0.125 * c8_zeta[l] * a * b;
-            }
+            for (int l = 0; l < 8; ++l) shape_der8(l, xi, eta, zeta, &der[3 * l]);
             double jac[9];
             for (int a = 0; a < 3; ++a)
                 for (int b = 0; b < 3; ++b) {

@@ -97,6 +97,9 @@ _SIGS = {
     "pf_set_fixed": [_VPP, _IP, ctypes.c_void_p, _DP],
     "pf_p122_solve": [_VPP, _IP, _DP, _DP, _DP, _IP, ctypes.c_void_p, _IP, _IP, _DP, _DP, ctypes.c_void_p,
                       ctypes.c_void_p, ctypes.c_void_p, _IP],
+    "pf_setup_solid8": [_VPP, _IP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    "pf_p122_solve_fixed": [_VPP, _IP, _DP, _DP, _DP, _IP, ctypes.c_void_p, _IP, _IP, _DP, _DP, ctypes.c_void_p,
+                            _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
     "pf_mesh_cube": [_IP, _IP, _IP, _DP, _DP, _DP, _IP, _IP, ctypes.c_void_p, ctypes.c_void_p],
     "pf_cube_restraints": [_IP, _IP, _IP, _IP, ctypes.c_void_p],
     "pf_number_equations": [_IP, _IP, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _IP],
@@ -278,6 +281,17 @@ class Solver:
         _check(lib().pf_setup_scalar8(self._ref, _i(nels), _i(nn), _i(neq), pn, pg, pc), "pf_setup_scalar8")
         self.nels, self.nn, self.neq = nels, int(nn), int(neq)
 
+    def setup_solid8(self, g_num, g_g, g_coord, nn, neq):
+        """8-node elasticity bricks, three freedoms per node (p122's demo deck)."""
+        g_num, pn = _arr(g_num, np.int32)
+        g_g, pg = _arr(g_g, np.int32)
+        g_coord, pc = _arr(g_coord, np.float64)
+        nels = g_num.shape[0]
+        if g_num.shape != (nels, 8) or g_g.shape != (nels, 24) or g_coord.shape != (nels, 3, 8):
+            raise ValueError("g_num (nels,8), g_g (nels,24), g_coord (nels,3,8) expected")
+        _check(lib().pf_setup_solid8(self._ref, _i(nels), _i(nn), _i(neq), pn, pg, pc), "pf_setup_solid8")
+        self.nels, self.nn, self.neq = nels, int(nn), int(neq)
+
     def form_storkc(self, nip, kx, ky, kz):
         _check(lib().pf_form_storkc(self._ref, _i(nip), _d(kx), _d(ky), _d(kz)), "pf_form_storkc")
 
@@ -301,6 +315,28 @@ class Solver:
         _check(lib().pf_p122_solve(self._ref, _i(nip), _d(phi), _d(c), _d(psi), _i(qinc.size), qinc.ctypes.data,
                                    _i(plasits), _i(cjits), _d(plastol), _d(cjtol), ld0.ctypes.data, res.ctypes.data,
                                    totd.ctypes.data if keep_totd else None, ctypes.byref(done)), "pf_p122_solve")
+        n = done.value
+        return res[:n], (totd[:n] if keep_totd else None)
+
+    def p122_solve_fixed(self, nip, phi, c, psi, qinc, plasits, cjits, plastol, cjtol, fix_eqs=(), fix_vals=(),
+                         ld0=None, keep_totd=False):
+        """p122's load increments with fixed freedoms (see pf_p122_solve_fixed):
+        results (incs_done, 6), totd (incs_done, neq) or None."""
+        qinc = np.ascontiguousarray(np.atleast_1d(qinc), dtype=np.float64)
+        fe = np.ascontiguousarray(np.atleast_1d(fix_eqs), dtype=np.int32)
+        fv = np.ascontiguousarray(np.atleast_1d(fix_vals), dtype=np.float64)
+        if fe.size != fv.size:
+            raise ValueError("fix_eqs and fix_vals differ in length")
+        ld = None if ld0 is None else np.ascontiguousarray(ld0, dtype=np.float64)
+        res = np.zeros((qinc.size, 6))
+        totd = np.zeros((qinc.size, self.neq)) if keep_totd else None
+        done = ctypes.c_int(0)
+        _check(lib().pf_p122_solve_fixed(self._ref, _i(nip), _d(phi), _d(c), _d(psi), _i(qinc.size),
+                                         qinc.ctypes.data, _i(plasits), _i(cjits), _d(plastol), _d(cjtol),
+                                         ld.ctypes.data if ld is not None else None, _i(fe.size),
+                                         fe.ctypes.data if fe.size else None, fv.ctypes.data if fv.size else None,
+                                         res.ctypes.data, totd.ctypes.data if keep_totd else None,
+                                         ctypes.byref(done)), "pf_p122_solve_fixed")
         n = done.value
         return res[:n], (totd[:n] if keep_totd else None)
 
