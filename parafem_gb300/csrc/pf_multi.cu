@@ -333,12 +333,16 @@ k_mr_elem_h16(int nels, int k, int c0, int nr, const unsigned char *__restrict__
         // the element records (A tile, 1/s_e), one bulk copy each, into the
         // ring of nr record stages
         if (lane == 0) {
+            int r = 0, lap = 0;   // t = lap * nr + r (nr is a launch parameter: no division per element)
             for (int t = 0; t < nmine; ++t) {
-                const int r = t % nr;
-                if (t >= nr && !wait(&rc_empty[r], (uint32_t)((t / nr - 1) & 1))) break;
+                if (t >= nr && !wait(&rc_empty[r], (uint32_t)((lap - 1) & 1))) break;
                 mbar_expect_tx(&rc_full[r], kRecBytes);
                 bulk_g2s(rstg + (size_t)r * kRecStage, rec + (size_t)elem(t) * kRecBytes, kRecBytes, &rc_full[r]);
                 r_last[r] = t;   // for the drain after a failure
+                if (++r == nr) {
+                    r = 0;
+                    ++lap;
+                }
             }
         }
         __syncwarp();
@@ -489,9 +493,10 @@ k_mr_elem_h16(int nels, int k, int c0, int nr, const unsigned char *__restrict__
         if (lane == 0) {
             // kind::f16 with both operands FP16 (the format is in the instruction descriptor)
             const uint32_t idesc = idesc_f16(128, 2u * kb);
+            int r = 0, rlap = 0;   // t = rlap * nr + r (no division per element)
             for (; t < nmine; ++t) {
-                const int r = t % nr, b = t % np, a = t % kNAcc;
-                const uint32_t pr = (uint32_t)((t / nr) & 1), pb = (uint32_t)((t / np) & 1),
+                const int b = t % np, a = t % kNAcc;
+                const uint32_t pr = (uint32_t)(rlap & 1), pb = (uint32_t)((t / np) & 1),
                                pa = (uint32_t)((t / kNAcc - 1) & 1);
                 // the three barriers tested at once; the bounded waits only when one is not ready
                 const bool ready = mbar_test(&rc_full[r], pr) & mbar_test(&tl_full[b], pb) &
@@ -512,6 +517,10 @@ k_mr_elem_h16(int nels, int k, int c0, int nr, const unsigned char *__restrict__
                              ks > 0 ? 1u : 0u);
                 mma_commit(&rc_empty[r]);
                 mma_commit(&ac_full[a]);
+                if (++r == nr) {
+                    r = 0;
+                    ++rlap;
+                }
             }
             s_count[1] = t;
         }
@@ -708,9 +717,12 @@ k_mr_scatter(int nn, int k, const int *__restrict__ ptr, const int *__restrict__
     if (skip && *skip) return;   // uniform: the flag does not change during the kernel
     const int j = threadIdx.x % k;
     double loc = 0.0;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < (size_t)nn * k;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const int n = (int)(t / k);
+    // the block size is a multiple of k: a thread's case stays j and its
+    // node advances by the stride over k (no division in the loop)
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int dn = (int)(stride / k);
+    int n = (int)(t0 / k);
+    for (size_t t = t0; t < (size_t)nn * k; t += stride, n += dn) {
         UT a0 = 0, a1 = 0, a2 = 0;   // FP32 products are summed in FP32, FP64 ones in FP64
         for (int q = ptr[n]; q < ptr[n + 1]; ++q) {
             const size_t base = (size_t)list[q] * 3 * k + j;   // list holds e*20+a
@@ -785,9 +797,11 @@ k_mr_init(int ns, int k, const double *__restrict__ F, const double *__restrict_
           double *__restrict__ part, int G)
 {
     double rd = 0.0, rr = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const double rv = F[t], dv = dinv[t / k] * rv;
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t ds = stride / k;   // the block size is a multiple of k
+    size_t s = t0 / k;
+    for (size_t t = t0; t < (size_t)ns * k; t += stride, s += ds) {
+        const double rv = F[t], dv = dinv[s] * rv;
         X[t] = 0.0;
         R[t] = rv;
         D[t] = dv;
@@ -840,12 +854,14 @@ k_mr_update1(int ns, int k, const MState *__restrict__ st, double *__restrict__ 
     const int j = threadIdx.x % k;
     const double alpha = st->alpha[j];
     double rd = 0.0, rr = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
-         t += (size_t)gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t ds = stride / k;   // the block size is a multiple of k
+    size_t s = t0 / k;
+    for (size_t t = t0; t < (size_t)ns * k; t += stride, s += ds) {
         X[t] = fma(P[t], alpha, X[t]);
         const double rn = fma(-U[t], alpha, R[t]);
         R[t] = rn;
-        const double dn = dinv[t / k] * rn;
+        const double dn = dinv[s] * rn;
         D[t] = dn;
         rd = fma(rn, dn, rd);
         rr = fma(rn, rn, rr);
@@ -931,10 +947,12 @@ k_mr_replace(int ns, int k, const MState *__restrict__ st, const double *__restr
     const int j = threadIdx.x % k;
     const bool act = st->active[j] != 0;
     double rd = 0.0, rr = 0.0;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)ns * k;
-         t += (size_t)gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x, t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const size_t ds = stride / k;   // the block size is a multiple of k
+    size_t s = t0 / k;
+    for (size_t t = t0; t < (size_t)ns * k; t += stride, s += ds) {
         if (!act) continue;
-        const double rv = RRES[t], dv = dinv[t / k] * rv;
+        const double rv = RRES[t], dv = dinv[s] * rv;
         R[t] = rv;
         D[t] = dv;
         rd = fma(rv, dv, rd);

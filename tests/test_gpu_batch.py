@@ -134,3 +134,20 @@ def test_graph_replay_matches_direct_launches(prec):
     for (it_g, rel_g, x_g), (it_d, rel_d, x_d) in zip(*runs):
         assert it_g == it_d and rel_g == rel_d
         assert np.array_equal(x_g, x_d)
+
+
+def test_batch_solution_matches_oracle_pcg():
+    """A batched solve of a small heterogeneous mesh against the C
+    restatement of p121's PCG (relative-residual stop at 1e-12) on the
+    oracle's own storkm, so the serving engine is pinned to the oracle
+    directly, not only through the single-mesh solver."""
+    from oracle import oracle as O
+    prob, e, v = request(SPECS[1])
+    with P.Batch(1 << 30, 4) as b:
+        sid = admit(b, prob, e, v, tol=1e-10)
+        it, rel, x = b.run_all(prob["neq"])[sid]
+    assert rel <= 1e-10
+    km = O.form_storkm(prob["g_coord"], 27, e, v)
+    dg = O.diag(prob["g_g"], km, prob["neq"])
+    _, xr, _ = O.pcg(prob["g_g"], km, dg, np.ascontiguousarray(prob["r"]), 1e-12, 20000, 1)
+    assert np.linalg.norm(x - xr) <= 1e-7 * np.linalg.norm(xr)
