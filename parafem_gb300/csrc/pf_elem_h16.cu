@@ -205,6 +205,10 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
             float *o = ut + (size_t)elem(k) * 80;   // node-padded: row i at (i/3)*4 + i%3
             o[(lane / 3) * 4 + lane % 3] = acc_a;
             o[(lane / 3 + 10) * 4 + lane % 3] = acc_b;
+            // and the padding words, so that every 32-byte sector of the
+            // results is written whole (a partly written one costs L2 a
+            // read from DRAM once the results outgrow it)
+            if (lane < 20) o[lane * 4 + 3] = 0.0f;
         }
         __syncwarp();   // every lane is done with stage s and the p slot
         if (lane == 0 && k + kStages < nmine) {
