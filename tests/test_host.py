@@ -27,6 +27,13 @@ def test_library_exports_every_declared_symbol():
     assert set(names) == set(P.pfgpu.exported_symbols())
 
 
+def test_integration_notes_cover_every_declared_symbol():
+    """Every entry point of the C-ABI is described in the integration notes."""
+    notes = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [n for n in header_functions() if not re.search(r"\b%s\b" % n, notes)]
+    assert not missing, missing
+
+
 @pytest.mark.parametrize("nxe,nye,nze", [(1, 1, 1), (2, 3, 4), (5, 2, 3)])
 def test_mesh_cube_matches_geometry_20bxz(nxe, nye, nze):
     aa, bb, cc = 0.5, 0.25, 0.75
