@@ -112,10 +112,13 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
+    // storkm and the results pass through L2 once: evict them first, so that
+    // p, which every element around a node gathers, stays in L2
+    const uint64_t pol = l2_evict_first_policy();
     if (lane == 0) {
         for (int s = 0; s < kStages && s < nmine; ++s) {
             mbar_expect_tx(&bar[s], kH16Bytes);
-            bulk_g2s(stage + s * kH16Words, kh + (size_t)elem(s) * kH16Words, kH16Bytes, &bar[s]);
+            bulk_g2s_hint(stage + s * kH16Words, kh + (size_t)elem(s) * kH16Words, kH16Bytes, &bar[s], pol);
         }
     }
 
@@ -203,18 +206,19 @@ k_elem_sym16(int nels, const uint32_t *__restrict__ kh, const int *__restrict__ 
         }
         if (active) {
             float *o = ut + (size_t)elem(k) * 80;   // node-padded: row i at (i/3)*4 + i%3
-            o[(lane / 3) * 4 + lane % 3] = acc_a;
-            o[(lane / 3 + 10) * 4 + lane % 3] = acc_b;
+            st_global_hint(o + (lane / 3) * 4 + lane % 3, acc_a, pol);
+            st_global_hint(o + (lane / 3 + 10) * 4 + lane % 3, acc_b, pol);
             // and the padding words, so that every 32-byte sector of the
             // results is written whole (a partly written one costs L2 a
             // read from DRAM once the results outgrow it)
-            if (lane < 20) o[lane * 4 + 3] = 0.0f;
+            if (lane < 20) st_global_hint(o + lane * 4 + 3, 0.0f, pol);
         }
         __syncwarp();   // every lane is done with stage s and the p slot
         if (lane == 0 && k + kStages < nmine) {
             fence_proxy_async();
             mbar_expect_tx(&bar[s], kH16Bytes);
-            bulk_g2s(stage + s * kH16Words, kh + (size_t)elem(k + kStages) * kH16Words, kH16Bytes, &bar[s]);
+            bulk_g2s_hint(stage + s * kH16Words, kh + (size_t)elem(k + kStages) * kH16Words, kH16Bytes, &bar[s],
+                          pol);
         }
         if (kAhead == 2) {
             pa = qa;

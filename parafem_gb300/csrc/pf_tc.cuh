@@ -84,6 +84,33 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
         : "memory");
 }
 
+// L2 policy for data a kernel touches once (streamed storkm, element
+// results): its lines are the first evicted, so that a vector gathered many
+// times (p) keeps its lines in L2 while gigabytes stream past.
+__device__ __forceinline__ uint64_t l2_evict_first_policy()
+{
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// bulk_g2s with an L2 cache policy (l2_evict_first_policy)
+__device__ __forceinline__ void bulk_g2s_hint(void *dst, const void *src, uint32_t bytes, uint64_t *bar,
+                                              uint64_t pol)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
+        : "memory");
+}
+
+// 4-byte global store with an L2 cache policy
+__device__ __forceinline__ void st_global_hint(float *dst, float v, uint64_t pol)
+{
+    asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(dst), "f"(v), "l"(pol) : "memory");
+}
+
 // 16-byte copy global -> shared that bypasses L1 (cp.async, both addresses
 // 16-byte aligned); completion is tracked per thread, see cp_async_arrive
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)
