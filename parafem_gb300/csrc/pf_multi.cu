@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(128) k_mr_pack(int nels, const double *__restr
 // waited on by one thread that passes its phases in turn, so no parity wait
 // can run two phases ahead.
 // Every wait is bounded; where a group of warps meets at a named barrier,
-// one thread waits and the group follows its verdict.  A wait that runs out
+// one thread waits and the group follows its outcome.  A wait that runs out
 // sets a shared failure flag that every role checks before its next wait,
 // writes 3 to the device error word, and the CTA waits (bounded) for the
 // copies and MMAs it has in flight before it frees its TMEM and returns.
