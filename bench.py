@@ -188,14 +188,17 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel_tag):
-    """DRAM bytes per launch from the committed ncu summary of that kernel, if any."""
+def ncu_traffic(kernel_tag, key="dram_bytes_per_launch_full_size"):
+    """A DRAM figure from the committed ncu summary of that kernel, if any:
+    bytes per full-size launch (the default key), or, with key
+    dram_per_algorithmic_byte, the DRAM bytes per algorithmic byte of a
+    smaller capture of the same kernel."""
     path = os.path.join(ROOT, "profiles", f"{kernel_tag}.md")
     try:
         txt = open(path).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", txt)
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", txt)
     return float(m.group(1)) if m else None
 
 
@@ -675,10 +678,14 @@ def multirhs_solves(n, k, seed, local, limit, precs=(16, 32), sequential=True, s
                 # results of its 60 dofs; the split P (8 B per value) once
                 b = nels * (16400 + 80 + 60 * k * 4) + 3 * prob["nn"] * k * 8
                 ms = s.multi_product_ms(R, 5)
+                # DRAM traffic: the 40^3 capture's bytes per algorithmic byte
+                # (the records and results grow with the elements, P with the nodes)
+                ratio = ncu_traffic("k_mr_elem_h16_cube40", "dram_per_algorithmic_byte")
                 out["roofline"] = {"kernel": "k_mr_elem_h16 (tcgen05 FP16x2, TMA gather4)", "bound": "hbm",
                                    "bytes_per_launch": b, "avg_launch_ms": ms,
                                    "achieved": b / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
-                                   "frac": b / (ms / 1e3) / 1e9 / peak, "peak_kind": f"{peak_kind} hbm_gbs"}
+                                   "frac": b / (ms / 1e3) / 1e9 / peak, "peak_kind": f"{peak_kind} hbm_gbs",
+                                   "traffic": b * ratio if ratio else None}
         first = {16: "block_tensor_cores", 32: "block_fp32_cuda_cores"}[precs[0]]
         if sequential:
             t0 = time.perf_counter()
@@ -780,7 +787,9 @@ def run_shared(args, rank, world, local, dist):
             "roofline": {"kernel": "k_elem_shared_tc (shared km, tcgen05 BF16x3)", "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": f"{peak_kind} hbm_gbs", "bytes_per_launch": b_launch,
-                         "avg_launch_ms": avg_s * 1e3, "traffic": None, "scatter_avg_ms": ms_scat / args.steps},
+                         "avg_launch_ms": avg_s * 1e3,
+                         "traffic": ncu_traffic("k_elem_shared_tc_cube100") if n == 100 else None,
+                         "scatter_avg_ms": ms_scat / args.steps},
             "fp64_step_ms": ms64 / k2, "fp64_elem_ms": ms64_elem / k2,
             "gpu_launches": int(launches), "clocks": clocks, "solves": out}
     if rank == 0:
