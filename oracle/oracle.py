@@ -201,6 +201,7 @@ def lib():
             L.orc_mocouf.restype = _D
             L.orc_mocouq.argtypes = [_D, _D, _D, ctypes.POINTER(_D), ctypes.POINTER(_D), ctypes.POINTER(_D)]
             L.orc_formm.argtypes = [_PD, _PD, _PD, _PD]
+            L.orc_form_storkm8.argtypes = [_I, _I, _PD, _D, _D, _PD]
             _lib = L
     return _lib
 
@@ -427,6 +428,16 @@ def form_storkc(g_coord, nip, kx, ky, kz):
     kc = np.zeros((nels, 8, 8))
     lib().orc_form_storkc(nels, nip, g_coord, kx, ky, kz, kc)
     return kc
+
+
+def form_storkm8(g_coord, nip, e, v):
+    """storkm of 8-node elasticity bricks (p122 with nod = 8): g_coord
+    (nels, 3, 8) -> (nels, 24, 24) with km[e, j, i] = K_e(i, j)."""
+    g_coord = np.ascontiguousarray(g_coord, dtype=np.float64)
+    nels = g_coord.shape[0]
+    km = np.zeros((nels, 24, 24))
+    lib().orc_form_storkm8(nels, nip, g_coord, e, v, km)
+    return km
 
 
 def diag8(g_g, storkc, neq, shared=False):

@@ -210,6 +210,12 @@ static void form_storkm8(int nels, int nip, const double *g_coord, double e, dou
     free(wts);
 }
 
+/* form_storkm8 for the tests: g_coord(8,3,nels) -> storkm(24,24,nels) */
+void orc_form_storkm8(int nels, int nip, const double *g_coord, double e, double v, double *storkm)
+{
+    form_storkm8(nels, nip, g_coord, e, v, storkm);
+}
+
 /* checon_par (src/modules/mpi/maths.f90:999-1069): converged when
  * max|xnew - x| / max|xnew| <= tol; then x = xnew.  Vectors are 1-based. */
 static int checon(int neq, const double *xnew, double tol, double *x)

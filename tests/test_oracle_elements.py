@@ -1,0 +1,119 @@
+"""Analytic checks of the oracle's element matrices (CPU, no recorded run).
+
+K_e = sum over the Gauss points of B'DB det w (p121.f90:54-64 for 20-node
+bricks, p122.f90:76-84 with nod = 8) and kc = sum of (kx dx dx' + ky dy dy' +
+kz dz dz') det w (p123.f90:70-85) must be symmetric and positive
+semi-definite, with null spaces that are exactly the rigid-body modes (six
+for elasticity, the constant for the Laplace brick) under full integration.
+A linear displacement field (constant strain) must store exactly the strain
+energy of that strain over the element's volume.  These pin the oracle's
+SAMPLE, SHAPE_DER, DEEMAT, BEEMAT, DETERMINANT and INVERT independently of
+the reference's recorded runs.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def _brick(nod, aa, bb, cc, distort, seed):
+    """One element of GEOMETRY_20BXZ / GEOMETRY_8BXZ, coord (3, nod); with
+    distort, every node moved by up to distort * the element size."""
+    coord = np.zeros((3, nod))
+    num = np.zeros(nod, np.int32)
+    geo = O.lib().orc_geometry_20bxz if nod == 20 else O.lib().orc_geometry_8bxz
+    geo(1, 1, 1, aa, bb, cc, coord, num)
+    if distort:
+        rng = np.random.default_rng(seed)
+        coord = coord + distort * rng.uniform(-1.0, 1.0, coord.shape) * np.array([[aa], [bb], [cc]])
+    return np.ascontiguousarray(coord)
+
+
+def _rigid_modes(coord):
+    """The six rigid-body modes of an elasticity element, dofs (x, y, z) per node."""
+    x, y, z = coord
+    nod = coord.shape[1]
+    r = np.zeros((6, 3 * nod))
+    for d in range(3):
+        r[d, d::3] = 1.0
+    r[3, 0::3], r[3, 1::3] = -y, x      # rotation about z
+    r[4, 1::3], r[4, 2::3] = -z, y      # about x
+    r[5, 0::3], r[5, 2::3] = z, -x      # about y
+    return r
+
+
+def _elasticity_k(nod, coord, nip, e, v, exact=False):
+    if nod == 20:
+        km = O.form_storkm(coord[None], nip, e, v, exact_weights=exact)[0]
+    else:
+        km = O.form_storkm8(coord[None], nip, e, v)[0]
+    return km.T   # km[j, i] = K(i, j)
+
+
+@pytest.mark.parametrize("nod,nip", [(20, 27), (20, 8), (8, 8)])
+@pytest.mark.parametrize("distort", [0.0, 0.12])
+def test_elasticity_matrix_is_symmetric_psd_with_rigid_null_space(nod, nip, distort):
+    coord = _brick(nod, 1.0, 2.0, 0.5, distort, seed=nod * 100 + nip)
+    k = _elasticity_k(nod, coord, nip, 100.0, 0.3)
+    scale = np.abs(k).max()
+    assert np.abs(k - k.T).max() <= 1e-13 * scale
+    r = _rigid_modes(coord)
+    for mode in r:
+        assert np.linalg.norm(k @ mode) <= 1e-12 * scale * np.linalg.norm(mode)
+    lam = np.linalg.eigvalsh(0.5 * (k + k.T))
+    assert lam.min() >= -1e-11 * lam.max()
+    # full integration: the rigid-body modes are the whole null space; the
+    # 20-node brick under the 2x2x2 rule has six spurious zero-energy modes
+    # besides them, the known rank deficiency of that reduced rule
+    n0 = int((lam <= 1e-9 * lam.max()).sum())
+    assert n0 == (12 if (nod, nip) == (20, 8) else 6), (n0, lam[:14] / lam.max())
+
+
+@pytest.mark.parametrize("nod,nip", [(20, 27), (20, 8), (8, 8)])
+def test_constant_strain_stores_its_exact_energy(nod, nip):
+    aa, bb, cc, e, v = 1.0, 2.0, 0.5, 100.0, 0.3
+    coord = _brick(nod, aa, bb, cc, 0.0, seed=0)
+    exact = nod == 20   # exact Gauss weights (the 27-point rule's default factors are FP32)
+    k = _elasticity_k(nod, coord, nip, e, v, exact=exact)
+    rng = np.random.default_rng(7 + nod + nip)
+    a = rng.normal(size=(3, 3))
+    eps = 0.5 * (a + a.T)
+    u = (eps @ coord).T.reshape(-1)     # u(node) = eps x(node), dofs (x, y, z) per node
+    lam_ = e * v / ((1 + v) * (1 - 2 * v))
+    mu = e / (2 * (1 + v))
+    energy = (lam_ * np.trace(eps) ** 2 + 2 * mu * np.sum(eps * eps)) * aa * bb * cc
+    assert abs(u @ k @ u - energy) <= 1e-11 * abs(energy)
+
+
+def test_default_27_point_weights_follow_the_single_precision_factors():
+    """SAMPLE's 27-point weights are products of 5./9. and 8./9. in single
+    precision (new_library.f90:1491-1514): the energy of a constant strain
+    then differs from the exact one by the FP32 rounding of those factors,
+    about 1e-8 relative, not by zero."""
+    coord = _brick(20, 1.0, 1.0, 1.0, 0.0, seed=0)
+    rng = np.random.default_rng(3)
+    a = rng.normal(size=(3, 3))
+    eps = 0.5 * (a + a.T)
+    u = (eps @ coord).T.reshape(-1)
+    w_exact = u @ _elasticity_k(20, coord, 27, 100.0, 0.3, exact=True) @ u
+    w_fp32 = u @ _elasticity_k(20, coord, 27, 100.0, 0.3, exact=False) @ u
+    rel = abs(w_fp32 - w_exact) / abs(w_exact)
+    assert 1e-10 < rel < 1e-6
+
+
+@pytest.mark.parametrize("distort", [0.0, 0.12])
+def test_laplace_matrix_has_the_constant_as_its_null_space(distort):
+    aa, bb, cc, kx, ky, kz = 1.0, 2.0, 0.5, 1.0, 2.0, 3.0
+    coord = _brick(8, aa, bb, cc, distort, seed=11)
+    kc = O.form_storkc(coord[None], 8, kx, ky, kz)[0].T
+    scale = np.abs(kc).max()
+    assert np.abs(kc - kc.T).max() <= 1e-13 * scale
+    assert np.abs(kc.sum(axis=1)).max() <= 1e-12 * scale
+    lam = np.linalg.eigvalsh(0.5 * (kc + kc.T))
+    assert lam.min() >= -1e-12 * lam.max()
+    assert int((lam <= 1e-9 * lam.max()).sum()) == 1
+    if distort == 0.0:
+        g = np.array([0.3, -1.2, 0.7])
+        phi = g @ coord                  # a linear potential, constant gradient g
+        energy = (kx * g[0] ** 2 + ky * g[1] ** 2 + kz * g[2] ** 2) * aa * bb * cc
+        assert abs(phi @ kc @ phi - energy) <= 1e-11 * energy
