@@ -117,3 +117,45 @@ def test_laplace_matrix_has_the_constant_as_its_null_space(distort):
         phi = g @ coord                  # a linear potential, constant gradient g
         energy = (kx * g[0] ** 2 + ky * g[1] ** 2 + kz * g[2] ** 2) * aa * bb * cc
         assert abs(phi @ kc @ phi - energy) <= 1e-11 * energy
+
+
+@pytest.mark.parametrize("exact_weights,bound", [(True, 1e-10), (False, 1e-7)])
+def test_oracle_solve_passes_the_patch_test(exact_weights, bound):
+    """The oracle's assembly, Jacobi diagonal and PCG (p121.f90:65-104) on a
+    3x3x3 cube with distorted interior nodes: rollers on the planes x = 0,
+    y = 0 and on the base, uniform pressure p on the top face.  The exact
+    field is uz = -p (z - z0)/E, ux = nu p x/E, uy = nu p y/E, a constant
+    stress state that every 20-node brick reproduces.  With SAMPLE's
+    single-precision 27-point factors (the reference's default) the stiffness
+    and the exactly integrated pressure loads differ by those factors'
+    rounding, a few 1e-8 relative."""
+    import parafem_gb300 as P   # host-side mesh, numbering and load functions (no GPU)
+    n, e, nu, pr = 3, 100.0, 0.3, 0.3
+    g_num, g_coord, nn = P.mesh_cube(n, n, n)
+    X = np.zeros((nn, 3))
+    for el in range(g_num.shape[0]):
+        X[g_num[el] - 1] = g_coord[el].T
+    lo, hi = X.min(axis=0), X.max(axis=0)
+    inner = np.all((X > lo + 1e-9) & (X < hi - 1e-9), axis=1)
+    X[inner] += np.random.default_rng(3).uniform(-0.12, 0.12, size=(inner.sum(), 3))
+    g_coord = np.ascontiguousarray(X[g_num - 1].transpose(0, 2, 1))
+    fix = np.ones((nn, 3), np.int32)
+    for d in range(3):
+        fix[np.abs(X[:, d] - lo[d]) < 1e-9, d] = 0
+    g_g, neq = P.number_equations(g_num, fix)
+    r = P.cube_top_pressure(n, n, g_g, neq, pr)
+    km = O.form_storkm(g_coord, 27, e, nu, exact_weights=exact_weights)
+    dg = O.diag(g_g, km, neq)
+    it, x, rel = O.pcg(g_g, km, dg, r, 1e-12, 20000, 1)
+    assert rel <= 1e-12 and it < 20000
+    node = np.zeros(neq, int)
+    dof = np.zeros(neq, int)
+    for el in range(g_num.shape[0]):
+        for a in range(20):
+            for d in range(3):
+                q = g_g[el, 3 * a + d]
+                if q > 0:
+                    node[q - 1], dof[q - 1] = g_num[el, a] - 1, d
+    strain = np.array([nu * pr / e, nu * pr / e, -pr / e])   # sigma_zz = -p
+    exact = strain[dof] * (X[node, dof] - lo[dof])
+    assert np.abs(x - exact).max() <= bound * np.abs(exact).max()
