@@ -6,9 +6,11 @@ kz dz dz') det w (p123.f90:70-85) must be symmetric and positive
 semi-definite, with null spaces that are exactly the rigid-body modes (six
 for elasticity, the constant for the Laplace brick) under full integration.
 A linear displacement field (constant strain) must store exactly the strain
-energy of that strain over the element's volume.  These pin the oracle's
-SAMPLE, SHAPE_DER, DEEMAT, BEEMAT, DETERMINANT and INVERT independently of
-the reference's recorded runs.
+energy of that strain over the element's volume.  The Gauss rule must
+integrate its polynomial degree exactly and the shape-function derivatives
+must be complete.  These pin the oracle's SAMPLE, SHAPE_DER, DEEMAT, BEEMAT,
+DETERMINANT and INVERT, and its assembly and PCG (a patch test),
+independently of the reference's recorded runs.
 """
 import numpy as np
 import pytest
@@ -159,3 +161,41 @@ def test_oracle_solve_passes_the_patch_test(exact_weights, bound):
     strain = np.array([nu * pr / e, nu * pr / e, -pr / e])   # sigma_zz = -p
     exact = strain[dof] * (X[node, dof] - lo[dof])
     assert np.abs(x - exact).max() <= bound * np.abs(exact).max()
+
+
+@pytest.mark.parametrize("nip,deg", [(8, 3), (27, 5)])
+def test_gauss_rule_integrates_its_polynomial_degree_exactly(nip, deg):
+    """SAMPLE('hexahedron', nip) (new_library.f90:1397-1520) with exact
+    weights: the tensor Gauss rule integrates xi^a eta^b zeta^c over the
+    reference cube exactly for a, b, c <= deg."""
+    pts, wts = np.zeros(3 * nip), np.zeros(nip)
+    O.lib().orc_sample(nip, pts, wts, 1)
+    s = pts.reshape(3, nip)
+    for a in range(deg + 1):
+        for b in range(deg + 1):
+            for c in range(deg + 1):
+                exact = np.prod([0.0 if k % 2 else 2.0 / (k + 1) for k in (a, b, c)])
+                got = np.sum(wts * s[0] ** a * s[1] ** b * s[2] ** c)
+                assert abs(got - exact) <= 1e-14, (a, b, c, got, exact)
+
+
+@pytest.mark.parametrize("nod", [20, 8])
+def test_shape_derivatives_are_complete(nod):
+    """SHAPE_DER (new_library.f90:865-896 for 20 nodes; the 8-node brick):
+    the derivatives sum to zero over the nodes at any point, and on a
+    box-shaped element the Jacobian is the same at every point, with
+    8 det J the element's volume."""
+    aa, bb, cc = 1.0, 2.0, 0.5
+    coord = _brick(nod, aa, bb, cc, 0.0, seed=0)
+    f = O.lib().orc_shape_der20 if nod == 20 else O.lib().orc_shape_der8
+    rng = np.random.default_rng(5)
+    jac0 = None
+    for xi, eta, zeta in rng.uniform(-1.0, 1.0, size=(20, 3)):
+        der = np.zeros(3 * nod)
+        f(der, xi, eta, zeta)
+        d = der.reshape(nod, 3).T          # d[direction, node]
+        assert np.abs(d.sum(axis=1)).max() <= 1e-14
+        jac = d @ coord.T
+        jac0 = jac if jac0 is None else jac0
+        assert np.abs(jac - jac0).max() <= 1e-13
+    assert abs(8.0 * abs(np.linalg.det(jac0)) - aa * bb * cc) <= 1e-13
