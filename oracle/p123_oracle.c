@@ -95,6 +95,10 @@ void orc_find_g4(const int *num, int nod, int *g, int nr, const int *rest)
 {
     for (int i = 0; i < nod; ++i) {
         int l = num[i], first = 1, last = nr;
+        if (nr < 1) {   /* no restrained node (outside find_g4's domain): node = equation */
+            g[i] = l;
+            continue;
+        }
         while (first != last) {
             int half = (first + last) / 2;
             if (l <= rest[2 * (half - 1)]) last = half;

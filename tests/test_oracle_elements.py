@@ -199,3 +199,34 @@ def test_shape_derivatives_are_complete(nod):
         jac0 = jac if jac0 is None else jac0
         assert np.abs(jac - jac0).max() <= 1e-13
     assert abs(8.0 * abs(np.linalg.det(jac0)) - aa * bb * cc) <= 1e-13
+
+
+def test_p123_oracle_passes_the_laplace_patch_test():
+    """p123's storkc, diagonal, penalty fixed freedoms and PCG
+    (p123.f90:70-148) on a 3x3x3 box of 8-node bricks with distorted
+    interior nodes: the potential fixed to 0 on x = 0 and to g on x = 1 by
+    the penalty method, no flux elsewhere.  The exact potential g x is
+    linear, which every 8-node brick reproduces."""
+    n, g, penalty = 3, 2.5, 1e20
+    g_num, g_coord = O.box8_mesh(n, n, n, 1.0 / n, 1.0 / n, 1.0 / n)
+    nn = (n + 1) ** 3
+    X = np.zeros((nn, 3))
+    for el in range(g_num.shape[0]):
+        X[g_num[el] - 1] = g_coord[el].T
+    lo, hi = X.min(axis=0), X.max(axis=0)
+    inner = np.all((X > lo + 1e-9) & (X < hi - 1e-9), axis=1)
+    X[inner] += np.random.default_rng(9).uniform(-0.04, 0.04, size=(inner.sum(), 3))
+    g_coord = np.ascontiguousarray(X[g_num - 1].transpose(0, 2, 1))
+    g_g, neq = np.ascontiguousarray(g_num, dtype=np.int32), nn   # no restrained node: equation = node
+    kc = O.form_storkc(g_coord, 8, 1.0, 1.0, 1.0)
+    dg = O.diag8(g_g, kc, neq)
+    fixed = np.flatnonzero((np.abs(X[:, 0] - lo[0]) < 1e-9) | (np.abs(X[:, 0] - hi[0]) < 1e-9))
+    value = g * (X[fixed, 0] - lo[0])
+    dg[fixed] += penalty
+    store = dg[fixed].copy()
+    r = np.zeros(neq)
+    r[fixed] = store * value
+    it, x, _ = O.pcg123(g_g, kc, dg, r, 1e-12, 5000, fix_eq=fixed + 1, fix_store=store)
+    assert it < 5000
+    exact = g * (X[:, 0] - lo[0])
+    assert np.abs(x - exact).max() <= 1e-9 * g
