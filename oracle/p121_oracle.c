@@ -200,6 +200,10 @@ void orc_find_g3(const int *num, int *g, int nr, const int *rest)
     for (int i = 1; i <= 20; ++i) {
         int l = num[i - 1];
         int first = 1, last = nr;
+        if (nr < 1) {   /* no restrained node (outside find_g3's domain): all freedoms free */
+            for (int j = 1; j <= 3; ++j) g[3 * i - 3 + j - 1] = 3 * (l - 1) + j;
+            continue;
+        }
         while (first != last) {
             int half = (first + last) / 2;
             if (l <= rest[(half - 1) * 4]) last = half;

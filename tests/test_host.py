@@ -132,3 +132,16 @@ def test_truncated_deck_is_reported(tmp_path, demo_job, ext, what):
             dst.writelines(lines[: len(lines) // 2] if e == ext else lines)
     with pytest.raises(P.PfError, match=rf"cannot read \d+ {what} from .*cut\.{ext}"):
         P.p121_run(job)
+
+
+def test_numbering_without_restraints_is_the_identity():
+    """No restrained node: the product numbers freedom d of node l as
+    3 (l - 1) + d, as the oracle's find_g3 does for an empty list, and the
+    8-node scalar numbering gives each node its own number."""
+    g_num, _, nn = P.mesh_cube(2, 2, 2)
+    g_g, neq = P.number_equations(g_num, np.ones((nn, 3), np.int32))
+    assert neq == 3 * nn
+    assert np.array_equal(g_g, O.steering(g_num, np.zeros((0, 4), np.int32)))
+    g8, _ = O.box8_mesh(2, 2, 2, 1.0, 1.0, 1.0, coords=False)
+    s8, neq8 = O.steering8(g8, np.zeros((0, 2), np.int32))
+    assert neq8 == 27 and np.array_equal(s8, g8)
