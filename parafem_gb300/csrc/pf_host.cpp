@@ -20,7 +20,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <fstream>
+#include <new>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -31,6 +33,27 @@ void set_error(const char *fmt, ...);
 using pf::set_error;
 
 namespace {
+
+// Rows reserved up front when a deck is read; beyond this the arrays grow
+// with the lines actually present, whatever counts the .dat record claims.
+constexpr int kReserveRows = 1 << 20;
+
+// The C entry points of this file are function-try-blocks: a C++ exception
+// (host memory exhausted, above all) becomes PF_FAILURE with a message
+// instead of crossing the C ABI, where it would end the calling program.
+int host_exception(const char *name)
+{
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        set_error("%s: out of host memory", name);
+    } catch (const std::exception &e) {
+        set_error("%s: %s", name, e.what());
+    } catch (...) {
+        set_error("%s: unexpected C++ exception", name);
+    }
+    return PF_FAILURE;
+}
 
 // ---------------------------------------------------------------------------
 // Fortran edit descriptors used by the decks and result files
@@ -280,30 +303,40 @@ int read_mesh_files(const std::string &job, Deck &D)
         set_error("cannot read %s.d", job.c_str());
         return 1;
     }
+    if (D.nn < 1 || D.nels < 1) {
+        set_error("%s.dat: %d elements and %d nodes", job.c_str(), D.nels, D.nn);
+        return 1;
+    }
     std::string line;
     std::getline(f, line);
     std::getline(f, line);
-    D.coords.assign((size_t)3 * D.nn, 0.0);
+    // the arrays grow with the lines actually read, not with the counts the
+    // .dat record claims
+    D.coords.clear();
+    D.coords.reserve((size_t)3 * std::min(D.nn, kReserveRows));
     for (int i = 0; i < D.nn; ++i) {
         if (!std::getline(f, line)) { set_error("%s.d: short node list", job.c_str()); return 1; }
         std::istringstream ss(line);
         std::string id, a, b, c;
         ss >> id >> a >> b >> c;
-        D.coords[3 * (size_t)i] = to_d(a);
-        D.coords[3 * (size_t)i + 1] = to_d(b);
-        D.coords[3 * (size_t)i + 2] = to_d(c);
+        D.coords.push_back(to_d(a));
+        D.coords.push_back(to_d(b));
+        D.coords.push_back(to_d(c));
     }
     std::getline(f, line);   // *ELEMENTS
     const int nod = D.nod;
     if (nod != 20 && nod != 8) { set_error("%s: %d-node elements are not supported", job.c_str(), nod); return 1; }
-    D.g_num.assign((size_t)nod * D.nels, 0);
+    D.g_num.clear();
+    D.g_num.reserve((size_t)nod * std::min(D.nels, kReserveRows));
     for (int e = 0; e < D.nels; ++e) {
         if (!std::getline(f, line)) { set_error("%s.d: short element list", job.c_str()); return 1; }
         std::istringstream ss(line);
         long long k;
+        int nd[20];
         ss >> k >> k >> k >> k;
-        for (int a = 0; a < nod; ++a) ss >> D.g_num[nod * (size_t)e + a];
+        for (int a = 0; a < nod; ++a) ss >> nd[a];
         if (!ss) { set_error("%s.d: bad element line %d", job.c_str(), e + 1); return 1; }
+        D.g_num.insert(D.g_num.end(), nd, nd + nod);
     }
     if (D.meshgen == 2) {   // ABAQUS2SG (new_library.f90:3569-3627): node i takes file node from[i]
         static const int from20[20] = {4, 12, 1, 9, 2, 10, 3, 11, 20, 17, 18, 19, 8, 16, 5, 13, 6, 14, 7, 15};
@@ -365,7 +398,7 @@ int rest_to_fix(int nn, int nr, const int *rest, std::vector<int> &fix)
 // ===========================================================================
 extern "C" int pf_mesh_cube(const int *nxe, const int *nye, const int *nze, const double *aa, const double *bb,
                             const double *cc, int *nels, int *nn, int *g_num, double *g_coord)
-{
+try {
     if (!nxe || !nye || !nze || !aa || !bb || !cc || !nels || !nn || *nxe < 1 || *nye < 1 || *nze < 1) {
         set_error("pf_mesh_cube: invalid arguments");
         return PF_FAILURE;
@@ -385,10 +418,12 @@ extern "C" int pf_mesh_cube(const int *nxe, const int *nye, const int *nze, cons
         if (g_coord) std::copy(co, co + 60, g_coord + 60 * e);
     }
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_mesh_cube");
 }
 
 extern "C" int pf_cube_restraints(const int *nxe, const int *nye, const int *nze, const int *bc, int *node_fix)
-{
+try {
     if (!nxe || !nye || !nze || !bc || !node_fix || (*bc != 0 && *bc != 1)) {
         set_error("pf_cube_restraints: invalid arguments");
         return PF_FAILURE;
@@ -397,11 +432,13 @@ extern "C" int pf_cube_restraints(const int *nxe, const int *nye, const int *nze
     cube_fix(*nxe, *nye, *nze, *bc, fix);
     std::copy(fix.begin(), fix.end(), node_fix);
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_cube_restraints");
 }
 
 extern "C" int pf_number_equations(const int *nels, const int *nn, const int *g_num, const int *node_fix, int *g_g,
                                    int *neq)
-{
+try {
     if (!nels || !nn || !g_num || !node_fix || !g_g || !neq) {
         set_error("pf_number_equations: null argument");
         return PF_FAILURE;
@@ -418,11 +455,13 @@ extern "C" int pf_number_equations(const int *nels, const int *nn, const int *g_
             for (int d = 0; d < 3; ++d) g_g[60 * e + 3 * a + d] = node_eq[(size_t)(nd - 1) * 3 + d];
         }
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_number_equations");
 }
 
 extern "C" int pf_cube_top_pressure(const int *nxe, const int *nze, const int *nels, const double *aa,
                                     const double *bb, const double *p, const int *g_g, const int *neq, double *r)
-{
+try {
     if (!nxe || !nze || !nels || !aa || !bb || !p || !g_g || !neq || !r) {
         set_error("pf_cube_top_pressure: null argument");
         return PF_FAILURE;
@@ -443,6 +482,8 @@ extern "C" int pf_cube_top_pressure(const int *nxe, const int *nze, const int *n
         }
     }
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_cube_top_pressure");
 }
 
 namespace {
@@ -472,7 +513,7 @@ void philox4x32(uint32_t ctr[4], uint32_t k0, uint32_t k1)
 
 extern "C" int pf_random_material(const int *nels, const long long *seed, const double *e_lo, const double *e_hi,
                                   const double *v_lo, const double *v_hi, double *e, double *v)
-{
+try {
     if (!nels || !seed || !e_lo || !e_hi || !v_lo || !v_hi || !e || !v || !(*e_lo > 0) || !(*e_hi >= *e_lo)) {
         set_error("pf_random_material: invalid arguments");
         return PF_FAILURE;
@@ -490,6 +531,8 @@ extern "C" int pf_random_material(const int *nels, const long long *seed, const 
         v[i] = *v_lo + u2 * (*v_hi - *v_lo);
     }
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_random_material");
 }
 
 // ---------------------------------------------------------------------------
@@ -497,7 +540,7 @@ static int p12meshgen_p123(const std::string &job, const std::vector<std::string
 static int p12meshgen_p122(const std::string &job, const std::vector<std::string> &t);
 
 extern "C" int pf_p12meshgen(const char *job_c)
-{
+try {
     if (!job_c) { set_error("pf_p12meshgen: null job name"); return PF_FAILURE; }
     const std::string job(job_c);
     std::vector<std::string> t;
@@ -517,7 +560,7 @@ extern "C" int pf_p12meshgen(const char *job_c)
     const double aa = to_d(t[7]), bb = to_d(t[8]), cc = to_d(t[9]), e = to_d(t[10]), v = to_d(t[11]);
     const double tol = to_d(t[12]);
     const int limit = atoi(t[13].c_str());
-    if (nod != 20 || iotype != "parafem" || nxe < 1 || nze < 1 || nels % (nxe * nze) != 0) {
+    if (nod != 20 || iotype != "parafem" || nxe < 1 || nze < 1 || nels < 1 || (long long)nxe * nze > nels || nels % (nxe * nze) != 0) {
         set_error("%s.mg: supported: 'parafem' decks of 20-node cubes (nels divisible by nxe*nze)", job.c_str());
         return PF_FAILURE;
     }
@@ -585,13 +628,15 @@ extern "C" int pf_p12meshgen(const char *job_c)
             fmt_I(limit, 8).c_str());
     fclose(ft);
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_p12meshgen");
 }
 
 // ---------------------------------------------------------------------------
 // The p121 job (p121.f90:1-141) with the solve on the GPU.
 extern "C" int pf_p121_run(const char *job_c, const int *device, const int *mode, int *iters_out,
                            double *central_out)
-{
+try {
     if (!job_c || !device || !mode) { set_error("pf_p121_run: null argument"); return PF_FAILURE; }
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
@@ -682,6 +727,8 @@ extern "C" int pf_p121_run(const char *job_c, const int *device, const int *mode
     if (iters_out) *iters_out = iters;
     if (central_out) *central_out = neq > 0 ? x[0] : 0.0;
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_p121_run");
 }
 
 // load_p121's patch on the top face (loading.f90:386-480) as a load vector:
@@ -689,7 +736,7 @@ extern "C" int pf_p121_run(const char *job_c, const int *device, const int *mode
 // SCATTER_NOADD (loading.f90:36-146): assignment, the last entry wins.
 extern "C" int pf_patch_loads(const int *nxe, const int *nze, const double *factor, const int *nels,
                               const int *g_num, const int *g_g, const int *neq, double *r)
-{
+try {
     if (!nxe || !nze || !factor || !nels || !g_num || !g_g || !neq || !r || *nxe < 5 || *nze < 1) {
         set_error("pf_patch_loads: invalid arguments (nxe >= 5)");
         return PF_FAILURE;
@@ -709,6 +756,8 @@ extern "C" int pf_patch_loads(const int *nxe, const int *nze, const double *fact
             if (q > 0 && q <= *neq) r[q - 1] = *factor * mult[which[nd]];
         }
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_patch_loads");
 }
 
 // ===========================================================================
@@ -804,25 +853,29 @@ int read_deck8(const std::string &job, Deck8 &D)
     std::string line;
     std::getline(f, line);
     std::getline(f, line);
-    D.coords.assign((size_t)3 * D.nn, 0.0);
+    D.coords.clear();   // grown with the lines read, as in read_mesh_files
+    D.coords.reserve((size_t)3 * std::min(D.nn, kReserveRows));
     for (int i = 0; i < D.nn; ++i) {
         if (!std::getline(f, line)) { set_error("%s.d: short node list", job.c_str()); return 1; }
         std::istringstream ss(line);
         std::string id, a, b, c;
         ss >> id >> a >> b >> c;
-        D.coords[3 * (size_t)i] = to_d(a);
-        D.coords[3 * (size_t)i + 1] = to_d(b);
-        D.coords[3 * (size_t)i + 2] = to_d(c);
+        D.coords.push_back(to_d(a));
+        D.coords.push_back(to_d(b));
+        D.coords.push_back(to_d(c));
     }
     std::getline(f, line);   // *ELEMENTS
-    D.g_num.assign((size_t)8 * D.nels, 0);
+    D.g_num.clear();
+    D.g_num.reserve((size_t)8 * std::min(D.nels, kReserveRows));
     for (int e = 0; e < D.nels; ++e) {
         if (!std::getline(f, line)) { set_error("%s.d: short element list", job.c_str()); return 1; }
         std::istringstream ss(line);
         long long k;
+        int nd[8];
         ss >> k >> k >> k >> k;
-        for (int a = 0; a < 8; ++a) ss >> D.g_num[8 * (size_t)e + a];
+        for (int a = 0; a < 8; ++a) ss >> nd[a];
         if (!ss) { set_error("%s.d: bad element line %d", job.c_str(), e + 1); return 1; }
+        D.g_num.insert(D.g_num.end(), nd, nd + 8);
     }
     if (D.meshgen == 2) {   // ABAQUS2SG, 8-node (new_library.f90:3604-3618)
         static const int from[8] = {1, 5, 6, 2, 4, 8, 7, 3};
@@ -870,7 +923,7 @@ int read_deck8(const std::string &job, Deck8 &D)
 
 extern "C" int pf_mesh_box8(const int *nxe, const int *nye, const int *nze, const double *aa, const double *bb,
                             const double *cc, int *g_num, double *g_coord)
-{
+try {
     if (!nxe || !nye || !nze || !aa || !bb || !cc || !g_num || !g_coord || *nxe < 1 || *nye < 1 || *nze < 1) {
         set_error("pf_mesh_box8: invalid arguments");
         return PF_FAILURE;
@@ -879,10 +932,12 @@ extern "C" int pf_mesh_box8(const int *nxe, const int *nye, const int *nze, cons
     for (long long iel = 1; iel <= nels; ++iel)
         box8_element((int)iel, *nxe, *nze, *aa, *bb, *cc, g_num + 8 * (iel - 1), g_coord + 24 * (iel - 1));
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_mesh_box8");
 }
 
 extern "C" int pf_box8_restraints(const int *nxe, const int *nye, const int *nze, int *node_fix)
-{
+try {
     if (!nxe || !nye || !nze || !node_fix || *nxe < 1 || *nye < 1 || *nze < 1) {
         set_error("pf_box8_restraints: invalid arguments");
         return PF_FAILURE;
@@ -891,11 +946,13 @@ extern "C" int pf_box8_restraints(const int *nxe, const int *nye, const int *nze
     box8_fix(*nxe, *nye, *nze, fix);
     std::copy(fix.begin(), fix.end(), node_fix);
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_box8_restraints");
 }
 
 extern "C" int pf_number_equations1(const int *nels, const int *nn, const int *nod, const int *g_num,
                                     const int *node_fix, int *g_g, int *neq)
-{
+try {
     if (!nels || !nn || !nod || !g_num || !node_fix || !g_g || !neq || *nels < 0 || *nn < 1 || *nod < 1) {
         set_error("pf_number_equations1: invalid arguments");
         return PF_FAILURE;
@@ -916,6 +973,8 @@ extern "C" int pf_number_equations1(const int *nels, const int *nn, const int *n
     }
     *neq = q;
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_number_equations1");
 }
 
 // p12meshgen's p123 case (src/tools/preprocessing/p12meshgen/p12meshgen.f90:
@@ -934,7 +993,7 @@ static int p12meshgen_p123(const std::string &job, const std::vector<std::string
                  kz = to_d(t[11]), tol = to_d(t[12]);
     const int limit = atoi(t[13].c_str()), loaded = atoi(t[14].c_str());
     const int fixed = t.size() > 15 ? atoi(t[15].c_str()) : 0;
-    if (iotype != "parafem" || nxe < 1 || nze < 1 || nels % (nxe * nze) != 0) {
+    if (iotype != "parafem" || nxe < 1 || nze < 1 || nels < 1 || (long long)nxe * nze > nels || nels % (nxe * nze) != 0) {
         set_error("%s.mg: supported: 'parafem' decks (nels divisible by nxe*nze)", job.c_str());
         return PF_FAILURE;
     }
@@ -1006,7 +1065,7 @@ static int p12meshgen_p123(const std::string &job, const std::vector<std::string
 
 // The p123 job (p123.f90:1-182) with the solve on the GPU.
 extern "C" int pf_p123_run(const char *job_c, const int *device, int *iters_out, double *potentials_out)
-{
+try {
     if (!job_c || !device) { set_error("pf_p123_run: null argument"); return PF_FAILURE; }
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
@@ -1107,6 +1166,8 @@ extern "C" int pf_p123_run(const char *job_c, const int *device, int *iters_out,
     fclose(fr);
     if (iters_out) *iters_out = iters;
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_p123_run");
 }
 
 // ===========================================================================
@@ -1128,7 +1189,7 @@ static int p12meshgen_p122(const std::string &job, const std::vector<std::string
     const double phi = to_d(t[11]), c = to_d(t[12]), psi = to_d(t[13]), e = to_d(t[14]), v = to_d(t[15]);
     const int plasits = atoi(t[16].c_str()), cjits = atoi(t[17].c_str());
     const double plastol = to_d(t[18]), cjtol = to_d(t[19]);
-    if (nod != 20 || iotype != "parafem" || nxe < 5 || nze < 1 || nels % (nxe * nze) != 0 || incs < 1 ||
+    if (nod != 20 || iotype != "parafem" || nxe < 5 || nze < 1 || nels < 1 || (long long)nxe * nze > nels || nels % (nxe * nze) != 0 || incs < 1 ||
         t.size() < (size_t)20 + incs) {
         set_error("%s.mg: supported: 'parafem' p122 decks of 20-node cubes (nxe >= 5) with incs qinc values",
                   job.c_str());
@@ -1201,7 +1262,7 @@ static int p12meshgen_p122(const std::string &job, const std::vector<std::string
 // node, sense, value; READ_FIXED, input.f90:2483-2564); writes job.res and
 // job.ensi.DISPL-0000nn for every increment.
 extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
-{
+try {
     if (!job_c || !device) { set_error("pf_p122_run: null argument"); return PF_FAILURE; }
     using clk = std::chrono::steady_clock;
     const auto t0 = clk::now();
@@ -1351,4 +1412,6 @@ extern "C" int pf_p122_run(const char *job_c, const int *device, int *incs_out)
     fclose(fr);
     if (incs_out) *incs_out = done;
     return PF_SUCCESS;
+} catch (...) {
+    return host_exception("pf_p122_run");
 }

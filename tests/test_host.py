@@ -145,3 +145,60 @@ def test_numbering_without_restraints_is_the_identity():
     g8, _ = O.box8_mesh(2, 2, 2, 1.0, 1.0, 1.0, coords=False)
     s8, neq8 = O.steering8(g8, np.zeros((0, 2), np.int32))
     assert neq8 == 27 and np.array_equal(s8, g8)
+
+
+_RUN_LIMITED = r"""
+import resource, sys
+resource.setrlimit(resource.RLIMIT_AS, (8 << 30, 8 << 30))   # a runaway allocation fails, not the machine
+sys.path.insert(0, sys.argv[1])
+import parafem_gb300 as P
+try:
+    getattr(P, sys.argv[2])(sys.argv[3])
+    print("NO ERROR")
+except P.PfError as e:
+    print("PfError:", e)
+"""
+
+
+def _run_limited(fn, job):
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _RUN_LIMITED, ROOT, fn, job], capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]   # no abort: every failure comes back as an error status
+    return r.stdout
+
+
+@pytest.mark.parametrize("token,value,match", [
+    (4, "2000000000", "short node list"),   # nn far beyond the node lines of the .d file
+    (3, "2000000000", "short element list"),
+    (4, "-7", "elements and -7 nodes"),
+    (3, "0", "0 elements and"),
+])
+def test_deck_counts_the_files_do_not_hold_are_reported(tmp_path, demo_job, token, value, match):
+    """The .dat record's counts do not size any array before the lines are
+    read, and a count the .d file does not hold is an error, not an
+    allocation the size of the claim."""
+    job = str(tmp_path / "claim")
+    for e in ("d", "bnd", "lds"):
+        with open(f"{demo_job}.{e}") as src, open(f"{job}.{e}", "w") as dst:
+            dst.write(src.read())
+    toks = open(f"{demo_job}.dat").read().split()
+    toks[token] = value
+    with open(f"{job}.dat", "w") as f:
+        f.write(" ".join(toks) + "\n")
+    out = _run_limited("p121_run", job)
+    assert out.startswith("PfError:") and match in out, out
+
+
+@pytest.mark.parametrize("case,body", [
+    ("p121", "p121\nparafem\n-6 2 3 20 27 1.0 1.0 1.0 100.0 0.3 1e-6 5000\n"),
+    ("p121", "p121\nparafem\n6 200000 300000 20 27 1.0 1.0 1.0 100.0 0.3 1e-6 5000\n"),
+    ("p123", "p123\nparafem\n-6 2 3 8 1.0 1.0 1.0 1.0 1.0 1.0 1e-5 500 1 0\n"),
+])
+def test_mesh_generator_rejects_element_counts_it_cannot_form(tmp_path, case, body):
+    job = str(tmp_path / case)
+    with open(job + ".mg", "w") as f:
+        f.write(body)
+    out = _run_limited("p12meshgen", job)
+    assert out.startswith("PfError:") and "supported" in out, out
