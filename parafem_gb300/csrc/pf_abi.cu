@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <string>
 #include <vector>
@@ -29,6 +30,20 @@ void set_error(const char *fmt, ...)
     vsnprintf(buf, sizeof buf, fmt, ap);
     va_end(ap);
     g_err = buf;
+}
+
+int host_exception(const char *name)
+{
+    try {
+        throw;
+    } catch (const std::bad_alloc &) {
+        set_error("%s: out of host memory", name);
+    } catch (const std::exception &e) {
+        set_error("%s: %s", name, e.what());
+    } catch (...) {
+        set_error("%s: unexpected C++ exception", name);
+    }
+    return PF_FAILURE;
 }
 
 #define CK(call)                                                                         \
@@ -253,14 +268,16 @@ using namespace pf;
 // ===========================================================================
 // xx3 layer (src/programs/dev/xx3/cuda_helpers.cu:183-368)
 extern "C" int set_gpu(const int *device_id)
-{
+try {
     if (!device_id) { set_error("set_gpu: null argument"); return PF_FAILURE; }
     CK(cudaSetDevice(*device_id));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("set_gpu");
 }
 
 extern "C" int allocate_memory_on_gpu(const int *n_elements, const int *element_size, void **device_pointer)
-{
+try {
     if (!n_elements || !element_size || !device_pointer || *n_elements < 0 || *element_size < 0) {
         set_error("allocate_memory_on_gpu: invalid arguments");
         return PF_FAILURE;
@@ -268,19 +285,23 @@ extern "C" int allocate_memory_on_gpu(const int *n_elements, const int *element_
     const size_t bytes = (size_t)*n_elements * (size_t)*element_size;
     CK(cudaMalloc(device_pointer, bytes ? bytes : 1));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("allocate_memory_on_gpu");
 }
 
 extern "C" int free_memory_on_gpu(void **device_pointer)
-{
+try {
     if (!device_pointer) { set_error("free_memory_on_gpu: null argument"); return PF_FAILURE; }
     CK(cudaFree(*device_pointer));
     *device_pointer = nullptr;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("free_memory_on_gpu");
 }
 
 extern "C" int copy_data_to_gpu(const int *n_elements, const int *element_size, const void *host_data,
                                 void **device_pointer)
-{
+try {
     if (!n_elements || !element_size || !device_pointer || (!host_data && *n_elements > 0)) {
         set_error("copy_data_to_gpu: invalid arguments");
         return PF_FAILURE;
@@ -288,11 +309,13 @@ extern "C" int copy_data_to_gpu(const int *n_elements, const int *element_size, 
     CK(cudaMemcpy(*device_pointer, host_data, (size_t)*n_elements * (size_t)*element_size,
                   cudaMemcpyHostToDevice));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("copy_data_to_gpu");
 }
 
 extern "C" int copy_data_from_gpu(const int *n_elements, const int *element_size, void *host_data,
                                   void **device_pointer)
-{
+try {
     if (!n_elements || !element_size || !device_pointer || (!host_data && *n_elements > 0)) {
         set_error("copy_data_from_gpu: invalid arguments");
         return PF_FAILURE;
@@ -300,13 +323,15 @@ extern "C" int copy_data_from_gpu(const int *n_elements, const int *element_size
     CK(cudaMemcpy(host_data, *device_pointer, (size_t)*n_elements * (size_t)*element_size,
                   cudaMemcpyDeviceToHost));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("copy_data_from_gpu");
 }
 
 static long long g_xx3_launches = 0;
 
 extern "C" int matrix_vector_multiplies(int *n_mat, int *n_row, int *n_col, void **d_lhs_vector,
                                         void **d_matrix, void **d_rhs_vector)
-{
+try {
     if (!n_mat || !n_row || !n_col || !d_lhs_vector || !d_matrix || !d_rhs_vector || *n_mat < 0 ||
         *n_row < 1 || *n_col < 1) {
         set_error("matrix_vector_multiplies: invalid arguments");
@@ -318,22 +343,26 @@ extern "C" int matrix_vector_multiplies(int *n_mat, int *n_row, int *n_col, void
         return PF_FAILURE;
     CK(cudaDeviceSynchronize());
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("matrix_vector_multiplies");
 }
 
 // ===========================================================================
 // solve layer
 extern "C" int pf_last_error(char *buf, const int *len)
-{
+try {
     if (!buf || !len || *len <= 0) return PF_FAILURE;
     const size_t n = (size_t)*len - 1;
     const size_t m = g_err.size() < n ? g_err.size() : n;
     memcpy(buf, g_err.data(), m);
     buf[m] = '\0';
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_last_error");
 }
 
 extern "C" int pf_ctx_create(const int *device, void **ctx)
-{
+try {
     if (!device || !ctx) { set_error("pf_ctx_create: null argument"); return PF_FAILURE; }
     *ctx = nullptr;
     int ndev = 0;
@@ -364,10 +393,12 @@ extern "C" int pf_ctx_create(const int *device, void **ctx)
     memset(c->hst, 0, sizeof(PcgState));
     *ctx = c;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_ctx_create");
 }
 
 extern "C" int pf_ctx_destroy(void **ctx)
-{
+try {
     if (!ctx || !*ctx) return PF_SUCCESS;
     Ctx *c = (Ctx *)*ctx;
     cudaSetDevice(c->device);
@@ -381,6 +412,8 @@ extern "C" int pf_ctx_destroy(void **ctx)
     delete c;
     *ctx = nullptr;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_ctx_destroy");
 }
 
 // Mesh tables of a context: nod nodes per element (20 or 8) with nodof
@@ -507,24 +540,30 @@ static int setup_mesh(void **ctx, const int *nels_p, const int *nn_p, const int 
 
 extern "C" int pf_setup(void **ctx, const int *nels, const int *nn, const int *neq, const int *g_num,
                         const int *g_g, const double *g_coord)
-{
+try {
     return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 20, 3);
+} catch (...) {
+    return pf::host_exception("pf_setup");
 }
 
 extern "C" int pf_setup_scalar8(void **ctx, const int *nels, const int *nn, const int *neq, const int *g_num,
                                 const int *g_g, const double *g_coord)
-{
+try {
     return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 8, 1);
+} catch (...) {
+    return pf::host_exception("pf_setup_scalar8");
 }
 
 extern "C" int pf_setup_solid8(void **ctx, const int *nels, const int *nn, const int *neq, const int *g_num,
                                const int *g_g, const double *g_coord)
-{
+try {
     return setup_mesh(ctx, nels, nn, neq, g_num, g_g, g_coord, 8, 3);
+} catch (...) {
+    return pf::host_exception("pf_setup_solid8");
 }
 
 extern "C" int pf_form_storkc(void **ctx, const int *nip, const double *kx, const double *ky, const double *kz)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -543,10 +582,12 @@ extern "C" int pf_form_storkc(void **ctx, const int *nip, const double *kx, cons
     TRY(sync(c));
     c.have_km = true;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_form_storkc");
 }
 
 extern "C" int pf_get_storkc(void **ctx, const int *first, const int *count, double *storkc)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -559,10 +600,12 @@ extern "C" int pf_get_storkc(void **ctx, const int *first, const int *count, dou
                        cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_get_storkc");
 }
 
 extern "C" int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const double *penalty)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -598,10 +641,12 @@ extern "C" int pf_set_fixed(void **ctx, const int *nfix, const int *eqs, const d
     if (bad && e != cudaSuccess) set_error("pf_set_fixed: %s", cudaGetErrorString(e));
     drop_graph(c);
     return bad ? PF_FAILURE : PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_fixed");
 }
 
 extern "C" int pf_set_material(void **ctx, const int *n, const double *e, const double *v)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -622,6 +667,8 @@ extern "C" int pf_set_material(void **ctx, const int *n, const double *e, const 
     CK(cudaMemcpyAsync(c.mat_v, v, *n * sizeof(double), cudaMemcpyHostToDevice, c.stream));
     CK(cudaStreamSynchronize(c.stream));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_material");
 }
 
 // The per-element storkm arrays (FP64, FP32, packed FP32), allocated on the
@@ -646,7 +693,7 @@ static int ensure_storkm(Ctx &c)
 }
 
 extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -679,10 +726,12 @@ extern "C" int pf_form_storkm(void **ctx, const int *nip, const int *flags)
     TRY(sync(c));
     c.have_km = true;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_form_storkm");
 }
 
 extern "C" int pf_set_storkm(void **ctx, const double *storkm)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -701,10 +750,12 @@ extern "C" int pf_set_storkm(void **ctx, const double *storkm)
     TRY(sync(c));
     c.have_km = true;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_storkm");
 }
 
 extern "C" int pf_form_km(void **ctx, const int *iel, const int *nip, const int *flags, double *km)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -739,10 +790,12 @@ extern "C" int pf_form_km(void **ctx, const int *iel, const int *nip, const int 
         return PF_FAILURE;
     }
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_form_km");
 }
 
 extern "C" int pf_set_shared_km(void **ctx, const double *km)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -782,10 +835,12 @@ extern "C" int pf_set_shared_km(void **ctx, const double *km)
     TRY(sync(c));
     c.have_km = true;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_shared_km");
 }
 
 extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, double *storkm)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -806,10 +861,12 @@ extern "C" int pf_get_storkm(void **ctx, const int *first, const int *count, dou
                        cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_get_storkm");
 }
 
 extern "C" int pf_get_diag(void **ctx, double *diag)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -818,10 +875,12 @@ extern "C" int pf_get_diag(void **ctx, double *diag)
     CK(cudaMemcpyAsync(diag, c.eqbuf, (size_t)c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_get_diag");
 }
 
 extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, double *u)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -840,6 +899,8 @@ extern "C" int pf_ebe_matvec(void **ctx, const int *prec, const double *p, doubl
     CK(cudaMemcpyAsync(u, c.eqbuf, (size_t)c.neq * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_ebe_matvec");
 }
 
 // Mixed precision, restarted defect correction: each outer step solves
@@ -912,7 +973,7 @@ static int solve_mixed(Ctx &c, double tol, int limit, double ff, double *dev2, i
 
 extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const int *limit, const int *mode,
                         double *xnew, int *iters, double *relres)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -977,19 +1038,23 @@ extern "C" int pf_solve(void **ctx, const double *r, const double *tol, const in
     *iters = (int)c.stats[0];
     if (relres) *relres = rel;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_solve");
 }
 
 extern "C" int pf_solve_stats(void **ctx, double *stats, const int *n)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp || !stats || !n) return PF_FAILURE;
     for (int i = 0; i < *n && i < 8; ++i) stats[i] = cp->stats[i];
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_solve_stats");
 }
 
 extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps, double *ms_total,
                                    double *ms_elem, double *ms_scatter)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -1044,10 +1109,12 @@ extern "C" int pf_bench_iterations(void **ctx, const int *prec, const int *steps
     if (ms_elem) *ms_elem = te;
     if (ms_scatter) *ms_scatter = ts;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_bench_iterations");
 }
 
 extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew, double *sigma)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -1066,11 +1133,13 @@ extern "C" int pf_centroid_stress(void **ctx, const int *iel, const double *xnew
     CK(cudaMemcpyAsync(sigma, sig, 6 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_centroid_stress");
 }
 
 extern "C" int pf_element_stresses(void **ctx, const double *xnew, const int *first, const int *count,
                                    double *sigma)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     Ctx &c = *cp;
@@ -1091,20 +1160,24 @@ extern "C" int pf_element_stresses(void **ctx, const double *xnew, const int *fi
     CK(cudaMemcpyAsync(sigma, sig, (size_t)6 * *count * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
     TRY(sync(c));
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_element_stresses");
 }
 
 extern "C" int pf_tuning(void **ctx, int *warps, int *stages, float *ms)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp || !warps || !stages || !ms) return PF_FAILURE;
     *warps = cp->sym_warps;
     *stages = cp->sym_stages;
     for (int i = 0; i < 3; ++i) ms[i] = cp->tune_ms[i];
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_tuning");
 }
 
 extern "C" int pf_tuning16(void **ctx, int *warps, int *stages, float *ms)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp || !warps || !stages || !ms) return PF_FAILURE;
     if (!cp->km16_ok) {
@@ -1114,10 +1187,12 @@ extern "C" int pf_tuning16(void **ctx, int *warps, int *stages, float *ms)
     if (h16_config(cp->h16_cfg, warps, stages)) return PF_FAILURE;
     for (int i = 0; i < 3; ++i) ms[i] = cp->tune16_ms[i];
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_tuning16");
 }
 
 extern "C" int pf_set_tuning(void **ctx, const int *config)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp || !config) return PF_FAILURE;
     Ctx &c = *cp;
@@ -1135,10 +1210,12 @@ extern "C" int pf_set_tuning(void **ctx, const int *config)
     }
     set_sym_config(c, *config);
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_tuning");
 }
 
 extern "C" int pf_check_wait_timeout(void **ctx, const int *polls)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     if (!polls || *polls < 1) {
@@ -1149,10 +1226,12 @@ extern "C" int pf_check_wait_timeout(void **ctx, const int *polls)
     if (check_kernel_error(*cp)) return PF_FAILURE;   // the timeout, reported as the kernels report it
     set_error("pf_check_wait_timeout: the wait completed, so the timeout path did not run");
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_check_wait_timeout");
 }
 
 extern "C" int pf_set_persistent(void **ctx, const int *on)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp) return PF_FAILURE;
     if (!on) {
@@ -1162,21 +1241,27 @@ extern "C" int pf_set_persistent(void **ctx, const int *on)
     cp->persistent = *on != 0;
     drop_graph(*cp);
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_persistent");
 }
 
 extern "C" int pf_set_graphs(void **ctx, const int *on)
-{
+try {
     Ctx *cp = get_ctx(ctx);
     if (!cp || !on) return PF_FAILURE;
     cp->use_graphs = *on != 0;
     if (!cp->use_graphs) drop_graph(*cp);
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_set_graphs");
 }
 
 extern "C" int pf_kernel_launches(void **ctx, long long *count)
-{
+try {
     if (!count) return PF_FAILURE;
     *count = g_xx3_launches;
     if (ctx && *ctx) *count += ((Ctx *)*ctx)->launches;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_kernel_launches");
 }

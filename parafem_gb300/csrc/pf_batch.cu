@@ -771,7 +771,7 @@ using namespace pf;
 // ===========================================================================
 extern "C" int pf_batch_create(const int *device, const long long *budget_bytes, const int *max_meshes,
                                const int *prec, void **batch)
-{
+try {
     if (!device || !budget_bytes || !max_meshes || !prec || !batch || *max_meshes < 1 ||
         *budget_bytes < (1LL << 20) || (*prec != 64 && *prec != 32 && *prec != 16)) {
         set_error("pf_batch_create: invalid arguments (prec must be 64, 32 or 16)");
@@ -852,10 +852,12 @@ extern "C" int pf_batch_create(const int *device, const long long *budget_bytes,
     for (int i = B->max_meshes - 1; i >= 0; --i) B->sid_free.push_back(i);
     *batch = B;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_create");
 }
 
 extern "C" int pf_batch_destroy(void **batch)
-{
+try {
     if (!batch || !*batch) return PF_SUCCESS;
     Batch *B = (Batch *)*batch;
     cudaSetDevice(B->device);
@@ -864,22 +866,26 @@ extern "C" int pf_batch_destroy(void **batch)
     delete B;
     *batch = nullptr;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_destroy");
 }
 
 extern "C" int pf_batch_capacity(void **batch, long long *elements, long long *nodes)
-{
+try {
     Batch *B = get_batch(batch);
     if (!B || !elements || !nodes) return PF_FAILURE;
     *elements = B->cap_el;
     *nodes = B->cap_nodes;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_capacity");
 }
 
 extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, const int *neq_p, const int *g_num,
                               const int *g_g, const double *g_coord, const int *nmat_p, const double *e,
                               const double *v, const int *nip_p, const double *rhs, const double *tol,
                               const int *limit, int *id_out)
-{
+try {
     Batch *Bp = get_batch(batch);
     if (!Bp) return PF_FAILURE;
     Batch &B = *Bp;
@@ -1059,10 +1065,12 @@ extern "C" int pf_batch_admit(void **batch, const int *nels_p, const int *nn_p, 
     B.dirty = true;
     *id_out = B.next_id - 1;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_admit");
 }
 
 extern "C" int pf_batch_launch(void **batch, const int *iters)
-{
+try {
     Batch *Bp = get_batch(batch);
     if (!Bp || !iters || *iters < 1) {
         if (Bp) set_error("pf_batch_launch: iters must be >= 1");
@@ -1076,10 +1084,12 @@ extern "C" int pf_batch_launch(void **batch, const int *iters)
     BCK(cudaGraphLaunch(B.g_exec, B.stream));
     B.launches += B.g_launches;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_launch");
 }
 
 extern "C" int pf_batch_sync(void **batch, int *n_active, int *n_done)
-{
+try {
     Batch *Bp = get_batch(batch);
     if (!Bp) return PF_FAILURE;
     Batch &B = *Bp;
@@ -1100,11 +1110,13 @@ extern "C" int pf_batch_sync(void **batch, int *n_active, int *n_done)
     if (n_active) *n_active = (int)(B.order.size() + B.pending.size());
     if (n_done) *n_done = (int)B.done.size();
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_sync");
 }
 
 extern "C" int pf_batch_collect(void **batch, int *id, int *iters, double *relres, double *x, const int *x_cap,
                                 int *neq)
-{
+try {
     Batch *Bp = get_batch(batch);
     if (!Bp || !id || !iters || !relres || !neq) return PF_FAILURE;
     Batch &B = *Bp;
@@ -1126,20 +1138,26 @@ extern "C" int pf_batch_collect(void **batch, int *id, int *iters, double *relre
     *relres = dn.relres;
     B.done.pop_front();
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_collect");
 }
 
 extern "C" int pf_batch_set_graphs(void **batch, const int *on)
-{
+try {
     Batch *B = get_batch(batch);
     if (!B || !on) return PF_FAILURE;
     B->use_graphs = *on != 0;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_set_graphs");
 }
 
 extern "C" int pf_batch_launches(void **batch, long long *count)
-{
+try {
     Batch *B = get_batch(batch);
     if (!B || !count) return PF_FAILURE;
     *count = B->launches;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_batch_launches");
 }

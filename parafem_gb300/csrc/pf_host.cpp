@@ -29,6 +29,7 @@
 
 namespace pf {
 void set_error(const char *fmt, ...);
+int host_exception(const char *name);   // pf_abi.cu: an exception -> PF_FAILURE
 }
 using pf::set_error;
 
@@ -37,23 +38,6 @@ namespace {
 // Rows reserved up front when a deck is read; beyond this the arrays grow
 // with the lines actually present, whatever counts the .dat record claims.
 constexpr int kReserveRows = 1 << 20;
-
-// The C entry points of this file are function-try-blocks: a C++ exception
-// (host memory exhausted, above all) becomes PF_FAILURE with a message
-// instead of crossing the C ABI, where it would end the calling program.
-int host_exception(const char *name)
-{
-    try {
-        throw;
-    } catch (const std::bad_alloc &) {
-        set_error("%s: out of host memory", name);
-    } catch (const std::exception &e) {
-        set_error("%s: %s", name, e.what());
-    } catch (...) {
-        set_error("%s: unexpected C++ exception", name);
-    }
-    return PF_FAILURE;
-}
 
 // ---------------------------------------------------------------------------
 // Fortran edit descriptors used by the decks and result files
@@ -419,7 +403,7 @@ try {
     }
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_mesh_cube");
+    return pf::host_exception("pf_mesh_cube");
 }
 
 extern "C" int pf_cube_restraints(const int *nxe, const int *nye, const int *nze, const int *bc, int *node_fix)
@@ -433,7 +417,7 @@ try {
     std::copy(fix.begin(), fix.end(), node_fix);
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_cube_restraints");
+    return pf::host_exception("pf_cube_restraints");
 }
 
 extern "C" int pf_number_equations(const int *nels, const int *nn, const int *g_num, const int *node_fix, int *g_g,
@@ -456,7 +440,7 @@ try {
         }
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_number_equations");
+    return pf::host_exception("pf_number_equations");
 }
 
 extern "C" int pf_cube_top_pressure(const int *nxe, const int *nze, const int *nels, const double *aa,
@@ -483,7 +467,7 @@ try {
     }
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_cube_top_pressure");
+    return pf::host_exception("pf_cube_top_pressure");
 }
 
 namespace {
@@ -532,7 +516,7 @@ try {
     }
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_random_material");
+    return pf::host_exception("pf_random_material");
 }
 
 // ---------------------------------------------------------------------------
@@ -629,7 +613,7 @@ try {
     fclose(ft);
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_p12meshgen");
+    return pf::host_exception("pf_p12meshgen");
 }
 
 // ---------------------------------------------------------------------------
@@ -728,7 +712,7 @@ try {
     if (central_out) *central_out = neq > 0 ? x[0] : 0.0;
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_p121_run");
+    return pf::host_exception("pf_p121_run");
 }
 
 // load_p121's patch on the top face (loading.f90:386-480) as a load vector:
@@ -757,7 +741,7 @@ try {
         }
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_patch_loads");
+    return pf::host_exception("pf_patch_loads");
 }
 
 // ===========================================================================
@@ -933,7 +917,7 @@ try {
         box8_element((int)iel, *nxe, *nze, *aa, *bb, *cc, g_num + 8 * (iel - 1), g_coord + 24 * (iel - 1));
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_mesh_box8");
+    return pf::host_exception("pf_mesh_box8");
 }
 
 extern "C" int pf_box8_restraints(const int *nxe, const int *nye, const int *nze, int *node_fix)
@@ -947,7 +931,7 @@ try {
     std::copy(fix.begin(), fix.end(), node_fix);
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_box8_restraints");
+    return pf::host_exception("pf_box8_restraints");
 }
 
 extern "C" int pf_number_equations1(const int *nels, const int *nn, const int *nod, const int *g_num,
@@ -974,7 +958,7 @@ try {
     *neq = q;
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_number_equations1");
+    return pf::host_exception("pf_number_equations1");
 }
 
 // p12meshgen's p123 case (src/tools/preprocessing/p12meshgen/p12meshgen.f90:
@@ -1167,7 +1151,7 @@ try {
     if (iters_out) *iters_out = iters;
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_p123_run");
+    return pf::host_exception("pf_p123_run");
 }
 
 // ===========================================================================
@@ -1413,5 +1397,5 @@ try {
     if (incs_out) *incs_out = done;
     return PF_SUCCESS;
 } catch (...) {
-    return host_exception("pf_p122_run");
+    return pf::host_exception("pf_p122_run");
 }

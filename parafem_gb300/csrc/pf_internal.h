@@ -23,6 +23,11 @@ __host__ __device__ constexpr int packed_off(int i, int k)
 // Records a formatted error message for pf_last_error (thread local).
 void set_error(const char *fmt, ...);
 
+// The C entry points are function-try-blocks whose handler calls this: a C++
+// exception (host memory exhausted, above all) becomes PF_FAILURE with a
+// message instead of crossing the C ABI, where it would end the caller.
+int host_exception(const char *name);
+
 // Scalars of one PCG run, resident on the device (pinned host mirror).
 // Only the single-block finish kernel of an iteration (or block 0 of a
 // persistent kernel, after its last barrier of the iteration) writes them,

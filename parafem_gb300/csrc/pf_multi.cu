@@ -1353,7 +1353,7 @@ static int mr_kernel_error(Ctx &c, const char *who)
 
 extern "C" int pf_solve_multi(void **ctx, const int *k_p, const double *r, const double *tol, const int *limit,
                               const int *prec, double *xnew, int *iters, double *relres)
-{
+try {
     if (!ctx || !*ctx || !k_p || !r || !tol || !limit || !prec || !xnew || !iters || !relres) {
         set_error("pf_solve_multi: null argument");
         return PF_FAILURE;
@@ -1484,12 +1484,14 @@ extern "C" int pf_solve_multi(void **ctx, const int *k_p, const double *r, const
     c.stats[5] = ms_iter;   // summed time of the iterations measured start to start
     c.stats[6] = total;     // iterations launched (including no-op ones after a flag)
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_solve_multi");
 }
 
 // Block product U = K P for k cases in equation order (tests): prec 16, 32
 // or 64.
 extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k_p, const int *prec, const double *p, double *u)
-{
+try {
     if (!ctx || !*ctx || !k_p || !prec || !p || !u) {
         set_error("pf_ebe_matvec_multi: null argument");
         return PF_FAILURE;
@@ -1520,10 +1522,12 @@ extern "C" int pf_ebe_matvec_multi(void **ctx, const int *k_p, const int *prec, 
     MCK(cudaStreamSynchronize(c.stream));
     if (mr_kernel_error(c, "pf_ebe_matvec_multi")) return PF_FAILURE;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_ebe_matvec_multi");
 }
 
 extern "C" int pf_multi_product_ms(void **ctx, const int *k_p, const double *p, const int *reps, double *ms)
-{
+try {
     if (!ctx || !*ctx || !k_p || !p || !reps || !ms || *reps < 1) {
         set_error("pf_multi_product_ms: null argument or reps < 1");
         return PF_FAILURE;
@@ -1560,10 +1564,12 @@ extern "C" int pf_multi_product_ms(void **ctx, const int *k_p, const double *p, 
     if (mr_kernel_error(c, "pf_multi_product_ms")) return PF_FAILURE;
     *ms = t / *reps;
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_multi_product_ms");
 }
 
 extern "C" int pf_multi_tuning(void **ctx, int *kb, int *cand, float *ms)
-{
+try {
     if (!ctx || !*ctx || !kb || !cand || !ms) {
         set_error("pf_multi_tuning: null argument");
         return PF_FAILURE;
@@ -1579,14 +1585,18 @@ extern "C" int pf_multi_tuning(void **ctx, int *kb, int *cand, float *ms)
         ms[i] = c.multi->cand_ms[i];
     }
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_multi_tuning");
 }
 
 extern "C" int pf_multi_free(void **ctx)
-{
+try {
     if (!ctx || !*ctx) return PF_SUCCESS;
     Ctx &c = *(Ctx *)*ctx;
     cudaSetDevice(c.device);
     cudaStreamSynchronize(c.stream);
     multi_release(c);
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_multi_free");
 }

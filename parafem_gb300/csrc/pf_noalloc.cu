@@ -27,6 +27,7 @@
 
 namespace pf {
 void set_error(const char *fmt, ...);
+int host_exception(const char *name);   // pf_abi.cu: an exception -> PF_FAILURE
 }
 using pf::set_error;
 
@@ -207,7 +208,7 @@ bool is_device_pointer(const void *p, int dev)
 // stream.  *nels = *neq = 0 does only that set-up.
 extern "C" int pf_ebe_matvec_noalloc(const int *nels_p, const int *neq_p, const double *d_storkm,
                                      const int *d_g_g, const double *d_p, double *d_u)
-{
+try {
     if (nels_p && neq_p && *nels_p == 0 && *neq_p == 0) {   // set-up only
         NoallocScratch *S = nullptr;
         return scratch_for_current_device(&S) ? PF_FAILURE : PF_SUCCESS;
@@ -263,4 +264,6 @@ extern "C" int pf_ebe_matvec_noalloc(const int *nels_p, const int *neq_p, const 
         return PF_FAILURE;
     }
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_ebe_matvec_noalloc");
 }

@@ -353,7 +353,7 @@ extern "C" int pf_p122_solve_fixed(void **ctx, const int *nip, const double *phi
                                    const int *cjits, const double *plastol, const double *cjtol, const double *ld0,
                                    const int *nfix_p, const int *fix_eqs, const double *fix_vals, double *results,
                                    double *totd_out, int *incs_done)
-{
+try {
     if (!ctx || !*ctx || !nip || !phi || !c_coh || !psi || !incs || !qinc || !plasits || !cjits || !plastol ||
         !cjtol || !nfix_p || !results || !incs_done) {
         set_error("pf_p122_solve: null argument");
@@ -521,13 +521,15 @@ extern "C" int pf_p122_solve_fixed(void **ctx, const int *nip, const double *phi
     PCK(cudaStreamSynchronize(c.stream));
     p122_free(q);
     return PF_SUCCESS;
+} catch (...) {
+    return pf::host_exception("pf_p122_solve_fixed");
 }
 
 extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, const double *c_coh, const double *psi,
                              const int *incs, const double *qinc, const int *plasits, const int *cjits,
                              const double *plastol, const double *cjtol, const double *ld0, double *results,
                              double *totd_out, int *incs_done)
-{
+try {
     if (!ld0) {
         set_error("pf_p122_solve: null argument");
         return PF_FAILURE;
@@ -535,4 +537,6 @@ extern "C" int pf_p122_solve(void **ctx, const int *nip, const double *phi, cons
     const int zero = 0;
     return pf_p122_solve_fixed(ctx, nip, phi, c_coh, psi, incs, qinc, plasits, cjits, plastol, cjtol, ld0, &zero,
                                nullptr, nullptr, results, totd_out, incs_done);
+} catch (...) {
+    return pf::host_exception("pf_p122_solve");
 }

@@ -202,3 +202,14 @@ def test_mesh_generator_rejects_element_counts_it_cannot_form(tmp_path, case, bo
         f.write(body)
     out = _run_limited("p12meshgen", job)
     assert out.startswith("PfError:") and "supported" in out, out
+
+
+def test_host_memory_exhaustion_is_an_error_status(tmp_path):
+    """A valid request that the host cannot hold (a 1000^3 cube's deck, about
+    100 GB of node and element arrays, under an 8 GB address-space limit)
+    comes back as PF_FAILURE through the entry point's exception handler."""
+    job = str(tmp_path / "huge")
+    with open(job + ".mg", "w") as f:
+        f.write("p121\nparafem\n1000000000 1000 1000 20 27 1.0 1.0 1.0 100.0 0.3 1e-6 5000\n")
+    out = _run_limited("p12meshgen", job)
+    assert out.startswith("PfError:") and "pf_p12meshgen: out of host memory" in out, out
