@@ -1,7 +1,9 @@
-"""CPU oracle for the p121 and p123 EBE-PCG paths (TEST INFRASTRUCTURE ONLY).
+"""CPU oracle for the p121, p122 and p123 EBE-PCG paths (TEST INFRASTRUCTURE ONLY).
 
-Wraps ``p121_oracle.c`` (a plain-C restatement of ParaFEM's p121 solve) and
-adds a numpy reader for p121 decks.  Only the tests, the smoke check and the
+Wraps ``p121_oracle.c`` (a plain-C restatement of ParaFEM's p121 solve),
+``p122_oracle.c`` and ``p123_oracle.c`` (the same for p122 and p123) and
+``p121_cpu.c`` (the timed CPU build of p121's PCG), and adds a numpy reader
+for p121 decks.  Only the tests, the smoke check and the
 CPU-baseline leg of ``bench.py`` import this module; the product library never
 does.
 
