@@ -408,7 +408,8 @@ try {
 
 extern "C" int pf_cube_restraints(const int *nxe, const int *nye, const int *nze, const int *bc, int *node_fix)
 try {
-    if (!nxe || !nye || !nze || !bc || !node_fix || (*bc != 0 && *bc != 1)) {
+    if (!nxe || !nye || !nze || !bc || !node_fix || (*bc != 0 && *bc != 1) || *nxe < 1 || *nye < 1 || *nze < 1 ||
+        cube_nn(*nxe, *nye, *nze) * 3 > 0x7fffffffLL) {
         set_error("pf_cube_restraints: invalid arguments");
         return PF_FAILURE;
     }
@@ -425,6 +426,10 @@ extern "C" int pf_number_equations(const int *nels, const int *nn, const int *g_
 try {
     if (!nels || !nn || !g_num || !node_fix || !g_g || !neq) {
         set_error("pf_number_equations: null argument");
+        return PF_FAILURE;
+    }
+    if (*nels < 0 || *nn < 1) {
+        set_error("pf_number_equations: %d elements and %d nodes", *nels, *nn);
         return PF_FAILURE;
     }
     std::vector<int> node_eq;
@@ -448,6 +453,10 @@ extern "C" int pf_cube_top_pressure(const int *nxe, const int *nze, const int *n
 try {
     if (!nxe || !nze || !nels || !aa || !bb || !p || !g_g || !neq || !r) {
         set_error("pf_cube_top_pressure: null argument");
+        return PF_FAILURE;
+    }
+    if (*nxe < 1 || *nze < 1 || *nels < 0) {
+        set_error("pf_cube_top_pressure: nxe=%d nze=%d nels=%d", *nxe, *nze, *nels);
         return PF_FAILURE;
     }
     const double A = *aa * *bb;
@@ -498,7 +507,8 @@ void philox4x32(uint32_t ctr[4], uint32_t k0, uint32_t k1)
 extern "C" int pf_random_material(const int *nels, const long long *seed, const double *e_lo, const double *e_hi,
                                   const double *v_lo, const double *v_hi, double *e, double *v)
 try {
-    if (!nels || !seed || !e_lo || !e_hi || !v_lo || !v_hi || !e || !v || !(*e_lo > 0) || !(*e_hi >= *e_lo)) {
+    if (!nels || !seed || !e_lo || !e_hi || !v_lo || !v_hi || !e || !v || *nels < 0 || !(*e_lo > 0) ||
+        !(*e_hi >= *e_lo)) {
         set_error("pf_random_material: invalid arguments");
         return PF_FAILURE;
     }
@@ -721,7 +731,7 @@ try {
 extern "C" int pf_patch_loads(const int *nxe, const int *nze, const double *factor, const int *nels,
                               const int *g_num, const int *g_g, const int *neq, double *r)
 try {
-    if (!nxe || !nze || !factor || !nels || !g_num || !g_g || !neq || !r || *nxe < 5 || *nze < 1) {
+    if (!nxe || !nze || !factor || !nels || !g_num || !g_g || !neq || !r || *nxe < 5 || *nze < 1 || *nels < 0) {
         set_error("pf_patch_loads: invalid arguments (nxe >= 5)");
         return PF_FAILURE;
     }

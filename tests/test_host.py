@@ -213,3 +213,54 @@ def test_host_memory_exhaustion_is_an_error_status(tmp_path):
         f.write("p121\nparafem\n1000000000 1000 1000 20 27 1.0 1.0 1.0 100.0 0.3 1e-6 5000\n")
     out = _run_limited("p12meshgen", job)
     assert out.startswith("PfError:") and "pf_p12meshgen: out of host memory" in out, out
+
+
+_DEGENERATE = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+import parafem_gb300 as P
+L = P.lib()
+i = lambda v: ctypes.byref(ctypes.c_int(v))
+dd = lambda v: ctypes.byref(ctypes.c_double(v))
+buf_i = np.ones(64, np.int32)
+buf_d = np.zeros(64)
+out = ctypes.c_int()
+calls = {
+    "mesh_cube nxe 0": lambda: L.pf_mesh_cube(i(0), i(1), i(1), dd(1), dd(1), dd(1), ctypes.byref(out),
+                                              ctypes.byref(out), None, None),
+    "cube_restraints nxe 0": lambda: L.pf_cube_restraints(i(0), i(1), i(1), i(0), buf_i.ctypes.data),
+    "cube_restraints nze -2": lambda: L.pf_cube_restraints(i(1), i(1), i(-2), i(0), buf_i.ctypes.data),
+    "number_equations nels -1": lambda: L.pf_number_equations(i(-1), i(1), buf_i.ctypes.data, buf_i.ctypes.data,
+                                                              buf_i.ctypes.data, ctypes.byref(out)),
+    "number_equations nn 0": lambda: L.pf_number_equations(i(1), i(0), buf_i.ctypes.data, buf_i.ctypes.data,
+                                                           buf_i.ctypes.data, ctypes.byref(out)),
+    "cube_top_pressure nxe 0": lambda: L.pf_cube_top_pressure(i(0), i(1), i(1), dd(1), dd(1), dd(1),
+                                                              buf_i.ctypes.data, i(1), buf_d.ctypes.data),
+    "random_material nels -1": lambda: L.pf_random_material(i(-1), ctypes.byref(ctypes.c_longlong(1)), dd(1),
+                                                            dd(2), dd(0.2), dd(0.3), buf_d.ctypes.data,
+                                                            buf_d.ctypes.data),
+    "patch_loads nels -1": lambda: L.pf_patch_loads(i(5), i(1), dd(1), i(-1), buf_i.ctypes.data, buf_i.ctypes.data,
+                                                    i(1), buf_d.ctypes.data),
+    "number_equations1 nels -1": lambda: L.pf_number_equations1(i(-1), i(1), i(8), buf_i.ctypes.data,
+                                                                buf_i.ctypes.data, buf_i.ctypes.data,
+                                                                ctypes.byref(out)),
+}
+for name, call in calls.items():
+    print(name, "=>", call(), P.pfgpu.last_error())
+"""
+
+
+def test_host_helpers_reject_degenerate_sizes():
+    """Zero, negative or overflowing sizes come back as PF_FAILURE with a
+    message: no division by zero, no loop over a wrapped count."""
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, "-c", _DEGENERATE, ROOT], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = r.stdout.strip().splitlines()
+    assert len(lines) == 9, r.stdout
+    for ln in lines:
+        name, rest = ln.split(" => ")
+        status, msg = rest.split(" ", 1)
+        assert status == "1" and msg.startswith("pf_"), ln
